@@ -1,0 +1,296 @@
+"""Benchmark: SBS primary-ray throughput (Mrays/s) on the large batched SBS workload.
+
+Workload ("sbs-batched-16view", the config the metric is quoted on): SDF of a
+seeded smooth union (k=0.05) of 48 spheres and 16 rounded boxes, sampled at
+octree depth 7 with 8-voxel bricks (1024^3 effective grid), DX layout 4 bytes
+per value (213,585 bricks, 623 MB); 16 views of uneven size (512..2048 per side,
+33.6 Mrays) on a radius-3 orbit, rendered in one persistent launch per step with
+the reference NEWTON finder, NORMAL mode, closest hit.  A step renders all 16
+views into a device hit buffer (t, primId, normal; 16 B per ray).
+
+Arms: default = this engine (CUDA, sm_103a); --impl reference = the reference's
+CPU algorithm for the same path (the oracle port in oracle/, OpenMP over all host
+cores) on a bounded pixel sample of the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SBS Mrays/s (plain finder, 16-view batched persistent launch)"
+UNIT = "Mrays/s"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--depth", type=int, default=7)
+    ap.add_argument("--brick", type=int, default=8)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = float(p[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def build_workload(args):
+    from litert_gb300 import lrt, scenes
+    t0 = time.time()
+    h, nodes, values = lrt.sbs_from_sdf(scenes.union_sdf(), args.depth, args.brick)
+    views = scenes.union_views()
+    return h, nodes, values, views, time.time() - t0
+
+
+def cpu_sample(views, n_target, seed=0):
+    """A strided pixel sample over all views: list of (view index, pixel ids)."""
+    total = sum(w * h for w, h, _, _ in views)
+    out = []
+    for vi, (w, h, _, _) in enumerate(views):
+        k = max(1, int(round(n_target * (w * h) / total)))
+        stride = max(1, (w * h) // k)
+        out.append((vi, np.arange(seed % stride, w * h, stride, dtype=np.uint32)[:k]))
+    return out
+
+
+def run_cpu_baseline(h, nodes, values, views, pairs, seconds):
+    """Oracle port of the reference CPU path, all host threads, bounded sample."""
+    from litert_gb300 import lrt
+    from oracle import oracle as orc
+    osc = orc.Scene("sbs", sbs=(orc.SbsHeader(h.brick_size, h.brick_pad, h.bytes_per_value, h.aux_data), nodes, values),
+                    pairs=pairs, intersect=2, render_mode=8, closest_hit=True)
+    cores = os.cpu_count() or 1
+
+    def run(n):
+        cnt_tot = np.zeros(6)
+        t0 = time.perf_counter()
+        rays = 0
+        for vi, pix in cpu_sample(views, n):
+            w, hh, wv, pj = views[vi]
+            _, cnt = osc.render_pixels(w, hh, lrt.inverse4x4(pj), lrt.inverse4x4(wv), pix, threads=cores)
+            cnt_tot += [cnt.n_fat, cnt.n_leaf, cnt.n_vox, cnt.n_vox_loaded, cnt.n_finder, cnt.n_tri]
+            rays += pix.size
+        return rays, time.perf_counter() - t0, cnt_tot
+
+    r0, t0, _ = run(20000)
+    n = int(min(4_000_000, max(20000, 20000 * seconds / max(t0, 1e-3))))
+    rays, dt, cnt = run(n)
+    return dict(value=rays / dt / 1e6, rays=rays, seconds=dt, cores=cores, counters=cnt)
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        h, nodes, values, views, tb = build_workload(args)
+        from litert_gb300 import lrt
+        from oracle import oracle as orc
+        pairs = lrt.build_bvh2(orc.node_boxes(nodes), 1)
+        per_step = []
+        cores = os.cpu_count() or 1
+        budget = max(2.0, 120.0 / max(1, args.steps + args.warmup))
+        res = None
+        for i in range(args.warmup + args.steps):
+            res = run_cpu_baseline(h, nodes, values, views, pairs, budget)
+            if i >= args.warmup:
+                per_step.append(res["value"])
+        v = statistics.median(per_step)
+        line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 33.596325e6 / (v * 1e6) * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "impl": "reference",
+                "config": {"workload": "sbs-batched-16view", "rays_per_step": 33596325, "depth": args.depth,
+                           "brick": args.brick, "finder": "NEWTON", "sample_rays_per_step": res["rays"]},
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                 "sample": f"{res['rays']} strided pixels of the 16 views per step"},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    from litert_gb300 import lrt
+    from oracle import oracle as orc
+
+    h, nodes, values, views, t_build = build_workload(args)
+    scene = lrt.Scene(local if world > 1 else 0)
+    g = scene.add_sbs(h, nodes, values)
+    scene.add_instance(g)
+    scene.commit_scene()
+    scene.set_preset(render_mode=lrt.RENDER_MODE_NORMAL, sdf_node_intersect=lrt.INTERSECT_NEWTON)
+    dev = torch.device("cuda", local if world > 1 else 0)
+    n_rays = sum(w * hh for w, hh, _, _ in views)
+    hits = torch.empty(n_rays * 4, dtype=torch.float32, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    va = lrt.make_views(views)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        scene.render_device(va, len(views), hits_ptr=hits.data_ptr(), stream=stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        flush.fill_(1.0)
+        step()
+    torch.cuda.synchronize(dev)
+
+    clocks = ClockSampler(dev.index)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    clocks.start()
+    launches = 0
+    for i in range(args.steps):
+        flush.fill_(float(i))            # L2 flush between timed steps, outside the events
+        evs[i][0].record(stream)
+        step()
+        evs[i][1].record(stream)
+        launches += scene.last_launch_count()
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    times = [a.elapsed_time(b) for a, b in evs]
+    ms = sum(times) / len(times)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * n_rays / (ms * 1e-3) / 1e6
+
+    # end to end through the C ABI with host buffers (views in, hit buffer out, pinned host memory)
+    host_hits = torch.empty(n_rays * 4, dtype=torch.float32, pin_memory=True)
+    e2e_times = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        lrt.lib().lrt_render_host(scene._ctx, lrt.C.cast(va, lrt.C.c_void_p), len(views),
+                                  lrt.C.c_void_p(host_hits.data_ptr()), None, None)
+        if i >= args.warmup:
+            e2e_times.append(time.perf_counter() - t0)
+    e2e = world * n_rays / statistics.median(e2e_times) / 1e6
+
+    line = None
+    if rank == 0:
+        # algorithmic bytes per ray (64 B per BVH2 fat pair, 16 B per brick node, 32 B per voxel's
+        # corners, 16 B per output record) counted by the oracle on a pixel sample with the
+        # engine's SAH BVH2 in the reference layout
+        pairs = lrt.build_bvh2(orc.node_boxes(nodes), 1)
+        cpu = None
+        if not args.no_cpu_baseline:
+            cpu = run_cpu_baseline(h, nodes, values, views, pairs, args.cpu_seconds)
+            c = cpu["counters"]
+            b_ray = (64 * c[0] + 16 * c[1] + 32 * c[2]) / cpu["rays"] + 16
+        else:
+            b_ray = None
+        peaks = {}
+        try:
+            peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        except OSError:
+            pass
+        peak = peaks.get("hbm_gbs", 6800.0)
+        achieved = (b_ray * n_rays / (ms * 1e-3) / 1e9) if b_ray else None
+        traffic = None
+        tp = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(tp):
+            traffic = json.load(open(tp)).get("render_kernel_sbs_batched_bytes_per_launch")
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "sbs-batched-16view", "rays_per_step": n_rays, "views": len(views),
+                       "depth": args.depth, "brick": args.brick, "bricks": int(nodes.shape[0]),
+                       "brick_bytes": int(values.nbytes), "finder": "NEWTON", "render_mode": "NORMAL",
+                       "l2": "256 MiB write between timed steps; scene data 623 MB > L2",
+                       "scene_build_s": round(t_build, 2), "parallelism": f"replicas{world}"},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(len(views) * 136),
+                    "d2h_bytes_per_step": int(n_rays * 16)},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                         "bytes_per_ray": b_ray,
+                         "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"},
+            "clocks": clk,
+        }
+        if cpu:
+            line["cpu_baseline"] = {"value": cpu["value"], "unit": UNIT, "cores": cpu["cores"], "kind": "port",
+                                    "sample": f"{cpu['rays']} strided pixels of the 16 views ({cpu['seconds']:.1f} s)"}
+        print(json.dumps(line))
+    scene.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

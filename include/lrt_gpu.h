@@ -1,0 +1,125 @@
+/*
+ * lrt — GB300 ray-query engine, C ABI.
+ *
+ * Plain pointers and sizes only.  Every call returns an lrt_status; on failure
+ * lrt_last_error(ctx) holds a message.  One context per host thread; all device
+ * work of a call is issued on the stream passed in (NULL = the legacy default
+ * stream).  Each entry point names the reference interface it replaces.
+ */
+#ifndef LRT_GPU_H
+#define LRT_GPU_H
+#include "lrt_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  LRT_OK = 0,
+  LRT_ERR_INVALID = 1,      /* bad argument */
+  LRT_ERR_OOM = 2,          /* device or host allocation failed */
+  LRT_ERR_CUDA = 3,         /* CUDA runtime error */
+  LRT_ERR_UNSUPPORTED = 4,  /* input the engine does not handle (layout, type, ...) */
+  LRT_ERR_TIMEOUT = 5,      /* a bounded device-side wait gave up */
+  LRT_ERR_BOUNDS = 6,       /* a device-side index check failed */
+  LRT_ERR_STATE = 7         /* call order (e.g. render before commit) */
+} lrt_status;
+
+typedef struct lrt_ctx lrt_ctx;
+
+/* ---- context (replaces CreateSceneRT / CreateMultiRenderer(DEVICE_GPU):
+ *      ISceneObject.h:14, BVH/BVH2Common_host.cpp:1799-1802,
+ *      Renderer/eye_ray_host.cpp:684-753) ---- */
+lrt_status  lrt_create(lrt_ctx **out, int device);
+void        lrt_destroy(lrt_ctx *ctx);
+const char *lrt_last_error(const lrt_ctx *ctx);
+const char *lrt_status_string(lrt_status s);
+
+/* ---- scene (ISceneObject / BVHRT surface, BVH/BVH2Common.h:100-173) ---- */
+/* BVHRT::ClearGeom, BVH/BVH2Common_host.cpp:82-108 */
+lrt_status lrt_clear_geom(lrt_ctx *ctx);
+/* BVHRT::AddGeom_SdfSBS, BVH/BVH2Common_host.cpp:567-666.  Layouts DX (1/2/4 bytes),
+ * ID32F_IRGB32F and ID32F_IRGB32F_IN.  Data are copied. */
+lrt_status lrt_add_sbs(lrt_ctx *ctx, const lrt_sbs_header *hdr, const lrt_sbs_node *nodes, uint32_t n_nodes,
+                       const uint32_t *values, uint32_t n_values, const float *values_f,
+                       uint32_t n_values_f, uint32_t *geom_id);
+/* BVHRT::AddGeom_SdfSVS, BVH/BVH2Common_host.cpp:502-565 */
+lrt_status lrt_add_svs(lrt_ctx *ctx, const lrt_svs_node *nodes, uint32_t n_nodes, uint32_t *geom_id);
+/* BVHRT::AddGeom_Triangles3f, BVH/BVH2Common_host.cpp:205-257 (primsInLeaf 2) */
+lrt_status lrt_add_triangles(lrt_ctx *ctx, const float *vpos, size_t n_vert, size_t v_byte_stride,
+                             const uint32_t *indices, size_t n_indices, uint32_t *geom_id);
+/* BVHRT::ClearScene, BVH/BVH2Common_host.cpp:1382-1388 */
+lrt_status lrt_clear_scene(lrt_ctx *ctx);
+/* BVHRT::AddInstance, BVH/BVH2Common_host.cpp:1450-1487 (matrix row-major) */
+lrt_status lrt_add_instance(lrt_ctx *ctx, uint32_t geom_id, const float matrix[16], uint32_t *inst_id);
+/* BVHRT::CommitScene, BVH/BVH2Common_host.cpp:1416-1448: builds the BVH and
+ * uploads the scene to the device.  One instance per scene. */
+lrt_status lrt_commit_scene(lrt_ctx *ctx);
+/* BVHRT::SetPreset / MultiRenderer::SetPreset, Renderer/eye_ray_host.cpp:549-556 */
+lrt_status lrt_set_preset(lrt_ctx *ctx, const lrt_preset *preset);
+
+/* ---- queries ---- */
+/* BVHRT::RayQuery_NearestHit, BVH/BVH2Common.cpp:3490-3559, batched: n rays of
+ * float4 (pos, tNear) and float4 (dir, tFar); tFar <= 0 requests any-hit
+ * (RayQuery_AnyHit, :3561-3566).  device_ptrs != 0: all three arrays are device
+ * memory and the call is asynchronous on `stream`; otherwise host memory and the
+ * call returns after the copy back. */
+lrt_status lrt_query_rays(lrt_ctx *ctx, const float *pos_near, const float *dir_far, uint32_t n,
+                          lrt_hit *out, int device_ptrs, void *stream);
+
+/* ---- rendering (MultiRenderer::Render / RenderFloat, Renderer/eye_ray_host.cpp:563-585,
+ *      batched over views in one persistent launch) ---- */
+/* Output offsets: view v starts at sum_{u<v} width_u*height_u pixels, row-major
+ * within a view.  Any of hits16 / rgba / rgba8 may be NULL.  All output pointers
+ * are device memory; asynchronous on `stream`. */
+lrt_status lrt_render(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, lrt_hit16 *hits16,
+                      float *rgba, uint32_t *rgba8, void *stream);
+/* Same, with host output buffers: copies views in and results out, synchronous. */
+lrt_status lrt_render_host(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, lrt_hit16 *hits16,
+                           float *rgba, uint32_t *rgba8);
+/* Number of our kernels launched by the last lrt_render / lrt_query_rays call. */
+uint32_t lrt_last_launch_count(const lrt_ctx *ctx);
+/* Per-ray traversal counters of the committed scene for the given views (a
+ * counting variant of the render kernel, not for timing): fat-node visits
+ * (BVH2-equivalent), leaf visits, voxel visits, finder calls.  out[4], summed. */
+lrt_status lrt_render_counters(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, uint64_t out[4]);
+
+/* The committed scene's BVH2 in the reference's fat-pair layout (root pair at 0),
+ * as CreateFatTreeArray produces it (BVH/cbvh_fat.cpp:100-142).  Host pointer
+ * owned by ctx, valid until the next commit. */
+lrt_status lrt_get_bvh2(lrt_ctx *ctx, const lrt_bvh_pair **pairs, uint32_t *n_pairs);
+
+/* The BVH builder alone, no device needed: fat pairs for n boxes (n x 6 floats,
+ * min xyz then max xyz).  prims_per_leaf 1: leaf payload is the box id; 2: leaf
+ * payload indexes *leaf_start_count (PackOffsetAndSize(start, count) into
+ * *order, the reordered primitive ids).  Arrays are malloc'd; free with
+ * lrt_free.  Replaces BuildBVHFatCustom / BuildBVHFat (BVH/cbvh_fat.cpp:148-183). */
+lrt_status lrt_build_bvh2(const float *boxes6, uint32_t n, uint32_t prims_per_leaf, lrt_bvh_pair **pairs,
+                          uint32_t *n_pairs, uint32_t **leaf_start_count, uint32_t *n_leaves, uint32_t **order);
+void lrt_free(void *p);
+
+/* ---- scene construction (utils/sdf_converter.cpp:118-181,
+ *      utils/sparse_octree_builder.cpp:72-444, :2346-2387) ---- */
+typedef struct lrt_sbs lrt_sbs;
+typedef struct lrt_svs lrt_svs;
+/* create_sdf_SBS: frame octree to `depth`, border bricks, DX layout quantisation. */
+lrt_status lrt_sbs_build_from_sdf(const lrt_sdf_desc *sdf, uint32_t depth, const lrt_sbs_header *hdr,
+                                  int threads, lrt_sbs **out);
+lrt_status lrt_sbs_data(const lrt_sbs *sbs, lrt_sbs_header *hdr, const lrt_sbs_node **nodes, uint32_t *n_nodes,
+                        const uint32_t **values, uint32_t *n_values);
+void       lrt_sbs_free(lrt_sbs *sbs);
+/* create_sdf_SVS */
+lrt_status lrt_svs_build_from_sdf(const lrt_sdf_desc *sdf, uint32_t depth, int threads, lrt_svs **out);
+lrt_status lrt_svs_data(const lrt_svs *svs, const lrt_svs_node **nodes, uint32_t *n_nodes);
+void       lrt_svs_free(lrt_svs *svs);
+
+/* ---- camera helpers (LiteMath::perspectiveMatrix / lookAt / inverse4x4 as used
+ *      by tests/tests.cpp:29-41 and Renderer/eye_ray_host.cpp:59-65) ---- */
+void lrt_perspective(float fov_deg, float aspect, float znear, float zfar, float out[16]);
+void lrt_look_at(const float eye[3], const float center[3], const float up[3], float out[16]);
+void lrt_inverse4x4(const float m[16], float out[16]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,691 @@
+// C ABI of the GB300 ray-query engine: context, scene staging and commit
+// (the BVHRT host side, BVH/BVH2Common_host.cpp), batched rendering and ray
+// queries.  Host code only; kernels live in trace.cu.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "lrt_internal.h"
+
+using namespace lrt;
+
+namespace {
+
+struct Geom {
+  uint32_t type = 0;
+  SbsData sbs;
+  std::vector<float> values_f;
+  std::vector<lrt_svs_node> svs;
+  std::vector<float> vpos;        // float4 per vertex
+  std::vector<uint32_t> indices;  // 3 per triangle
+  float bmin[3] = {-1, -1, -1}, bmax[3] = {1, 1, 1};
+};
+
+struct Inst {
+  uint32_t geom = 0;
+  float m[16], inv[16], inv_t[16];
+  float bmin[3], bmax[3];
+};
+
+template <typename T>
+struct DevBuf {
+  T *p = nullptr;
+  size_t cap = 0;  // elements
+  cudaError_t ensure(size_t n) {
+    if (n <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T));
+    if (e == cudaSuccess) cap = n;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+}  // namespace
+
+struct lrt_ctx {
+  int device = 0;
+  int num_sms = 0;
+  std::string err;
+  std::vector<Geom> geoms;
+  std::vector<Inst> insts;
+  lrt_preset preset{};
+  bool committed = false;
+  DevScene dev{};
+  BvhData bvh;
+  // committed scene buffers
+  DevBuf<WNode4> d_nodes;
+  DevBuf<lrt_sbs_node> d_bricks;
+  DevBuf<uint32_t> d_values;
+  DevBuf<float> d_values_f;
+  DevBuf<lrt_svs_node> d_svs;
+  DevBuf<float4> d_tri_verts;
+  DevBuf<uint32_t> d_prim_indices;
+  // per-call scratch
+  DevBuf<uint32_t> d_tile_counter;
+  DevBuf<DevView> d_views;
+  DevBuf<unsigned long long> d_counters;
+  DevView *h_views = nullptr;  // pinned staging for view uploads
+  size_t h_views_cap = 0;
+  // host-buffer entry points
+  DevBuf<lrt_hit16> d_out_hits;
+  DevBuf<float4> d_out_rgba;
+  DevBuf<uint32_t> d_out_rgba8;
+  DevBuf<float4> d_q_pos, d_q_dir;
+  DevBuf<lrt_hit> d_q_out;
+  uint32_t last_launches = 0;
+};
+
+static lrt_status fail(lrt_ctx *ctx, lrt_status s, const std::string &msg) {
+  if (ctx) ctx->err = msg;
+  return s;
+}
+
+static lrt_status cuda_fail(lrt_ctx *ctx, cudaError_t e, const char *where) {
+  return fail(ctx, e == cudaErrorMemoryAllocation ? LRT_ERR_OOM : LRT_ERR_CUDA,
+              std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define LRT_CUDA(ctx, call)                                   \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call);  \
+  } while (0)
+
+// ---------------------------------------------------------------- matrices
+static void mat_mul_vec4(const float m[16], const float v[4], float r[4]) {
+  for (int i = 0; i < 4; i++) r[i] = m[i * 4 + 0] * v[0] + m[i * 4 + 1] * v[1] + m[i * 4 + 2] * v[2] + m[i * 4 + 3] * v[3];
+}
+
+extern "C" void lrt_inverse4x4(const float m[16], float out[16]) {
+  double a[4][8];
+  for (int i = 0; i < 4; i++)
+    for (int j = 0; j < 8; j++) a[i][j] = j < 4 ? double(m[i * 4 + j]) : (j - 4 == i ? 1.0 : 0.0);
+  for (int c = 0; c < 4; c++) {
+    int p = c;
+    for (int r = c + 1; r < 4; r++)
+      if (std::fabs(a[r][c]) > std::fabs(a[p][c])) p = r;
+    if (p != c)
+      for (int j = 0; j < 8; j++) std::swap(a[c][j], a[p][j]);
+    const double inv = 1.0 / a[c][c];
+    for (int j = 0; j < 8; j++) a[c][j] *= inv;
+    for (int r = 0; r < 4; r++)
+      if (r != c) {
+        const double f = a[r][c];
+        for (int j = 0; j < 8; j++) a[r][j] -= f * a[c][j];
+      }
+  }
+  for (int i = 0; i < 4; i++)
+    for (int j = 0; j < 4; j++) out[i * 4 + j] = float(a[i][j + 4]);
+}
+
+extern "C" void lrt_perspective(float fov_deg, float aspect, float znear, float zfar, float out[16]) {
+  std::memset(out, 0, 16 * sizeof(float));
+  const float ymax = znear * std::tan(fov_deg * 3.14159265358979323846f / 180.0f * 0.5f);
+  const float xmax = ymax * aspect;
+  const float l = -xmax, r = xmax, b = -ymax, t = ymax;
+  out[0] = 2.0f * znear / (r - l);
+  out[2] = (r + l) / (r - l);
+  out[5] = 2.0f * znear / (t - b);
+  out[6] = (t + b) / (t - b);
+  out[10] = (-zfar - znear) / (zfar - znear);
+  out[11] = (-2.0f * znear * zfar) / (zfar - znear);
+  out[14] = -1.0f;
+}
+
+extern "C" void lrt_look_at(const float eye[3], const float center[3], const float up[3], float out[16]) {
+  float z[3] = {eye[0] - center[0], eye[1] - center[1], eye[2] - center[2]};
+  const float lz = std::sqrt(z[0] * z[0] + z[1] * z[1] + z[2] * z[2]);
+  for (float &v : z) v /= lz;
+  float x[3] = {up[1] * z[2] - up[2] * z[1], up[2] * z[0] - up[0] * z[2], up[0] * z[1] - up[1] * z[0]};
+  const float lx = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+  for (float &v : x) v /= lx;
+  const float y[3] = {z[1] * x[2] - z[2] * x[1], z[2] * x[0] - z[0] * x[2], z[0] * x[1] - z[1] * x[0]};
+  std::memset(out, 0, 16 * sizeof(float));
+  for (int i = 0; i < 3; i++) {
+    out[i] = x[i];
+    out[4 + i] = y[i];
+    out[8 + i] = z[i];
+  }
+  out[3] = -(x[0] * eye[0] + x[1] * eye[1] + x[2] * eye[2]);
+  out[7] = -(y[0] * eye[0] + y[1] * eye[1] + y[2] * eye[2]);
+  out[11] = -(z[0] * eye[0] + z[1] * eye[1] + z[2] * eye[2]);
+  out[15] = 1.0f;
+}
+
+// ---------------------------------------------------------------- context
+extern "C" const char *lrt_status_string(lrt_status s) {
+  switch (s) {
+    case LRT_OK: return "ok";
+    case LRT_ERR_INVALID: return "invalid argument";
+    case LRT_ERR_OOM: return "out of memory";
+    case LRT_ERR_CUDA: return "CUDA error";
+    case LRT_ERR_UNSUPPORTED: return "unsupported";
+    case LRT_ERR_TIMEOUT: return "device wait timed out";
+    case LRT_ERR_BOUNDS: return "device bounds check failed";
+    case LRT_ERR_STATE: return "bad call order";
+  }
+  return "unknown";
+}
+
+extern "C" lrt_status lrt_create(lrt_ctx **out, int device) {
+  if (!out) return LRT_ERR_INVALID;
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) return LRT_ERR_CUDA;
+  if (device < 0 || device >= n) return LRT_ERR_INVALID;
+  if (cudaSetDevice(device) != cudaSuccess) return LRT_ERR_CUDA;
+  lrt_ctx *ctx = new (std::nothrow) lrt_ctx();
+  if (!ctx) return LRT_ERR_OOM;
+  ctx->device = device;
+  cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+  ctx->preset.render_mode = LRT_RENDER_MODE_LAMBERT_NO_TEX;   // getDefaultPreset, render_settings.h:97-108
+  ctx->preset.sdf_node_intersect = LRT_INTERSECT_ST;
+  ctx->preset.normal_mode = 0;
+  ctx->preset.ray_gen_mode = 0;
+  ctx->preset.interpolation_mode = 0;
+  ctx->preset.representation_mode = 1;
+  ctx->preset.spp = 1;
+  if (ctx->d_tile_counter.ensure(1) != cudaSuccess || ctx->d_counters.ensure(4) != cudaSuccess) {
+    delete ctx;
+    return LRT_ERR_OOM;
+  }
+  *out = ctx;
+  return LRT_OK;
+}
+
+static void release_scene(lrt_ctx *ctx) {
+  ctx->d_nodes.release();
+  ctx->d_bricks.release();
+  ctx->d_values.release();
+  ctx->d_values_f.release();
+  ctx->d_svs.release();
+  ctx->d_tri_verts.release();
+  ctx->d_prim_indices.release();
+  ctx->committed = false;
+}
+
+extern "C" void lrt_destroy(lrt_ctx *ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  release_scene(ctx);
+  ctx->d_tile_counter.release();
+  ctx->d_views.release();
+  ctx->d_counters.release();
+  ctx->d_out_hits.release();
+  ctx->d_out_rgba.release();
+  ctx->d_out_rgba8.release();
+  ctx->d_q_pos.release();
+  ctx->d_q_dir.release();
+  ctx->d_q_out.release();
+  if (ctx->h_views) cudaFreeHost(ctx->h_views);
+  delete ctx;
+}
+
+extern "C" const char *lrt_last_error(const lrt_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+extern "C" uint32_t lrt_last_launch_count(const lrt_ctx *ctx) { return ctx ? ctx->last_launches : 0; }
+
+// ---------------------------------------------------------------- geometry
+extern "C" lrt_status lrt_clear_geom(lrt_ctx *ctx) {
+  if (!ctx) return LRT_ERR_INVALID;
+  ctx->geoms.clear();
+  ctx->insts.clear();
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_add_sbs(lrt_ctx *ctx, const lrt_sbs_header *hdr, const lrt_sbs_node *nodes, uint32_t n_nodes,
+                                  const uint32_t *values, uint32_t n_values, const float *values_f, uint32_t n_values_f,
+                                  uint32_t *geom_id) {
+  if (!ctx) return LRT_ERR_INVALID;
+  if (!hdr || !nodes || !values || n_nodes == 0 || n_values == 0)
+    return fail(ctx, LRT_ERR_INVALID, "lrt_add_sbs: empty SBS");
+  // BVH/BVH2Common_host.cpp:569-570
+  if (n_nodes >= (1u << 28) || n_values >= (1u << 28)) return fail(ctx, LRT_ERR_INVALID, "lrt_add_sbs: SBS too large");
+  if (hdr->brick_size < 1 || hdr->brick_size > 16 || hdr->brick_pad > 1 ||
+      !(hdr->bytes_per_value == 1 || hdr->bytes_per_value == 2 || hdr->bytes_per_value == 4))
+    return fail(ctx, LRT_ERR_INVALID, "lrt_add_sbs: bad header");
+  const uint32_t layout = hdr->aux_data & 0xFF000000u;
+  uint32_t type;
+  const bool indexed = layout == LRT_SBS_LAYOUT_ID32F_IRGB32F || layout == LRT_SBS_LAYOUT_ID32F_IRGB32F_IN;
+  if (layout == LRT_SBS_LAYOUT_UNDEFINED || layout == LRT_SBS_LAYOUT_DX) type = LRT_TYPE_SDF_SBS;
+  else if (indexed) type = LRT_TYPE_SDF_SBS_COL;
+  else return fail(ctx, LRT_ERR_UNSUPPORTED, "lrt_add_sbs: only DX and ID32F_IRGB32F(_IN) layouts are supported");
+  if (indexed && (!values_f || n_values_f == 0))
+    return fail(ctx, LRT_ERR_INVALID, "lrt_add_sbs: indexed layout needs values_f");
+  // every brick's data must lie inside `values`
+  const uint32_t v_size = hdr->brick_size + 2 * hdr->brick_pad + 1, v3 = v_size * v_size * v_size;
+  const uint32_t words = indexed ? v3 + 8 + (layout == LRT_SBS_LAYOUT_ID32F_IRGB32F_IN ? 27 : 0)
+                                 : (v3 + 4 / hdr->bytes_per_value - 1) / (4 / hdr->bytes_per_value);
+  for (uint32_t i = 0; i < n_nodes; i++) {
+    if (uint64_t(nodes[i].data_offset) + words > n_values)
+      return fail(ctx, LRT_ERR_INVALID, "lrt_add_sbs: brick data_offset out of range");
+    if ((nodes[i].pos_z_lod_size & 0xFFFF) == 0) return fail(ctx, LRT_ERR_INVALID, "lrt_add_sbs: zero LOD size");
+  }
+  if (indexed) {   // distance indices, then 8 colour indices (3 floats each) per brick
+    for (uint32_t i = 0; i < n_nodes; i++) {
+      const uint32_t *w = values + nodes[i].data_offset;
+      for (uint32_t j = 0; j < v3; j++)
+        if (w[j] >= n_values_f) return fail(ctx, LRT_ERR_INVALID, "lrt_add_sbs: distance index out of range");
+      for (uint32_t j = v3; j < v3 + 8; j++)
+        if (uint64_t(w[j]) + 3 > n_values_f) return fail(ctx, LRT_ERR_INVALID, "lrt_add_sbs: colour index out of range");
+    }
+  }
+  Geom g;
+  g.type = type;
+  g.sbs.hdr = *hdr;
+  g.sbs.nodes.assign(nodes, nodes + n_nodes);
+  g.sbs.values.assign(values, values + n_values);
+  if (indexed) g.values_f.assign(values_f, values_f + n_values_f);
+  ctx->geoms.push_back(std::move(g));
+  if (geom_id) *geom_id = uint32_t(ctx->geoms.size() - 1);
+  ctx->committed = false;
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_add_svs(lrt_ctx *ctx, const lrt_svs_node *nodes, uint32_t n_nodes, uint32_t *geom_id) {
+  if (!ctx) return LRT_ERR_INVALID;
+  if (!nodes || n_nodes == 0) return fail(ctx, LRT_ERR_INVALID, "lrt_add_svs: empty SVS");
+  if (n_nodes >= (1u << 28)) return fail(ctx, LRT_ERR_INVALID, "lrt_add_svs: SVS too large");
+  for (uint32_t i = 0; i < n_nodes; i++)
+    if ((nodes[i].pos_z_lod_size & 0xFFFF) == 0) return fail(ctx, LRT_ERR_INVALID, "lrt_add_svs: zero LOD size");
+  Geom g;
+  g.type = LRT_TYPE_SDF_SVS;
+  g.svs.assign(nodes, nodes + n_nodes);
+  ctx->geoms.push_back(std::move(g));
+  if (geom_id) *geom_id = uint32_t(ctx->geoms.size() - 1);
+  ctx->committed = false;
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_add_triangles(lrt_ctx *ctx, const float *vpos, size_t n_vert, size_t v_byte_stride,
+                                        const uint32_t *indices, size_t n_indices, uint32_t *geom_id) {
+  if (!ctx) return LRT_ERR_INVALID;
+  if (!vpos || !indices || n_vert == 0 || n_indices < 3 || n_indices % 3 != 0 || v_byte_stride < 12 ||
+      v_byte_stride % 4 != 0)
+    return fail(ctx, LRT_ERR_INVALID, "lrt_add_triangles: bad mesh");
+  if (n_indices / 3 >= (1u << 24)) return fail(ctx, LRT_ERR_UNSUPPORTED, "lrt_add_triangles: too many triangles");
+  for (size_t i = 0; i < n_indices; i++)
+    if (indices[i] >= n_vert) return fail(ctx, LRT_ERR_INVALID, "lrt_add_triangles: index out of range");
+  Geom g;
+  g.type = LRT_TYPE_MESH_TRIANGLE;
+  const size_t st = v_byte_stride / 4;
+  g.vpos.resize(4 * n_vert);
+  for (int k = 0; k < 3; k++) { g.bmin[k] = 3.4e38f; g.bmax[k] = -3.4e38f; }
+  for (size_t i = 0; i < n_vert; i++) {
+    for (int k = 0; k < 3; k++) {
+      const float v = vpos[i * st + k];
+      g.vpos[4 * i + k] = v;
+      g.bmin[k] = std::min(g.bmin[k], v);
+      g.bmax[k] = std::max(g.bmax[k], v);
+    }
+    g.vpos[4 * i + 3] = 1.0f;
+  }
+  g.indices.assign(indices, indices + n_indices);
+  ctx->geoms.push_back(std::move(g));
+  if (geom_id) *geom_id = uint32_t(ctx->geoms.size() - 1);
+  ctx->committed = false;
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_clear_scene(lrt_ctx *ctx) {
+  if (!ctx) return LRT_ERR_INVALID;
+  ctx->insts.clear();
+  ctx->committed = false;
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_add_instance(lrt_ctx *ctx, uint32_t geom_id, const float matrix[16], uint32_t *inst_id) {
+  if (!ctx) return LRT_ERR_INVALID;
+  geom_id &= 0x7fffffffu;   // CRT_GEOM_MASK_AABB_BIT, BVH/BVH2Common_host.cpp:1452-1453
+  if (geom_id >= ctx->geoms.size() || !matrix) return fail(ctx, LRT_ERR_INVALID, "lrt_add_instance: bad geometry id");
+  const Geom &g = ctx->geoms[geom_id];
+  Inst in;
+  in.geom = geom_id;
+  std::memcpy(in.m, matrix, sizeof(in.m));
+  lrt_inverse4x4(matrix, in.inv);
+  for (int i = 0; i < 4; i++)
+    for (int j = 0; j < 4; j++) in.inv_t[i * 4 + j] = in.inv[j * 4 + i];
+  // transformed corners of the geometry box, BVH/BVH2Common_host.cpp:1460-1475
+  for (int k = 0; k < 3; k++) { in.bmin[k] = 3.4e38f; in.bmax[k] = -3.4e38f; }
+  for (int c = 0; c < 8; c++) {
+    const float v[4] = {(c & 1) ? g.bmax[0] : g.bmin[0], (c & 2) ? g.bmax[1] : g.bmin[1], (c & 4) ? g.bmax[2] : g.bmin[2], 1.0f};
+    float r[4];
+    mat_mul_vec4(matrix, v, r);
+    for (int k = 0; k < 3; k++) { in.bmin[k] = std::min(in.bmin[k], r[k]); in.bmax[k] = std::max(in.bmax[k], r[k]); }
+  }
+  ctx->insts.push_back(in);
+  if (inst_id) *inst_id = uint32_t(ctx->insts.size() - 1);
+  ctx->committed = false;
+  return LRT_OK;
+}
+
+template <typename T>
+static cudaError_t upload(DevBuf<T> &b, const T *src, size_t n) {
+  cudaError_t e = b.ensure(n);
+  if (e != cudaSuccess || n == 0) return e;
+  return cudaMemcpy(b.p, src, n * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+extern "C" lrt_status lrt_commit_scene(lrt_ctx *ctx) {
+  if (!ctx) return LRT_ERR_INVALID;
+  if (ctx->insts.size() != 1)
+    return fail(ctx, ctx->insts.empty() ? LRT_ERR_STATE : LRT_ERR_UNSUPPORTED,
+                "lrt_commit_scene: exactly one instance per scene is supported");
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  release_scene(ctx);
+  const Inst &in = ctx->insts[0];
+  const Geom &g = ctx->geoms[in.geom];
+  std::vector<float> boxes;
+  DevScene s{};
+  s.type = g.type;
+  s.geom_id = in.geom;
+  lrt_status st = LRT_OK;
+  if (g.type == LRT_TYPE_MESH_TRIANGLE) {
+    const size_t nt = g.indices.size() / 3;
+    boxes.resize(6 * nt);
+    for (size_t t = 0; t < nt; t++)
+      for (int k = 0; k < 3; k++) {
+        float lo = 3.4e38f, hi = -3.4e38f;
+        for (int v = 0; v < 3; v++) {
+          const float x = g.vpos[4 * size_t(g.indices[3 * t + v]) + k];
+          lo = std::min(lo, x);
+          hi = std::max(hi, x);
+        }
+        boxes[6 * t + k] = lo;
+        boxes[6 * t + 3 + k] = hi;
+      }
+    st = build_bvh(boxes.data(), uint32_t(nt), false, ctx->bvh);
+  } else {
+    // one AABB per brick / voxel, BVH/BVH2Common_host.cpp:546-555, 640-653
+    const bool sbs = g.type != LRT_TYPE_SDF_SVS;
+    const size_t n = sbs ? g.sbs.nodes.size() : g.svs.size();
+    boxes.resize(6 * n);
+    for (size_t i = 0; i < n; i++) {
+      const uint32_t pxy = sbs ? g.sbs.nodes[i].pos_xy : g.svs[i].pos_xy;
+      const uint32_t pzl = sbs ? g.sbs.nodes[i].pos_z_lod_size : g.svs[i].pos_z_lod_size;
+      const float px = float(pxy >> 16), py = float(pxy & 0x0000FFFF), pz = float(pzl >> 16), sz = float(pzl & 0x0000FFFF);
+      const float lo[3] = {-1 + 2.0f * px / sz, -1 + 2.0f * py / sz, -1 + 2.0f * pz / sz};
+      for (int k = 0; k < 3; k++) {
+        boxes[6 * i + k] = lo[k];
+        boxes[6 * i + 3 + k] = lo[k] + 2.0f * 1 / sz;
+      }
+    }
+    st = build_bvh(boxes.data(), uint32_t(n), true, ctx->bvh);
+  }
+  if (st != LRT_OK) return fail(ctx, st, "lrt_commit_scene: BVH build failed");
+  if (3 * int(ctx->bvh.max_depth) + 4 > kStackSize)
+    return fail(ctx, LRT_ERR_UNSUPPORTED, "lrt_commit_scene: BVH deeper than the traversal stack");
+
+  cudaError_t e;
+  if ((e = upload(ctx->d_nodes, ctx->bvh.wnodes.data(), ctx->bvh.wnodes.size())) != cudaSuccess)
+    return cuda_fail(ctx, e, "upload nodes");
+  s.nodes = ctx->d_nodes.p;
+  if (g.type == LRT_TYPE_MESH_TRIANGLE) {
+    const size_t nt = g.indices.size() / 3;
+    std::vector<float4> tv(3 * nt);
+    for (size_t r = 0; r < nt; r++) {
+      const uint32_t t = ctx->bvh.order[r];
+      for (int v = 0; v < 3; v++) {
+        const float *p = &g.vpos[4 * size_t(g.indices[3 * size_t(t) + v])];
+        tv[3 * r + v] = make_float4(p[0], p[1], p[2], p[3]);
+      }
+    }
+    if ((e = upload(ctx->d_tri_verts, tv.data(), tv.size())) != cudaSuccess) return cuda_fail(ctx, e, "upload tris");
+    if ((e = upload(ctx->d_prim_indices, ctx->bvh.order.data(), ctx->bvh.order.size())) != cudaSuccess)
+      return cuda_fail(ctx, e, "upload prim indices");
+    s.tri_verts = ctx->d_tri_verts.p;
+    s.prim_indices = ctx->d_prim_indices.p;
+  } else if (g.type == LRT_TYPE_SDF_SVS) {
+    if ((e = upload(ctx->d_svs, g.svs.data(), g.svs.size())) != cudaSuccess) return cuda_fail(ctx, e, "upload svs");
+    s.svs = ctx->d_svs.p;
+  } else {
+    if ((e = upload(ctx->d_bricks, g.sbs.nodes.data(), g.sbs.nodes.size())) != cudaSuccess)
+      return cuda_fail(ctx, e, "upload bricks");
+    if ((e = upload(ctx->d_values, g.sbs.values.data(), g.sbs.values.size())) != cudaSuccess)
+      return cuda_fail(ctx, e, "upload values");
+    if (!g.values_f.empty() && (e = upload(ctx->d_values_f, g.values_f.data(), g.values_f.size())) != cudaSuccess)
+      return cuda_fail(ctx, e, "upload values_f");
+    s.sbs_hdr = g.sbs.hdr;
+    s.bricks = ctx->d_bricks.p;
+    s.values = ctx->d_values.p;
+    s.values_f = ctx->d_values_f.p;
+  }
+  for (int k = 0; k < 3; k++) { s.inst_bmin[k] = in.bmin[k]; s.inst_bmax[k] = in.bmax[k]; }
+  std::memcpy(s.inst_inv, in.inv, sizeof(s.inst_inv));
+  std::memcpy(s.inst_inv_t, in.inv_t, sizeof(s.inst_inv_t));
+  s.preset = ctx->preset;
+  ctx->dev = s;
+  ctx->committed = true;
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_set_preset(lrt_ctx *ctx, const lrt_preset *preset) {
+  if (!ctx || !preset) return LRT_ERR_INVALID;
+  if (preset->sdf_node_intersect > LRT_INTERSECT_IT) return fail(ctx, LRT_ERR_INVALID, "lrt_set_preset: bad intersect mode");
+  if (preset->interpolation_mode != 0)
+    return fail(ctx, LRT_ERR_UNSUPPORTED, "lrt_set_preset: only trilinear interpolation is supported");
+  if (preset->ray_gen_mode != 0) return fail(ctx, LRT_ERR_UNSUPPORTED, "lrt_set_preset: only regular ray generation");
+  if (preset->spp == 0 || preset->spp > 1024) return fail(ctx, LRT_ERR_INVALID, "lrt_set_preset: bad spp");
+  ctx->preset = *preset;
+  ctx->dev.preset = *preset;
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_get_bvh2(lrt_ctx *ctx, const lrt_bvh_pair **pairs, uint32_t *n_pairs) {
+  if (!ctx || !pairs || !n_pairs) return LRT_ERR_INVALID;
+  if (!ctx->committed) return fail(ctx, LRT_ERR_STATE, "lrt_get_bvh2: no committed scene");
+  *pairs = ctx->bvh.pairs.data();
+  *n_pairs = uint32_t(ctx->bvh.pairs.size());
+  return LRT_OK;
+}
+
+// ---------------------------------------------------------------- rendering
+static lrt_status prepare_views(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, cudaStream_t st,
+                                uint32_t *total_tiles, uint64_t *total_pix) {
+  if (!views || n_views == 0) return fail(ctx, LRT_ERR_INVALID, "render: no views");
+  if (ctx->h_views_cap < n_views) {
+    if (ctx->h_views) cudaFreeHost(ctx->h_views);
+    ctx->h_views = nullptr;
+    ctx->h_views_cap = 0;
+    LRT_CUDA(ctx, cudaMallocHost(&ctx->h_views, n_views * sizeof(DevView)));
+    ctx->h_views_cap = n_views;
+  }
+  // The pinned staging buffer is reused; wait for the previous upload to finish.
+  LRT_CUDA(ctx, cudaStreamSynchronize(st));
+  uint64_t pix = 0, tiles = 0;
+  for (uint32_t v = 0; v < n_views; v++) {
+    const lrt_view &in = views[v];
+    if (in.width == 0 || in.height == 0 || in.width > 65535 || in.height > 65535)
+      return fail(ctx, LRT_ERR_INVALID, "render: bad view size");
+    DevView &o = ctx->h_views[v];
+    std::memset(&o, 0, sizeof(o));
+    o.width = in.width;
+    o.height = in.height;
+    o.pix_offset = uint32_t(pix);
+    o.tile_offset = uint32_t(tiles);
+    o.tiles_x = (in.width + 7) / 8;
+    lrt_inverse4x4(in.proj, o.proj_inv);       // UpdateCamera, Renderer/eye_ray_host.cpp:59-65
+    lrt_inverse4x4(in.world_view, o.wv_inv);
+    pix += uint64_t(in.width) * in.height;
+    tiles += uint64_t(o.tiles_x) * ((in.height + 3) / 4);
+  }
+  if (pix >= (1ull << 32) || tiles >= (1ull << 32)) return fail(ctx, LRT_ERR_INVALID, "render: batch too large");
+  LRT_CUDA(ctx, ctx->d_views.ensure(n_views));
+  LRT_CUDA(ctx, cudaMemcpyAsync(ctx->d_views.p, ctx->h_views, n_views * sizeof(DevView), cudaMemcpyHostToDevice, st));
+  *total_tiles = uint32_t(tiles);
+  *total_pix = pix;
+  return LRT_OK;
+}
+
+static lrt_status render_impl(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, lrt_hit16 *hits16, float *rgba,
+                              uint32_t *rgba8, cudaStream_t st, unsigned long long *counters) {
+  if (!ctx->committed) return fail(ctx, LRT_ERR_STATE, "render: commit the scene first");
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  uint32_t tiles = 0;
+  uint64_t pix = 0;
+  lrt_status s = prepare_views(ctx, views, n_views, st, &tiles, &pix);
+  if (s != LRT_OK) return s;
+  RenderLaunch L;
+  L.views = ctx->d_views.p;
+  L.n_views = n_views;
+  L.total_tiles = tiles;
+  L.hits16 = hits16;
+  L.rgba = reinterpret_cast<float4 *>(rgba);
+  L.rgba8 = rgba8;
+  L.tile_counter = ctx->d_tile_counter.p;
+  L.counters = counters;
+  LRT_CUDA(ctx, cudaMemsetAsync(ctx->d_tile_counter.p, 0, sizeof(uint32_t), st));
+  LRT_CUDA(ctx, launch_render(ctx->dev, L, ctx->num_sms, st, counters != nullptr));
+  ctx->last_launches = 1;
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_render(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, lrt_hit16 *hits16, float *rgba,
+                                 uint32_t *rgba8, void *stream) {
+  if (!ctx) return LRT_ERR_INVALID;
+  return render_impl(ctx, views, n_views, hits16, rgba, rgba8, static_cast<cudaStream_t>(stream), nullptr);
+}
+
+extern "C" lrt_status lrt_render_host(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, lrt_hit16 *hits16,
+                                      float *rgba, uint32_t *rgba8) {
+  if (!ctx) return LRT_ERR_INVALID;
+  if (!views || n_views == 0) return fail(ctx, LRT_ERR_INVALID, "render: no views");
+  uint64_t pix = 0;
+  for (uint32_t v = 0; v < n_views; v++) pix += uint64_t(views[v].width) * views[v].height;
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  if (hits16) LRT_CUDA(ctx, ctx->d_out_hits.ensure(pix));
+  if (rgba) LRT_CUDA(ctx, ctx->d_out_rgba.ensure(pix));
+  if (rgba8) LRT_CUDA(ctx, ctx->d_out_rgba8.ensure(pix));
+  const cudaStream_t st = nullptr;
+  lrt_status s = render_impl(ctx, views, n_views, hits16 ? ctx->d_out_hits.p : nullptr,
+                             rgba ? reinterpret_cast<float *>(ctx->d_out_rgba.p) : nullptr,
+                             rgba8 ? ctx->d_out_rgba8.p : nullptr, st, nullptr);
+  if (s != LRT_OK) return s;
+  if (hits16) LRT_CUDA(ctx, cudaMemcpyAsync(hits16, ctx->d_out_hits.p, pix * sizeof(lrt_hit16), cudaMemcpyDeviceToHost, st));
+  if (rgba) LRT_CUDA(ctx, cudaMemcpyAsync(rgba, ctx->d_out_rgba.p, pix * sizeof(float4), cudaMemcpyDeviceToHost, st));
+  if (rgba8) LRT_CUDA(ctx, cudaMemcpyAsync(rgba8, ctx->d_out_rgba8.p, pix * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  LRT_CUDA(ctx, cudaStreamSynchronize(st));
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_render_counters(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, uint64_t out[4]) {
+  if (!ctx || !out) return LRT_ERR_INVALID;
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  LRT_CUDA(ctx, cudaMemset(ctx->d_counters.p, 0, 4 * sizeof(unsigned long long)));
+  lrt_status s = render_impl(ctx, views, n_views, nullptr, nullptr, nullptr, nullptr, ctx->d_counters.p);
+  if (s != LRT_OK) return s;
+  unsigned long long h[4];
+  LRT_CUDA(ctx, cudaMemcpy(h, ctx->d_counters.p, sizeof(h), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < 4; i++) out[i] = h[i];
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_query_rays(lrt_ctx *ctx, const float *pos_near, const float *dir_far, uint32_t n,
+                                     lrt_hit *out, int device_ptrs, void *stream) {
+  if (!ctx) return LRT_ERR_INVALID;
+  if (!ctx->committed) return fail(ctx, LRT_ERR_STATE, "lrt_query_rays: commit the scene first");
+  if (n == 0) return LRT_OK;
+  if (!pos_near || !dir_far || !out) return fail(ctx, LRT_ERR_INVALID, "lrt_query_rays: null array");
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (device_ptrs) {
+    LRT_CUDA(ctx, launch_query(ctx->dev, reinterpret_cast<const float4 *>(pos_near),
+                               reinterpret_cast<const float4 *>(dir_far), n, out, st));
+    ctx->last_launches = 1;
+    return LRT_OK;
+  }
+  LRT_CUDA(ctx, ctx->d_q_pos.ensure(n));
+  LRT_CUDA(ctx, ctx->d_q_dir.ensure(n));
+  LRT_CUDA(ctx, ctx->d_q_out.ensure(n));
+  LRT_CUDA(ctx, cudaMemcpyAsync(ctx->d_q_pos.p, pos_near, size_t(n) * 16, cudaMemcpyHostToDevice, st));
+  LRT_CUDA(ctx, cudaMemcpyAsync(ctx->d_q_dir.p, dir_far, size_t(n) * 16, cudaMemcpyHostToDevice, st));
+  LRT_CUDA(ctx, launch_query(ctx->dev, ctx->d_q_pos.p, ctx->d_q_dir.p, n, ctx->d_q_out.p, st));
+  LRT_CUDA(ctx, cudaMemcpyAsync(out, ctx->d_q_out.p, size_t(n) * sizeof(lrt_hit), cudaMemcpyDeviceToHost, st));
+  LRT_CUDA(ctx, cudaStreamSynchronize(st));
+  ctx->last_launches = 1;
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_build_bvh2(const float *boxes6, uint32_t n, uint32_t prims_per_leaf, lrt_bvh_pair **pairs,
+                                     uint32_t *n_pairs, uint32_t **leaf_start_count, uint32_t *n_leaves,
+                                     uint32_t **order) {
+  if (!boxes6 || n == 0 || !pairs || !n_pairs || (prims_per_leaf != 1 && prims_per_leaf != 2)) return LRT_ERR_INVALID;
+  BvhData b;
+  const lrt_status s = build_bvh(boxes6, n, prims_per_leaf == 1, b);
+  if (s != LRT_OK) return s;
+  *pairs = static_cast<lrt_bvh_pair *>(std::malloc(b.pairs.size() * sizeof(lrt_bvh_pair)));
+  if (!*pairs) return LRT_ERR_OOM;
+  std::memcpy(*pairs, b.pairs.data(), b.pairs.size() * sizeof(lrt_bvh_pair));
+  *n_pairs = uint32_t(b.pairs.size());
+  if (leaf_start_count) {
+    *leaf_start_count = static_cast<uint32_t *>(std::malloc(std::max<size_t>(1, b.leaf_start_count.size()) * 4));
+    std::memcpy(*leaf_start_count, b.leaf_start_count.data(), b.leaf_start_count.size() * 4);
+  }
+  if (n_leaves) *n_leaves = uint32_t(b.leaf_start_count.size());
+  if (order) {
+    *order = static_cast<uint32_t *>(std::malloc(b.order.size() * 4));
+    std::memcpy(*order, b.order.data(), b.order.size() * 4);
+  }
+  return LRT_OK;
+}
+
+extern "C" void lrt_free(void *p) { std::free(p); }
+
+// ---------------------------------------------------------------- scene construction
+struct lrt_sbs { SbsData d; };
+struct lrt_svs { std::vector<lrt_svs_node> nodes; };
+
+extern "C" lrt_status lrt_sbs_build_from_sdf(const lrt_sdf_desc *sdf, uint32_t depth, const lrt_sbs_header *hdr,
+                                             int threads, lrt_sbs **out) {
+  if (!sdf || !hdr || !out || (sdf->n_spheres + sdf->n_boxes) == 0) return LRT_ERR_INVALID;
+  lrt_sbs *r = new (std::nothrow) lrt_sbs();
+  if (!r) return LRT_ERR_OOM;
+  lrt_status s = build_sbs(*sdf, depth, *hdr, threads, r->d);
+  if (s != LRT_OK) { delete r; return s; }
+  *out = r;
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_sbs_data(const lrt_sbs *sbs, lrt_sbs_header *hdr, const lrt_sbs_node **nodes, uint32_t *n_nodes,
+                                   const uint32_t **values, uint32_t *n_values) {
+  if (!sbs) return LRT_ERR_INVALID;
+  if (hdr) *hdr = sbs->d.hdr;
+  if (nodes) *nodes = sbs->d.nodes.data();
+  if (n_nodes) *n_nodes = uint32_t(sbs->d.nodes.size());
+  if (values) *values = sbs->d.values.data();
+  if (n_values) *n_values = uint32_t(sbs->d.values.size());
+  return LRT_OK;
+}
+
+extern "C" void lrt_sbs_free(lrt_sbs *sbs) { delete sbs; }
+
+extern "C" lrt_status lrt_svs_build_from_sdf(const lrt_sdf_desc *sdf, uint32_t depth, int threads, lrt_svs **out) {
+  if (!sdf || !out || (sdf->n_spheres + sdf->n_boxes) == 0) return LRT_ERR_INVALID;
+  lrt_svs *r = new (std::nothrow) lrt_svs();
+  if (!r) return LRT_ERR_OOM;
+  lrt_status s = build_svs(*sdf, depth, threads, r->nodes);
+  if (s != LRT_OK) { delete r; return s; }
+  *out = r;
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_svs_data(const lrt_svs *svs, const lrt_svs_node **nodes, uint32_t *n_nodes) {
+  if (!svs) return LRT_ERR_INVALID;
+  if (nodes) *nodes = svs->nodes.data();
+  if (n_nodes) *n_nodes = uint32_t(svs->nodes.size());
+  return LRT_OK;
+}
+
+extern "C" void lrt_svs_free(lrt_svs *svs) { delete svs; }

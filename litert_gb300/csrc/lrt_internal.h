@@ -1,0 +1,98 @@
+// Internal declarations shared by the host library (C++) and the CUDA kernels.
+#pragma once
+#include <cstdint>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/lrt_gpu.h"
+
+namespace lrt {
+
+constexpr uint32_t kLeafBit = 0x80000000u;     // LEAF_BIT, raytrace_common.h:43
+constexpr uint32_t kEmptyChild = 0xFFFFFFFFu;  // unused slot of a wide node
+constexpr uint32_t kMiss = 0xFFFFFFFFu;        // primId of a miss, Renderer/eye_ray.cpp:174
+constexpr int kStackSize = 64;                 // traversal stack entries per ray
+
+// 4-wide BVH node, one 128-byte line.  Child boxes are stored axis-major so a
+// lane reads each slab bound of all four children with one 16-byte load.
+// child[i]: internal -> wide node index; leaf -> kLeafBit | payload (box id for
+// SBS/SVS, (count << 24) | start for triangle ranges); empty -> kEmptyChild.
+struct alignas(128) WNode4 {
+  float lo_x[4], hi_x[4], lo_y[4], hi_y[4], lo_z[4], hi_z[4];
+  uint32_t child[4];
+  uint32_t pad[4];
+};
+static_assert(sizeof(WNode4) == 128, "WNode4 must be one 128-byte line");
+
+struct SbsData {
+  lrt_sbs_header hdr;
+  std::vector<lrt_sbs_node> nodes;
+  std::vector<uint32_t> values;
+};
+
+struct BvhData {
+  std::vector<WNode4> wnodes;            // root at 0
+  std::vector<uint32_t> order;           // primitive order of the leaves
+  std::vector<lrt_bvh_pair> pairs;       // reference fat-pair layout
+  std::vector<uint32_t> leaf_start_count;  // triangles: per fat-pair leaf
+  uint32_t max_depth = 0;                // wide-node depth
+};
+
+float sdf_eval(const lrt_sdf_desc &f, float x, float y, float z);
+lrt_status build_sbs(const lrt_sdf_desc &f, uint32_t depth, const lrt_sbs_header &hdr, int threads, SbsData &out);
+lrt_status build_svs(const lrt_sdf_desc &f, uint32_t depth, int threads, std::vector<lrt_svs_node> &out);
+// boxes6: n x (min xyz, max xyz).  boxes=true: one box per leaf, payload = box
+// id; boxes=false: triangles, up to two per leaf, payload = range in `order`.
+lrt_status build_bvh(const float *boxes6, uint32_t n, bool boxes, BvhData &out);
+
+// ------------------------------------------------------------------ device side
+// Scene as the kernels see it (all pointers device memory).
+struct DevScene {
+  uint32_t type;                 // LRT_TYPE_*
+  uint32_t geom_id;              // geometry id reported in hits
+  const WNode4 *nodes;
+  // SBS
+  lrt_sbs_header sbs_hdr;
+  const lrt_sbs_node *bricks;
+  const uint32_t *values;
+  const float *values_f;
+  // SVS
+  const lrt_svs_node *svs;
+  // triangles: vertex positions gathered per reordered triangle (A,B,C as float4)
+  const float4 *tri_verts;
+  const uint32_t *prim_indices;  // reordered -> original triangle id
+  // single instance
+  float inst_bmin[3], inst_bmax[3];
+  float inst_inv[16], inst_inv_t[16];
+  lrt_preset preset;
+};
+
+// A view prepared for the kernel: inverse matrices and its place in the
+// flattened pixel and tile spaces.
+struct DevView {
+  uint32_t width, height;
+  uint32_t pix_offset;   // first pixel in the batched outputs
+  uint32_t tile_offset;  // first 8x4 tile in the global tile space
+  uint32_t tiles_x;      // tiles per row
+  uint32_t _pad[3];
+  float proj_inv[16];
+  float wv_inv[16];
+};
+
+struct RenderLaunch {
+  const DevView *views;  // device
+  uint32_t n_views;
+  uint32_t total_tiles;
+  lrt_hit16 *hits16;
+  float4 *rgba;
+  uint32_t *rgba8;
+  uint32_t *tile_counter;       // scratch: persistent work queue head (zeroed before launch)
+  unsigned long long *counters; // optional traversal counters [4]
+};
+
+cudaError_t launch_render(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st, bool count);
+cudaError_t launch_query(const DevScene &s, const float4 *pos_near, const float4 *dir_far, uint32_t n,
+                         lrt_hit *out, cudaStream_t st);
+
+}  // namespace lrt

@@ -1,0 +1,107 @@
+// Device-side restatement of the reference's per-ray arithmetic.  Every
+// expression keeps the reference's operation order; this translation unit is
+// compiled with --fmad=false (no multiply-add contraction) and IEEE division and
+// square root, so results match the reference's x86-64 build bit for bit.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "lrt_internal.h"
+
+namespace lrt {
+namespace dev {
+
+__device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
+__device__ __forceinline__ float3 add(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 sub(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 mul(float3 a, float3 b) { return f3(a.x * b.x, a.y * b.y, a.z * b.z); }
+__device__ __forceinline__ float3 scl(float s, float3 a) { return f3(s * a.x, s * a.y, s * a.z); }
+__device__ __forceinline__ float3 scr(float3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float dot(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float3 cross(float3 a, float3 b) {
+  return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+// std::min / std::max semantics (NaN and signed-zero behaviour included)
+__device__ __forceinline__ float mn(float a, float b) { return (b < a) ? b : a; }
+__device__ __forceinline__ float mx(float a, float b) { return (a < b) ? b : a; }
+__device__ __forceinline__ float clampf(float x, float lo, float hi) { return mn(mx(x, lo), hi); }
+// LiteMath sign(): -1, 0, +1
+__device__ __forceinline__ float signf(float a) { return a > 0.0f ? 1.0f : (a < 0.0f ? -1.0f : 0.0f); }
+// normalize(u) = u / sqrt(dot(u,u))
+__device__ __forceinline__ float3 normalize(float3 a) {
+  const float l = sqrtf(dot(a, a));
+  return f3(a.x / l, a.y / l, a.z / l);
+}
+// float4x4 (row-major) times (v, 1) and (v, 0): raytrace_common.h:84-92
+__device__ __forceinline__ float3 matmul4x3(const float *m, float3 v) {
+  return f3(m[0] * v.x + m[1] * v.y + m[2] * v.z + m[3] * 1.0f, m[4] * v.x + m[5] * v.y + m[6] * v.z + m[7] * 1.0f,
+            m[8] * v.x + m[9] * v.y + m[10] * v.z + m[11] * 1.0f);
+}
+__device__ __forceinline__ float3 matmul3x3(const float *m, float3 v) {
+  return f3(m[0] * v.x + m[1] * v.y + m[2] * v.z + m[3] * 0.0f, m[4] * v.x + m[5] * v.y + m[6] * v.z + m[7] * 0.0f,
+            m[8] * v.x + m[9] * v.y + m[10] * v.z + m[11] * 0.0f);
+}
+
+// SafeInverse, raytrace_common.h:59-67
+__device__ __forceinline__ float3 safe_inverse(float3 d) {
+  const float ooeps = 1.0e-36f;
+  return f3(1.0f / (fabsf(d.x) > ooeps ? d.x : fabsf(ooeps) * signf(d.x)),
+            1.0f / (fabsf(d.y) > ooeps ? d.y : fabsf(ooeps) * signf(d.y)),
+            1.0f / (fabsf(d.z) > ooeps ? d.z : fabsf(ooeps) * signf(d.z)));
+}
+
+// RayBoxIntersection2, raytrace_common.h:69-82
+__device__ __forceinline__ float2 ray_box(float3 o, float3 inv, float lox, float loy, float loz, float hix,
+                                          float hiy, float hiz) {
+  const float lo = inv.x * (lox - o.x), hi = inv.x * (hix - o.x);
+  const float lo1 = inv.y * (loy - o.y), hi1 = inv.y * (hiy - o.y);
+  const float lo2 = inv.z * (loz - o.z), hi2 = inv.z * (hiz - o.z);
+  const float tmin = mx(mn(lo, hi), mn(lo1, hi1));
+  const float tmax = mn(mx(lo, hi), mx(lo1, hi1));
+  return make_float2(mx(tmin, mn(lo2, hi2)), mn(tmax, mx(lo2, hi2)));
+}
+
+// octahedral encode, BVH/BVH2Common.cpp:29-35
+__device__ __forceinline__ float2 encode_normal(float3 v) {
+  const float s = 1.0f / (fabsf(v.x) + fabsf(v.y) + fabsf(v.z));
+  const float px = v.x * s, py = v.y * s;
+  const float sx = (px >= 0.0f) ? 1.0f : -1.0f, sy = (py >= 0.0f) ? 1.0f : -1.0f;
+  if (v.z <= 0.0f) return make_float2((1.0f - fabsf(py)) * sx, (1.0f - fabsf(px)) * sy);
+  return make_float2(px, py);
+}
+
+// octahedral decode, Renderer/eye_ray.cpp:22-33
+__device__ __forceinline__ float3 decode_normal(float ex, float ey) {
+  float3 v = f3(ex, ey, 1.0f - fabsf(ex) - fabsf(ey));
+  if (v.z < 0) {
+    const float vx = v.x;
+    v.x = (1.0f - fabsf(v.y)) * ((v.x >= 0.0) ? +1.0f : -1.0f);
+    v.y = (1.0f - fabsf(vx)) * ((v.y >= 0.0) ? +1.0f : -1.0f);
+  }
+  return normalize(v);
+}
+
+// eval_dist_trilinear, BVH/BVH2Common.cpp:62-72
+__device__ __forceinline__ float trilinear(const float v[8], float3 dp) {
+  return (1 - dp.x) * (1 - dp.y) * (1 - dp.z) * v[0] + (1 - dp.x) * (1 - dp.y) * (dp.z) * v[1] +
+         (1 - dp.x) * (dp.y) * (1 - dp.z) * v[2] + (1 - dp.x) * (dp.y) * (dp.z) * v[3] +
+         (dp.x) * (1 - dp.y) * (1 - dp.z) * v[4] + (dp.x) * (1 - dp.y) * (dp.z) * v[5] +
+         (dp.x) * (dp.y) * (1 - dp.z) * v[6] + (dp.x) * (dp.y) * (dp.z) * v[7];
+}
+
+__device__ __forceinline__ bool need_normal(uint32_t render_mode) {   // BVH/BVH2Common.cpp:20-27
+  return render_mode == 1 || render_mode == 8 || render_mode == 12 || render_mode == 17 || render_mode == 18;
+}
+
+// A hit under construction (CRT_Hit plus the reordered triangle id for shading).
+struct Hit {
+  float t;
+  uint32_t prim;      // brick / voxel / reordered triangle id (remapped at the end)
+  uint32_t geom;      // geomId | type << 24
+  float c0, c1, c2, c3;
+};
+
+struct Counters { uint32_t nodes, leaves, voxels, finder; };
+
+}  // namespace dev
+}  // namespace lrt
