@@ -41,6 +41,9 @@ def parse():
     ap.add_argument("--brick", type=int, default=8)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--variant", type=int, default=0, help="render kernel: 0 per-lane rays, 1 warp packet")
+    ap.add_argument("--block-warps", type=int, default=4)
+    ap.add_argument("--stage", type=int, default=0, help="packet kernel: stage bricks in shared memory")
     return ap.parse_args()
 
 
@@ -135,7 +138,8 @@ def run_cpu_baseline(h, nodes, values, views, pairs, seconds):
         return rays, time.perf_counter() - t0, cnt_tot
 
     r0, t0, _ = run(20000)
-    n = int(min(4_000_000, max(20000, 20000 * seconds / max(t0, 1e-3))))
+    total = sum(w * hh for w, hh, _, _ in views)
+    n = int(min(total, max(20000, 20000 * seconds / max(t0, 1e-3))))
     rays, dt, cnt = run(n)
     return dict(value=rays / dt / 1e6, rays=rays, seconds=dt, cores=cores, counters=cnt)
 
@@ -188,6 +192,9 @@ def main():
     scene.add_instance(g)
     scene.commit_scene()
     scene.set_preset(render_mode=lrt.RENDER_MODE_NORMAL, sdf_node_intersect=lrt.INTERSECT_NEWTON)
+    scene.set_tuning("variant", args.variant)
+    scene.set_tuning("block_warps", args.block_warps)
+    scene.set_tuning("stage", args.stage)
     dev = torch.device("cuda", local if world > 1 else 0)
     n_rays = sum(w * hh for w, hh, _, _ in views)
     hits = torch.empty(n_rays * 4, dtype=torch.float32, device=dev)

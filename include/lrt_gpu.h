@@ -58,6 +58,13 @@ lrt_status lrt_commit_scene(lrt_ctx *ctx);
 /* BVHRT::SetPreset / MultiRenderer::SetPreset, Renderer/eye_ray_host.cpp:549-556 */
 lrt_status lrt_set_preset(lrt_ctx *ctx, const lrt_preset *preset);
 
+/* Launch-shape and kernel choices; no reference counterpart (the reference's
+ * device path is generated by kernel_slicer).  Keys: "variant" (0 = one ray per
+ * lane, 1 = warp packet traversal, default), "stage" (packet kernel: 1 = stage
+ * each brick in shared memory), "block_warps" (1..8).  Results do not depend on
+ * these. */
+lrt_status lrt_set_tuning(lrt_ctx *ctx, const char *key, int value);
+
 /* ---- queries ---- */
 /* BVHRT::RayQuery_NearestHit, BVH/BVH2Common.cpp:3490-3559, batched: n rays of
  * float4 (pos, tNear) and float4 (dir, tFar); tFar <= 0 requests any-hit

@@ -1,0 +1,469 @@
+// Leaf intersectors, eye rays and shading shared by the primary-ray kernels.
+// Each function restates a reference function in its FP32 operation order
+// (see trace_common.cuh); the citing comment names the reference lines.
+#pragma once
+#include "trace_common.cuh"
+
+namespace lrt {
+namespace dev {
+
+// LocalSurfaceIntersection, BVH/BVH2Common.cpp:274-631 (trilinear; ST, ANALYTIC,
+// NEWTON, BBOX, IT).  Updates `hit` when the crossing is closer.
+template <bool COUNT, int MODE = -1>
+__device__ __forceinline__ void local_surface(const lrt_preset &pr, const DevScene &s, uint32_t type, float3 ray_dir,
+                                              const float values[8], uint32_t prim_id, float d, float qNear,
+                                              float qFar, float2 fNearFar, float3 start_q, Hit &hit,
+                                              Counters &cnt) {
+  const uint32_t mode = MODE >= 0 ? uint32_t(MODE) : pr.sdf_node_intersect;
+  const float EPS = 1e-6f;
+  const float d_inv = 1.0f / d;
+  float t = qNear;
+  bool is_hit = false;
+  unsigned iter = 0;
+  float start_sign = 1;
+  float start_dist = trilinear(values, add(start_q, scl(t, ray_dir)));
+  if (COUNT) cnt.finder++;
+  if (pr.representation_mode == 0) start_sign = signf(start_dist);
+  start_dist *= start_sign;
+
+  if (start_dist <= EPS || mode == LRT_INTERSECT_BBOX) {
+    is_hit = true;
+  } else if (mode == LRT_INTERSECT_ST) {
+    float dist = start_dist;
+    while (t < qFar && dist > EPS && iter < 256u) {
+      t += dist * d_inv;
+      dist = start_sign * trilinear(values, add(start_q, scl(t, ray_dir)));
+      iter++;
+    }
+    is_hit = (dist <= EPS);
+  } else {
+    const float s000 = values[0] * d_inv, s001 = values[1] * d_inv, s010 = values[2] * d_inv,
+                s011 = values[3] * d_inv, s100 = values[4] * d_inv, s101 = values[5] * d_inv,
+                s110 = values[6] * d_inv, s111 = values[7] * d_inv;
+    const float a = s101 - s001;
+    const float k0 = s000, k1 = s100 - s000, k2 = s010 - s000, k3 = s110 - s010 - k1;
+    const float k4 = k0 - s001, k5 = k1 - a, k6 = k2 - (s011 - s001), k7 = k3 - (s111 - s011 - a);
+    const float3 o = start_q, d3 = ray_dir;
+    const float m0 = o.x * o.y, m1 = d3.x * d3.y, m2 = o.x * d3.y + o.y * d3.x;
+    const float m3 = k5 * o.z - k1, m4 = k6 * o.z - k2, m5 = k7 * o.z - k3;
+    const float c0 = (k4 * o.z - k0) + o.x * m3 + o.y * m4 + m0 * m5;
+    const float c1 = d3.x * m3 + d3.y * m4 + m2 * m5 + d3.z * (k4 + k5 * o.x + k6 * o.y + k7 * m0);
+    const float c2 = m1 * m5 + d3.z * (k5 * d3.x + k6 * d3.y + k7 * m2);
+    const float c3 = k7 * m1 * d3.z;
+
+    if (mode == LRT_INTERSECT_NEWTON) {                             // :437-522
+      const float aa = 3 * c3, b = 2 * c2, c = c1;
+      const float t0 = 0, t3 = qFar;
+      float t1 = qFar, t2 = qFar;
+      const float D = b * b - 4 * aa * c;
+      if (D >= 0) {
+        const float q = -0.5f * (b + signf(b) * sqrtf(D));
+        t1 = fabsf(aa) > EPS ? q / aa : t0;
+        t2 = fabsf(q) > EPS ? c / q : qFar;
+        const float tmp = mn(t1, t2);
+        t2 = mx(t1, t2);
+        t1 = tmp;
+        t1 = clampf(t1, t0, t3);
+        t2 = clampf(t2, t0, t3);
+      }
+      const bool s0 = c0 > 0;
+      const bool s1 = (c0 + t1 * (c1 + t1 * (c2 + t1 * c3))) > 0;
+      const bool s2 = (c0 + t2 * (c1 + t2 * (c2 + t2 * c3))) > 0;
+      const bool s3 = (c0 + t3 * (c1 + t3 * (c2 + t3 * c3))) > 0;
+      float nwt_min = t0, nwt_max = t0;
+      if (s0 != s1) { nwt_min = t0; nwt_max = t1; }
+      else if (s1 != s2) { nwt_min = t1; nwt_max = t2; }
+      else if (s2 != s3) { nwt_min = t2; nwt_max = t3; }
+      if (nwt_min < nwt_max) {
+        unsigned it = 0;
+        float rtn = 0.5f * (nwt_min + nwt_max);
+        float f = 1000;
+        while (it < 10u && fabsf(f) >= EPS) {
+          f = c0 + rtn * (c1 + rtn * (c2 + rtn * c3));
+          const float df = c1 + rtn * (2 * c2 + rtn * 3 * c3);
+          const float dx = f / (df + signf(df) * 1e-9f);
+          rtn -= dx;
+          it++;
+        }
+        t = rtn;
+        is_hit = (t >= 0 && t <= qFar && fabsf(f) < EPS);
+      } else {
+        is_hit = false;
+      }
+    } else if (mode == LRT_INTERSECT_ANALYTIC) {                     // :367-436
+      float x1 = 1000, x2 = 1000, x3 = 1000;
+      if (fabsf(c3) > 1e-2) {
+        const float aa = c2 / c3, b = c1 / c3, c = c0 / c3;
+        const float Q = (aa * aa - 3 * b) / 9;
+        const float R = (2 * aa * aa - 9 * aa * b + 27 * c) / 54;
+        const float Q3 = Q * Q * Q;
+        if (R * R < Q3) {
+          const float theta = acosf(R / sqrtf(Q3));
+          x1 = -2 * sqrtf(Q) * cosf(theta / 3) - aa / 3;
+          x2 = -2 * sqrtf(Q) * cosf((theta + 2 * 3.14159265358979323846f) / 3) - aa / 3;
+          x3 = -2 * sqrtf(Q) * cosf((theta - 2 * 3.14159265358979323846f) / 3) - aa / 3;
+        } else {
+          const float A = -signf(R) * powf(fabsf(R) + sqrtf(R * R - Q3), 1.0f / 3.0f);
+          const float B = fabsf(A) > EPS ? Q / A : 0;
+          x1 = A + B - aa / 3;
+        }
+      } else if (fabsf(c2) > 1e-4) {
+        const float D = c1 * c1 - 4 * c2 * c0;
+        if (D > 0) {
+          const float q = -0.5f * (c1 + signf(c1) * sqrtf(D));
+          x1 = q / c2;
+          if (fabsf(q) > EPS) x2 = c0 / q;
+        }
+      } else if (fabsf(c1) > EPS) {
+        x1 = -c0 / c1;
+      }
+      x1 = x1 < 0 ? 1000 : x1;
+      x2 = x2 < 0 ? 1000 : x2;
+      x3 = x3 < 0 ? 1000 : x3;
+      t = mn(x1, mn(x2, x3));
+      is_hit = (t >= 0 && t <= qFar);
+    } else {                                                        // IT, :523-550
+      float e = 0.1f * qFar;
+      const float t_max = fabsf(c3) < EPS ? 1e6f : -c2 / (3 * c3);
+      const float df_max = 3 * c3 * t_max * t_max + 2 * c2 * t_max + c1;
+      float dist = start_dist;
+      while (t < qFar && dist > EPS && iter < 256u) {
+        const float df_1 = 3 * c3 * t * t + 2 * c2 * t + c1;
+        const float df_2 = 3 * c3 * (t + e) * (t + e) + 2 * c2 * (t + e) + c1;
+        float L = (t_max > t && t_max < t + e) ? mx(df_max, mx(df_1, df_2)) : mx(df_1, df_2);
+        L = mx(L, EPS);
+        const float st = mn((dist * d_inv) / L, e);
+        t += st;
+        e = 2 * st;
+        dist = start_sign * trilinear(values, add(start_q, scl(t, ray_dir)));
+        iter++;
+      }
+      is_hit = (dist <= EPS);
+    }
+  }
+
+  const float tReal = fNearFar.x + d * t;
+  if (t <= qFar && is_hit && tReal < hit.t) {                      // :569-601
+    float3 norm = f3(0, 0, 1);
+    if (need_normal(pr.render_mode)) {
+      const float3 p0 = add(start_q, scl(t, ray_dir));
+      const float h = 0.001f;
+      const float ddx = (trilinear(values, add(p0, f3(h, 0, 0))) - trilinear(values, add(p0, f3(-h, 0, 0)))) / (2 * h);
+      const float ddy = (trilinear(values, add(p0, f3(0, h, 0))) - trilinear(values, add(p0, f3(0, -h, 0)))) / (2 * h);
+      const float ddz = (trilinear(values, add(p0, f3(0, 0, h))) - trilinear(values, add(p0, f3(0, 0, -h)))) / (2 * h);
+      norm = scl(start_sign, normalize(matmul4x3(s.inst_inv_t, f3(ddx, ddy, ddz))));
+    }
+    const float2 en = encode_normal(norm);
+    hit.t = tReal;
+    hit.prim = (pr.render_mode == 10) ? iter : prim_id;
+    hit.geom = s.geom_id | (type << 24);
+    hit.c0 = 0;
+    hit.c1 = 0;
+    hit.c2 = en.x;
+    hit.c3 = en.y;
+  }
+}
+
+// Decode of one stored distance value, BVH/BVH2Common.cpp:749-759: DX layout
+// fixed point -d_max + mult*q; `lg` = log2(values per 32-bit word).
+__device__ __forceinline__ float decode_dx(const uint32_t *data, uint32_t vId, uint32_t lg, uint32_t bits,
+                                           uint32_t max_val, float d_max, float mult) {
+  const uint32_t q = (__ldg(&data[vId >> lg]) >> (bits * (vId & ((1u << lg) - 1u)))) & max_val;
+  return -d_max + mult * float(q);
+}
+
+// load_distance_values, BVH/BVH2Common.cpp:725-762 (SBS_v_to_i, sdfScene/sdf_scene.h:201-204),
+// reading the brick from global memory.
+struct GlobalLoader {
+  const DevScene *s;
+  const uint32_t *data;   // brick's first word
+  uint32_t v_size, pad, lg, bits, max_val;
+  float d_max, mult;
+  bool indexed;
+  __device__ __forceinline__ GlobalLoader(const DevScene &sc, uint32_t data_offset, float sz_inv) {
+    const lrt_sbs_header &h = sc.sbs_hdr;
+    s = &sc;
+    data = sc.values + data_offset;
+    v_size = h.brick_size + 2 * h.brick_pad + 1;
+    pad = h.brick_pad;
+    const uint32_t layout = h.aux_data & 0xFF000000u;
+    indexed = layout == LRT_SBS_LAYOUT_ID32F_IRGB32F || layout == LRT_SBS_LAYOUT_ID32F_IRGB32F_IN;
+    lg = h.bytes_per_value == 4 ? 0u : (h.bytes_per_value == 2 ? 1u : 2u);
+    bits = 8 * h.bytes_per_value;
+    max_val = h.bytes_per_value == 4 ? 0xFFFFFFFFu : ((1u << bits) - 1);
+    d_max = 1.73205081f * sz_inv;
+    mult = 2 * d_max / float(max_val);
+  }
+  __device__ __forceinline__ float load(float3 vp, float values[8]) const {
+    float vmin = 1e6f;
+    const uint32_t ix = uint32_t(vp.x), iy = uint32_t(vp.y), iz = uint32_t(vp.z);
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      const uint32_t vId = (ix + ((i & 4) >> 2) + pad) * v_size * v_size + (iy + ((i & 2) >> 1) + pad) * v_size +
+                           (iz + (i & 1) + pad);
+      values[i] = indexed ? __ldg(&s->values_f[__ldg(&data[vId])]) : decode_dx(data, vId, lg, bits, max_val, d_max, mult);
+      vmin = mn(vmin, values[i]);
+    }
+    return vmin;
+  }
+};
+
+// The same corner fetch from a brick already decoded into shared memory
+// (v_size^3 floats in SBS_v_to_i order).
+struct SharedLoader {
+  const float *vals;
+  uint32_t v_size, pad;
+  __device__ __forceinline__ float load(float3 vp, float values[8]) const {
+    float vmin = 1e6f;
+    const uint32_t base = (uint32_t(vp.x) + pad) * v_size * v_size + (uint32_t(vp.y) + pad) * v_size + uint32_t(vp.z) + pad;
+    const uint32_t vv = v_size * v_size;
+    const uint32_t off[8] = {0u, 1u, v_size, v_size + 1u, vv, vv + 1u, vv + v_size, vv + v_size + 1u};
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      values[i] = vals[base + off[i]];
+      vmin = mn(vmin, values[i]);
+    }
+    return vmin;
+  }
+};
+
+// OctreeBrickIntersect, BVH/BVH2Common.cpp:764-984 (trilinear, colour for indexed
+// layouts).  The voxel walk is the reference's: the voxel is recomputed from the
+// current entry distance, the distance advances past the voxel's exit plane by
+// 1e-6, and a voxel is intersected when its entry lies beyond tNear and a corner
+// value is <= 0.  Two exact shortcuts: the "a corner is <= 0" test reads the
+// brick's occupancy bit (built from the same decoded values) so empty voxels
+// load no corners, and the exit distance is taken from the far planes alone --
+// for each axis max(lo, hi) is the plane the ray direction points to, so the
+// value equals RayBoxIntersection2's.  The near planes are evaluated only in
+// occupied voxels.
+template <bool COUNT, bool STAGED, int MODE = -1>
+__device__ void brick_intersect(const DevScene &s, float3 ray_pos, float3 ray_dir, float3 inv, float tNear,
+                                uint32_t brick, Hit &hit, Counters &cnt, const float *staged = nullptr) {
+  const lrt_sbs_header &h = s.sbs_hdr;
+  const lrt_preset &pr = s.preset;
+  const uint32_t type = s.type;
+  const uint32_t v_size = h.brick_size + 2 * h.brick_pad + 1;
+  const uint32_t bsz = h.brick_size;
+  const uint4 nd = __ldg(reinterpret_cast<const uint4 *>(s.bricks) + brick);
+  const float px = float(nd.x >> 16), py = float(nd.x & 0x0000FFFF);
+  const float pz = float(nd.y >> 16), sz = float(nd.y & 0x0000FFFF);
+  const float sz_inv = 2.0f / sz;
+  const float bs = float(bsz);
+  const float d = 2.0f / (sz * bs);
+  const float3 bmin = add(f3(-1, -1, -1), scl(sz_inv, f3(px, py, pz)));
+  const float3 bmax = add(bmin, scl(sz_inv, f3(1, 1, 1)));
+  float2 bnf = ray_box(ray_pos, inv, bmin.x, bmin.y, bmin.z, bmax.x, bmax.y, bmax.z);
+  const float old_t = hit.t;
+  const float scale = 0.5f * sz * bs;
+  const uint32_t *occ = s.occ + size_t(brick) * s.occ_words;
+  const bool posx = inv.x > 0.0f, posy = inv.y > 0.0f, posz = inv.z > 0.0f;
+  float values[8];
+  if (COUNT) cnt.leaves++;
+  // A ray crosses at most 3*brick_size voxels.  The reference's loop has no
+  // bound; its +1e-6 step stops advancing beyond t ~ 32, where a degenerate
+  // voxel would loop forever.  The bound below never binds otherwise.
+  const uint32_t max_steps = 8u * bsz + 16u;
+  const GlobalLoader gl(s, nd.z, sz_inv);
+  const SharedLoader sl{staged, v_size, h.brick_pad};
+  for (uint32_t step = 0; bnf.x < bnf.y && hit.t == old_t && step < max_steps; step++) {
+    const float3 hit_pos = add(ray_pos, scl(bnf.x, ray_dir));
+    const float3 local_pos = scr(sub(hit_pos, bmin), scale);
+    const float3 vp = f3(floorf(fmn(fmx(local_pos.x, 1e-6f), bs - 1e-6f)), floorf(fmn(fmx(local_pos.y, 1e-6f), bs - 1e-6f)),
+                         floorf(fmn(fmx(local_pos.z, 1e-6f), bs - 1e-6f)));
+    const float3 min_pos = add(bmin, scl(d, vp));
+    // exit distance: far plane per axis (max_pos = min_pos + d*1)
+    const float fx = inv.x * ((posx ? min_pos.x + d : min_pos.x) - ray_pos.x);
+    const float fy = inv.y * ((posy ? min_pos.y + d : min_pos.y) - ray_pos.y);
+    const float fz = inv.z * ((posz ? min_pos.z + d : min_pos.z) - ray_pos.z);
+    const float exit_t = fmn(fmn(fx, fy), fz);
+    const uint32_t vid = (uint32_t(vp.x) * bsz + uint32_t(vp.y)) * bsz + uint32_t(vp.z);
+    if (COUNT) cnt.voxels++;
+    if ((__ldg(&occ[vid >> 5]) >> (vid & 31u)) & 1u) {
+      const float nx = inv.x * ((posx ? min_pos.x : min_pos.x + d) - ray_pos.x);
+      const float ny = inv.y * ((posy ? min_pos.y : min_pos.y + d) - ray_pos.y);
+      const float nz = inv.z * ((posz ? min_pos.z : min_pos.z + d) - ray_pos.z);
+      const float2 fnf = make_float2(fmx(fmx(nx, ny), nz), exit_t);
+      if (tNear < fnf.x) {
+        float vmin;
+        if (STAGED) vmin = sl.load(vp, values);
+        else vmin = gl.load(vp, values);
+        if (vmin <= 0.0f) {
+          const float3 start_pos = add(ray_pos, scl(fnf.x, ray_dir));
+          const float3 start_q = scr(sub(start_pos, min_pos), scale);
+          const float qFar = (fnf.y - fnf.x) * scale;
+          local_surface<COUNT, MODE>(pr, s, type, ray_dir, values, brick, d, 0.0f, qFar, fnf, start_q, hit, cnt);
+        }
+      }
+    }
+    bnf.x += fmx(0.0f, exit_t - bnf.x) + 1e-6f;
+  }
+  if (hit.t < old_t) {
+    const uint32_t layout = h.aux_data & 0xFF000000u;
+    if (layout == LRT_SBS_LAYOUT_ID32F_IRGB32F || layout == LRT_SBS_LAYOUT_ID32F_IRGB32F_IN) {
+      const float3 pos = add(ray_pos, scl(hit.t, ray_dir));
+      const float3 dp = scr(sub(pos, bmin), 0.5f * sz);
+      const uint32_t t_off = nd.z + v_size * v_size * v_size;
+      const float w[8] = {(1 - dp.x) * (1 - dp.y) * (1 - dp.z), (1 - dp.x) * (1 - dp.y) * (dp.z),
+                          (1 - dp.x) * (dp.y) * (1 - dp.z),     (1 - dp.x) * (dp.y) * (dp.z),
+                          (dp.x) * (1 - dp.y) * (1 - dp.z),     (dp.x) * (1 - dp.y) * (dp.z),
+                          (dp.x) * (dp.y) * (1 - dp.z),         (dp.x) * (dp.y) * (dp.z)};
+      float3 col = f3(0, 0, 0);
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        const float *c = &s.values_f[__ldg(&s.values[t_off + i])];
+        const float3 ci = f3(w[i] * c[0], w[i] * c[1], w[i] * c[2]);
+        col = i == 0 ? ci : add(col, ci);
+      }
+      col = f3(clampf(floorf(255.0f * col.x + 0.5f), 0.0f, 255.0f), clampf(floorf(255.0f * col.y + 0.5f), 0.0f, 255.0f),
+               clampf(floorf(255.0f * col.z + 0.5f), 0.0f, 255.0f));
+      hit.c0 = col.x + col.y / 256.0f;
+      hit.c1 = col.z;
+    }
+  }
+}
+
+// SVS voxel: OctreeNodeIntersect + RayNodeIntersection, BVH/BVH2Common.cpp:126-153, 633-655
+template <bool COUNT, int MODE = -1>
+__device__ void svs_intersect(const DevScene &s, float3 ray_pos, float3 ray_dir, float tNear, uint32_t node_id,
+                              Hit &hit, Counters &cnt) {
+  const uint4 nd = __ldg(reinterpret_cast<const uint4 *>(s.svs) + node_id);
+  const float px = float(nd.x >> 16), py = float(nd.x & 0x0000FFFF);
+  const float pz = float(nd.y >> 16), sz = float(nd.y & 0x0000FFFF);
+  const float d_max = 2 * 1.73205081f / sz;
+  const float3 min_pos = add(f3(-1, -1, -1), f3(2.0f * px / sz, 2.0f * py / sz, 2.0f * pz / sz));
+  const float3 max_pos = add(min_pos, f3(2.0f * 1 / sz, 2.0f * 1 / sz, 2.0f * 1 / sz));
+  const float3 size = sub(max_pos, min_pos);
+  float values[8];
+  // -d_max + 2*d_max*(1.0/255.0f)*q: the double literal promotes the sum to double
+  const double c = double(2 * d_max) * (1.0 / 255.0);
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    const uint32_t word = (i < 4) ? nd.z : nd.w;
+    const double q = double((word >> (8 * (i % 4))) & 0xFF);
+    values[i] = float(double(-d_max) + c * q);
+  }
+  const float2 fnf = ray_box(ray_pos, safe_inverse(ray_dir), min_pos.x, min_pos.y, min_pos.z, max_pos.x, max_pos.y,
+                             max_pos.z);
+  const float3 start_pos = add(ray_pos, scl(fnf.x, ray_dir));
+  const float d = mx(size.x, mx(size.y, size.z));
+  const float3 start_q = f3((start_pos.x - min_pos.x) / d, (start_pos.y - min_pos.y) / d, (start_pos.z - min_pos.z) / d);
+  const float qFar = (fnf.y - fnf.x) / d;
+  const float qNear = tNear > fnf.x ? (tNear - fnf.x) / d : 0.0f;
+  if (COUNT) { cnt.leaves++; cnt.voxels++; }
+  if (qNear > 0.0f) return;
+  local_surface<COUNT, MODE>(s.preset, s, LRT_TYPE_SDF_SVS, ray_dir, values, node_id, d, qNear, qFar, fnf, start_q, hit, cnt);
+}
+
+// IntersectAllTrianglesInLeaf, BVH/BVH2Common.cpp:2776-2840 (geometry normal)
+template <bool COUNT>
+__device__ void tri_intersect(const DevScene &s, float3 ray_pos, float3 ray_dir, float tNear, uint32_t start,
+                              uint32_t count, Hit &hit, Counters &cnt) {
+  for (uint32_t tri = start; tri < start + count; tri++) {
+    const float4 a = __ldg(&s.tri_verts[3 * tri + 0]);
+    const float4 b = __ldg(&s.tri_verts[3 * tri + 1]);
+    const float4 c = __ldg(&s.tri_verts[3 * tri + 2]);
+    const float3 A = f3(a.x, a.y, a.z), B = f3(b.x, b.y, b.z), C = f3(c.x, c.y, c.z);
+    const float3 edge1 = sub(B, A), edge2 = sub(C, A);
+    const float3 pvec = cross(ray_dir, edge2);
+    const float3 tvec = sub(ray_pos, A);
+    const float3 qvec = cross(tvec, edge1);
+    const float invDet = 1.0f / dot(edge1, pvec);
+    const float v = dot(tvec, pvec) * invDet;
+    const float u = dot(qvec, ray_dir) * invDet;
+    const float t = dot(edge2, qvec) * invDet;
+    if (COUNT) cnt.voxels++;
+    if (v >= -1e-6f && u >= -1e-6f && (u + v <= 1.0f + 1e-6f) && t > tNear && t < hit.t) {
+      hit.t = t;
+      hit.prim = tri;
+      hit.geom = s.geom_id | (LRT_TYPE_MESH_TRIANGLE << 24);
+      hit.c0 = u;
+      hit.c1 = v;
+      if (need_normal(s.preset.render_mode)) {
+        const float3 n = normalize(matmul4x3(s.inst_inv_t, cross(edge1, edge2)));
+        const float2 en = encode_normal(n);
+        hit.c2 = en.x;
+        hit.c3 = en.y;
+      } else {
+        hit.c2 = 0;
+        hit.c3 = 0;
+      }
+    }
+  }
+}
+
+
+__device__ __forceinline__ void mat_vec4(const float *m, const float v[4], float r[4]) {
+#pragma unroll
+  for (int i = 0; i < 4; i++) r[i] = m[i * 4 + 0] * v[0] + m[i * 4 + 1] * v[1] + m[i * 4 + 2] * v[2] + m[i * 4 + 3] * v[3];
+}
+
+// kernel_InitEyeRay, Renderer/eye_ray.cpp:146-160 with EyeRayDirNormalized and
+// transform_ray3f, render_common.h:25-55
+__device__ __forceinline__ void eye_ray(uint32_t x, uint32_t y, uint32_t w, uint32_t h, float dx, float dy,
+                                        const float *proj_inv, const float *wv_inv, float3 &pos, float3 &dir) {
+  const float fx = (float(x) + dx) / float(w), fy = (float(y) + dy) / float(h);
+  const float v[4] = {2.0f * fx - 1.0f, -2.0f * fy + 1.0f, 1.0f, 1.0f};
+  float r[4];
+  mat_vec4(proj_inv, v, r);
+  const float ww = r[3];
+  float3 d0 = normalize(f3(r[0] / ww, r[1] / ww, r[2] / ww));
+  const float3 p00 = f3(0, 0, 0);
+  const float3 p0 = matmul4x3(wv_inv, p00);
+  const float3 p2 = matmul4x3(wv_inv, add(p00, scl(100.0f, d0)));
+  pos = p0;
+  dir = normalize(sub(p2, p0));
+}
+
+// kernel_RayTrace shading, Renderer/eye_ray.cpp:162-489 (MASK, LAMBERT_NO_TEX,
+// LAMBERT for coloured bricks, DEPTH, LINEAR_DEPTH, INVERSE_LINEAR_DEPTH, NORMAL)
+__device__ inline float4 shade(const DevScene &s, const Hit &hit, float3 dir) {
+  if (hit.prim == kMiss) return make_float4(0, 0, 0, 1);
+  const float z = hit.t, z_near = 0.1f, z_far = 10;
+  const uint32_t type = hit.geom >> 24;
+  float3 norm;
+  if (type == LRT_TYPE_MESH_TRIANGLE) {
+    const float4 a = s.tri_verts[3 * hit.prim + 0], b = s.tri_verts[3 * hit.prim + 1], c = s.tri_verts[3 * hit.prim + 2];
+    const float3 e1 = f3(b.x - a.x, b.y - a.y, b.z - a.z), e2 = f3(c.x - a.x, c.y - a.y, c.z - a.z);
+    norm = normalize(matmul4x3(s.inst_inv_t, cross(e1, e2)));
+  } else {
+    norm = decode_normal(hit.c2, hit.c3);
+  }
+  const float ns = signf(dot(scl(-1.0f, dir), norm));
+  norm = scl(ns, norm);
+  switch (s.preset.render_mode) {
+    case LRT_RENDER_MODE_MASK: return make_float4(1, 1, 1, 1);
+    case LRT_RENDER_MODE_DEPTH: { const float d = (1 / z - 1 / z_near) / (1 / z_far - 1 / z_near); return make_float4(d, d, d, 1); }
+    case LRT_RENDER_MODE_LINEAR_DEPTH: { const float d = ((z - z_near) / (z_far - z_near)); return make_float4(d, d, d, 1); }
+    case LRT_RENDER_MODE_INVERSE_LINEAR_DEPTH: { const float d = 1 - ((z - z_near) / (z_far - z_near)); return make_float4(d, d, d, 1); }
+    case LRT_RENDER_MODE_NORMAL: return make_float4(fabsf(norm.x), fabsf(norm.y), fabsf(norm.z), 1);
+    case LRT_RENDER_MODE_LAMBERT_NO_TEX:
+    case LRT_RENDER_MODE_LAMBERT: {
+      float3 color = f3(1, 1, 1);
+      if (s.preset.render_mode == LRT_RENDER_MODE_LAMBERT && type == LRT_TYPE_SDF_SBS_COL) {
+        color.x = roundf(hit.c0) / 255.0f;
+        color.y = hit.c0 - floorf(hit.c0);
+        color.z = roundf(hit.c1) / 255.0f;
+      }
+      // default lights, Renderer/eye_ray_host.cpp:40
+      const float3 ldir = normalize(f3(1, 1, 1));
+      const float lc = 2.0f / 3.0f;
+      float3 fc = f3(0, 0, 0);
+      const float q = mx(0.0f, dot(norm, ldir));
+      fc = add(fc, scl(q, mul(f3(lc, lc, lc), color)));
+      fc = add(fc, mul(f3(0.25f, 0.25f, 0.25f), color));
+      return make_float4(fc.x, fc.y, fc.z, 1);
+    }
+    default: return make_float4(1, 0, 1, 1);
+  }
+}
+
+__device__ __forceinline__ uint32_t encode_rgba8(float4 c) {   // Renderer/eye_ray.cpp:111-115
+  const uint32_t r = uint32_t(255 * clampf(c.x, 0.0f, 1.0f)), g = uint32_t(255 * clampf(c.y, 0.0f, 1.0f));
+  const uint32_t b = uint32_t(255 * clampf(c.z, 0.0f, 1.0f)), a = uint32_t(255 * clampf(c.w, 0.0f, 1.0f));
+  return (a << 24) | (b << 16) | (g << 8) | r;
+}
+
+
+}  // namespace dev
+}  // namespace lrt

@@ -67,6 +67,8 @@ struct lrt_ctx {
   // committed scene buffers
   DevBuf<WNode4> d_nodes;
   DevBuf<lrt_sbs_node> d_bricks;
+  DevBuf<float4> d_leaf_boxes;
+  DevBuf<uint32_t> d_occ;
   DevBuf<uint32_t> d_values;
   DevBuf<float> d_values_f;
   DevBuf<lrt_svs_node> d_svs;
@@ -85,6 +87,8 @@ struct lrt_ctx {
   DevBuf<float4> d_q_pos, d_q_dir;
   DevBuf<lrt_hit> d_q_out;
   uint32_t last_launches = 0;
+  uint32_t brick_stride = 0;   // device words per brick (16-byte multiple)
+  Tuning tuning;
 };
 
 static lrt_status fail(lrt_ctx *ctx, lrt_status s, const std::string &msg) {
@@ -209,6 +213,8 @@ extern "C" lrt_status lrt_create(lrt_ctx **out, int device) {
 static void release_scene(lrt_ctx *ctx) {
   ctx->d_nodes.release();
   ctx->d_bricks.release();
+  ctx->d_leaf_boxes.release();
+  ctx->d_occ.release();
   ctx->d_values.release();
   ctx->d_values_f.release();
   ctx->d_svs.release();
@@ -451,10 +457,40 @@ extern "C" lrt_status lrt_commit_scene(lrt_ctx *ctx) {
     if ((e = upload(ctx->d_svs, g.svs.data(), g.svs.size())) != cudaSuccess) return cuda_fail(ctx, e, "upload svs");
     s.svs = ctx->d_svs.p;
   } else {
-    if ((e = upload(ctx->d_bricks, g.sbs.nodes.data(), g.sbs.nodes.size())) != cudaSuccess)
-      return cuda_fail(ctx, e, "upload bricks");
-    if ((e = upload(ctx->d_values, g.sbs.values.data(), g.sbs.values.size())) != cudaSuccess)
-      return cuda_fail(ctx, e, "upload values");
+    // Device layout: every brick's words start on a 16-byte boundary (stride
+    // rounded up to 4 words) so a warp can stage a brick with 16-byte loads.
+    const lrt_sbs_header &hd = g.sbs.hdr;
+    const uint32_t layout = hd.aux_data & 0xFF000000u;
+    const uint32_t v_size = hd.brick_size + 2 * hd.brick_pad + 1, v3 = v_size * v_size * v_size;
+    const bool indexed = layout == LRT_SBS_LAYOUT_ID32F_IRGB32F || layout == LRT_SBS_LAYOUT_ID32F_IRGB32F_IN;
+    const uint32_t vpi = 4 / hd.bytes_per_value;
+    const uint32_t words = indexed ? v3 + 8 + (layout == LRT_SBS_LAYOUT_ID32F_IRGB32F_IN ? 27 : 0) : (v3 + vpi - 1) / vpi;
+    const uint32_t stride = (words + 3u) & ~3u;
+    const size_t nb = g.sbs.nodes.size();
+    if (uint64_t(nb) * stride >= (1ull << 32))
+      return fail(ctx, LRT_ERR_UNSUPPORTED, "lrt_commit_scene: brick data exceeds 2^32 words");
+    std::vector<uint32_t> dv(nb * stride, 0u);
+    std::vector<lrt_sbs_node> dn(g.sbs.nodes);
+    for (size_t i = 0; i < nb; i++) {
+      std::memcpy(&dv[i * stride], &g.sbs.values[g.sbs.nodes[i].data_offset], size_t(words) * 4);
+      dn[i].data_offset = uint32_t(i * stride);
+    }
+    ctx->brick_stride = stride;
+    std::vector<float4> lb(2 * nb);   // the BVH leaf boxes computed above
+    for (size_t i = 0; i < nb; i++) {
+      lb[2 * i] = make_float4(boxes[6 * i], boxes[6 * i + 1], boxes[6 * i + 2], 0.0f);
+      lb[2 * i + 1] = make_float4(boxes[6 * i + 3], boxes[6 * i + 4], boxes[6 * i + 5], 0.0f);
+    }
+    if ((e = upload(ctx->d_leaf_boxes, lb.data(), lb.size())) != cudaSuccess) return cuda_fail(ctx, e, "upload boxes");
+    s.leaf_boxes = ctx->d_leaf_boxes.p;
+    const uint32_t occ_words = (hd.brick_size * hd.brick_size * hd.brick_size + 31u) / 32u;
+    std::vector<uint32_t> occ;
+    build_occupancy(g.sbs, g.values_f, occ_words, occ);
+    if ((e = upload(ctx->d_occ, occ.data(), occ.size())) != cudaSuccess) return cuda_fail(ctx, e, "upload occupancy");
+    s.occ = ctx->d_occ.p;
+    s.occ_words = occ_words;
+    if ((e = upload(ctx->d_bricks, dn.data(), dn.size())) != cudaSuccess) return cuda_fail(ctx, e, "upload bricks");
+    if ((e = upload(ctx->d_values, dv.data(), dv.size())) != cudaSuccess) return cuda_fail(ctx, e, "upload values");
     if (!g.values_f.empty() && (e = upload(ctx->d_values_f, g.values_f.data(), g.values_f.size())) != cudaSuccess)
       return cuda_fail(ctx, e, "upload values_f");
     s.sbs_hdr = g.sbs.hdr;
@@ -480,6 +516,24 @@ extern "C" lrt_status lrt_set_preset(lrt_ctx *ctx, const lrt_preset *preset) {
   if (preset->spp == 0 || preset->spp > 1024) return fail(ctx, LRT_ERR_INVALID, "lrt_set_preset: bad spp");
   ctx->preset = *preset;
   ctx->dev.preset = *preset;
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_set_tuning(lrt_ctx *ctx, const char *key, int value) {
+  if (!ctx || !key) return LRT_ERR_INVALID;
+  const std::string k(key);
+  if (k == "variant") {
+    if (value < 0 || value > 1) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: variant is 0 or 1");
+    ctx->tuning.variant = value;
+  } else if (k == "block_warps") {
+    if (value < 1 || value > 8) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: block_warps in 1..8");
+    ctx->tuning.block_warps = value;
+  } else if (k == "stage") {
+    if (value < 0 || value > 1) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: stage is 0 or 1");
+    ctx->tuning.stage = value;
+  } else {
+    return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: unknown key " + k);
+  }
   return LRT_OK;
 }
 
@@ -547,7 +601,7 @@ static lrt_status render_impl(lrt_ctx *ctx, const lrt_view *views, uint32_t n_vi
   L.tile_counter = ctx->d_tile_counter.p;
   L.counters = counters;
   LRT_CUDA(ctx, cudaMemsetAsync(ctx->d_tile_counter.p, 0, sizeof(uint32_t), st));
-  LRT_CUDA(ctx, launch_render(ctx->dev, L, ctx->num_sms, st, counters != nullptr));
+  LRT_CUDA(ctx, launch_render(ctx->dev, L, ctx->num_sms, st, counters != nullptr, ctx->tuning));
   ctx->last_launches = 1;
   return LRT_OK;
 }

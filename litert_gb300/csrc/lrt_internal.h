@@ -42,6 +42,11 @@ struct BvhData {
 float sdf_eval(const lrt_sdf_desc &f, float x, float y, float z);
 lrt_status build_sbs(const lrt_sdf_desc &f, uint32_t depth, const lrt_sbs_header &hdr, int threads, SbsData &out);
 lrt_status build_svs(const lrt_sdf_desc &f, uint32_t depth, int threads, std::vector<lrt_svs_node> &out);
+// Voxel occupancy of every brick: bit (i*bs + j)*bs + k of brick b is set when
+// the smallest of the voxel's 8 decoded corner values is <= 0 -- exactly the
+// voxel test of OctreeBrickIntersect (BVH/BVH2Common.cpp:821).
+void build_occupancy(const SbsData &sbs, const std::vector<float> &values_f, uint32_t occ_words,
+                     std::vector<uint32_t> &occ);
 // boxes6: n x (min xyz, max xyz).  boxes=true: one box per leaf, payload = box
 // id; boxes=false: triangles, up to two per leaf, payload = range in `order`.
 lrt_status build_bvh(const float *boxes6, uint32_t n, bool boxes, BvhData &out);
@@ -55,6 +60,9 @@ struct DevScene {
   // SBS
   lrt_sbs_header sbs_hdr;
   const lrt_sbs_node *bricks;
+  const float4 *leaf_boxes;      // per brick: (min xyz, -), (max xyz, -) exactly as the BVH leaf box
+  const uint32_t *occ;           // per brick: one bit per voxel, set when a corner value is <= 0
+  uint32_t occ_words;            // 32-bit words of occupancy per brick
   const uint32_t *values;
   const float *values_f;
   // SVS
@@ -91,7 +99,18 @@ struct RenderLaunch {
   unsigned long long *counters; // optional traversal counters [4]
 };
 
-cudaError_t launch_render(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st, bool count);
+// Launch-shape and kernel choices (set through lrt_set_tuning).
+struct Tuning {
+  int variant = 0;          // render kernel: 0 = one ray per lane (while-while), 1 = warp packet traversal
+  int block_warps = 4;      // warps per block
+  int stage = 0;            // packet kernel: 1 = stage each brick in shared memory, 0 = read corners from global
+};
+
+cudaError_t launch_render(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st, bool count,
+                          const Tuning &tu);
+// Warp-packet SBS render kernel (trace_pkt.cu).
+cudaError_t launch_render_packet(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st, bool count,
+                                 const Tuning &tu);
 cudaError_t launch_query(const DevScene &s, const float4 *pos_near, const float4 *dir_far, uint32_t n,
                          lrt_hit *out, cudaStream_t st);
 

@@ -293,6 +293,43 @@ lrt_status build_sbs(const lrt_sdf_desc &f, uint32_t depth, const lrt_sbs_header
   return LRT_OK;
 }
 
+void build_occupancy(const SbsData &sbs, const std::vector<float> &values_f, uint32_t occ_words,
+                     std::vector<uint32_t> &occ) {
+  const lrt_sbs_header &h = sbs.hdr;
+  const uint32_t bs = h.brick_size, pad = h.brick_pad, v = bs + 2 * pad + 1;
+  const uint32_t layout = h.aux_data & 0xFF000000u;
+  const bool indexed = layout == LRT_SBS_LAYOUT_ID32F_IRGB32F || layout == LRT_SBS_LAYOUT_ID32F_IRGB32F_IN;
+  const uint32_t vpi = 4 / h.bytes_per_value, bits = 8 * h.bytes_per_value;
+  const uint32_t max_val = h.bytes_per_value == 4 ? 0xFFFFFFFFu : ((1u << bits) - 1);
+  const long nb = long(sbs.nodes.size());
+  occ.assign(size_t(nb) * occ_words, 0u);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (long b = 0; b < nb; b++) {
+    const lrt_sbs_node &nd = sbs.nodes[b];
+    const float sz = float(nd.pos_z_lod_size & 0x0000FFFF);
+    const float sz_inv = 2.0f / sz;
+    const float d_max = 1.73205081f * sz_inv;          // load_distance_values, BVH/BVH2Common.cpp:749-759
+    const float mult = 2 * d_max / float(max_val);
+    auto value = [&](uint32_t vid) -> float {
+      if (indexed) return values_f[sbs.values[nd.data_offset + vid]];
+      const uint32_t q = (sbs.values[nd.data_offset + vid / vpi] >> (bits * (vid % vpi))) & max_val;
+      return -d_max + mult * float(q);
+    };
+    uint32_t *o = &occ[size_t(b) * occ_words];
+    for (uint32_t i = 0; i < bs; i++)
+      for (uint32_t j = 0; j < bs; j++)
+        for (uint32_t k = 0; k < bs; k++) {
+          bool any = false;
+          for (int c = 0; c < 8 && !any; c++) {
+            const uint32_t vid = (i + ((c & 4) >> 2) + pad) * v * v + (j + ((c & 2) >> 1) + pad) * v + (k + (c & 1) + pad);
+            any = value(vid) <= 0.0f;
+          }
+          const uint32_t bit = (i * bs + j) * bs + k;
+          if (any) o[bit >> 5] |= 1u << (bit & 31);
+        }
+  }
+}
+
 // frame_octree_to_SVS_rec, utils/sparse_octree_builder.cpp:2346-2387
 static void svs_rec(const Frame &fr, uint32_t idx, uint32_t px, uint32_t py, uint32_t pz, uint32_t lod,
                     std::vector<lrt_svs_node> &out) {

@@ -25,8 +25,9 @@ __device__ __forceinline__ float3 cross(float3 a, float3 b) {
 __device__ __forceinline__ float mn(float a, float b) { return (b < a) ? b : a; }
 __device__ __forceinline__ float mx(float a, float b) { return (a < b) ? b : a; }
 __device__ __forceinline__ float clampf(float x, float lo, float hi) { return mn(mx(x, lo), hi); }
-// LiteMath sign(): -1, 0, +1
-__device__ __forceinline__ float signf(float a) { return a > 0.0f ? 1.0f : (a < 0.0f ? -1.0f : 0.0f); }
+// LiteMath sign(): -1 for negative, +1 otherwise (never 0: SafeInverse relies on
+// it to avoid a division by zero, raytrace_common.h:59-67)
+__device__ __forceinline__ float signf(float a) { return a < 0.0f ? -1.0f : 1.0f; }
 // normalize(u) = u / sqrt(dot(u,u))
 __device__ __forceinline__ float3 normalize(float3 a) {
   const float l = sqrtf(dot(a, a));
@@ -50,15 +51,22 @@ __device__ __forceinline__ float3 safe_inverse(float3 d) {
             1.0f / (fabsf(d.z) > ooeps ? d.z : fabsf(ooeps) * signf(d.z)));
 }
 
+// Hardware min/max (FMNMX).  For non-NaN operands they return the same value as
+// std::min/std::max except possibly the sign of a zero result; slab distances
+// and voxel coordinates are never NaN for finite rays (SafeInverse keeps the
+// inverse direction finite), and a zero's sign never reaches an output there.
+__device__ __forceinline__ float fmn(float a, float b) { return fminf(a, b); }
+__device__ __forceinline__ float fmx(float a, float b) { return fmaxf(a, b); }
+
 // RayBoxIntersection2, raytrace_common.h:69-82
 __device__ __forceinline__ float2 ray_box(float3 o, float3 inv, float lox, float loy, float loz, float hix,
                                           float hiy, float hiz) {
   const float lo = inv.x * (lox - o.x), hi = inv.x * (hix - o.x);
   const float lo1 = inv.y * (loy - o.y), hi1 = inv.y * (hiy - o.y);
   const float lo2 = inv.z * (loz - o.z), hi2 = inv.z * (hiz - o.z);
-  const float tmin = mx(mn(lo, hi), mn(lo1, hi1));
-  const float tmax = mn(mx(lo, hi), mx(lo1, hi1));
-  return make_float2(mx(tmin, mn(lo2, hi2)), mn(tmax, mx(lo2, hi2)));
+  const float tmin = fmx(fmn(lo, hi), fmn(lo1, hi1));
+  const float tmax = fmn(fmx(lo, hi), fmx(lo1, hi1));
+  return make_float2(fmx(tmin, fmn(lo2, hi2)), fmn(tmax, fmx(lo2, hi2)));
 }
 
 // octahedral encode, BVH/BVH2Common.cpp:29-35

@@ -105,6 +105,7 @@ def lib():
             "lrt_build_bvh2": (I, [VP, U32, U32, C.POINTER(VP), C.POINTER(U32), C.POINTER(VP), C.POINTER(U32),
                                    C.POINTER(VP)]),
             "lrt_free": (None, [VP]),
+            "lrt_set_tuning": (I, [P, C.c_char_p, I]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -240,6 +241,10 @@ class Scene:
 
     def _chk(self, s):
         _check(s, self._ctx)
+
+    def set_tuning(self, key, value):
+        """Kernel choices that never change results ("variant", "block_warps")."""
+        self._chk(lib().lrt_set_tuning(self._ctx, key.encode(), int(value)))
 
     def clear_geom(self):
         self._chk(lib().lrt_clear_geom(self._ctx))

@@ -31,8 +31,9 @@ static inline f3 cross3(f3 a, f3 b) {
 static inline f3 normalize3(f3 a) { float l = sqrtf(dot3(a, a)); return mk3(a.x / l, a.y / l, a.z / l); }
 static inline float fminf_(float a, float b) { return (b < a) ? b : a; }  /* std::min */
 static inline float fmaxf_(float a, float b) { return (a < b) ? b : a; }  /* std::max */
-/* LiteMath/GLSL sign: -1, 0, +1 (restated convention). */
-static inline float signf_(float a) { return a > 0.0f ? 1.0f : (a < 0.0f ? -1.0f : 0.0f); }
+/* LiteMath sign (restated convention): -1 for negative, +1 otherwise.  Never 0,
+ * which SafeInverse needs to avoid its division by zero (raytrace_common.h:59-67). */
+static inline float signf_(float a) { return a < 0.0f ? -1.0f : 1.0f; }
 static inline float clampf_(float x, float lo, float hi) { return fminf_(fmaxf_(x, lo), hi); }
 
 /* LiteMath float4x4 (row-major here: m[r*4+c]) times float4; sum in column order. */

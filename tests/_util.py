@@ -14,8 +14,10 @@ def sbs_scene(sdf_params, depth, brick_size, pad=0, bpv=4):
     return h, nodes, values
 
 
-def gpu_scene_sbs(h, nodes, values, values_f=None, **preset):
+def gpu_scene_sbs(h, nodes, values, values_f=None, variant=None, **preset):
     s = lrt.Scene(0)
+    if variant is not None:
+        s.set_tuning("variant", variant)
     g = s.add_sbs(h, nodes, values, values_f)
     s.add_instance(g)
     s.commit_scene()
@@ -30,6 +32,22 @@ def oracle_render(osc, view):
     return hits, col, cnt
 
 
+def canon_bits(a):
+    """Float32 bit patterns with every NaN mapped to one pattern (CPU and GPU
+    produce different NaN payloads, e.g. the normal of a zero gradient)."""
+    a = np.ascontiguousarray(a, np.float32)
+    b = a.view(np.uint32).copy()
+    b[np.isnan(a)] = 0x7FC00000
+    return b
+
+
+def records_equal(ga, oa):
+    """Bitwise equality of structured hit arrays, NaN == NaN."""
+    fa = np.ascontiguousarray(ga).view(np.float32)
+    fb = np.ascontiguousarray(oa).view(np.float32)
+    return np.array_equal(canon_bits(fa), canon_bits(fb))
+
+
 def compare_hits16(g, o):
     """g: HIT16 records from the GPU, o: full oracle hits.  Returns dict of mismatch counts."""
     miss_g = g["primId"] == lrt.MISS
@@ -39,9 +57,9 @@ def compare_hits16(g, o):
         n=g.size,
         hits=int((~miss_o).sum()),
         mask=int((miss_g != miss_o).sum()),
-        t=int((g["t"][both].view(np.uint32) != o["t"][both].view(np.uint32)).sum()),
+        t=int((canon_bits(g["t"][both]) != canon_bits(o["t"][both])).sum()),
         prim=int((g["primId"][both] != o["primId"][both]).sum()),
-        nx=int((g["nx"][both].view(np.uint32) != o["coords"][both, 2].view(np.uint32)).sum()),
-        ny=int((g["ny"][both].view(np.uint32) != o["coords"][both, 3].view(np.uint32)).sum()),
+        nx=int((canon_bits(g["nx"][both]) != canon_bits(o["coords"][both, 2])).sum()),
+        ny=int((canon_bits(g["ny"][both]) != canon_bits(o["coords"][both, 3])).sum()),
         max_dt=float(np.abs(g["t"][both] - o["t"][both]).max()) if both.any() else 0.0,
     )

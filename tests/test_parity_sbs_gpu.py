@@ -13,16 +13,16 @@ import pytest
 from litert_gb300 import lrt, scenes
 from oracle import oracle as orc
 
-from _util import compare_hits16, gpu_scene_sbs, orc_header, oracle_render, sbs_scene
+from _util import compare_hits16, gpu_scene_sbs, orc_header, oracle_render, records_equal, sbs_scene
 
 pytestmark = pytest.mark.gpu
 EXTENT = 2.0
 
 
-def _run(params, depth, bs, view, intersect=lrt.INTERSECT_NEWTON, render_mode=lrt.RENDER_MODE_NORMAL, pad=0, bpv=4,
+def _run(params, depth, bs, view, intersect=lrt.INTERSECT_NEWTON, render_mode=lrt.RENDER_MODE_NORMAL, pad=0, bpv=4, variant=1,
          representation_mode=1):
     h, n, v = sbs_scene(params, depth, bs, pad, bpv)
-    g = gpu_scene_sbs(h, n, v, render_mode=render_mode, sdf_node_intersect=intersect,
+    g = gpu_scene_sbs(h, n, v, variant=variant, render_mode=render_mode, sdf_node_intersect=intersect,
                       representation_mode=representation_mode)
     out = g.render_host([view], hits=True, rgba=True, rgba8=True)
     osc = orc.Scene("sbs", sbs=(orc_header(h), n, v), intersect=intersect, render_mode=render_mode,
@@ -32,9 +32,13 @@ def _run(params, depth, bs, view, intersect=lrt.INTERSECT_NEWTON, render_mode=lr
     return out, hits, col
 
 
+VARIANTS = [0, 1]   # one ray per lane / warp packet with shared-memory brick staging
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
 @pytest.mark.parametrize("intersect", [lrt.INTERSECT_NEWTON, lrt.INTERSECT_ST, lrt.INTERSECT_BBOX, lrt.INTERSECT_IT])
-def test_sphere_config_bit_exact(intersect):
-    out, hits, col = _run(scenes.SPHERE_SDF, 4, 4, scenes.sphere_view(), intersect=intersect)
+def test_sphere_config_bit_exact(intersect, variant):
+    out, hits, col = _run(scenes.SPHERE_SDF, 4, 4, scenes.sphere_view(), intersect=intersect, variant=variant)
     r = compare_hits16(out["hits"], hits)
     assert r["hits"] > 5000, r
     assert r["mask"] == 0 and r["t"] == 0 and r["prim"] == 0 and r["nx"] == 0 and r["ny"] == 0, r
@@ -59,17 +63,19 @@ def test_sphere_literal_depth6():
     assert r["mask"] == 0 and r["t"] == 0 and r["prim"] == 0 and r["nx"] == 0, r
 
 
-@pytest.mark.parametrize("bpv,pad,bs", [(1, 0, 4), (2, 1, 2), (4, 1, 8), (1, 0, 1)])
-def test_layout_variants(bpv, pad, bs):
-    out, hits, _ = _run(scenes.SPHERE_SDF, 4, bs, scenes.sphere_view(128, 96), pad=pad, bpv=bpv)
+@pytest.mark.parametrize("variant", VARIANTS)
+@pytest.mark.parametrize("bpv,pad,bs", [(1, 0, 4), (2, 1, 2), (4, 1, 8), (1, 0, 1), (2, 0, 16)])
+def test_layout_variants(bpv, pad, bs, variant):
+    out, hits, _ = _run(scenes.SPHERE_SDF, 4, bs, scenes.sphere_view(128, 96), pad=pad, bpv=bpv, variant=variant)
     r = compare_hits16(out["hits"], hits)
     assert r["mask"] == 0 and r["t"] == 0 and r["prim"] == 0 and r["nx"] == 0 and r["ny"] == 0, r
 
 
 @pytest.mark.parametrize("mode", [lrt.RENDER_MODE_MASK, lrt.RENDER_MODE_LAMBERT_NO_TEX, lrt.RENDER_MODE_DEPTH,
                                   lrt.RENDER_MODE_LINEAR_DEPTH, lrt.RENDER_MODE_INVERSE_LINEAR_DEPTH])
-def test_render_modes(mode):
-    out, hits, col = _run(scenes.SPHERE_SDF, 4, 4, scenes.sphere_view(96, 64), render_mode=mode)
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_render_modes(mode, variant):
+    out, hits, col = _run(scenes.SPHERE_SDF, 4, 4, scenes.sphere_view(96, 64), render_mode=mode, variant=variant)
     assert np.array_equal(out["rgba"].view(np.uint32), col.view(np.uint32))
     # RGBA8 packing of MultiRenderer::CastRaySingle (Renderer/eye_ray.cpp:111-115)
     c = np.clip(col, 0, 1)
@@ -84,12 +90,16 @@ def test_surface_representation_mode():
     assert r["mask"] == 0 and r["t"] == 0 and r["nx"] == 0, r
 
 
-def test_union_scene_multi_view():
-    """Config-3 scene at reduced depth, three views of different sizes in one launch."""
+@pytest.mark.parametrize("variant,stage", [(0, 0), (1, 0), (1, 1)])
+def test_union_scene_multi_view(variant, stage):
+    """Config-3 scene at reduced depth, three views of different sizes in one launch;
+    the packet kernel with and without shared-memory brick staging."""
     p = scenes.union_params()
     h, n, v = sbs_scene(p, 5, 4)
     views = scenes.union_views(n_views=3, lo=96, hi=200)
-    g = gpu_scene_sbs(h, n, v, render_mode=lrt.RENDER_MODE_NORMAL, sdf_node_intersect=lrt.INTERSECT_NEWTON)
+    g = gpu_scene_sbs(h, n, v, variant=variant, render_mode=lrt.RENDER_MODE_NORMAL,
+                      sdf_node_intersect=lrt.INTERSECT_NEWTON)
+    g.set_tuning("stage", stage)
     out = g.render_host(views, hits=True)
     osc = orc.Scene("sbs", sbs=(orc_header(h), n, v), intersect=lrt.INTERSECT_NEWTON, render_mode=lrt.RENDER_MODE_NORMAL)
     off = 0
@@ -118,7 +128,7 @@ def test_query_rays_random_and_anyhit():
     gh = g.query_rays(pos, dirs)
     osc = orc.Scene("sbs", sbs=(orc_header(h), n, v), intersect=lrt.INTERSECT_NEWTON, render_mode=lrt.RENDER_MODE_NORMAL)
     oh = osc.query_rays(pos, dirs)
-    assert np.array_equal(gh.view(np.uint32).reshape(N, -1), oh.view(np.uint32).reshape(N, -1))
+    assert records_equal(gh, oh)
     # any-hit (tFar < 0): hit/miss agrees with the nearest-hit query
     dirs[:, 3] = -1e9
     ga = g.query_rays(pos, dirs)
