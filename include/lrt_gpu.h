@@ -60,7 +60,7 @@ lrt_status lrt_set_preset(lrt_ctx *ctx, const lrt_preset *preset);
 
 /* Launch-shape and kernel choices; no reference counterpart (the reference's
  * device path is generated by kernel_slicer).  Keys: "variant" (0 = one ray per
- * lane, 1 = warp packet traversal, default), "stage" (packet kernel: 1 = stage
+ * lane, default; 1 = warp packet traversal), "stage" (packet kernel: 1 = stage
  * each brick in shared memory), "block_warps" (1..8).  Results do not depend on
  * these. */
 lrt_status lrt_set_tuning(lrt_ctx *ctx, const char *key, int value);
