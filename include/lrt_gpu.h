@@ -84,6 +84,28 @@ lrt_status lrt_render(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, lrt
 /* Same, with host output buffers: copies views in and results out, synchronous. */
 lrt_status lrt_render_host(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, lrt_hit16 *hits16,
                            float *rgba, uint32_t *rgba8);
+/* Rendering that allocates nothing.  No counterpart in the reference.
+ *
+ * For callers that must not allocate device memory during rendering: a host
+ * application whose own pool allocator has reserved the GPU's memory up front
+ * (a cudaMalloc from the library would fail or fragment that pool), and a
+ * real-time frame loop where cudaMalloc's implicit device synchronisation and
+ * latency are not acceptable.  Same results as lrt_render for the committed
+ * scene (the inputs were allocated once, by lrt_commit_scene).  The per-call
+ * scratch -- the persistent kernel's work-queue head and the per-view table --
+ * lives in one file-scope device array of 256 + LRT_NOALLOC_MAX_VIEWS * 160
+ * bytes that every GPU loading the library keeps until exit.  At most
+ * LRT_NOALLOC_MAX_VIEWS views per call; more returns LRT_ERR_INVALID.  The
+ * first call on a device looks up the array's device address: make that first
+ * call before any stream capture.  All calls share the array, which keeps the
+ * last call's contents (the queue head is cleared on every call): calls whose
+ * GPU work overlaps -- on different streams, or from several host threads --
+ * race on it; serialise them on one stream.  Outputs are device memory, as in
+ * lrt_render; asynchronous on `stream`.  Errors are reported through the
+ * status only (lrt_last_error is not updated, which could allocate). */
+#define LRT_NOALLOC_MAX_VIEWS 64
+lrt_status lrt_render_noalloc(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, lrt_hit16 *hits16,
+                              float *rgba, uint32_t *rgba8, void *stream);
 /* Number of our kernels launched by the last lrt_render / lrt_query_rays call. */
 uint32_t lrt_last_launch_count(const lrt_ctx *ctx);
 /* Per-ray traversal counters of the committed scene for the given views (a

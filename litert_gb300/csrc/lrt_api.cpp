@@ -634,6 +634,40 @@ extern "C" lrt_status lrt_render_host(lrt_ctx *ctx, const lrt_view *views, uint3
   return LRT_OK;
 }
 
+// No allocation anywhere on this path: the view table is built in a stack array
+// and copied into the file-scope scratch array of trace.cu; errors are returned
+// as codes only.
+extern "C" lrt_status lrt_render_noalloc(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, lrt_hit16 *hits16,
+                                         float *rgba, uint32_t *rgba8, void *stream) {
+  if (!ctx || !views || n_views == 0 || n_views > LRT_NOALLOC_MAX_VIEWS) return LRT_ERR_INVALID;
+  if (!ctx->committed) return LRT_ERR_STATE;
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return LRT_ERR_CUDA;
+  DevView hv[LRT_NOALLOC_MAX_VIEWS];
+  uint64_t pix = 0, tiles = 0;
+  for (uint32_t v = 0; v < n_views; v++) {
+    const lrt_view &in = views[v];
+    if (in.width == 0 || in.height == 0 || in.width > 65535 || in.height > 65535) return LRT_ERR_INVALID;
+    DevView &o = hv[v];
+    std::memset(&o, 0, sizeof(o));
+    o.width = in.width;
+    o.height = in.height;
+    o.pix_offset = uint32_t(pix);
+    o.tile_offset = uint32_t(tiles);
+    o.tiles_x = (in.width + 7) / 8;
+    lrt_inverse4x4(in.proj, o.proj_inv);       // UpdateCamera, Renderer/eye_ray_host.cpp:59-65
+    lrt_inverse4x4(in.world_view, o.wv_inv);
+    pix += uint64_t(in.width) * in.height;
+    tiles += uint64_t(o.tiles_x) * ((in.height + 3) / 4);
+  }
+  if (pix >= (1ull << 32) || tiles >= (1ull << 32)) return LRT_ERR_INVALID;
+  const cudaError_t e = launch_render_noalloc(ctx->dev, hv, n_views, uint32_t(tiles), hits16,
+                                              reinterpret_cast<float4 *>(rgba), rgba8, ctx->device, ctx->num_sms,
+                                              static_cast<cudaStream_t>(stream), ctx->tuning);
+  if (e != cudaSuccess) return e == cudaErrorInvalidValue ? LRT_ERR_INVALID : LRT_ERR_CUDA;
+  ctx->last_launches = 1;
+  return LRT_OK;
+}
+
 extern "C" lrt_status lrt_render_counters(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, uint64_t out[4]) {
   if (!ctx || !out) return LRT_ERR_INVALID;
   LRT_CUDA(ctx, cudaSetDevice(ctx->device));

@@ -256,3 +256,66 @@ cudaError_t launch_query(const DevScene &s, const float4 *pos_near, const float4
 }
 
 }  // namespace lrt
+
+// ---------------------------------------------------------------- rendering without allocation
+// Scratch of lrt_render_noalloc: the persistent kernel's work-queue head and the
+// per-view table live in this file-scope device array instead of context
+// buffers, so that entry point allocates nothing.  Every GPU that loads the
+// library holds the array until exit.  Host code must not pass the symbol
+// itself to a kernel (on the host it is only a stand-in); the device address
+// is looked up once per device with cudaGetSymbolAddress, with that device
+// current, on the first call on that device.
+#include <mutex>
+
+namespace lrt {
+namespace {
+constexpr size_t kNoAllocViewOffset = 256;   // [0, 256): queue head; then the view table
+constexpr size_t kNoAllocScratchBytes = kNoAllocViewOffset + size_t(LRT_NOALLOC_MAX_VIEWS) * sizeof(DevView);
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void *g_noalloc_addr[kNoAllocMaxDevices];   // device address of g_noalloc_scratch, per device
+
+cudaError_t noalloc_scratch(int device, unsigned char **out) {
+  if (device < 0 || device >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_addr[device]) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);   // `device` is current
+    if (e != cudaSuccess) return e;
+    g_noalloc_addr[device] = p;
+  }
+  *out = static_cast<unsigned char *>(g_noalloc_addr[device]);
+  return cudaSuccess;
+}
+}  // namespace
+
+cudaError_t launch_render_noalloc(const DevScene &s, const DevView *host_views, uint32_t n_views,
+                                  uint32_t total_tiles, lrt_hit16 *hits16, float4 *rgba, uint32_t *rgba8,
+                                  int device, int num_sms, cudaStream_t st, const Tuning &tu) {
+  if (n_views == 0 || n_views > LRT_NOALLOC_MAX_VIEWS) return cudaErrorInvalidValue;
+  unsigned char *scratch = nullptr;
+  cudaError_t e = noalloc_scratch(device, &scratch);
+  if (e != cudaSuccess) return e;
+  uint32_t *head = reinterpret_cast<uint32_t *>(scratch);
+  DevView *views = reinterpret_cast<DevView *>(scratch + kNoAllocViewOffset);
+  // The array keeps the previous call's contents: the view table is rewritten and
+  // the queue head cleared on every call.
+  e = cudaMemcpyAsync(views, host_views, n_views * sizeof(DevView), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(head, 0, sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  RenderLaunch L;
+  L.views = views;
+  L.n_views = n_views;
+  L.total_tiles = total_tiles;
+  L.hits16 = hits16;
+  L.rgba = rgba;
+  L.rgba8 = rgba8;
+  L.tile_counter = head;
+  L.counters = nullptr;
+  return launch_render(s, L, num_sms, st, false, tu);
+}
+
+}  // namespace lrt

@@ -106,6 +106,7 @@ def lib():
                                    C.POINTER(VP)]),
             "lrt_free": (None, [VP]),
             "lrt_set_tuning": (I, [P, C.c_char_p, I]),
+            "lrt_render_noalloc": (I, [P, VP, U32, VP, VP, VP, VP]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
