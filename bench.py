@@ -268,9 +268,11 @@ def main():
         peak = peaks.get("hbm_gbs", 6800.0)
         achieved = (b_ray * n_rays / (ms * 1e-3) / 1e9) if b_ray else None
         traffic = None
-        tp = os.path.join(ROOT, "profiles", "traffic.json")
-        if os.path.exists(tp):
-            traffic = json.load(open(tp)).get("render_kernel_sbs_batched_bytes_per_launch")
+        tp = os.path.join(ROOT, "profiles", "render_kernel_sbs_batched16.md")
+        if os.path.exists(tp):   # dram read+write of one launch, from the committed ncu summary
+            for ln in open(tp):
+                if ln.startswith("traffic_bytes_per_launch:"):
+                    traffic = int(ln.split(":")[1])
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
