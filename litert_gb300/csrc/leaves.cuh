@@ -97,13 +97,15 @@ __device__ __forceinline__ void local_surface(const lrt_preset &pr, const DevSce
         const float Q = (aa * aa - 3 * b) / 9;
         const float R = (2 * aa * aa - 9 * aa * b + 27 * c) / 54;
         const float Q3 = Q * Q * Q;
+        // The reference's unqualified sqrt(float) is ::sqrt(double): these
+        // expressions are evaluated in double, with std::cos(float) in float.
         if (R * R < Q3) {
-          const float theta = acosf(R / sqrtf(Q3));
-          x1 = -2 * sqrtf(Q) * cosf(theta / 3) - aa / 3;
-          x2 = -2 * sqrtf(Q) * cosf((theta + 2 * 3.14159265358979323846f) / 3) - aa / 3;
-          x3 = -2 * sqrtf(Q) * cosf((theta - 2 * 3.14159265358979323846f) / 3) - aa / 3;
+          const float theta = float(acos(double(R) / sqrt(double(Q3))));
+          x1 = float(-2 * sqrt(double(Q)) * double(cosf(theta / 3)) - double(aa / 3));
+          x2 = float(-2 * sqrt(double(Q)) * double(cosf((theta + 2 * 3.14159265358979323846f) / 3)) - double(aa / 3));
+          x3 = float(-2 * sqrt(double(Q)) * double(cosf((theta - 2 * 3.14159265358979323846f) / 3)) - double(aa / 3));
         } else {
-          const float A = -signf(R) * powf(fabsf(R) + sqrtf(R * R - Q3), 1.0f / 3.0f);
+          const float A = float(double(-signf(R)) * pow(double(fabsf(R)) + sqrt(double(R * R - Q3)), double(1.0f / 3.0f)));
           const float B = fabsf(A) > EPS ? Q / A : 0;
           x1 = A + B - aa / 3;
         }

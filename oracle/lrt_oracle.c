@@ -157,14 +157,17 @@ static void local_surface_intersection(const orc_scene *s, uint32_t type, f3 ray
         float Q = (aa * aa - 3 * b) / 9;
         float R = (2 * aa * aa - 9 * aa * b + 27 * c) / 54;
         float Q3 = Q * Q * Q;
+        /* The reference's unqualified sqrt(float) resolves to ::sqrt(double), which
+         * promotes these expressions to double; std::acos/std::pow then take the
+         * double overloads, std::cos(float) stays float.  LiteMath::M_PI is float. */
         if (R * R < Q3) {
-          float theta = acosf(R / sqrtf(Q3));
-          x1 = -2 * sqrtf(Q) * cosf(theta / 3) - aa / 3;
-          /* LiteMath::M_PI is a float constant */
-          x2 = -2 * sqrtf(Q) * cosf((theta + 2 * 3.14159265358979323846f) / 3) - aa / 3;
-          x3 = -2 * sqrtf(Q) * cosf((theta - 2 * 3.14159265358979323846f) / 3) - aa / 3;
+          float theta = (float)acos((double)R / sqrt((double)Q3));
+          x1 = (float)(-2 * sqrt((double)Q) * (double)cosf(theta / 3) - (double)(aa / 3));
+          x2 = (float)(-2 * sqrt((double)Q) * (double)cosf((theta + 2 * 3.14159265358979323846f) / 3) - (double)(aa / 3));
+          x3 = (float)(-2 * sqrt((double)Q) * (double)cosf((theta - 2 * 3.14159265358979323846f) / 3) - (double)(aa / 3));
         } else {
-          float A = -signf_(R) * powf(fabsf(R) + sqrtf(R * R - Q3), 1.0f / 3.0f);
+          float A = (float)((double)(-signf_(R)) *
+                            pow((double)fabsf(R) + sqrt((double)(R * R - Q3)), (double)(1.0f / 3.0f)));
           float B = fabsf(A) > EPS ? Q / A : 0;
           x1 = A + B - aa / 3;
         }
@@ -645,6 +648,12 @@ orc_counters orc_render_pixels(const orc_scene *s, uint32_t w, uint32_t h, const
                                const float wv_inv[16], const uint32_t *pix, uint32_t n_pix,
                                orc_hit *hits, int threads) {
   return render_impl(s, w, h, proj_inv, wv_inv, pix, n_pix, hits, NULL, threads);
+}
+
+void orc_eye_rays(uint32_t w, uint32_t h, const float proj_inv[16], const float wv_inv[16], const uint32_t *pix,
+                  uint32_t n, float dx, float dy, float *pos_near, float *dir_far) {
+  for (uint32_t i = 0; i < n; i++)
+    orc_eye_ray(pix[i] % w, pix[i] / w, w, h, dx, dy, proj_inv, wv_inv, pos_near + 4 * i, dir_far + 4 * i);
 }
 
 void orc_query_rays(const orc_scene *s, const float *pos_near, const float *dir_far, uint32_t n, orc_hit *out,

@@ -88,6 +88,10 @@ orc_hit orc_ray_query_nearest(const orc_scene *s, const float pos_near[4], const
 void orc_query_rays(const orc_scene *s, const float *pos_near, const float *dir_far, uint32_t n, orc_hit *out,
                     int threads);
 
+/* Eye rays of the pixels pix[0..n) of a w x h view (sub-pixel offset dx, dy). */
+void orc_eye_rays(uint32_t w, uint32_t h, const float proj_inv[16], const float wv_inv[16], const uint32_t *pix,
+                  uint32_t n, float dx, float dy, float *pos_near, float *dir_far);
+
 /* Eye ray (Renderer/eye_ray.cpp:146-160, render_common.h:25-55). */
 void orc_eye_ray(uint32_t x, uint32_t y, uint32_t w, uint32_t h, float dx, float dy,
                  const float proj_inv[16], const float world_view_inv[16],

@@ -117,6 +117,17 @@ def build_svs(spheres, boxes, k, depth):
     return nodes
 
 
+def eye_rays(w, h, proj_inv, wv_inv, pix, dx=0.5, dy=0.5):
+    pix = np.ascontiguousarray(pix, np.uint32)
+    pi = np.ascontiguousarray(proj_inv, np.float32).reshape(16)
+    wi = np.ascontiguousarray(wv_inv, np.float32).reshape(16)
+    pos = np.zeros((pix.size, 4), np.float32)
+    dr = np.zeros((pix.size, 4), np.float32)
+    lib().orc_eye_rays(C.c_uint32(w), C.c_uint32(h), _p(pi), _p(wi), _p(pix), C.c_uint32(pix.size), C.c_float(dx),
+                       C.c_float(dy), _p(pos), _p(dr))
+    return pos, dr
+
+
 def node_boxes(nodes):
     """Per-node AABB exactly as AddGeom_SdfSBS / AddGeom_SdfSVS compute it
     (BVH/BVH2Common_host.cpp:546-555, 640-653), float32 arithmetic."""
