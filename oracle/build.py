@@ -1,6 +1,7 @@
 """Build recipe for the CPU oracle (test infrastructure).
 
-Compiles the plain-C restatement (lrt_oracle.c, lrt_oracle_build.c) into
+Compiles the plain-C restatement (lrt_oracle.c, lrt_oracle_build.c,
+lrt_oracle_dr.c) into
 oracle/_build/liblrt_oracle.so with OpenMP and -ffp-contract=off.  Only tests,
 __graft_entry__.smoke() and bench.py's CPU legs load it.
 """
@@ -16,7 +17,8 @@ LIB = os.path.join(OUT, "liblrt_oracle.so")
 def build():
     os.makedirs(OUT, exist_ok=True)
     cmd = ["gcc", "-O2", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-Wall",
-           "-o", LIB, os.path.join(HERE, "lrt_oracle.c"), os.path.join(HERE, "lrt_oracle_build.c"), "-lm"]
+           "-o", LIB, os.path.join(HERE, "lrt_oracle.c"), os.path.join(HERE, "lrt_oracle_build.c"),
+           os.path.join(HERE, "lrt_oracle_dr.c"), "-lm"]
     r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if r.returncode != 0:
         sys.stderr.write(r.stdout)

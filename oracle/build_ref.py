@@ -1,7 +1,8 @@
-"""Compile the reference's ray-query translation unit in place (oracle pinning).
+"""Compile the reference's ray-query translation units in place (oracle pinning).
 
 Builds oracle/_ref/libref_bvh.so from the reference tree's own
-BVH/BVH2Common.cpp (read where it lies; nothing is copied) plus
+BVH/BVH2Common.cpp and diff_render/BVH2DR.cpp (read where they lie; nothing is
+copied) plus
 oracle/ref_driver.cpp, against the project's shims for the reference's missing
 dependencies (oracle/ref_shim/: a LiteMath stand-in and the CrossRT
 ISceneObject interface).  Leaf types off the path are compiled out with the
@@ -33,6 +34,7 @@ def build():
              "-I" + REF] + ["-D" + d for d in DEFINES]
     objs = []
     for src, obj in ((os.path.join(REF, "BVH", "BVH2Common.cpp"), "bvh2common.o"),
+                     (os.path.join(REF, "diff_render", "BVH2DR.cpp"), "bvh2dr.o"),
                      (os.path.join(HERE, "ref_driver.cpp"), "ref_driver.o")):
         o = os.path.join(OUT, obj)
         r = subprocess.run(["g++", *flags, "-c", src, "-o", o], stdout=subprocess.PIPE, stderr=subprocess.STDOUT,

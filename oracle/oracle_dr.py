@@ -1,0 +1,198 @@
+"""ctypes binding of the differentiable-render part of the CPU oracle
+(oracle/lrt_oracle_dr.c in oracle/_build/liblrt_oracle.so).
+
+TEST INFRASTRUCTURE ONLY: used by tests/ and bench.py's CPU legs as the checker
+of the GPU DR kernels.  The product never imports this module.
+"""
+import ctypes as C
+
+import numpy as np
+
+from .oracle import SbsHeader, _p, _sdf_desc, lib, node_boxes, bvh2_build
+
+VP = C.c_void_p
+
+# RayQuery_NearestHitWithGrad record: 576 32-bit words (oracle/ref_driver.cpp)
+HITDR = [("t", "<f4"), ("primId", "<u4"), ("instId", "<u4"), ("geomId", "<u4"), ("color", "<f4", (3,)),
+         ("sdf", "<f4"), ("normal", "<f4", (3,)), ("check_vox_border", "<u4"), ("_pad", "<u4", (2,))]
+PD_DIST = [("dDiffuse", "<f4", (3,)), ("index", "<u4"), ("dNorm", "<f4", (3,)), ("dDist", "<f4")]
+RECORD_DTYPE = np.dtype([("hit", HITDR), ("missed_hit", HITDR), ("missed_indices", "<u4", (8,)),
+                         ("missed_dSDF_dtheta", "<f4", (8,)), ("dc", [("index", "<u4"), ("value", "<f4")], (8,)),
+                         ("dd", PD_DIST, (64,)), ("_tail", "<u4", (4,))])
+assert RECORD_DTYPE.itemsize == 576 * 4
+
+FLAG_DDIFFUSE_DCOLOR, FLAG_DDIFFUSE_DPOS, FLAG_DNORM_DPOS, FLAG_BORDER, FLAG_DDIST_DPOS = 1, 2, 4, 8, 16
+RENDER_DIFFUSE, RENDER_LAMBERT, RENDER_MASK, RENDER_LINEAR_DEPTH, RENDER_NORMAL = 0, 1, 2, 3, 4
+RECON_COLOR, RECON_GEOMETRY = 1, 2
+LAYOUT_ID32F_IRGB32F, LAYOUT_ID32F_IRGB32F_IN = 4 << 24, 5 << 24
+
+
+class DrScene_(C.Structure):
+    _fields_ = [("hdr", SbsHeader), ("nodes", VP), ("n_nodes", C.c_uint32), ("values", VP), ("n_values", C.c_uint32),
+                ("n_params", C.c_uint32), ("pairs", VP), ("n_pairs", C.c_uint32), ("inst_bmin", C.c_float * 3),
+                ("inst_bmax", C.c_float * 3), ("inst_inv", C.c_float * 16), ("need_normal", C.c_int)]
+
+
+class Light(C.Structure):
+    _fields_ = [("type", C.c_uint32), ("dir", C.c_float * 3), ("color", C.c_float * 3)]
+
+
+class DrPreset(C.Structure):
+    _fields_ = [("render_mode", C.c_uint32), ("reconstruction_flags", C.c_uint32), ("input_type", C.c_uint32),
+                ("loss_function", C.c_uint32), ("spp", C.c_uint32), ("border_spp", C.c_uint32),
+                ("border_relax_eps", C.c_float), ("seed", C.c_uint32), ("n_lights", C.c_uint32),
+                ("lights", Light * 4), ("lr", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float),
+                ("eps", C.c_float), ("accumulate_batch", C.c_uint32)]
+
+
+class DrView(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("proj_inv", C.c_float * 16),
+                ("wv_inv", C.c_float * 16), ("proj", C.c_float * 16), ("world_view", C.c_float * 16)]
+
+
+_bound = False
+
+
+def _lib():
+    global _bound
+    L = lib()
+    if not _bound:
+        L.orc_dr_query.argtypes = [C.POINTER(DrScene_), VP, C.c_uint32, VP, VP, C.c_uint32, VP]
+        L.orc_dr_render.restype = C.c_double
+        L.orc_dr_render.argtypes = [C.POINTER(DrScene_), VP, C.POINTER(DrPreset), C.POINTER(DrView), VP, VP, VP, VP,
+                                    VP, C.c_int]
+        L.orc_dr_loss_f64.restype = C.c_double
+        L.orc_dr_loss_f64.argtypes = [C.POINTER(DrScene_), VP, C.POINTER(DrPreset), C.POINTER(DrView), VP, VP]
+        L.orc_dr_step.argtypes = [C.POINTER(DrScene_), VP, C.POINTER(DrPreset), VP, VP, C.c_uint32, C.c_uint32, VP,
+                                  VP, VP, VP, C.c_int]
+        L.orc_dr_adam.argtypes = [C.c_uint32, VP, VP, VP, C.c_uint32, C.c_float, C.c_float, C.c_float, C.c_float]
+        L.orc_dr_grid_sbs.restype = C.c_uint32
+        L.orc_dr_grid_sbs.argtypes = [C.c_uint32, C.c_uint32, C.c_void_p, VP, C.POINTER(SbsHeader), C.POINTER(VP),
+                                      C.POINTER(VP), C.POINTER(C.c_uint32), C.POINTER(VP), C.POINTER(C.c_uint32)]
+        _bound = True
+    return L
+
+
+def default_lights():
+    """MultiRenderer's default lights (Renderer/eye_ray_host.cpp:40): a direct
+    light along normalize(1,1,1) with colour 2/3 and an ambient 0.25."""
+    d = np.ones(3, np.float32)
+    d = d / np.sqrt(np.float32(3.0))
+    return [(0, d, np.full(3, np.float32(2.0) / np.float32(3.0), np.float32)),
+            (2, np.zeros(3, np.float32), np.full(3, 0.25, np.float32))]
+
+
+def make_preset(render_mode=RENDER_LAMBERT, reconstruction=RECON_COLOR | RECON_GEOMETRY, input_type=0, loss=0,
+                spp=1, border_spp=256, border_relax_eps=1e-3, seed=1, lights=None, lr=3e-3, beta1=0.9, beta2=0.999,
+                eps=1e-8, accumulate_batch=0):
+    p = DrPreset()
+    p.render_mode, p.reconstruction_flags, p.input_type, p.loss_function = render_mode, reconstruction, input_type, loss
+    p.spp, p.border_spp, p.border_relax_eps, p.seed = spp, border_spp, border_relax_eps, seed
+    lights = default_lights() if lights is None else lights
+    p.n_lights = len(lights)
+    for i, (t, d, c) in enumerate(lights):
+        p.lights[i].type = t
+        p.lights[i].dir[:] = [float(x) for x in np.asarray(d, np.float32)]
+        p.lights[i].color[:] = [float(x) for x in np.asarray(c, np.float32)]
+    p.lr, p.beta1, p.beta2, p.eps, p.accumulate_batch = lr, beta1, beta2, eps, accumulate_batch
+    return p
+
+
+def make_view(width, height, world_view, proj, inverse4x4):
+    v = DrView()
+    v.width, v.height = width, height
+    wv = np.asarray(world_view, np.float32).reshape(16)
+    pj = np.asarray(proj, np.float32).reshape(16)
+    v.proj_inv[:] = np.asarray(inverse4x4(pj), np.float32).reshape(16).tolist()
+    v.wv_inv[:] = np.asarray(inverse4x4(wv), np.float32).reshape(16).tolist()
+    v.proj[:] = pj.tolist()
+    v.world_view[:] = wv.tolist()
+    return v
+
+
+def grid_sbs(brick_count, brick_size, spheres=None, boxes=None, k=0.0, color=None):
+    """create_grid_sbs + neighbour table; returns (header, nodes[n,4], values, params)."""
+    d, keep = _sdf_desc(spheres, boxes, k)
+    L = _lib()
+    hdr = SbsHeader()
+    pn, pv, pp = VP(), VP(), VP()
+    nv, npar = C.c_uint32(), C.c_uint32()
+    col = None if color is None else np.ascontiguousarray(color, np.float32)
+    n = L.orc_dr_grid_sbs(brick_count, brick_size, C.cast(C.pointer(d), VP), _p(col), C.byref(hdr), C.byref(pn),
+                          C.byref(pv), C.byref(nv), C.byref(pp), C.byref(npar))
+    nodes = np.ctypeslib.as_array(C.cast(pn, C.POINTER(C.c_uint32)), (n * 4,)).copy().reshape(-1, 4)
+    values = np.ctypeslib.as_array(C.cast(pv, C.POINTER(C.c_uint32)), (nv.value,)).copy()
+    params = np.ctypeslib.as_array(C.cast(pp, C.POINTER(C.c_float)), (npar.value,)).copy()
+    for q in (pn, pv, pp):
+        L.orc_free(q)
+    return hdr, nodes, values, params
+
+
+class DrScene:
+    """An indexed SBS (ID32F_IRGB32F or _IN layout) with its BVH2 and one identity instance."""
+
+    def __init__(self, hdr, nodes, values, n_params, pairs=None, need_normal=True):
+        s = DrScene_()
+        nodes = np.ascontiguousarray(nodes, np.uint32).reshape(-1, 4)
+        values = np.ascontiguousarray(values, np.uint32)
+        if pairs is None:
+            pairs = bvh2_build(node_boxes(nodes), 1)[0]
+        pairs = np.ascontiguousarray(pairs)
+        self.keep = [nodes, values, pairs]
+        s.hdr = SbsHeader(hdr.brick_size, hdr.brick_pad, hdr.bytes_per_value, hdr.aux_data)
+        s.nodes, s.n_nodes, s.values, s.n_values = _p(nodes), nodes.shape[0], _p(values), values.size
+        s.n_params = n_params
+        s.pairs, s.n_pairs = _p(pairs), pairs.nbytes // 64
+        s.inst_bmin[:] = [-1.0, -1.0, -1.0]
+        s.inst_bmax[:] = [1.0, 1.0, 1.0]
+        s.inst_inv[:] = np.eye(4, dtype=np.float32).reshape(16).tolist()
+        s.need_normal = 1 if need_normal else 0
+        self.s = s
+        self.pairs = pairs
+
+    def query(self, params, flags, pos_near, dir_far):
+        P = np.ascontiguousarray(params, np.float32)
+        pos = np.ascontiguousarray(pos_near, np.float32).reshape(-1, 4)
+        dr = np.ascontiguousarray(dir_far, np.float32).reshape(-1, 4)
+        out = np.zeros(pos.shape[0], RECORD_DTYPE)
+        _lib().orc_dr_query(C.byref(self.s), _p(P), flags, _p(pos), _p(dr), pos.shape[0], _p(out))
+        return out
+
+    def render(self, params, preset, view, image_ref, threads=0):
+        P = np.ascontiguousarray(params, np.float32)
+        n = view.width * view.height
+        ref = np.ascontiguousarray(image_ref, np.float32).reshape(n, 4)
+        img = np.zeros((n, 4), np.float32)
+        dep = np.zeros(n, np.float32)
+        grad = np.zeros(P.size, np.float32)
+        border = np.zeros(n, np.uint8)
+        loss = _lib().orc_dr_render(C.byref(self.s), _p(P), C.byref(preset), C.byref(view), _p(ref), _p(img), _p(dep),
+                                    _p(grad), _p(border), threads)
+        return dict(loss=loss, image=img, depth=dep, grad=grad, border=border.astype(bool))
+
+    def loss_f64(self, params_d, preset, view, image_ref):
+        P = np.ascontiguousarray(params_d, np.float64)
+        n = view.width * view.height
+        ref = np.ascontiguousarray(image_ref, np.float32).reshape(n, 4)
+        hc = np.zeros(n, np.uint8)
+        loss = _lib().orc_dr_loss_f64(C.byref(self.s), _p(P), C.byref(preset), C.byref(view), _p(ref), _p(hc))
+        return loss, hc
+
+    def step(self, params, preset, views, images, it, adam_state, threads=0):
+        """One OptimizeFixedStructure iteration; params and adam_state are updated in place."""
+        assert params.dtype == np.float32 and params.flags.c_contiguous
+        assert adam_state.dtype == np.float32 and adam_state.size == 2 * params.size
+        nv = len(views)
+        va = (DrView * nv)(*views)
+        imgs = np.ascontiguousarray(np.concatenate([np.asarray(i, np.float32).reshape(-1, 4) for i in images]))
+        grad = np.zeros(params.size, np.float32)
+        losses = np.zeros(nv, np.float64)
+        out_imgs = np.zeros_like(imgs)
+        _lib().orc_dr_step(C.byref(self.s), _p(params), C.byref(preset), C.cast(va, VP), _p(imgs), nv, it,
+                           _p(adam_state), _p(grad), _p(losses), _p(out_imgs), threads)
+        return dict(grad=grad, losses=losses, images=out_imgs)
+
+
+def adam(it, g, x, state, lr, b1=0.9, b2=0.999, eps=1e-8):
+    g = np.ascontiguousarray(g, np.float32)
+    _lib().orc_dr_adam(it, _p(g), _p(x), _p(state), x.size, lr, b1, b2, eps)

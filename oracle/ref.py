@@ -1,5 +1,6 @@
 """ctypes binding of oracle/_ref/libref_bvh.so: the reference's own
-BVHRT::RayQuery_NearestHit and eye-ray code compiled in place (see
+BVHRT::RayQuery_NearestHit, dr::BVHDR::RayQuery_NearestHitWithGrad and
+eye-ray code compiled in place (see
 oracle/build_ref.py).  Test infrastructure: used to pin the oracle and to
 generate tests/golden/ fixtures.  Available only where the reference tree is.
 """
@@ -37,6 +38,7 @@ def lib():
         L.ref_free.argtypes = [VP]
         L.ref_query.argtypes = [VP, VP, VP, C.c_uint32, VP]
         L.ref_eye_rays.argtypes = [C.c_uint32, C.c_uint32, VP, VP, VP, C.c_uint32, C.c_float, C.c_float, VP, VP]
+        L.ref_dr_query.argtypes = [VP, C.c_uint32, VP, VP, C.c_uint32, VP]
         _lib = L
     return _lib
 
@@ -83,6 +85,15 @@ class RefScene:
         dr = np.ascontiguousarray(dir_far, np.float32).reshape(-1, 4)
         out = np.zeros(pos.shape[0], HIT_DTYPE)
         lib().ref_query(self.h, _p(pos), _p(dr), pos.shape[0], _p(out))
+        return out
+
+    def dr_query(self, flags, pos_near, dir_far):
+        """dr::BVHDR::RayQuery_NearestHitWithGrad records (oracle.oracle_dr.RECORD_DTYPE)."""
+        from .oracle_dr import RECORD_DTYPE
+        pos = np.ascontiguousarray(pos_near, np.float32).reshape(-1, 4)
+        dr = np.ascontiguousarray(dir_far, np.float32).reshape(-1, 4)
+        out = np.zeros(pos.shape[0], RECORD_DTYPE)
+        lib().ref_dr_query(self.h, flags, _p(pos), _p(dr), pos.shape[0], _p(out))
         return out
 
     def __del__(self):

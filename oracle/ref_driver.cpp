@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "BVH/BVH2Common.h"
+#include "diff_render/BVH2DR.h"
 #include "render_common.h"
 
 // ---- off-path members of BVHRT (BVH/BVH2Common_host.cpp), stubbed ----
@@ -30,7 +31,7 @@ void BVHRT::AppendTreeData(const std::vector<BVHNodePair> &, const std::vector<u
 
 namespace {
 struct RefScene {
-  BVHRT rt{"", ""};
+  dr::BVHDR rt;   // BVHDR adds only non-virtual gradient queries to BVHRT
 };
 
 template <typename T>
@@ -144,6 +145,53 @@ void ref_query(void *p, const float *pos_near, const float *dir_far, uint32_t n,
   for (uint32_t i = 0; i < n; i++) {
     const float *a = pos_near + 4 * size_t(i), *b = dir_far + 4 * size_t(i);
     out[i] = rt.RayQuery_NearestHit(float4(a[0], a[1], a[2], a[3]), float4(b[0], b[1], b[2], b[3]));
+  }
+}
+
+// dr::BVHDR::RayQuery_NearestHitWithGrad (diff_render/BVH2DR.cpp:12-102) on n
+// rays with the given DR_RAY_FLAG_* bits.  Each ray writes one flat record of
+// 576 32-bit words: [0,14) the hit, [14,28) payload.missed_hit (each as t,
+// primId, instId, geomId, color.xyz, sdf, normal.xyz, check_vox_border),
+// [28,36) missed_indices, [36,44) missed_dSDF_dtheta, [44,60) dDiffuse_dSc as
+// (index, value) pairs, [60,572) dDiffuseNormal_dSd as (dDiffuse.xyz, index,
+// dNorm.xyz, dDist), [572,576) zero.
+static void put_hit(uint32_t *o, const dr::CRT_HitDR &h) {
+  std::memcpy(o + 0, &h.t, 4);
+  o[1] = h.primId; o[2] = h.instId; o[3] = h.geomId;
+  std::memcpy(o + 4, &h.color.x, 4); std::memcpy(o + 5, &h.color.y, 4); std::memcpy(o + 6, &h.color.z, 4);
+  std::memcpy(o + 7, &h.sdf, 4);
+  std::memcpy(o + 8, &h.normal.x, 4); std::memcpy(o + 9, &h.normal.y, 4); std::memcpy(o + 10, &h.normal.z, 4);
+  o[11] = h.check_vox_border;
+  o[12] = o[13] = 0;
+}
+
+void ref_dr_query(void *p, uint32_t ray_flags, const float *pos_near, const float *dir_far, uint32_t n,
+                  uint32_t *out) {
+  dr::BVHDR &rt = static_cast<RefScene *>(p)->rt;
+  for (uint32_t i = 0; i < n; i++) {
+    const float *a = pos_near + 4 * size_t(i), *b = dir_far + 4 * size_t(i);
+    dr::RayDiffPayload pl;
+    std::memset(&pl, 0, sizeof(pl));
+    const dr::CRT_HitDR h = rt.RayQuery_NearestHitWithGrad(ray_flags, float4(a[0], a[1], a[2], a[3]),
+                                                           float4(b[0], b[1], b[2], b[3]), &pl);
+    uint32_t *o = out + 576 * size_t(i);
+    std::memset(o, 0, 576 * 4);
+    put_hit(o, h);
+    put_hit(o + 14, pl.missed_hit);
+    for (int k = 0; k < 8; k++) {
+      o[28 + k] = pl.missed_indices[k];
+      std::memcpy(o + 36 + k, &pl.missed_dSDF_dtheta[k], 4);
+      o[44 + 2 * k] = pl.dDiffuse_dSc[k].index;
+      std::memcpy(o + 45 + 2 * k, &pl.dDiffuse_dSc[k].value, 4);
+    }
+    for (int k = 0; k < 64; k++) {
+      const dr::PDDist &d = pl.dDiffuseNormal_dSd[k];
+      uint32_t *q = o + 60 + 8 * k;
+      std::memcpy(q + 0, &d.dDiffuse.x, 4); std::memcpy(q + 1, &d.dDiffuse.y, 4); std::memcpy(q + 2, &d.dDiffuse.z, 4);
+      q[3] = d.index;
+      std::memcpy(q + 4, &d.dNorm.x, 4); std::memcpy(q + 5, &d.dNorm.y, 4); std::memcpy(q + 6, &d.dNorm.z, 4);
+      std::memcpy(q + 7, &d.dDist, 4);
+    }
   }
 }
 

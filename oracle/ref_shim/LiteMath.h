@@ -171,6 +171,17 @@ struct float3x3 {
   float operator()(int r, int c) const { return row[r][c]; }
 };
 static inline float3 operator*(const float3x3 &m, float3 v) { return float3(dot(m.row[0], v), dot(m.row[1], v), dot(m.row[2], v)); }
+static inline float3x3 make_float3x3(float3 r0, float3 r1, float3 r2) {
+  float3x3 m; m.row[0] = r0; m.row[1] = r1; m.row[2] = r2; return m;
+}
+static inline float3x3 make_float3x3_by_columns(float3 c0, float3 c1, float3 c2) {
+  float3x3 m;
+  m.row[0] = float3(c0.x, c1.x, c2.x); m.row[1] = float3(c0.y, c1.y, c2.y); m.row[2] = float3(c0.z, c1.z, c2.z);
+  return m;
+}
+static inline float3x3 &operator+=(float3x3 &a, const float3x3 &b) {
+  a.row[0] += b.row[0]; a.row[1] += b.row[1]; a.row[2] += b.row[2]; return a;
+}
 
 struct float4x4 {
   float m[16];   // row-major
