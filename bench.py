@@ -44,6 +44,9 @@ def parse():
     ap.add_argument("--variant", type=int, default=0, help="render kernel: 0 per-lane rays, 1 warp packet")
     ap.add_argument("--block-warps", type=int, default=4)
     ap.add_argument("--stage", type=int, default=0, help="packet kernel: stage bricks in shared memory")
+    ap.add_argument("--no-dr", action="store_true", help="skip the differentiable-render measurement")
+    ap.add_argument("--dr-iters", type=int, default=200, help="reconstruction iterations (the first 10 untimed)")
+    ap.add_argument("--dr-aggregate", type=int, default=1, help="warp-aggregated gradient atomics")
     return ap.parse_args()
 
 
@@ -142,6 +145,114 @@ def run_cpu_baseline(h, nodes, values, views, pairs, seconds):
     n = int(min(total, max(20000, 20000 * seconds / max(t0, 1e-3))))
     rays, dt, cnt = run(n)
     return dict(value=rays / dt / 1e6, rays=rays, seconds=dt, cores=cores, counters=cnt)
+
+
+def dr_setup(dev_index=0):
+    """Differentiable reconstruction workload: target images rendered by the DR
+    forward from the 256^3 target grid; the 128^3 sphere-initialised grid to optimise."""
+    from litert_gb300 import dr, scenes
+    t0 = time.time()
+    target, init, views = scenes.dr_workload()
+    R = dr.MultiRendererDR(dev_index)
+    R.SetScene(*target)
+    R.SetPreset(dr.default_preset(reconstruction_flags=0, border_spp=0))
+    R.SetReference([np.zeros((v[1], v[0], 4), np.float32) for v in views], [v[2] for v in views],
+                   [v[3] for v in views])
+    imgs = []
+    for i in range(len(views)):
+        R.render_grad(i)
+        imgs.append(R.getLastImage(i).copy())
+    R.SetScene(*init)
+    R.SetReference(imgs, [v[2] for v in views], [v[3] for v in views])
+    return R, init, views, imgs, time.time() - t0
+
+
+def dr_preset(aggregate=1):
+    from litert_gb300 import dr
+    # Lambert, colour + geometry, spp 1, border_spp 256, Adam lr 3e-3; the batch's
+    # gradients are summed (the reference keeps only the last view's: same work)
+    return dr.default_preset(opt_lr=3e-3, spp=1, border_spp=256, seed=1, accumulate_batch=1,
+                             warp_aggregate=aggregate)
+
+
+def run_dr_cpu(R, init, views, imgs, preset, seconds_hint=True):
+    """The oracle port of RenderDR (all host threads) on one of the views: the CPU
+    time of one reconstruction iteration is 8x that (Adam is negligible)."""
+    from litert_gb300 import lrt
+    from oracle import oracle as orc
+    from oracle import oracle_dr as od
+    hdr, nodes, values, params = init
+    osc = od.DrScene(orc.SbsHeader(hdr.brick_size, hdr.brick_pad, hdr.bytes_per_value, hdr.aux_data), nodes, values,
+                     params.size, pairs=R.bvh2())
+    lights = [(preset.lights[i].type, np.array(preset.lights[i].dir[:], np.float32),
+               np.array(preset.lights[i].color[:], np.float32)) for i in range(preset.n_lights)]
+    op = od.make_preset(render_mode=preset.render_mode, reconstruction=preset.reconstruction_flags, spp=preset.spp,
+                        border_spp=preset.border_spp, seed=preset.seed, lights=lights, lr=preset.opt_lr)
+    w, h, wv, pj = views[0]
+    ov = od.make_view(w, h, wv, pj, lrt.inverse4x4)
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    osc.render(params, op, ov, imgs[0], threads=cores)
+    dt = time.perf_counter() - t0
+    return dict(ms_per_iter=dt * len(views) * 1e3, cores=cores, seconds=dt)
+
+
+def run_dr(args, dev, torch):
+    """Differentiable SDF reconstruction: ms per OptimizeFixedStructure iteration
+    (8 views at 512^2: forward + adjoint + border integral + Adam), device-timed."""
+    R, init, views, imgs, t_setup = dr_setup(dev.index)
+    preset = dr_preset(args.dr_aggregate)
+    R.SetPreset(preset)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    warm = min(10, max(3, args.dr_iters // 10))
+    first_losses = R.step(0)
+    for i in range(1, warm):
+        R.step(i, want_losses=False)
+    torch.cuda.synchronize(dev)
+    n_timed = max(1, args.dr_iters - warm)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n_timed)]
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    launches = 0
+    for k in range(n_timed):
+        flush.fill_(float(k))
+        evs[k][0].record(stream)
+        R.step(warm + k, want_losses=False)
+        evs[k][1].record(stream)
+        launches += R.last_launch_count()
+    torch.cuda.synchronize(dev)
+    clk = clocks.stop()
+    times = sorted(a.elapsed_time(b) for a, b in evs)
+    ms = statistics.median(times)
+    # end to end: the C-ABI step with the per-view losses read back to the host
+    e2e = []
+    for k in range(5):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        last_losses = R.step(warm + n_timed + k)
+        e2e.append((time.perf_counter() - t0) * 1e3)
+    out = {"metric": "DR backward ms/iter", "value": ms, "unit": "ms/iter", "higher_is_better": False,
+           "mean_ms": sum(times) / len(times), "min_ms": times[0], "max_ms": times[-1],
+           "iterations": warm + n_timed + 5, "timed_iterations": n_timed, "gpu_launches": launches,
+           "launches_per_iter": launches / n_timed,
+           "e2e": {"value": statistics.median(e2e), "unit": "ms/iter", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 8 * len(views)},
+           "loss_first": float(np.mean(first_losses)), "loss_last": float(np.mean(last_losses)),
+           "config": {"workload": "dr-reconstruction-8view", "views": len(views), "size": 512,
+                      "target": "smooth-union grid 32^3 bricks x 8 voxels, position colours",
+                      "optimised": "grid 32^3 bricks x 4 voxels (129^3 distances + 33^3 RGB)",
+                      "params": int(init[3].size), "render_mode": "LAMBERT", "spp": 1, "border_spp": 256,
+                      "adam_lr": 3e-3, "batch": "8 views summed", "warp_aggregate": args.dr_aggregate,
+                      "l2": "256 MiB write between timed iterations", "setup_s": round(t_setup, 2)},
+           "clocks": clk}
+    if not args.no_cpu_baseline:
+        cpu = run_dr_cpu(R, [init[0], init[1], init[2], R.get(0)], views, imgs, preset)
+        out["cpu_baseline"] = {"value": cpu["ms_per_iter"], "unit": "ms/iter", "cores": cpu["cores"], "kind": "port",
+                               "sample": f"RenderDR of 1 of the 8 views on the current parameters "
+                                         f"({cpu['seconds']:.1f} s), x8"}
+    R.close()
+    return out
 
 
 def main():
@@ -294,6 +405,8 @@ def main():
         if cpu:
             line["cpu_baseline"] = {"value": cpu["value"], "unit": UNIT, "cores": cpu["cores"], "kind": "port",
                                     "sample": f"{cpu['rays']} strided pixels of the 16 views ({cpu['seconds']:.1f} s)"}
+        if not args.no_dr and world == 1:
+            line["dr"] = run_dr(args, dev, torch)
         print(json.dumps(line))
     scene.close()
     if world > 1:

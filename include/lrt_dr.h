@@ -1,0 +1,118 @@
+/*
+ * lrt — differentiable SDF render (MultiRendererDR), C ABI.
+ *
+ * Replaces dr::MultiRendererDR (diff_render/MultiRendererDR.h:71-155) for
+ * indexed sparse-brick sets (SDF_SBS_NODE_LAYOUT_ID32F_IRGB32F and _IN): the
+ * parameters are the SBS's float array (values_f: distances, then RGB colours)
+ * and every call works on the context's device.  Conventions as lrt_gpu.h:
+ * plain pointers and sizes, an lrt_status per call, lrt_last_error(ctx) for a
+ * message.  The gradient, images and parameters stay in device memory between
+ * calls; lrt_dr_get copies them out.
+ */
+#ifndef LRT_DR_H
+#define LRT_DR_H
+#include "lrt_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* DR_RENDER_MODE_*, diff_render/DR_common.h:83-88 */
+enum { LRT_DR_RENDER_DIFFUSE = 0, LRT_DR_RENDER_LAMBERT = 1, LRT_DR_RENDER_MASK = 2,
+       LRT_DR_RENDER_LINEAR_DEPTH = 3, LRT_DR_RENDER_NORMAL = 4 };
+/* DR_RECONSTRUCTION_FLAG_*, diff_render/DR_common.h:112-113 */
+enum { LRT_DR_RECON_COLOR = 1, LRT_DR_RECON_GEOMETRY = 2 };
+/* light types, Renderer/eye_ray.h:44-46 (point lights are not supported by the reference DR) */
+enum { LRT_DR_LIGHT_DIRECT = 0, LRT_DR_LIGHT_AMBIENT = 2 };
+
+/* Light (create_direct_light / create_ambient_light, Renderer/eye_ray.h:60-74):
+ * dir is used as given (the reference normalises it on creation). */
+typedef struct { uint32_t type; float dir[3]; float color[3]; } lrt_dr_light;
+
+/* The MultiRendererDRPreset fields this path reads (diff_render/DR_common.h:134-196),
+ * the renderer's seed and lights, and the Adam settings.  The finder is NEWTON,
+ * ray generation RANDOM and normals SDF_SMOOTHED, as OptimizeFixedStructure
+ * forces (diff_render/MultiRendererDR.cpp:324-326). */
+typedef struct {
+  uint32_t render_mode;          /* LRT_DR_RENDER_* */
+  uint32_t reconstruction_flags; /* LRT_DR_RECON_* */
+  uint32_t input_type;           /* 0 colour images, 1 linear depth */
+  uint32_t loss_function;        /* 0 MSE, 1 MAE */
+  uint32_t spp;                  /* 1..64 */
+  uint32_t border_spp;           /* rays per border pixel (0 = no border integral) */
+  float border_relax_eps;
+  uint32_t seed;                 /* MultiRenderer::setSeed */
+  uint32_t n_lights;             /* 0..4 */
+  lrt_dr_light lights[4];
+  float opt_lr, opt_beta_1, opt_beta_2, opt_eps;
+  /* 0: the reference's batch behaviour (its per-thread gradient buffer is
+   * refilled for every image of a batch, so only the last image's gradient
+   * reaches Adam, divided by the batch size); 1: the batch's gradients are summed */
+  uint32_t accumulate_batch;
+  /* 1: warp-aggregated gradient atomics (default), 0: one atomic per contribution */
+  uint32_t warp_aggregate;
+} lrt_dr_preset;
+
+/* getDefaultPresetDR (diff_render/MultiRendererDR.h:12-66) with the colour+geometry
+ * Lambert reconstruction and MultiRenderer's default lights (Renderer/eye_ray_host.cpp:40). */
+void lrt_dr_default_preset(lrt_dr_preset *p);
+
+/* MultiRendererDR::SetScene for OptimizeFixedStructure (diff_render/MultiRendererDR.cpp:353-355):
+ * the indexed SBS (copied to the device) and its BVH2, built by the project's
+ * builder unless `pairs` is given (n_pairs fat pairs, root at 0). */
+lrt_status lrt_dr_set_scene(lrt_ctx *ctx, const lrt_sbs_header *hdr, const lrt_sbs_node *nodes, uint32_t n_nodes,
+                            const uint32_t *values, uint64_t n_values, const float *params, uint32_t n_params,
+                            const lrt_bvh_pair *pairs, uint32_t n_pairs);
+/* The BVH2 in use (host copy owned by ctx). */
+lrt_status lrt_dr_get_bvh2(lrt_ctx *ctx, const lrt_bvh_pair **pairs, uint32_t *n_pairs);
+
+/* MultiRendererDR::SetReference (diff_render/MultiRendererDR.cpp:147-160): target
+ * images (float RGBA, row-major, view after view) and their cameras.  Resets the
+ * optimiser state. */
+lrt_status lrt_dr_set_reference(lrt_ctx *ctx, uint32_t n_views, const lrt_view *views, const float *images);
+
+lrt_status lrt_dr_set_preset(lrt_ctx *ctx, const lrt_dr_preset *preset);
+
+/* Replaces the parameters (values_f) and resets the optimiser state. */
+lrt_status lrt_dr_set_params(lrt_ctx *ctx, const float *params, uint32_t n_params);
+
+/* MultiRendererDR::RenderDR for one view (diff_render/MultiRendererDR.cpp:578-750):
+ * renders it, computes dLoss/dparams (interior + border integral, scaled by
+ * getBaseGradientMult) into the gradient buffer (overwritten) and returns the
+ * mean pixel loss.  Asynchronous on the context's stream except for *loss. */
+lrt_status lrt_dr_render_grad(lrt_ctx *ctx, uint32_t view, double *loss);
+
+/* One iteration of OptimizeFixedStructure (diff_render/MultiRendererDR.cpp:390-486):
+ * every view renders with gradients (batch = all views, in order), the batch
+ * gradient is divided by the batch size and OptimizeStepAdam updates the
+ * parameters.  losses (n_views) may be NULL; when given the call waits for them. */
+lrt_status lrt_dr_step(lrt_ctx *ctx, uint32_t iter, double *losses);
+
+/* OptimizeFixedStructure: `iterations` steps from iteration `first_iter` (Adam's
+ * bias correction uses the iteration number); the parameters stay on the device. */
+lrt_status lrt_dr_optimize(lrt_ctx *ctx, uint32_t first_iter, uint32_t iterations, double *last_losses);
+
+/* Copies out device state.  what: LRT_DR_PARAMS (n_params floats),
+ * LRT_DR_GRAD (n_params floats, the last gradient before Adam's batch division),
+ * LRT_DR_IMAGE (view's W*H float4 = getLastImage), LRT_DR_DEPTH (W*H floats,
+ * depth-discontinuity thresholds), LRT_DR_BORDER (W*H bytes, border-pixel mask),
+ * LRT_DR_ADAM (2*n_params floats: first then second moments).  bytes must match. */
+enum { LRT_DR_PARAMS = 0, LRT_DR_GRAD = 1, LRT_DR_IMAGE = 2, LRT_DR_DEPTH = 3, LRT_DR_BORDER = 4, LRT_DR_ADAM = 5 };
+lrt_status lrt_dr_get(lrt_ctx *ctx, uint32_t what, uint32_t view, void *out, uint64_t bytes);
+
+/* Number of kernel launches of the last lrt_dr_render_grad / lrt_dr_step call. */
+uint32_t lrt_dr_last_launch_count(const lrt_ctx *ctx);
+
+/* create_grid_sbs (diff_render/DR_common.cpp:47-146) followed by
+ * SBS_ind_to_SBS_ind_with_neighbors (utils/sparse_octree_builder.cpp:2761-2850):
+ * a dense brick_count^3 grid of brick_size^3 bricks over [-1,1]^3 in the
+ * ID32F_IRGB32F_IN layout, distances from `sdf`, colours constant (color3) or,
+ * with color3 NULL, 0.5 + 0.5 p.  Host only; arrays malloc'd, free with lrt_free. */
+lrt_status lrt_dr_grid_sbs(uint32_t brick_count, uint32_t brick_size, const lrt_sdf_desc *sdf, const float *color3,
+                           lrt_sbs_header *hdr, lrt_sbs_node **nodes, uint32_t *n_nodes, uint32_t **values,
+                           uint64_t *n_values, float **params, uint32_t *n_params);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,113 @@
+// Host-side context of the C ABI (lrt_ctx) and its helpers, shared by the
+// ray-query driver (lrt_api.cpp) and the differentiable-render driver
+// (dr_api.cpp).  Host code only.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "lrt_internal.h"
+
+namespace lrt {
+struct DrState;
+void dr_state_free(DrState *st);
+}  // namespace lrt
+
+namespace lrt {
+
+struct Geom {
+  uint32_t type = 0;
+  SbsData sbs;
+  std::vector<float> values_f;
+  std::vector<lrt_svs_node> svs;
+  std::vector<float> vpos;        // float4 per vertex
+  std::vector<uint32_t> indices;  // 3 per triangle
+  float bmin[3] = {-1, -1, -1}, bmax[3] = {1, 1, 1};
+};
+
+struct Inst {
+  uint32_t geom = 0;
+  float m[16], inv[16], inv_t[16];
+  float bmin[3], bmax[3];
+};
+
+template <typename T>
+struct DevBuf {
+  T *p = nullptr;
+  size_t cap = 0;  // elements
+  cudaError_t ensure(size_t n) {
+    if (n <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T));
+    if (e == cudaSuccess) cap = n;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+}  // namespace lrt
+
+using namespace lrt;   // internal header: the context is built from lrt:: types
+
+struct lrt_ctx {
+  int device = 0;
+  int num_sms = 0;
+  std::string err;
+  std::vector<Geom> geoms;
+  std::vector<Inst> insts;
+  lrt_preset preset{};
+  bool committed = false;
+  DevScene dev{};
+  BvhData bvh;
+  // committed scene buffers
+  DevBuf<WNode4> d_nodes;
+  DevBuf<lrt_sbs_node> d_bricks;
+  DevBuf<float4> d_leaf_boxes;
+  DevBuf<uint32_t> d_occ;
+  DevBuf<uint32_t> d_values;
+  DevBuf<float> d_values_f;
+  DevBuf<lrt_svs_node> d_svs;
+  DevBuf<float4> d_tri_verts;
+  DevBuf<uint32_t> d_prim_indices;
+  // per-call scratch
+  DevBuf<uint32_t> d_tile_counter;
+  DevBuf<DevView> d_views;
+  DevBuf<unsigned long long> d_counters;
+  DevView *h_views = nullptr;  // pinned staging for view uploads
+  size_t h_views_cap = 0;
+  // host-buffer entry points
+  DevBuf<lrt_hit16> d_out_hits;
+  DevBuf<float4> d_out_rgba;
+  DevBuf<uint32_t> d_out_rgba8;
+  DevBuf<float4> d_q_pos, d_q_dir;
+  DevBuf<lrt_hit> d_q_out;
+  uint32_t last_launches = 0;
+  uint32_t brick_stride = 0;   // device words per brick (16-byte multiple)
+  Tuning tuning;
+  lrt::DrState *dr = nullptr;  // differentiable-render state (dr_api.cpp)
+};
+
+static inline lrt_status fail(lrt_ctx *ctx, lrt_status s, const std::string &msg) {
+  if (ctx) ctx->err = msg;
+  return s;
+}
+
+static inline lrt_status cuda_fail(lrt_ctx *ctx, cudaError_t e, const char *where) {
+  return fail(ctx, e == cudaErrorMemoryAllocation ? LRT_ERR_OOM : LRT_ERR_CUDA,
+              std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define LRT_CUDA(ctx, call)                                   \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call);  \
+  } while (0)
+

@@ -1,0 +1,562 @@
+// C ABI of the differentiable SDF render (dr::MultiRendererDR replacement):
+// scene / reference / preset staging, per-view gradient rendering, the
+// OptimizeFixedStructure iteration with Adam, and the create_grid_sbs fixture.
+// Host code only; kernels live in dr.cu.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "ctx_internal.h"
+#include "dr_internal.h"
+#include "lrt_dr.h"
+
+namespace lrt {
+
+struct DrState {
+  lrt_sbs_header hdr{};
+  uint32_t n_nodes = 0, n_params = 0;
+  uint64_t n_values = 0;
+  std::vector<lrt_bvh_pair> pairs;
+  DevBuf<uint4> d_nodes;
+  DevBuf<uint32_t> d_values;
+  DevBuf<float> d_params, d_grad, d_adam;
+  DevBuf<float4> d_pairs;
+  // views
+  std::vector<lrt_view> views;
+  std::vector<size_t> off;     // pixel offset of each view
+  size_t n_pix = 0, max_view_pix = 0;
+  DevBuf<float4> d_ref, d_img;
+  DevBuf<float> d_depth;
+  DevBuf<uint8_t> d_border_mask;
+  DevBuf<uint32_t> d_border_list, d_border_count, d_status;
+  DevBuf<double> d_loss;
+  lrt_dr_preset preset{};
+  bool has_scene = false, has_ref = false;
+  uint32_t last_launches = 0;
+};
+
+void dr_state_free(DrState *st) {
+  if (!st) return;
+  for (auto *b : {&st->d_params, &st->d_grad, &st->d_adam}) b->release();
+  st->d_nodes.release();
+  st->d_values.release();
+  st->d_pairs.release();
+  st->d_ref.release();
+  st->d_img.release();
+  st->d_depth.release();
+  st->d_border_mask.release();
+  st->d_border_list.release();
+  st->d_border_count.release();
+  st->d_status.release();
+  st->d_loss.release();
+  delete st;
+}
+
+}  // namespace lrt
+
+namespace {
+
+lrt_status ensure_state(lrt_ctx *ctx) {
+  if (!ctx) return LRT_ERR_INVALID;
+  if (!ctx->dr) {
+    ctx->dr = new (std::nothrow) DrState();
+    if (!ctx->dr) return fail(ctx, LRT_ERR_OOM, "DR state allocation failed");
+    lrt_dr_default_preset(&ctx->dr->preset);
+  }
+  return LRT_OK;
+}
+
+template <typename T>
+cudaError_t upload(DevBuf<T> &b, const T *h, size_t n) {
+  cudaError_t e = b.ensure(n);
+  if (e != cudaSuccess) return e;
+  return cudaMemcpy(b.p, h, n * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+// m_proj * m_worldView (TransformWorldToScreenSpace, diff_render/MultiRendererDR.cpp:1296-1301)
+void mat4_mul(const float *a, const float *b, float *r) {
+  for (int i = 0; i < 4; i++)
+    for (int j = 0; j < 4; j++)
+      r[i * 4 + j] = a[i * 4 + 0] * b[0 * 4 + j] + a[i * 4 + 1] * b[1 * 4 + j] + a[i * 4 + 2] * b[2 * 4 + j] +
+                     a[i * 4 + 3] * b[3 * 4 + j];
+}
+
+// ray flags of CastRayWithGrad (diff_render/MultiRendererDR.cpp:1113-1140)
+uint32_t pixel_flags(const lrt_dr_preset &p) {
+  if (p.input_type == 1) return 16u;
+  uint32_t f = 0;
+  if (p.reconstruction_flags & LRT_DR_RECON_COLOR) f |= 1u;
+  if (p.reconstruction_flags & LRT_DR_RECON_GEOMETRY) {
+    if (p.render_mode == LRT_DR_RENDER_DIFFUSE) f |= 2u;
+    else if (p.render_mode == LRT_DR_RENDER_LAMBERT) f |= 2u | 4u;
+    else if (p.render_mode == LRT_DR_RENDER_NORMAL) f |= 4u;
+  }
+  return f;
+}
+
+// BVHRT::need_normal of the MultiRenderer mode the DR mode maps to
+// (diff_render/MultiRendererDR.cpp:98-116, BVH/BVH2Common.cpp:20-27)
+bool dr_need_normal(uint32_t render_mode) {
+  return render_mode == LRT_DR_RENDER_LAMBERT || render_mode == LRT_DR_RENDER_NORMAL;
+}
+
+drk::DevScene dev_scene(lrt_ctx *ctx) {
+  DrState &st = *ctx->dr;
+  drk::DevScene s{};
+  s.nodes = st.d_nodes.p;
+  s.values = st.d_values.p;
+  s.P = st.d_params.p;
+  s.grad = st.d_grad.p;
+  s.pairs = st.d_pairs.p;
+  s.n_pairs = uint32_t(st.pairs.size());
+  s.brick_size = st.hdr.brick_size;
+  s.v_size = st.hdr.brick_size + 2 * st.hdr.brick_pad + 1;
+  s.layout_in = (st.hdr.aux_data & 0xFF000000u) == (5u << 24) ? 1u : 0u;
+  s.need_normal = dr_need_normal(st.preset.render_mode) ? 1u : 0u;
+  for (int k = 0; k < 3; k++) { s.inst_bmin[k] = -1.0f; s.inst_bmax[k] = 1.0f; }
+  const float id[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+  std::memcpy(s.inst_inv, id, sizeof(id));
+  s.status = st.d_status.p;
+  return s;
+}
+
+drk::DevPreset dev_preset(const DrState &st) {
+  const lrt_dr_preset &p = st.preset;
+  drk::DevPreset d{};
+  d.render_mode = p.render_mode;
+  d.recon = p.reconstruction_flags;
+  d.input_type = p.input_type;
+  d.loss_fn = p.loss_function;
+  d.spp = p.spp;
+  d.border_spp = p.border_spp;
+  d.seed = p.seed;
+  d.n_lights = p.n_lights;
+  d.relax_eps = p.border_relax_eps;
+  for (uint32_t i = 0; i < 4; i++) {
+    d.light_type[i] = p.lights[i].type;
+    for (int k = 0; k < 3; k++) { d.light_dir[i][k] = p.lights[i].dir[k]; d.light_col[i][k] = p.lights[i].color[k]; }
+  }
+  d.agg = p.warp_aggregate;
+  d.flags = pixel_flags(p);
+  return d;
+}
+
+drk::DevView dev_view(DrState &st, uint32_t v) {
+  const lrt_view &lv = st.views[v];
+  drk::DevView d{};
+  d.width = lv.width;
+  d.height = lv.height;
+  lrt_inverse4x4(lv.proj, d.proj_inv);
+  lrt_inverse4x4(lv.world_view, d.wv_inv);
+  mat4_mul(lv.proj, lv.world_view, d.pv);
+  d.ref = st.d_ref.p + st.off[v];
+  d.img = st.d_img.p + st.off[v];
+  d.depth = st.d_depth.p + st.off[v];
+  d.border_mask = st.d_border_mask.p + st.off[v];
+  d.border_list = st.d_border_list.p;
+  d.border_count = st.d_border_count.p + v;
+  d.loss = st.d_loss.p + v;
+  return d;
+}
+
+// RenderDR for view v, gradients added into d_grad (:578-750)
+lrt_status render_view(lrt_ctx *ctx, uint32_t v, cudaStream_t stream) {
+  DrState &st = *ctx->dr;
+  const drk::DevScene s = dev_scene(ctx);
+  drk::DevPreset p = dev_preset(st);
+  const drk::DevView dv = dev_view(st, v);
+  const uint32_t W = dv.width, H = dv.height;
+  p.g_mult = float(std::pow(st.n_params + 1.0, 2.0 / 3.0) / (double(W) * double(H)));   // getBaseGradientMult :140-145
+  LRT_CUDA(ctx, cudaMemsetAsync(dv.loss, 0, sizeof(double), stream));
+  LRT_CUDA(ctx, cudaMemsetAsync(dv.border_count, 0, sizeof(uint32_t), stream));
+  drk::launch_pixels(s, p, dv, stream);
+  drk::launch_border_detect(p, dv, stream);
+  st.last_launches += 2;
+  if ((st.preset.reconstruction_flags & LRT_DR_RECON_GEOMETRY) && st.preset.border_spp > 0) {
+    drk::launch_border(s, p, dv, W * H, ctx->num_sms, stream);
+    st.last_launches += 1;
+  }
+  LRT_CUDA(ctx, cudaGetLastError());
+  return LRT_OK;
+}
+
+lrt_status check_ready(lrt_ctx *ctx) {
+  if (!ctx || !ctx->dr || !ctx->dr->has_scene) return fail(ctx, LRT_ERR_STATE, "lrt_dr_set_scene first");
+  if (!ctx->dr->has_ref) return fail(ctx, LRT_ERR_STATE, "lrt_dr_set_reference first");
+  return LRT_OK;
+}
+
+lrt_status read_status(lrt_ctx *ctx) {
+  uint32_t status = 0;
+  LRT_CUDA(ctx, cudaMemcpy(&status, ctx->dr->d_status.p, 4, cudaMemcpyDeviceToHost));
+  if (status & drk::kStatusStackOverflow)
+    return fail(ctx, LRT_ERR_BOUNDS, "BVH traversal stack (80 entries, the reference's STACK_SIZE) overflowed");
+  if (status & drk::kStatusTraversalBound)
+    return fail(ctx, LRT_ERR_BOUNDS, "BVH traversal visited more nodes than the tree holds (malformed BVH)");
+  return LRT_OK;
+}
+
+}  // namespace
+
+extern "C" void lrt_dr_default_preset(lrt_dr_preset *p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->render_mode = LRT_DR_RENDER_LAMBERT;
+  p->reconstruction_flags = LRT_DR_RECON_COLOR | LRT_DR_RECON_GEOMETRY;
+  p->input_type = 0;
+  p->loss_function = 0;
+  p->spp = 1;
+  p->border_spp = 256;
+  p->border_relax_eps = 1e-3f;
+  p->seed = 1;
+  p->n_lights = 2;
+  const float inv = 1.0f / std::sqrt(3.0f);
+  p->lights[0] = lrt_dr_light{LRT_DR_LIGHT_DIRECT, {inv, inv, inv}, {2.0f / 3.0f, 2.0f / 3.0f, 2.0f / 3.0f}};
+  p->lights[1] = lrt_dr_light{LRT_DR_LIGHT_AMBIENT, {0, 0, 0}, {0.25f, 0.25f, 0.25f}};
+  p->opt_lr = 0.01f;
+  p->opt_beta_1 = 0.9f;
+  p->opt_beta_2 = 0.999f;
+  p->opt_eps = 1e-8f;
+  p->accumulate_batch = 0;
+  p->warp_aggregate = 1;
+}
+
+extern "C" lrt_status lrt_dr_set_scene(lrt_ctx *ctx, const lrt_sbs_header *hdr, const lrt_sbs_node *nodes,
+                                       uint32_t n_nodes, const uint32_t *values, uint64_t n_values,
+                                       const float *params, uint32_t n_params, const lrt_bvh_pair *pairs,
+                                       uint32_t n_pairs) {
+  lrt_status s = ensure_state(ctx);
+  if (s != LRT_OK) return s;
+  if (!hdr || !nodes || !values || !params || n_nodes == 0 || n_values == 0 || n_params == 0)
+    return fail(ctx, LRT_ERR_INVALID, "lrt_dr_set_scene: empty scene");
+  const uint32_t layout = hdr->aux_data & 0xFF000000u;
+  if (layout != (4u << 24) && layout != (5u << 24))
+    return fail(ctx, LRT_ERR_UNSUPPORTED, "DR needs the ID32F_IRGB32F or ID32F_IRGB32F_IN layout");
+  if (n_nodes > 0x00FFFFFFu) return fail(ctx, LRT_ERR_UNSUPPORTED, "more bricks than a BVH leaf can address");
+  const uint64_t v3 = uint64_t(hdr->brick_size + 2 * hdr->brick_pad + 1) * (hdr->brick_size + 2 * hdr->brick_pad + 1) *
+                      (hdr->brick_size + 2 * hdr->brick_pad + 1);
+  const uint64_t per = v3 + 8 + (layout == (5u << 24) ? 27 : 0);
+  // host-side bounds: every index the kernels follow must stay inside the arrays
+  for (uint32_t i = 0; i < n_nodes; i++) {
+    if (uint64_t(nodes[i].data_offset) + per > n_values)
+      return fail(ctx, LRT_ERR_BOUNDS, "node data_offset beyond the values array");
+    const uint32_t *b = values + nodes[i].data_offset;
+    for (uint64_t k = 0; k < v3; k++)
+      if (b[k] >= n_params) return fail(ctx, LRT_ERR_BOUNDS, "distance index beyond the parameters");
+    for (int k = 0; k < 8; k++)
+      if (uint64_t(b[v3 + k]) + 3 > n_params) return fail(ctx, LRT_ERR_BOUNDS, "colour index beyond the parameters");
+    if (layout == (5u << 24))
+      for (int k = 0; k < 27; k++)
+        if (b[v3 + 8 + k] != drk::kInvalidIdx && b[v3 + 8 + k] >= n_nodes)
+          return fail(ctx, LRT_ERR_BOUNDS, "neighbour index beyond the nodes");
+  }
+  DrState &st = *ctx->dr;
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  st.hdr = *hdr;
+  st.n_nodes = n_nodes;
+  st.n_values = n_values;
+  st.n_params = n_params;
+  if (pairs && n_pairs) {
+    st.pairs.assign(pairs, pairs + n_pairs);
+  } else {
+    std::vector<float> boxes(6 * size_t(n_nodes));
+    for (uint32_t i = 0; i < n_nodes; i++) {   // AddGeom_SdfSBS boxes, BVH/BVH2Common_host.cpp:640-653
+      const float px = float(nodes[i].pos_xy >> 16), py = float(nodes[i].pos_xy & 0xFFFF);
+      const float pz = float(nodes[i].pos_z_lod_size >> 16), sz = float(nodes[i].pos_z_lod_size & 0xFFFF);
+      const float lo[3] = {-1 + 2.0f * px / sz, -1 + 2.0f * py / sz, -1 + 2.0f * pz / sz};
+      for (int k = 0; k < 3; k++) {
+        boxes[6 * i + k] = lo[k];
+        boxes[6 * i + 3 + k] = lo[k] + 2.0f * 1 / sz;
+      }
+    }
+    BvhData b;
+    s = build_bvh(boxes.data(), n_nodes, true, b);
+    if (s != LRT_OK) return fail(ctx, s, "BVH build failed");
+    st.pairs.assign(reinterpret_cast<const lrt_bvh_pair *>(b.pairs.data()),
+                    reinterpret_cast<const lrt_bvh_pair *>(b.pairs.data()) + b.pairs.size());
+  }
+  // every child reference of the BVH2 must be a pair index or a leaf of a valid brick
+  for (const lrt_bvh_pair &p : st.pairs)
+    for (const lrt_bvh_node *c : {&p.left, &p.right}) {
+      const uint32_t o = c->leftOffset;
+      if (o == 0xFFFFFFFFu) continue;
+      if (o & 0x80000000u) {
+        if ((o & 0x00FFFFFFu) >= n_nodes) return fail(ctx, LRT_ERR_BOUNDS, "BVH leaf beyond the nodes");
+      } else if (o >= st.pairs.size()) {
+        return fail(ctx, LRT_ERR_BOUNDS, "BVH child beyond the pairs");
+      }
+    }
+  cudaError_t e;
+  if ((e = upload(st.d_nodes, reinterpret_cast<const uint4 *>(nodes), n_nodes)) != cudaSuccess)
+    return cuda_fail(ctx, e, "upload nodes");
+  if ((e = upload(st.d_values, values, size_t(n_values))) != cudaSuccess) return cuda_fail(ctx, e, "upload values");
+  if ((e = upload(st.d_params, params, n_params)) != cudaSuccess) return cuda_fail(ctx, e, "upload params");
+  if ((e = upload(st.d_pairs, reinterpret_cast<const float4 *>(st.pairs.data()), st.pairs.size() * 4)) != cudaSuccess)
+    return cuda_fail(ctx, e, "upload BVH");
+  LRT_CUDA(ctx, st.d_grad.ensure(n_params));
+  LRT_CUDA(ctx, st.d_adam.ensure(2 * size_t(n_params)));
+  LRT_CUDA(ctx, cudaMemset(st.d_grad.p, 0, sizeof(float) * n_params));
+  LRT_CUDA(ctx, cudaMemset(st.d_adam.p, 0, sizeof(float) * 2 * size_t(n_params)));
+  LRT_CUDA(ctx, st.d_status.ensure(1));
+  LRT_CUDA(ctx, cudaMemset(st.d_status.p, 0, 4));
+  st.has_scene = true;
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_dr_get_bvh2(lrt_ctx *ctx, const lrt_bvh_pair **pairs, uint32_t *n_pairs) {
+  if (!ctx || !ctx->dr || !ctx->dr->has_scene || !pairs || !n_pairs) return LRT_ERR_INVALID;
+  *pairs = ctx->dr->pairs.data();
+  *n_pairs = uint32_t(ctx->dr->pairs.size());
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_dr_set_reference(lrt_ctx *ctx, uint32_t n_views, const lrt_view *views, const float *images) {
+  lrt_status s = ensure_state(ctx);
+  if (s != LRT_OK) return s;
+  if (n_views == 0 || !views || !images) return fail(ctx, LRT_ERR_INVALID, "lrt_dr_set_reference: no views");
+  DrState &st = *ctx->dr;
+  st.views.assign(views, views + n_views);
+  st.off.assign(n_views, 0);
+  size_t n = 0, mx = 0;
+  for (uint32_t v = 0; v < n_views; v++) {
+    if (views[v].width == 0 || views[v].height == 0 || views[v].width > 16384 || views[v].height > 16384)
+      return fail(ctx, LRT_ERR_INVALID, "view size out of range");
+    st.off[v] = n;
+    const size_t px = size_t(views[v].width) * views[v].height;
+    n += px;
+    mx = std::max(mx, px);
+  }
+  st.n_pix = n;
+  st.max_view_pix = mx;
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaError_t e;
+  if ((e = upload(st.d_ref, reinterpret_cast<const float4 *>(images), n)) != cudaSuccess)
+    return cuda_fail(ctx, e, "upload reference images");
+  LRT_CUDA(ctx, st.d_img.ensure(n));
+  LRT_CUDA(ctx, st.d_depth.ensure(n));
+  LRT_CUDA(ctx, st.d_border_mask.ensure(n));
+  LRT_CUDA(ctx, st.d_border_list.ensure(mx));
+  LRT_CUDA(ctx, st.d_border_count.ensure(n_views));
+  LRT_CUDA(ctx, st.d_loss.ensure(n_views));
+  LRT_CUDA(ctx, cudaMemset(st.d_img.p, 0, n * sizeof(float4)));
+  LRT_CUDA(ctx, cudaMemset(st.d_border_count.p, 0, n_views * 4));
+  LRT_CUDA(ctx, cudaMemset(st.d_loss.p, 0, n_views * sizeof(double)));
+  if (st.d_adam.p) LRT_CUDA(ctx, cudaMemset(st.d_adam.p, 0, sizeof(float) * 2 * size_t(st.n_params)));
+  st.has_ref = true;
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_dr_set_preset(lrt_ctx *ctx, const lrt_dr_preset *preset) {
+  lrt_status s = ensure_state(ctx);
+  if (s != LRT_OK) return s;
+  if (!preset) return fail(ctx, LRT_ERR_INVALID, "null preset");
+  if (preset->spp == 0 || preset->spp > drk::kMaxSpp) return fail(ctx, LRT_ERR_INVALID, "spp must be 1..64");
+  if (preset->n_lights > 4) return fail(ctx, LRT_ERR_INVALID, "at most 4 lights");
+  if (preset->render_mode > LRT_DR_RENDER_NORMAL || preset->loss_function > 1 || preset->input_type > 1)
+    return fail(ctx, LRT_ERR_INVALID, "unknown render mode, loss or input type");
+  for (uint32_t i = 0; i < preset->n_lights; i++)
+    if (preset->lights[i].type != LRT_DR_LIGHT_DIRECT && preset->lights[i].type != LRT_DR_LIGHT_AMBIENT)
+      return fail(ctx, LRT_ERR_UNSUPPORTED, "only direct and ambient lights");
+  if (!(preset->border_relax_eps > 0.0f)) return fail(ctx, LRT_ERR_INVALID, "border_relax_eps must be > 0");
+  ctx->dr->preset = *preset;
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_dr_set_params(lrt_ctx *ctx, const float *params, uint32_t n_params) {
+  if (!ctx || !ctx->dr || !ctx->dr->has_scene) return fail(ctx, LRT_ERR_STATE, "lrt_dr_set_scene first");
+  DrState &st = *ctx->dr;
+  if (!params || n_params != st.n_params) return fail(ctx, LRT_ERR_INVALID, "parameter count differs from the scene");
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  LRT_CUDA(ctx, cudaMemcpy(st.d_params.p, params, sizeof(float) * n_params, cudaMemcpyHostToDevice));
+  LRT_CUDA(ctx, cudaMemset(st.d_adam.p, 0, sizeof(float) * 2 * size_t(n_params)));
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_dr_render_grad(lrt_ctx *ctx, uint32_t view, double *loss) {
+  lrt_status s = check_ready(ctx);
+  if (s != LRT_OK) return s;
+  DrState &st = *ctx->dr;
+  if (view >= st.views.size()) return fail(ctx, LRT_ERR_INVALID, "view index out of range");
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  st.last_launches = 0;
+  LRT_CUDA(ctx, cudaMemsetAsync(st.d_grad.p, 0, sizeof(float) * st.n_params, 0));
+  if ((s = render_view(ctx, view, 0)) != LRT_OK) return s;
+  if (loss) {
+    double l = 0;
+    LRT_CUDA(ctx, cudaMemcpy(&l, st.d_loss.p + view, sizeof(double), cudaMemcpyDeviceToHost));
+    *loss = l / double(size_t(st.views[view].width) * st.views[view].height);
+    if ((s = read_status(ctx)) != LRT_OK) return s;
+  }
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_dr_step(lrt_ctx *ctx, uint32_t iter, double *losses) {
+  lrt_status s = check_ready(ctx);
+  if (s != LRT_OK) return s;
+  DrState &st = *ctx->dr;
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  st.last_launches = 0;
+  const uint32_t nv = uint32_t(st.views.size());
+  if (st.preset.accumulate_batch) LRT_CUDA(ctx, cudaMemsetAsync(st.d_grad.p, 0, sizeof(float) * st.n_params, 0));
+  for (uint32_t v = 0; v < nv; v++) {
+    // the reference refills its gradient buffer for every image of the batch (:412)
+    if (!st.preset.accumulate_batch) LRT_CUDA(ctx, cudaMemsetAsync(st.d_grad.p, 0, sizeof(float) * st.n_params, 0));
+    if ((s = render_view(ctx, v, 0)) != LRT_OK) return s;
+  }
+  const lrt_dr_preset &p = st.preset;
+  const double c1 = 1.0 - std::pow(double(p.opt_beta_1), double(iter + 1));
+  const double c2 = 1.0 - std::pow(double(p.opt_beta_2), double(iter + 1));
+  drk::launch_adam(st.d_params.p, st.d_adam.p, st.d_adam.p + st.n_params, st.d_grad.p, st.n_params, float(nv),
+                   p.opt_lr, p.opt_beta_1, p.opt_beta_2, p.opt_eps, c1, c2, 0);
+  st.last_launches += 1;
+  LRT_CUDA(ctx, cudaGetLastError());
+  if (losses) {
+    std::vector<double> l(nv);
+    LRT_CUDA(ctx, cudaMemcpy(l.data(), st.d_loss.p, nv * sizeof(double), cudaMemcpyDeviceToHost));
+    for (uint32_t v = 0; v < nv; v++) losses[v] = l[v] / double(size_t(st.views[v].width) * st.views[v].height);
+    if ((s = read_status(ctx)) != LRT_OK) return s;
+  }
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_dr_optimize(lrt_ctx *ctx, uint32_t first_iter, uint32_t iterations, double *last_losses) {
+  lrt_status s = check_ready(ctx);
+  if (s != LRT_OK) return s;
+  for (uint32_t i = 0; i < iterations; i++)
+    if ((s = lrt_dr_step(ctx, first_iter + i, i + 1 == iterations ? last_losses : nullptr)) != LRT_OK) return s;
+  LRT_CUDA(ctx, cudaDeviceSynchronize());
+  return read_status(ctx);
+}
+
+extern "C" lrt_status lrt_dr_get(lrt_ctx *ctx, uint32_t what, uint32_t view, void *out, uint64_t bytes) {
+  if (!ctx || !ctx->dr || !ctx->dr->has_scene || !out) return fail(ctx, LRT_ERR_STATE, "lrt_dr_set_scene first");
+  DrState &st = *ctx->dr;
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  const void *src = nullptr;
+  uint64_t want = 0;
+  if (what == LRT_DR_PARAMS) { src = st.d_params.p; want = 4ull * st.n_params; }
+  else if (what == LRT_DR_GRAD) { src = st.d_grad.p; want = 4ull * st.n_params; }
+  else if (what == LRT_DR_ADAM) { src = st.d_adam.p; want = 8ull * st.n_params; }
+  else {
+    if (!st.has_ref || view >= st.views.size()) return fail(ctx, LRT_ERR_INVALID, "no such view");
+    const uint64_t px = uint64_t(st.views[view].width) * st.views[view].height;
+    if (what == LRT_DR_IMAGE) { src = st.d_img.p + st.off[view]; want = 16 * px; }
+    else if (what == LRT_DR_DEPTH) { src = st.d_depth.p + st.off[view]; want = 4 * px; }
+    else if (what == LRT_DR_BORDER) { src = st.d_border_mask.p + st.off[view]; want = px; }
+    else return fail(ctx, LRT_ERR_INVALID, "unknown item");
+  }
+  if (bytes != want) return fail(ctx, LRT_ERR_INVALID, "output size mismatch");
+  LRT_CUDA(ctx, cudaMemcpy(out, src, bytes, cudaMemcpyDeviceToHost));
+  return LRT_OK;
+}
+
+extern "C" uint32_t lrt_dr_last_launch_count(const lrt_ctx *ctx) {
+  return (ctx && ctx->dr) ? ctx->dr->last_launches : 0;
+}
+
+extern "C" lrt_status lrt_dr_grid_sbs(uint32_t bc, uint32_t bs, const lrt_sdf_desc *sdf, const float *color3,
+                                      lrt_sbs_header *hdr, lrt_sbs_node **nodes_out, uint32_t *n_nodes,
+                                      uint32_t **values_out, uint64_t *n_values, float **params_out,
+                                      uint32_t *n_params) {
+  if (!sdf || !hdr || !nodes_out || !n_nodes || !values_out || !n_values || !params_out || !n_params || bc == 0 ||
+      bs == 0 || bc > 1024 || bs > 64 || (sdf->n_spheres + sdf->n_boxes) == 0)
+    return LRT_ERR_INVALID;
+  const uint64_t v = bs + 1, dist_per_node = v * v * v, pc = uint64_t(bc) * bs + 1, cc = uint64_t(bc) + 1;
+  const uint64_t c_off = pc * pc * pc, nn = uint64_t(bc) * bc * bc;
+  const uint64_t per_old = dist_per_node + 8, per_new = dist_per_node + 8 + 27;
+  const uint64_t np = pc * pc * pc + 3 * cc * cc * cc;
+  if (np >= 0x80000000ull || nn * per_new >= (1ull << 40)) return LRT_ERR_UNSUPPORTED;
+  float *P = static_cast<float *>(std::malloc(np * sizeof(float)));
+  lrt_sbs_node *nodes = static_cast<lrt_sbs_node *>(std::calloc(nn, sizeof(lrt_sbs_node)));
+  uint32_t *vals = static_cast<uint32_t *>(std::malloc(nn * per_new * sizeof(uint32_t)));
+  if (!P || !nodes || !vals) {
+    std::free(P); std::free(nodes); std::free(vals);
+    return LRT_ERR_OOM;
+  }
+  hdr->brick_size = bs;
+  hdr->brick_pad = 0;
+  hdr->bytes_per_value = 4;
+  hdr->aux_data = 5u << 24;   // SDF_SBS_NODE_LAYOUT_ID32F_IRGB32F_IN
+  // distances at 2 * (i / (bc * bs)) - 1 (DR_common.cpp:72-85)
+  const float gdiv = float(bc * bs);
+#pragma omp parallel for schedule(static)
+  for (int64_t x = 0; x < int64_t(pc); x++)
+    for (uint64_t y = 0; y < pc; y++)
+      for (uint64_t z = 0; z < pc; z++)
+        P[uint64_t(x) * pc * pc + y * pc + z] = sdf_eval(*sdf, 2.0f * (float(x) / gdiv) - 1.0f,
+                                                         2.0f * (float(y) / gdiv) - 1.0f, 2.0f * (float(z) / gdiv) - 1.0f);
+  // colours at the brick corners (:87-102)
+  const float cdiv = float(bc);
+  for (uint64_t x = 0; x < cc; x++)
+    for (uint64_t y = 0; y < cc; y++)
+      for (uint64_t z = 0; z < cc; z++) {
+        const uint64_t idx = x * cc * cc + y * cc + z;
+        float c[3];
+        if (color3) {
+          c[0] = color3[0]; c[1] = color3[1]; c[2] = color3[2];
+        } else {
+          const float q[3] = {2.0f * (float(x) / cdiv) - 1.0f, 2.0f * (float(y) / cdiv) - 1.0f,
+                              2.0f * (float(z) / cdiv) - 1.0f};
+          for (int k = 0; k < 3; k++) c[k] = 0.5f + 0.5f * q[k];
+        }
+        for (int k = 0; k < 3; k++) P[c_off + 3 * idx + k] = c[k];
+      }
+  // nodes and indices (:104-143)
+  for (uint64_t bx = 0; bx < bc; bx++)
+    for (uint64_t by = 0; by < bc; by++)
+      for (uint64_t bz = 0; bz < bc; bz++) {
+        const uint64_t n = bx * bc * bc + by * bc + bz, off = n * per_new;
+        nodes[n].pos_xy = uint32_t((bx << 16) | by);
+        nodes[n].pos_z_lod_size = uint32_t((bz << 16) | bc);
+        nodes[n].data_offset = uint32_t(off);
+        for (uint64_t x = 0; x < v; x++)
+          for (uint64_t y = 0; y < v; y++)
+            for (uint64_t z = 0; z < v; z++)
+              vals[off + x * v * v + y * v + z] = uint32_t((bx * bs + x) * pc * pc + (by * bs + y) * pc + (bz * bs + z));
+        for (uint64_t k = 0; k < 8; k++) {
+          const uint64_t x = k >> 2, y = (k >> 1) & 1, z = k & 1;
+          vals[off + dist_per_node + k] = uint32_t(c_off + 3 * ((bx + x) * cc * cc + (by + y) * cc + (bz + z)));
+        }
+        for (int k = 0; k < 27; k++) vals[off + per_old + k] = drk::kInvalidIdx;
+      }
+  // neighbours through shared corners (utils/sparse_octree_builder.cpp:2802-2850): for every
+  // brick-corner value, the bricks holding it and at which corner; bricks sharing a corner
+  // value are neighbours, the direction being the difference of their corner positions.
+  // Only the 8 corners of each brick take part, so the table is indexed by corner record
+  // (sorted by value) instead of by every value as the reference's adjacency list is.
+  struct CornerRef { uint32_t value, node, r; };
+  std::vector<CornerRef> refs(8 * nn);
+  for (uint64_t n = 0; n < nn; n++)
+    for (uint32_t r = 0; r < 8; r++) {
+      const uint64_t ix = (v - 1) * ((r & 4) >> 2), iy = (v - 1) * ((r & 2) >> 1), iz = (v - 1) * (r & 1);
+      refs[8 * n + r] = CornerRef{vals[nodes[n].data_offset + ix * v * v + iy * v + iz], uint32_t(n), r};
+    }
+  std::sort(refs.begin(), refs.end(), [](const CornerRef &a, const CornerRef &b) {
+    return a.value != b.value ? a.value < b.value : a.r < b.r;
+  });
+  for (size_t a = 0; a < refs.size();) {
+    size_t b = a;
+    while (b < refs.size() && refs[b].value == refs[a].value) b++;
+    for (size_t i = a; i < b; i++)
+      for (size_t j = a; j < b; j++) {
+        if (refs[i].r == refs[j].r) continue;
+        const uint32_t r1 = refs[i].r, r2 = refs[j].r;
+        const int dx = int((r2 & 4) >> 2) - int((r1 & 4) >> 2) + 1, dy = int((r2 & 2) >> 1) - int((r1 & 2) >> 1) + 1,
+                  dz = int(r2 & 1) - int(r1 & 1) + 1;
+        vals[uint64_t(nodes[refs[j].node].data_offset) + per_old + uint64_t(9 * dx + 3 * dy + dz)] = refs[i].node;
+      }
+    a = b;
+  }
+  *nodes_out = nodes;
+  *n_nodes = uint32_t(nn);
+  *values_out = vals;
+  *n_values = nn * per_new;
+  *params_out = P;
+  *n_params = uint32_t(np);
+  return LRT_OK;
+}

@@ -1,0 +1,64 @@
+// Device-side state of the differentiable SDF render (MultiRendererDR path):
+// shared between the CUDA kernels (dr.cu) and the host driver (dr_api.cpp).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace lrt {
+namespace drk {
+
+constexpr uint32_t kInvalidIdx = 1u << 31;   // empty neighbour slot, sdfScene/sdf_scene.h:42
+constexpr uint32_t kNoIndex = 0xFFFFFFFFu;   // unset PD index, diff_render/DR_common.h:24
+constexpr int kStack = 80;                   // STACK_SIZE, raytrace_common.h:36
+constexpr uint32_t kMaxSpp = 64;             // samples per pixel kept for the depth threshold
+
+// status bits written by the kernels (read back by the host after a step)
+constexpr uint32_t kStatusStackOverflow = 1u;
+constexpr uint32_t kStatusTraversalBound = 2u;   // more node visits than the BVH has pairs (a cycle)
+
+// Indexed SBS (ID32F_IRGB32F or _IN) with its BVH2, one identity-or-given instance.
+struct DevScene {
+  const uint4 *nodes;        // SdfSBSNode: pos_xy, pos_z_lod_size, data_offset, unused
+  const uint32_t *values;    // per node: v^3 distance indices, 8 colour indices, [27 neighbours]
+  const float *P;            // parameters (values_f): distances then RGB colours
+  float *grad;               // dLoss/dP
+  const float4 *pairs;       // BVH2 fat pairs: 4 float4 each (left min|offset, left max|escape, right ...)
+  uint32_t n_pairs;
+  uint32_t brick_size, v_size, layout_in, need_normal;
+  float inst_bmin[3], inst_bmax[3];
+  float inst_inv[12];        // rows 0..2 of the instance's inverse transform
+  uint32_t *status;
+};
+
+struct DevPreset {
+  uint32_t render_mode, recon, input_type, loss_fn;
+  uint32_t spp, border_spp, seed, n_lights;
+  float relax_eps, g_mult;
+  uint32_t light_type[4];
+  float light_dir[4][3], light_col[4][3];
+  uint32_t agg;              // 1: warp-aggregated gradient atomics, 0: one atomic per contribution
+  uint32_t flags;            // DR_RAY_FLAG_* of CastRayWithGrad for this preset
+};
+
+struct DevView {
+  uint32_t width, height;
+  float proj_inv[16], wv_inv[16], pv[16];
+  const float4 *ref;         // target image
+  float4 *img;               // rendered image (rgb, hit fraction)
+  float *depth;              // depth-discontinuity threshold (out_image_depth .w)
+  uint8_t *border_mask;
+  uint32_t *border_list;
+  uint32_t *border_count;
+  double *loss;              // sum of pixel losses
+};
+
+void launch_pixels(const DevScene &s, const DevPreset &p, const DevView &v, cudaStream_t st);
+void launch_border_detect(const DevPreset &p, const DevView &v, cudaStream_t st);
+void launch_border(const DevScene &s, const DevPreset &p, const DevView &v, uint32_t max_pixels, int n_sm,
+                   cudaStream_t st);
+void launch_adam(float *x, float *V, float *S, const float *g, uint32_t n, float inv_batch, float lr, float b1,
+                 float b2, float eps, double c1, double c2, cudaStream_t st);
+void launch_scale(float *g, uint32_t n, float s, cudaStream_t st);
+
+}  // namespace drk
+}  // namespace lrt

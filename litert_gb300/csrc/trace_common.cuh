@@ -101,6 +101,28 @@ __device__ __forceinline__ bool need_normal(uint32_t render_mode) {   // BVH/BVH
   return render_mode == 1 || render_mode == 8 || render_mode == 12 || render_mode == 17 || render_mode == 18;
 }
 
+__device__ __forceinline__ void mat_vec4(const float *m, const float v[4], float r[4]) {
+#pragma unroll
+  for (int i = 0; i < 4; i++) r[i] = m[i * 4 + 0] * v[0] + m[i * 4 + 1] * v[1] + m[i * 4 + 2] * v[2] + m[i * 4 + 3] * v[3];
+}
+
+// kernel_InitEyeRay, Renderer/eye_ray.cpp:146-160 with EyeRayDirNormalized and
+// transform_ray3f, render_common.h:25-55
+__device__ __forceinline__ void eye_ray(uint32_t x, uint32_t y, uint32_t w, uint32_t h, float dx, float dy,
+                                        const float *proj_inv, const float *wv_inv, float3 &pos, float3 &dir) {
+  const float fx = (float(x) + dx) / float(w), fy = (float(y) + dy) / float(h);
+  const float v[4] = {2.0f * fx - 1.0f, -2.0f * fy + 1.0f, 1.0f, 1.0f};
+  float r[4];
+  mat_vec4(proj_inv, v, r);
+  const float ww = r[3];
+  float3 d0 = normalize(f3(r[0] / ww, r[1] / ww, r[2] / ww));
+  const float3 p00 = f3(0, 0, 0);
+  const float3 p0 = matmul4x3(wv_inv, p00);
+  const float3 p2 = matmul4x3(wv_inv, add(p00, scl(100.0f, d0)));
+  pos = p0;
+  dir = normalize(sub(p2, p0));
+}
+
 // A hit under construction (CRT_Hit plus the reordered triangle id for shading).
 struct Hit {
   float t;

@@ -168,3 +168,40 @@ def mesh_view(seed=2, width=1920, height=1080, fov=45.0):
     eye = 3.0 * d
     up = np.array([0, 1, 0], np.float32) if abs(d[1]) < 0.99 else np.array([1, 0, 0], np.float32)
     return camera(eye, (0, 0, 0), up, fov, width, height)
+
+
+# ---------------------------------------------------------------- config 5: differentiable reconstruction
+def turntable_cameras(count, center=(0.0, 0.0, 0.0), radius=3.0, height=1.0):
+    """get_cameras_turntable semantics (diff_render/DR_common.cpp:243-257): cameras on a
+    circle at the given height, (eye, center, up) each."""
+    c = np.asarray(center, np.float32)
+    out = []
+    for i in range(count):
+        phi = 2.0 * np.pi * i / count
+        vd = np.array([np.sin(phi), -height / radius, np.cos(phi)], np.float32)
+        tangent = np.cross(vd, -np.array([0, 1, 0], np.float32))
+        tangent /= np.linalg.norm(tangent)
+        up = np.cross(vd, tangent)
+        up /= np.linalg.norm(up)
+        out.append((c - radius * vd, c, up))
+    return out
+
+
+def dr_views(n_views=8, size=512, fov=60.0, radius=3.0, height=1.0):
+    """The reconstruction's cameras: a turntable of n_views at `size` x `size`."""
+    return [camera(e, c, u, fov, size, size, znear=0.01, zfar=100.0)
+            for e, c, u in turntable_cameras(n_views, radius=radius, height=height)]
+
+
+def dr_workload(target_bricks=32, target_brick_size=8, opt_bricks=32, opt_brick_size=4, n_views=8, size=512):
+    """Differentiable SDF reconstruction: targets are the smooth-union scene sampled
+    on a dense 256^3 grid (32^3 bricks of 8 voxels) with position colours,
+    rendered from the turntable; the optimised grid is 128^3 (32^3 bricks of 4
+    voxels) initialised to a sphere of radius 0.5 with a single colour.
+    Returns (target sbs, initial sbs, views); each sbs = [hdr, nodes, values, params]."""
+    from . import dr
+    up = union_params()
+    target = list(dr.grid_sbs(target_bricks, target_brick_size, lrt.Sdf(up["spheres"], up["boxes"], up["k"]), None))
+    init = list(dr.grid_sbs(opt_bricks, opt_brick_size, lrt.Sdf(spheres=np.array([[0, 0, 0, 0.5]], np.float32)),
+                            [1.0, 0.0, 0.0]))
+    return target, init, dr_views(n_views, size)
