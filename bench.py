@@ -47,6 +47,10 @@ def parse():
     ap.add_argument("--no-dr", action="store_true", help="skip the differentiable-render measurement")
     ap.add_argument("--dr-iters", type=int, default=200, help="reconstruction iterations (the first 10 untimed)")
     ap.add_argument("--dr-aggregate", type=int, default=1, help="warp-aggregated gradient atomics")
+    ap.add_argument("--only-dr", action="store_true", help="measure the differentiable render alone (profiling)")
+    ap.add_argument("--no-configs", action="store_true", help="skip the sphere and triangle-mesh lines")
+    ap.add_argument("--no-autotune", action="store_true", help="use --variant/--block-warps/--stage as given")
+    ap.add_argument("--no-graph", action="store_true", help="launch directly instead of replaying a CUDA graph")
     return ap.parse_args()
 
 
@@ -145,6 +149,82 @@ def run_cpu_baseline(h, nodes, values, views, pairs, seconds):
     n = int(min(total, max(20000, 20000 * seconds / max(t0, 1e-3))))
     rays, dt, cnt = run(n)
     return dict(value=rays / dt / 1e6, rays=rays, seconds=dt, cores=cores, counters=cnt)
+
+
+def run_small_configs(args, dev, torch):
+    """The other primary-ray configurations, device-timed like the headline:
+    sphere SBS (64^3 effective: depth 4, 4-voxel bricks; one 256^2 view and the
+    same view replicated 16x in one launch) and the displaced icosphere mesh
+    (327,680 triangles, 1920x1080).  Each with its oracle-port CPU rate."""
+    from litert_gb300 import lrt, scenes
+    from oracle import oracle as orc
+    out = []
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def timed(scene, views, steps):
+        n = sum(w * h for w, h, _, _ in views)
+        hits = torch.empty(n * 4, dtype=torch.float32, device=dev)
+        va = lrt.make_views(views)
+        for _ in range(3):
+            scene.render_device(va, len(views), hits_ptr=hits.data_ptr(), stream=stream.cuda_stream)
+        torch.cuda.synchronize(dev)
+        ts = []
+        for i in range(steps):
+            flush.fill_(float(i))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            scene.render_device(va, len(views), hits_ptr=hits.data_ptr(), stream=stream.cuda_stream)
+            b.record(stream)
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+        ms = statistics.median(ts)
+        return n, ms, n / (ms * 1e-3) / 1e6
+
+    def cpu_rate(osc, views):
+        cores = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        rays = 0
+        for w, h, wv, pj in views[:1]:
+            osc.render(w, h, lrt.inverse4x4(pj), lrt.inverse4x4(wv), threads=cores)
+            rays += w * h
+        return rays / (time.perf_counter() - t0) / 1e6, cores
+
+    # config 1: sphere
+    h, nodes, values = lrt.sbs_from_sdf(scenes.sphere_sdf(), 4, 4)
+    sc = lrt.Scene(dev.index)
+    g = sc.add_sbs(h, nodes, values)
+    sc.add_instance(g)
+    sc.commit_scene()
+    sc.set_preset(render_mode=lrt.RENDER_MODE_NORMAL, sdf_node_intersect=lrt.INTERSECT_NEWTON)
+    v1 = [scenes.sphere_view(256, 256)]
+    osc = orc.Scene("sbs", sbs=(orc.SbsHeader(h.brick_size, h.brick_pad, h.bytes_per_value, h.aux_data), nodes, values),
+                    intersect=2, render_mode=8)
+    cpu, cores = cpu_rate(osc, v1)
+    for name, views in (("sphere-sbs-256", v1), ("sphere-sbs-256-x16", v1 * 16)):
+        n, ms, mr = timed(sc, views, max(args.steps, 10))
+        out.append({"workload": name, "value": mr, "unit": UNIT, "ms_per_step": ms, "rays_per_step": n,
+                    "bricks": int(nodes.shape[0]),
+                    "cpu_baseline": {"value": cpu, "unit": UNIT, "cores": cores, "kind": "port",
+                                     "sample": "the 256x256 view"}})
+    sc.close()
+    # config 2: triangles
+    verts, faces = scenes.displaced_icosphere(subdiv=7)
+    sc = lrt.Scene(dev.index)
+    g = sc.add_triangles(verts, faces)
+    sc.add_instance(g)
+    sc.commit_scene()
+    sc.set_preset(render_mode=lrt.RENDER_MODE_NORMAL)
+    v2 = [scenes.mesh_view()]
+    n, ms, mr = timed(sc, v2, max(args.steps, 10))
+    osc = orc.Scene("mesh", mesh=(verts, faces), render_mode=8)
+    cpu, cores = cpu_rate(osc, v2)
+    out.append({"workload": "icosphere-327k-1920x1080", "value": mr, "unit": UNIT, "ms_per_step": ms,
+                "rays_per_step": n, "triangles": int(faces.shape[0]),
+                "cpu_baseline": {"value": cpu, "unit": UNIT, "cores": cores, "kind": "port",
+                                 "sample": "the 1920x1080 view"}})
+    sc.close()
+    return out
 
 
 def dr_setup(dev_index=0):
@@ -290,6 +370,9 @@ def main():
         return 0
 
     import torch
+    if args.only_dr:
+        print(json.dumps(run_dr(args, torch.device("cuda", 0), torch)))
+        return 0
     if world > 1:
         import torch.distributed as dist
         torch.cuda.set_device(local)
@@ -312,9 +395,16 @@ def main():
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     va = lrt.make_views(views)
     stream = torch.cuda.current_stream(dev)
+    tuned, tried = None, []
+    if not args.no_autotune:
+        tuned, tried = scene.autotune(views, reps=3)
+    graph = None if args.no_graph else scene.graph_create(views, hits_ptr=hits.data_ptr())
 
     def step():
-        scene.render_device(va, len(views), hits_ptr=hits.data_ptr(), stream=stream.cuda_stream)
+        if graph is not None:
+            scene.graph_launch(graph, stream.cuda_stream)
+        else:
+            scene.render_device(va, len(views), hits_ptr=hits.data_ptr(), stream=stream.cuda_stream)
 
     for _ in range(args.warmup):
         flush.fill_(1.0)
@@ -392,7 +482,9 @@ def main():
                        "depth": args.depth, "brick": args.brick, "bricks": int(nodes.shape[0]),
                        "brick_bytes": int(values.nbytes), "finder": "NEWTON", "render_mode": "NORMAL",
                        "l2": "256 MiB write between timed steps; scene data 623 MB > L2",
-                       "scene_build_s": round(t_build, 2), "parallelism": f"replicas{world}"},
+                       "scene_build_s": round(t_build, 2), "parallelism": f"replicas{world}",
+                       "launch": "CUDA graph replay" if graph is not None else "direct",
+                       "tuning": tuned, "autotune_candidates": len(tried)},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(len(views) * 136),
                     "d2h_bytes_per_step": int(n_rays * 16)},
             "gpu_launches": launches,
@@ -407,7 +499,11 @@ def main():
                                     "sample": f"{cpu['rays']} strided pixels of the 16 views ({cpu['seconds']:.1f} s)"}
         if not args.no_dr and world == 1:
             line["dr"] = run_dr(args, dev, torch)
+        if world == 1 and not args.no_configs:
+            line["other_configs"] = run_small_configs(args, dev, torch)
         print(json.dumps(line))
+    if graph is not None:
+        lrt.Scene.graph_destroy(graph)
     scene.close()
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -100,6 +100,15 @@ lrt_status lrt_dr_optimize(lrt_ctx *ctx, uint32_t first_iter, uint32_t iteration
 enum { LRT_DR_PARAMS = 0, LRT_DR_GRAD = 1, LRT_DR_IMAGE = 2, LRT_DR_DEPTH = 3, LRT_DR_BORDER = 4, LRT_DR_ADAM = 5 };
 lrt_status lrt_dr_get(lrt_ctx *ctx, uint32_t what, uint32_t view, void *out, uint64_t bytes);
 
+/* dr::BVHDR::RayQuery_NearestHitWithGrad (diff_render/BVH2DR.cpp:12-102) on n rays
+ * (float4 pos+tNear, float4 dir+tFar, host memory) with DR_RAY_FLAG_* bits
+ * (1 dDiffuse/dColour, 2 dDiffuse/dPos, 4 dNorm/dPos, 8 border, 16 dDist/dPos)
+ * and the render mode of the current preset.  Writes 32 words per ray: hit t,
+ * primId, colour[3], normal[3]; the border relaxation point missed_hit t, sdf,
+ * colour[3], normal[3]; missed_indices[8]; missed_dSDF_dtheta[8]. */
+lrt_status lrt_dr_query_rays(lrt_ctx *ctx, uint32_t flags, const float *pos_near, const float *dir_far, uint32_t n,
+                             uint32_t *out);
+
 /* Number of kernel launches of the last lrt_dr_render_grad / lrt_dr_step call. */
 uint32_t lrt_dr_last_launch_count(const lrt_ctx *ctx);
 

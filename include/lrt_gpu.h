@@ -61,9 +61,33 @@ lrt_status lrt_set_preset(lrt_ctx *ctx, const lrt_preset *preset);
 /* Launch-shape and kernel choices; no reference counterpart (the reference's
  * device path is generated by kernel_slicer).  Keys: "variant" (0 = one ray per
  * lane, default; 1 = warp packet traversal), "stage" (packet kernel: 1 = stage
- * each brick in shared memory), "block_warps" (1..8).  Results do not depend on
- * these. */
+ * each brick in shared memory), "block_warps" (1..8), "tile_w" (a warp's pixel
+ * tile is tile_w x 32/tile_w: 4, 8 (default), 16, 32), "stack" (traversal stack
+ * entries: 64 (default) or 32, which renders refuse for trees too deep for it).
+ * Results do not depend on these. */
 lrt_status lrt_set_tuning(lrt_ctx *ctx, const char *key, int value);
+
+/* One launch shape and its median time. */
+typedef struct { int variant, block_warps, stage, tile_w, stack; float ms; } lrt_tuning_choice;
+/* Autotuner: renders the views into a device buffer with each candidate shape
+ * (tile shapes 4x8/8x4/16x2 x stack 32/64 for the per-lane kernel; the packet
+ * kernel with and without brick staging at 2 and 4 warps per block), `reps`
+ * timed runs each after a warm-up, sets the fastest on the context and returns
+ * it; `all` (capacity cap, may be NULL) receives every candidate tried. */
+lrt_status lrt_autotune(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, uint32_t reps, lrt_tuning_choice *best,
+                        lrt_tuning_choice *all, uint32_t cap, uint32_t *n_tried);
+
+/* A batched render captured as a CUDA graph (work-queue reset + the persistent
+ * kernel) for a fixed set of view sizes and output pointers (device memory),
+ * with the context's tuning at capture time.  Launch replays it on `stream`;
+ * set_views changes the cameras (same sizes) for later replays.  The graph owns
+ * its view table; destroy it before the context. */
+typedef struct lrt_graph lrt_graph;
+lrt_status lrt_render_graph_create(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, lrt_hit16 *hits16,
+                                   float *rgba, uint32_t *rgba8, lrt_graph **out);
+lrt_status lrt_render_graph_launch(lrt_ctx *ctx, lrt_graph *graph, void *stream);
+lrt_status lrt_render_graph_set_views(lrt_ctx *ctx, lrt_graph *graph, const lrt_view *views, uint32_t n_views);
+void       lrt_render_graph_destroy(lrt_graph *graph);
 
 /* ---- queries ---- */
 /* BVHRT::RayQuery_NearestHit, BVH/BVH2Common.cpp:3490-3559, batched: n rays of

@@ -245,13 +245,20 @@ __device__ __forceinline__ Brick brick_of(const DevScene &s, uint32_t node) {
 
 __device__ __forceinline__ uint32_t vid(uint32_t x, uint32_t y, uint32_t z, uint32_t v) { return x * v * v + y * v + z; }
 
-__device__ __forceinline__ void load_vals(const DevScene &s, uint32_t off, float3 vox, float values[8], uint32_t idx[8]) {
+// the 8 corner values of a voxel from the per-brick gathered copy of the
+// parameters (one load each instead of index-then-value)
+__device__ __forceinline__ void load_vals(const DevScene &s, uint32_t node, float3 vox, float values[8]) {
+  const uint32_t vx = (uint32_t)vox.x, vy = (uint32_t)vox.y, vz = (uint32_t)vox.z;
+  const float *b = s.bvals + (size_t)node * (s.v_size * s.v_size * s.v_size);
+#pragma unroll
+  for (int i = 0; i < 8; i++) values[i] = __ldg(&b[vid(vx + ((i & 4) >> 2), vy + ((i & 2) >> 1), vz + (i & 1), s.v_size)]);
+}
+// their parameter indices (load_distance_values_with_indices, diff_render/BVH2DR.cpp:1092-1106)
+__device__ __forceinline__ void load_idx(const DevScene &s, uint32_t off, float3 vox, uint32_t idx[8]) {
   const uint32_t vx = (uint32_t)vox.x, vy = (uint32_t)vox.y, vz = (uint32_t)vox.z;
 #pragma unroll
-  for (int i = 0; i < 8; i++) {
+  for (int i = 0; i < 8; i++)
     idx[i] = __ldg(&s.values[off + vid(vx + ((i & 4) >> 2), vy + ((i & 2) >> 1), vz + (i & 1), s.v_size)]);
-    values[i] = __ldg(&s.P[idx[i]]);
-  }
 }
 
 __device__ __forceinline__ void load_colors(const DevScene &s, uint32_t t_off, float3 c[8]) {
@@ -273,6 +280,25 @@ struct HitRec {
 
 // voxel walk of one brick (OctreeBrickIntersectWithGrad :1160-1240, 1605-1608),
 // bounded at 8*brick_size+16 steps where the reference's loop is unbounded
+//
+// Skips (exact): where every corner value v of a voxel (or brick) satisfies
+// min v > skip_margin(max |v|), the voxel's cubic has no root on the segment
+// even after rounding, so the finder cannot report a hit; and in border mode
+// no point of the segment can bring the relaxation SDF below min v, so the
+// only effects of the reference's Intersect call are its resets of the
+// candidate and of check_vox_border, which are applied here.  The margin
+// bounds the rounding of the cubic's coefficients and of Horner's evaluation
+// on [0, qFar] (qFar <= sqrt 3) with a wide safety factor.
+__device__ __forceinline__ float skip_margin(float maxabs) { return 2e-3f * maxabs + 1e-6f; }
+
+template <bool BORDER>
+__device__ __forceinline__ void skipped_intersect(Relax *rl) {
+  if (BORDER) {
+    rl->csdf = 1000.f;
+    if (rl->cvb == 1) rl->cvb = 0;
+  }
+}
+
 template <bool BORDER>
 __device__ bool brick_visit(const DevScene &s, uint32_t node, float3 pos, float3 dir, float3 inv, float tNear,
                             HitRec &hr, Relax *rl) {
@@ -280,6 +306,25 @@ __device__ bool brick_visit(const DevScene &s, uint32_t node, float3 pos, float3
   float2 bnf = ray_box(pos, inv, B.bmin.x, B.bmin.y, B.bmin.z, B.bmax.x, B.bmax.y, B.bmax.z);
   const float bs = float(s.brick_size);
   const uint32_t max_steps = 8u * s.brick_size + 16u;
+  if (!(bnf.x < bnf.y)) return false;
+  {
+    const float2 bb = __ldg(&s.brick_bounds[node]);   // min v, max |v| over the brick
+    const float thr = (BORDER ? rl->sdf : 0.0f) + skip_margin(bb.y);
+    if (bb.x > thr) {
+      if (!BORDER) return false;
+      // border mode: the walk would call Intersect at least once if its first voxel does
+      const float3 lp = scr(sub(add(pos, scl(bnf.x, dir)), B.bmin), B.scale);
+      const float3 vox = f3(floorf(clampf(lp.x, 1e-6f, bs - 1e-6f)), floorf(clampf(lp.y, 1e-6f, bs - 1e-6f)),
+                            floorf(clampf(lp.z, 1e-6f, bs - 1e-6f)));
+      const float3 min_pos = add(B.bmin, scl(B.d, vox));
+      const float3 max_pos = add(min_pos, scl(B.d, f3(1, 1, 1)));
+      const float2 fnf = ray_box(pos, inv, min_pos.x, min_pos.y, min_pos.z, max_pos.x, max_pos.y, max_pos.z);
+      if (tNear < fnf.x) {
+        skipped_intersect<BORDER>(rl);
+        return false;
+      }
+    }
+  }
   for (uint32_t step = 0; bnf.x < bnf.y && step < max_steps; step++) {
     const float3 hit_pos = add(pos, scl(bnf.x, dir));
     const float3 lp = scr(sub(hit_pos, B.bmin), B.scale);
@@ -288,10 +333,14 @@ __device__ bool brick_visit(const DevScene &s, uint32_t node, float3 pos, float3
     const float3 min_pos = add(B.bmin, scl(B.d, vox));
     const float3 max_pos = add(min_pos, scl(B.d, f3(1, 1, 1)));
     float values[8];
-    uint32_t mi[8];
-    load_vals(s, B.data_offset, vox, values, mi);
+    load_vals(s, node, vox, values);
     const float2 fnf = ray_box(pos, inv, min_pos.x, min_pos.y, min_pos.z, max_pos.x, max_pos.y, max_pos.z);
-    if (tNear < fnf.x) {
+    float vmin = values[0], vmax = fabsf(values[0]);
+#pragma unroll
+    for (int i = 1; i < 8; i++) { vmin = fminf(vmin, values[i]); vmax = fmaxf(vmax, fabsf(values[i])); }
+    if (tNear < fnf.x && vmin > (BORDER ? rl->sdf : 0.0f) + skip_margin(vmax)) {
+      skipped_intersect<BORDER>(rl);
+    } else if (tNear < fnf.x) {
       const float3 start_q = scr(sub(add(pos, scl(fnf.x, dir)), min_pos), B.scale);
       const float qFar = (fnf.y - fnf.x) * B.scale;
       const float prev = BORDER ? rl->sdf : 0.0f;
@@ -319,8 +368,7 @@ __device__ bool brick_visit(const DevScene &s, uint32_t node, float3 pos, float3
             load_colors(s, B.data_offset + s.v_size * s.v_size * s.v_size, cols);
             rl->color = tri3(cols, dp_ast);
             rl->normal = divs(g, gl);
-#pragma unroll
-            for (int i = 0; i < 8; i++) rl->idx[i] = mi[i];
+            load_idx(s, B.data_offset, vox, rl->idx);
           }
         }
       }
@@ -389,12 +437,12 @@ __device__ void traverse(const DevScene &s, float3 pos, float3 dir, float tNear,
 // RayQuery_NearestHitWithGrad (:12-102): TLAS leaf box of the single instance,
 // ray to object space, BLAS traversal, candidate merge of the relaxation point
 template <bool BORDER>
-__device__ void query(const DevScene &s, float3 P, float3 D, HitRec &hr, Relax *rl) {
-  hr.t = 1e9f;
+__device__ void query(const DevScene &s, float3 P, float3 D, float tfar, HitRec &hr, Relax *rl) {
+  hr.t = tfar;
   hr.prim = kNoIndex;
   if (BORDER) {
-    rl->t = 1e9f; rl->sdf = 1000.0f; rl->cvb = 1;
-    rl->ct = 1e9f; rl->csdf = 1000.0f;
+    rl->t = tfar; rl->sdf = 1000.0f; rl->cvb = 1;
+    rl->ct = tfar; rl->csdf = 1000.0f;
     rl->color = f3(0, 0, 0); rl->normal = f3(1, 0, 0);
 #pragma unroll
     for (int i = 0; i < 8; i++) { rl->idx[i] = kNoIndex; rl->dth[i] = 0.0f; }
@@ -470,8 +518,7 @@ __device__ void shade_hit(const DevScene &s, const HitRec &hr, Shade &sh, bool f
         const Nbr n = neighbour(s, hr.prim, B.data_offset, hr.vox, dp, i);
         if (n.node != kInvalidIdx) {
           float vn[8];
-          uint32_t in_[8];
-          load_vals(s, __ldg(&s.nodes[n.node]).z, n.nvox, vn, in_);
+          load_vals(s, n.node, n.nvox, vn);
           sh.nrm[i] = normalize(tri_diff(vn, sub(dp, n.dvox)));
         }
       }
@@ -479,8 +526,7 @@ __device__ void shade_hit(const DevScene &s, const HitRec &hr, Shade &sh, bool f
       sh.normal = normalize(sh.tr3);
     } else {
       float values[8];
-      uint32_t mi[8];
-      load_vals(s, B.data_offset, hr.vox, values, mi);
+      load_vals(s, hr.prim, hr.vox, values);
       if (fd_residue) {
         const float delta = 0.001f;
 #pragma unroll
@@ -606,7 +652,8 @@ __device__ void scatter_hit_pds(const DevScene &s, const DevPreset &p, const Hit
   uint32_t mi[8] = {kNoIndex, kNoIndex, kNoIndex, kNoIndex, kNoIndex, kNoIndex, kNoIndex, kNoIndex};
   if (act) {
     B = brick_of(s, hr.prim);
-    load_vals(s, B.data_offset, hr.vox, values, mi);
+    load_vals(s, hr.prim, hr.vox, values);
+    load_idx(s, B.data_offset, hr.vox, mi);
   }
   // colour PDs (:1500-1510, 1217-1225)
   if (flags & F_DCOLOR) {
@@ -664,7 +711,8 @@ __device__ void scatter_hit_pds(const DevScene &s, const DevPreset &p, const Hit
         const Nbr n = neighbour(s, hr.prim, B.data_offset, hr.vox, sh.dp, i);
         valid = n.node != kInvalidIdx;
         if (valid) {
-          load_vals(s, __ldg(&s.nodes[n.node]).z, n.nvox, vn, in_);
+          load_vals(s, n.node, n.nvox, vn);
+          load_idx(s, __ldg(&s.nodes[n.node]).z, n.nvox, in_);
           ndp = sub(sh.dp, n.dvox);
           const float3 g = tri_diff(vn, ndp);
           Mi = nrm_diff(g);
@@ -788,7 +836,7 @@ __global__ void __launch_bounds__(128) dr_pixel_kernel(DevScene s, DevPreset p, 
       const float2 d = rand2(x, y, i, p.seed);
       float3 P, D;
       eye_ray(x, y, v.width, v.height, d.x, d.y, v.proj_inv, v.wv_inv, P, D);
-      query<false>(s, P, D, hr, nullptr);
+      query<false>(s, P, D, 1e9f, hr, nullptr);
       if (hr.prim == kNoIndex) continue;
       shade_hit(s, hr, sh, (p.flags & (F_DDIFFUSE | F_DNORM | F_DDIST)) != 0);
       dCdD = M3{f3(1, 0, 0), f3(0, 1, 0), f3(0, 0, 1)};
@@ -841,7 +889,7 @@ __global__ void __launch_bounds__(128) dr_pixel_kernel(DevScene s, DevPreset p, 
       const float2 d = rand2(x, y, i, p.seed);
       float3 P, D;
       eye_ray(x, y, v.width, v.height, d.x, d.y, v.proj_inv, v.wv_inv, P, D);
-      query<false>(s, P, D, hr, nullptr);
+      query<false>(s, P, D, 1e9f, hr, nullptr);
       act = hr.prim != kNoIndex;
       if (act) {
         shade_hit(s, hr, sh, true);
@@ -887,9 +935,9 @@ __device__ __forceinline__ float3 color_plain(const DevPreset &p, float t, float
   return color_grad(p, t, c, n, a, b);
 }
 
-// CastBorderRay + CalculateBorderRayDerivatives (:1319-1499): one warp per border
-// pixel (grid-stride over the compacted list), border_spp samples over the lanes
-__global__ void __launch_bounds__(128) dr_border_kernel(DevScene s, DevPreset p, DevView v) {
+// CastBorderRay + CalculateBorderRayDerivatives (:1319-1499): a warp per (border
+// pixel, 32 of its border_spp samples), grid-stride over the compacted list
+__global__ void __launch_bounds__(128, 4) dr_border_kernel(DevScene s, DevPreset p, DevView v) {
   __shared__ float ws_all[4][32];
   float *ws = ws_all[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
@@ -898,11 +946,14 @@ __global__ void __launch_bounds__(128) dr_border_kernel(DevScene s, DevPreset p,
   const uint32_t nb = *v.border_count;
   const uint32_t W = v.width, H = v.height;
   const float pdf = 1.0f / float(p.border_spp);
-  for (uint32_t bi = warp; bi < nb; bi += n_warps) {
-    const uint32_t pix = v.border_list[bi];
+  // work item = (border pixel, chunk of 32 samples): a pixel's samples spread over
+  // several warps so that the few border pixels still fill the GPU
+  const uint32_t chunks = (p.border_spp + 31) / 32;
+  for (uint32_t item = warp; item < nb * chunks; item += n_warps) {
+    const uint32_t pix = v.border_list[item / chunks];
     const uint32_t x = pix % W, y = pix / W;
-    for (uint32_t s0 = 0; s0 < p.border_spp; s0 += 32) {
-      const uint32_t sid = s0 + lane;
+    {
+      const uint32_t sid = (item % chunks) * 32 + lane;
       HitRec hr;
       Relax rl;
       bool br = false;
@@ -910,7 +961,7 @@ __global__ void __launch_bounds__(128) dr_border_kernel(DevScene s, DevPreset p,
       if (sid < p.border_spp) {
         const float2 d = rand2(x, y, sid, p.seed);
         eye_ray(x, y, W, H, d.x, d.y, v.proj_inv, v.wv_inv, P, D);
-        query<true>(s, P, D, hr, &rl);
+        query<true>(s, P, D, 1e9f, hr, &rl);
         br = rl.sdf < p.relax_eps;
       }
       float cd[4] = {0, 0, 0, 0};
@@ -969,18 +1020,98 @@ __global__ void __launch_bounds__(128) dr_border_kernel(DevScene s, DevPreset p,
 }
 
 // OptimizeStepAdam (:828-853) after the batch division (:475-476)
+// The bias corrections 1 - beta^(iter+1) are formed in double on the host as the
+// reference does; the divisions by them run in float here (the reference
+// divides in double, a difference of at most one rounding).
 __global__ void dr_adam_kernel(float *x, float *V, float *S, const float *g, uint32_t n, float batch, float lr,
-                               float b1, float b2, float eps, double c1, double c2) {
+                               float b1, float b2, float eps, float c1, float c2) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float gi = g[i] / batch;
     const float Vi = b1 * V[i] + (1 - b1) * gi;
     V[i] = Vi;
-    const float Vh = (float)((double)Vi / c1);
+    const float Vh = Vi / c1;
     const float Si = b2 * S[i] + (1 - b2) * gi * gi;
     S[i] = Si;
-    const float Sh = (float)((double)Si / c2);
+    const float Sh = Si / c2;
     x[i] = clampf(x[i] - lr * Vh / (sqrtf(Sh) + eps), -1000.0f, 1000.0f);
   }
+}
+
+// RayQuery_NearestHitWithGrad on a batch of rays (diff_render/BVH2DR.cpp:12-102):
+// the hit (t, primId, colour, normal) and the border relaxation point (t, sdf,
+// colour, normal, indices, dSDF/dtheta), 32 words per ray
+__global__ void dr_query_kernel(DevScene s, uint32_t flags, const float4 *pos, const float4 *dir, uint32_t n,
+                                uint32_t *out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 P4 = pos[i], D4 = dir[i];
+  const float3 P = f3(P4.x, P4.y, P4.z), D = f3(D4.x, D4.y, D4.z);
+  // the reference's ray query takes tFar from dir.w (a non-positive w asks for any-hit: its magnitude)
+  const float tfar = D4.w <= 0.0f ? -D4.w : D4.w;
+  HitRec hr;
+  Relax rl;
+  if (flags & F_BORDER) {
+    query<true>(s, P, D, tfar, hr, &rl);
+  } else {
+    query<false>(s, P, D, tfar, hr, nullptr);
+    rl.t = tfar; rl.sdf = 1000.0f;
+    rl.color = f3(0, 0, 0); rl.normal = f3(1, 0, 0);
+#pragma unroll
+    for (int k = 0; k < 8; k++) { rl.idx[k] = kNoIndex; rl.dth[k] = 0.0f; }
+  }
+  uint32_t *o = out + 32 * (size_t)i;
+  float3 hc = f3(0, 0, 0), hn = f3(1, 0, 0);
+  float ht = tfar;
+  if (hr.prim != kNoIndex) {
+    Shade sh;
+    shade_hit(s, hr, sh, (flags & (F_DDIFFUSE | F_DNORM | F_DDIST)) != 0);
+    hc = sh.color;
+    hn = sh.normal;
+    ht = hr.t;
+  }
+  o[0] = __float_as_uint(ht);
+  o[1] = hr.prim;
+  o[2] = __float_as_uint(hc.x); o[3] = __float_as_uint(hc.y); o[4] = __float_as_uint(hc.z);
+  o[5] = __float_as_uint(hn.x); o[6] = __float_as_uint(hn.y); o[7] = __float_as_uint(hn.z);
+  o[8] = __float_as_uint(rl.t); o[9] = __float_as_uint(rl.sdf);
+  o[10] = __float_as_uint(rl.color.x); o[11] = __float_as_uint(rl.color.y); o[12] = __float_as_uint(rl.color.z);
+  o[13] = __float_as_uint(rl.normal.x); o[14] = __float_as_uint(rl.normal.y); o[15] = __float_as_uint(rl.normal.z);
+#pragma unroll
+  for (int k = 0; k < 8; k++) { o[16 + k] = rl.idx[k]; o[24 + k] = __float_as_uint(rl.dth[k]); }
+}
+
+void launch_query(const DevScene &s, uint32_t flags, const float4 *pos, const float4 *dir, uint32_t n, uint32_t *out,
+                  cudaStream_t st) {
+  dr_query_kernel<<<(n + 127) / 128, 128, 0, st>>>(s, flags, pos, dir, n, out);
+}
+
+// per brick: its distance values gathered from the parameters (a float copy in
+// the brick's own order) with their min v and max |v| (one warp per brick),
+// refreshed whenever the parameters change
+__global__ void dr_brick_bounds_kernel(const uint4 *nodes, const uint32_t *values, const float *P, uint32_t n_nodes,
+                                       uint32_t v3, float2 *out, float *bvals) {
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= n_nodes) return;
+  const uint32_t off = __ldg(&nodes[warp]).z;
+  float mn_ = 3.0e38f, mx_ = 0.0f;
+  for (uint32_t k = lane; k < v3; k += 32) {
+    const float v = __ldg(&P[__ldg(&values[off + k])]);
+    bvals[(size_t)warp * v3 + k] = v;
+    mn_ = fminf(mn_, v);
+    mx_ = fmaxf(mx_, fabsf(v));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    mn_ = fminf(mn_, __shfl_xor_sync(0xFFFFFFFFu, mn_, o));
+    mx_ = fmaxf(mx_, __shfl_xor_sync(0xFFFFFFFFu, mx_, o));
+  }
+  if (lane == 0) out[warp] = make_float2(mn_, mx_);
+}
+
+void launch_brick_bounds(const DevScene &s, uint32_t n_nodes, float2 *out, cudaStream_t st) {
+  const uint32_t v3 = s.v_size * s.v_size * s.v_size;
+  dr_brick_bounds_kernel<<<(n_nodes + 7) / 8, 256, 0, st>>>(s.nodes, s.values, s.P, n_nodes, v3, out,
+                                                             const_cast<float *>(s.bvals));
 }
 
 __global__ void dr_scale_kernel(float *g, uint32_t n, float s) {
@@ -999,8 +1130,11 @@ void launch_border_detect(const DevPreset &p, const DevView &v, cudaStream_t st)
 
 void launch_border(const DevScene &s, const DevPreset &p, const DevView &v, uint32_t max_pixels, int n_sm,
                    cudaStream_t st) {
-  // one warp per border pixel; enough resident warps to cover the SMs, grid-stride beyond
-  uint32_t blocks = (max_pixels + 3) / 4;
+  // warps take (border pixel, 32-sample chunk) items; enough resident warps to cover
+  // the SMs, grid-stride beyond
+  const uint32_t chunks = (p.border_spp + 31) / 32;
+  uint32_t blocks = uint32_t((uint64_t(max_pixels) * chunks + 3) / 4 > 0xFFFFFFFFull ? 0xFFFFFFFFu
+                                                                                     : (uint64_t(max_pixels) * chunks + 3) / 4);
   const uint32_t cap = (uint32_t)n_sm * 16;
   if (blocks > cap) blocks = cap;
   if (blocks == 0) blocks = 1;
@@ -1010,7 +1144,7 @@ void launch_border(const DevScene &s, const DevPreset &p, const DevView &v, uint
 void launch_adam(float *x, float *V, float *S, const float *g, uint32_t n, float batch, float lr, float b1, float b2,
                  float eps, double c1, double c2, cudaStream_t st) {
   dr_adam_kernel<<<(n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096, 256, 0, st>>>(x, V, S, g, n, batch, lr, b1, b2,
-                                                                                  eps, c1, c2);
+                                                                                  eps, float(c1), float(c2));
 }
 
 void launch_scale(float *g, uint32_t n, float s, cudaStream_t st) {

@@ -26,6 +26,8 @@ struct DrState {
   DevBuf<uint32_t> d_values;
   DevBuf<float> d_params, d_grad, d_adam;
   DevBuf<float4> d_pairs;
+  DevBuf<float2> d_bounds;     // per-brick distance bounds for the exact skips
+  DevBuf<float> d_bvals;       // per-brick gathered distance values
   // views
   std::vector<lrt_view> views;
   std::vector<size_t> off;     // pixel offset of each view
@@ -46,6 +48,8 @@ void dr_state_free(DrState *st) {
   st->d_nodes.release();
   st->d_values.release();
   st->d_pairs.release();
+  st->d_bounds.release();
+  st->d_bvals.release();
   st->d_ref.release();
   st->d_img.release();
   st->d_depth.release();
@@ -114,6 +118,8 @@ drk::DevScene dev_scene(lrt_ctx *ctx) {
   s.grad = st.d_grad.p;
   s.pairs = st.d_pairs.p;
   s.n_pairs = uint32_t(st.pairs.size());
+  s.brick_bounds = st.d_bounds.p;
+  s.bvals = st.d_bvals.p;
   s.brick_size = st.hdr.brick_size;
   s.v_size = st.hdr.brick_size + 2 * st.hdr.brick_pad + 1;
   s.layout_in = (st.hdr.aux_data & 0xFF000000u) == (5u << 24) ? 1u : 0u;
@@ -304,6 +310,8 @@ extern "C" lrt_status lrt_dr_set_scene(lrt_ctx *ctx, const lrt_sbs_header *hdr, 
   LRT_CUDA(ctx, cudaMemset(st.d_adam.p, 0, sizeof(float) * 2 * size_t(n_params)));
   LRT_CUDA(ctx, st.d_status.ensure(1));
   LRT_CUDA(ctx, cudaMemset(st.d_status.p, 0, 4));
+  LRT_CUDA(ctx, st.d_bounds.ensure(n_nodes));
+  LRT_CUDA(ctx, st.d_bvals.ensure(size_t(n_nodes) * v3));
   st.has_scene = true;
   return LRT_OK;
 }
@@ -385,6 +393,8 @@ extern "C" lrt_status lrt_dr_render_grad(lrt_ctx *ctx, uint32_t view, double *lo
   LRT_CUDA(ctx, cudaSetDevice(ctx->device));
   st.last_launches = 0;
   LRT_CUDA(ctx, cudaMemsetAsync(st.d_grad.p, 0, sizeof(float) * st.n_params, 0));
+  drk::launch_brick_bounds(dev_scene(ctx), st.n_nodes, st.d_bounds.p, 0);
+  st.last_launches += 1;
   if ((s = render_view(ctx, view, 0)) != LRT_OK) return s;
   if (loss) {
     double l = 0;
@@ -403,6 +413,8 @@ extern "C" lrt_status lrt_dr_step(lrt_ctx *ctx, uint32_t iter, double *losses) {
   st.last_launches = 0;
   const uint32_t nv = uint32_t(st.views.size());
   if (st.preset.accumulate_batch) LRT_CUDA(ctx, cudaMemsetAsync(st.d_grad.p, 0, sizeof(float) * st.n_params, 0));
+  drk::launch_brick_bounds(dev_scene(ctx), st.n_nodes, st.d_bounds.p, 0);
+  st.last_launches += 1;
   for (uint32_t v = 0; v < nv; v++) {
     // the reference refills its gradient buffer for every image of the batch (:412)
     if (!st.preset.accumulate_batch) LRT_CUDA(ctx, cudaMemsetAsync(st.d_grad.p, 0, sizeof(float) * st.n_params, 0));
@@ -453,6 +465,32 @@ extern "C" lrt_status lrt_dr_get(lrt_ctx *ctx, uint32_t what, uint32_t view, voi
   if (bytes != want) return fail(ctx, LRT_ERR_INVALID, "output size mismatch");
   LRT_CUDA(ctx, cudaMemcpy(out, src, bytes, cudaMemcpyDeviceToHost));
   return LRT_OK;
+}
+
+extern "C" lrt_status lrt_dr_query_rays(lrt_ctx *ctx, uint32_t flags, const float *pos_near, const float *dir_far,
+                                        uint32_t n, uint32_t *out) {
+  if (!ctx || !ctx->dr || !ctx->dr->has_scene) return fail(ctx, LRT_ERR_STATE, "lrt_dr_set_scene first");
+  if (!pos_near || !dir_far || !out || n == 0) return fail(ctx, LRT_ERR_INVALID, "empty ray batch");
+  if (flags & ~31u) return fail(ctx, LRT_ERR_INVALID, "unknown ray flags");
+  DrState &st = *ctx->dr;
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  DevBuf<float4> dp, dd;
+  DevBuf<uint32_t> dout;
+  cudaError_t e;
+  if ((e = upload(dp, reinterpret_cast<const float4 *>(pos_near), n)) != cudaSuccess ||
+      (e = upload(dd, reinterpret_cast<const float4 *>(dir_far), n)) != cudaSuccess ||
+      (e = dout.ensure(size_t(n) * 32)) != cudaSuccess) {
+    dp.release(); dd.release(); dout.release();
+    return cuda_fail(ctx, e, "lrt_dr_query_rays buffers");
+  }
+  drk::launch_brick_bounds(dev_scene(ctx), st.n_nodes, st.d_bounds.p, 0);
+  drk::DevScene s = dev_scene(ctx);
+  drk::launch_query(s, flags, dp.p, dd.p, n, dout.p, 0);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(out, dout.p, size_t(n) * 32 * 4, cudaMemcpyDeviceToHost);
+  dp.release(); dd.release(); dout.release();
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "lrt_dr_query_rays");
+  return read_status(ctx);
 }
 
 extern "C" uint32_t lrt_dr_last_launch_count(const lrt_ctx *ctx) {

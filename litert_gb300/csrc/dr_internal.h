@@ -24,6 +24,8 @@ struct DevScene {
   float *grad;               // dLoss/dP
   const float4 *pairs;       // BVH2 fat pairs: 4 float4 each (left min|offset, left max|escape, right ...)
   uint32_t n_pairs;
+  const float2 *brick_bounds; // per brick: min distance value, max |distance value|
+  const float *bvals;         // per brick: its v^3 distance values gathered from P
   uint32_t brick_size, v_size, layout_in, need_normal;
   float inst_bmin[3], inst_bmax[3];
   float inst_inv[12];        // rows 0..2 of the instance's inverse transform
@@ -59,6 +61,9 @@ void launch_border(const DevScene &s, const DevPreset &p, const DevView &v, uint
 void launch_adam(float *x, float *V, float *S, const float *g, uint32_t n, float inv_batch, float lr, float b1,
                  float b2, float eps, double c1, double c2, cudaStream_t st);
 void launch_scale(float *g, uint32_t n, float s, cudaStream_t st);
+void launch_brick_bounds(const DevScene &s, uint32_t n_nodes, float2 *out, cudaStream_t st);
+void launch_query(const DevScene &s, uint32_t flags, const float4 *pos, const float4 *dir, uint32_t n, uint32_t *out,
+                  cudaStream_t st);
 
 }  // namespace drk
 }  // namespace lrt

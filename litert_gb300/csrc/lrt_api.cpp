@@ -441,6 +441,13 @@ extern "C" lrt_status lrt_set_tuning(lrt_ctx *ctx, const char *key, int value) {
   } else if (k == "stage") {
     if (value < 0 || value > 1) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: stage is 0 or 1");
     ctx->tuning.stage = value;
+  } else if (k == "tile_w") {
+    if (value != 4 && value != 8 && value != 16 && value != 32)
+      return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: tile_w is 4, 8, 16 or 32");
+    ctx->tuning.tile_w = value;
+  } else if (k == "stack") {
+    if (value != 32 && value != 64) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: stack is 32 or 64");
+    ctx->tuning.stack = value;
   } else {
     return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: unknown key " + k);
   }
@@ -479,11 +486,13 @@ static lrt_status prepare_views(lrt_ctx *ctx, const lrt_view *views, uint32_t n_
     o.height = in.height;
     o.pix_offset = uint32_t(pix);
     o.tile_offset = uint32_t(tiles);
-    o.tiles_x = (in.width + 7) / 8;
+    const uint32_t tw = uint32_t(ctx->tuning.tile_w), th = 32u / tw;
+    o.tile_w_log2 = tw == 4 ? 2u : tw == 16 ? 4u : tw == 32 ? 5u : 3u;
+    o.tiles_x = (in.width + tw - 1) / tw;
     lrt_inverse4x4(in.proj, o.proj_inv);       // UpdateCamera, Renderer/eye_ray_host.cpp:59-65
     lrt_inverse4x4(in.world_view, o.wv_inv);
     pix += uint64_t(in.width) * in.height;
-    tiles += uint64_t(o.tiles_x) * ((in.height + 3) / 4);
+    tiles += uint64_t(o.tiles_x) * ((in.height + th - 1) / th);
   }
   if (pix >= (1ull << 32) || tiles >= (1ull << 32)) return fail(ctx, LRT_ERR_INVALID, "render: batch too large");
   LRT_CUDA(ctx, ctx->d_views.ensure(n_views));
@@ -493,9 +502,13 @@ static lrt_status prepare_views(lrt_ctx *ctx, const lrt_view *views, uint32_t n_
   return LRT_OK;
 }
 
+// the tuned stack must hold the committed tree: (W-1)*depth + 1 entries, plus slack
+static bool stack_fits(const lrt_ctx *ctx) { return 3 * int(ctx->bvh.max_depth) + 4 <= ctx->tuning.stack; }
+
 static lrt_status render_impl(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, lrt_hit16 *hits16, float *rgba,
                               uint32_t *rgba8, cudaStream_t st, unsigned long long *counters) {
   if (!ctx->committed) return fail(ctx, LRT_ERR_STATE, "render: commit the scene first");
+  if (!stack_fits(ctx)) return fail(ctx, LRT_ERR_UNSUPPORTED, "render: the tuned stack is too small for this BVH");
   LRT_CUDA(ctx, cudaSetDevice(ctx->device));
   uint32_t tiles = 0;
   uint64_t pix = 0;
@@ -563,13 +576,16 @@ extern "C" lrt_status lrt_render_noalloc(lrt_ctx *ctx, const lrt_view *views, ui
     o.height = in.height;
     o.pix_offset = uint32_t(pix);
     o.tile_offset = uint32_t(tiles);
-    o.tiles_x = (in.width + 7) / 8;
+    const uint32_t tw = uint32_t(ctx->tuning.tile_w), th = 32u / tw;
+    o.tile_w_log2 = tw == 4 ? 2u : tw == 16 ? 4u : tw == 32 ? 5u : 3u;
+    o.tiles_x = (in.width + tw - 1) / tw;
     lrt_inverse4x4(in.proj, o.proj_inv);       // UpdateCamera, Renderer/eye_ray_host.cpp:59-65
     lrt_inverse4x4(in.world_view, o.wv_inv);
     pix += uint64_t(in.width) * in.height;
-    tiles += uint64_t(o.tiles_x) * ((in.height + 3) / 4);
+    tiles += uint64_t(o.tiles_x) * ((in.height + th - 1) / th);
   }
   if (pix >= (1ull << 32) || tiles >= (1ull << 32)) return LRT_ERR_INVALID;
+  if (!stack_fits(ctx)) return LRT_ERR_UNSUPPORTED;
   const cudaError_t e = launch_render_noalloc(ctx->dev, hv, n_views, uint32_t(tiles), hits16,
                                               reinterpret_cast<float4 *>(rgba), rgba8, ctx->device, ctx->num_sms,
                                               static_cast<cudaStream_t>(stream), ctx->tuning);
@@ -687,3 +703,191 @@ extern "C" lrt_status lrt_svs_data(const lrt_svs *svs, const lrt_svs_node **node
 }
 
 extern "C" void lrt_svs_free(lrt_svs *svs) { delete svs; }
+
+// ---------------------------------------------------------------- CUDA graph of a batched render
+// The persistent launch of a fixed view batch captured once (work-queue reset +
+// kernel) and replayed; the graph owns its view table and queue head, so
+// replays and ordinary renders on the same context do not interfere.
+struct lrt_graph {
+  int device = 0;
+  uint32_t n_views = 0;
+  std::vector<lrt_view> views;
+  DevBuf<DevView> d_views;
+  DevBuf<uint32_t> d_head;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+static lrt_status fill_views(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, std::vector<DevView> &out,
+                             uint32_t *total_tiles) {
+  uint64_t pix = 0, tiles = 0;
+  out.assign(n_views, DevView{});
+  const uint32_t tw = uint32_t(ctx->tuning.tile_w), th = 32u / tw;
+  for (uint32_t v = 0; v < n_views; v++) {
+    const lrt_view &in = views[v];
+    if (in.width == 0 || in.height == 0 || in.width > 65535 || in.height > 65535)
+      return fail(ctx, LRT_ERR_INVALID, "render: bad view size");
+    DevView &o = out[v];
+    o.width = in.width;
+    o.height = in.height;
+    o.pix_offset = uint32_t(pix);
+    o.tile_offset = uint32_t(tiles);
+    o.tile_w_log2 = tw == 4 ? 2u : tw == 16 ? 4u : tw == 32 ? 5u : 3u;
+    o.tiles_x = (in.width + tw - 1) / tw;
+    lrt_inverse4x4(in.proj, o.proj_inv);
+    lrt_inverse4x4(in.world_view, o.wv_inv);
+    pix += uint64_t(in.width) * in.height;
+    tiles += uint64_t(o.tiles_x) * ((in.height + th - 1) / th);
+  }
+  if (pix >= (1ull << 32) || tiles >= (1ull << 32)) return fail(ctx, LRT_ERR_INVALID, "render: batch too large");
+  *total_tiles = uint32_t(tiles);
+  return LRT_OK;
+}
+
+extern "C" void lrt_render_graph_destroy(lrt_graph *g) {
+  if (!g) return;
+  cudaSetDevice(g->device);
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  g->d_views.release();
+  g->d_head.release();
+  delete g;
+}
+
+extern "C" lrt_status lrt_render_graph_create(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views,
+                                              lrt_hit16 *hits16, float *rgba, uint32_t *rgba8, lrt_graph **out) {
+  if (!ctx || !views || n_views == 0 || !out) return LRT_ERR_INVALID;
+  if (!ctx->committed) return fail(ctx, LRT_ERR_STATE, "graph: commit the scene first");
+  if (!stack_fits(ctx)) return fail(ctx, LRT_ERR_UNSUPPORTED, "graph: the tuned stack is too small for this BVH");
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  std::vector<DevView> hv;
+  uint32_t tiles = 0;
+  lrt_status s = fill_views(ctx, views, n_views, hv, &tiles);
+  if (s != LRT_OK) return s;
+  lrt_graph *g = new (std::nothrow) lrt_graph();
+  if (!g) return fail(ctx, LRT_ERR_OOM, "graph allocation failed");
+  g->device = ctx->device;
+  g->n_views = n_views;
+  g->views.assign(views, views + n_views);
+  cudaError_t e = g->d_views.ensure(n_views);
+  if (e == cudaSuccess) e = g->d_head.ensure(1);
+  if (e == cudaSuccess) e = cudaMemcpy(g->d_views.p, hv.data(), n_views * sizeof(DevView), cudaMemcpyHostToDevice);
+  cudaStream_t cs = nullptr;
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+  if (e == cudaSuccess) {
+    RenderLaunch L;
+    L.views = g->d_views.p;
+    L.n_views = n_views;
+    L.total_tiles = tiles;
+    L.hits16 = hits16;
+    L.rgba = reinterpret_cast<float4 *>(rgba);
+    L.rgba8 = rgba8;
+    L.tile_counter = g->d_head.p;
+    L.counters = nullptr;
+    e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed);
+    if (e == cudaSuccess) {
+      cudaError_t e1 = cudaMemsetAsync(g->d_head.p, 0, sizeof(uint32_t), cs);
+      cudaError_t e2 = e1 == cudaSuccess ? launch_render(ctx->dev, L, ctx->num_sms, cs, false, ctx->tuning) : e1;
+      e = cudaStreamEndCapture(cs, &g->graph);
+      if (e == cudaSuccess) e = e2;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+  }
+  if (cs) cudaStreamDestroy(cs);
+  if (e != cudaSuccess) {
+    lrt_render_graph_destroy(g);
+    return cuda_fail(ctx, e, "lrt_render_graph_create");
+  }
+  *out = g;
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_render_graph_launch(lrt_ctx *ctx, lrt_graph *g, void *stream) {
+  if (!ctx || !g) return LRT_ERR_INVALID;
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  LRT_CUDA(ctx, cudaGraphLaunch(g->exec, static_cast<cudaStream_t>(stream)));
+  ctx->last_launches = 1;
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_render_graph_set_views(lrt_ctx *ctx, lrt_graph *g, const lrt_view *views, uint32_t n_views) {
+  if (!ctx || !g || !views || n_views != g->n_views) return fail(ctx, LRT_ERR_INVALID, "graph: view count differs");
+  for (uint32_t v = 0; v < n_views; v++)
+    if (views[v].width != g->views[v].width || views[v].height != g->views[v].height)
+      return fail(ctx, LRT_ERR_INVALID, "graph: view sizes are fixed at capture");
+  std::vector<DevView> hv;
+  uint32_t tiles = 0;
+  lrt_status s = fill_views(ctx, views, n_views, hv, &tiles);
+  if (s != LRT_OK) return s;
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  LRT_CUDA(ctx, cudaMemcpy(g->d_views.p, hv.data(), n_views * sizeof(DevView), cudaMemcpyHostToDevice));
+  g->views.assign(views, views + n_views);
+  return LRT_OK;
+}
+
+// ---------------------------------------------------------------- autotuner
+// Times each candidate launch shape on the given views (device hit buffer,
+// CUDA events, median of `reps` after one warm-up), keeps the fastest in the
+// context and reports every candidate.  Results do not depend on the choice.
+extern "C" lrt_status lrt_autotune(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, uint32_t reps,
+                                   lrt_tuning_choice *best, lrt_tuning_choice *all, uint32_t cap, uint32_t *n_tried) {
+  if (!ctx || !views || n_views == 0 || reps == 0 || !best) return LRT_ERR_INVALID;
+  if (!ctx->committed) return fail(ctx, LRT_ERR_STATE, "autotune: commit the scene first");
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  uint64_t pix = 0;
+  for (uint32_t v = 0; v < n_views; v++) pix += uint64_t(views[v].width) * views[v].height;
+  LRT_CUDA(ctx, ctx->d_out_hits.ensure(size_t(pix)));
+  const bool sbs = ctx->dev.type == LRT_TYPE_SDF_SBS || ctx->dev.type == LRT_TYPE_SDF_SBS_COL;
+  std::vector<lrt_tuning_choice> cand;
+  for (int tw : {4, 8, 16})
+    for (int stk : {32, 64}) cand.push_back(lrt_tuning_choice{0, 4, 0, tw, stk, 0.0f});
+  if (sbs)
+    for (int stage : {0, 1})
+      for (int bw : {2, 4}) cand.push_back(lrt_tuning_choice{1, bw, stage, 8, 64, 0.0f});
+  const Tuning saved = ctx->tuning;
+  cudaEvent_t a = nullptr, b = nullptr;
+  LRT_CUDA(ctx, cudaEventCreate(&a));
+  LRT_CUDA(ctx, cudaEventCreate(&b));
+  lrt_tuning_choice win{};
+  win.ms = 3.0e38f;
+  uint32_t tried = 0;
+  lrt_status st = LRT_OK;
+  for (lrt_tuning_choice &c : cand) {
+    ctx->tuning.variant = c.variant;
+    ctx->tuning.block_warps = c.block_warps;
+    ctx->tuning.stage = c.stage;
+    ctx->tuning.tile_w = c.tile_w;
+    ctx->tuning.stack = c.stack;
+    if (!stack_fits(ctx)) continue;
+    std::vector<float> ts;
+    for (uint32_t r = 0; r <= reps && st == LRT_OK; r++) {
+      cudaEventRecord(a, nullptr);
+      st = render_impl(ctx, views, n_views, ctx->d_out_hits.p, nullptr, nullptr, nullptr, nullptr);
+      cudaEventRecord(b, nullptr);
+      cudaEventSynchronize(b);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, a, b);
+      if (r > 0) ts.push_back(ms);
+    }
+    if (st != LRT_OK) break;
+    std::sort(ts.begin(), ts.end());
+    c.ms = ts[ts.size() / 2];
+    if (all && tried < cap) all[tried] = c;
+    tried++;
+    if (c.ms < win.ms) win = c;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (st != LRT_OK) {
+    ctx->tuning = saved;
+    return st;
+  }
+  ctx->tuning.variant = win.variant;
+  ctx->tuning.block_warps = win.block_warps;
+  ctx->tuning.stage = win.stage;
+  ctx->tuning.tile_w = win.tile_w;
+  ctx->tuning.stack = win.stack;
+  *best = win;
+  if (n_tried) *n_tried = tried;
+  return LRT_OK;
+}

@@ -81,9 +81,10 @@ struct DevScene {
 struct DevView {
   uint32_t width, height;
   uint32_t pix_offset;   // first pixel in the batched outputs
-  uint32_t tile_offset;  // first 8x4 tile in the global tile space
+  uint32_t tile_offset;  // first tile in the global tile space
   uint32_t tiles_x;      // tiles per row
-  uint32_t _pad[3];
+  uint32_t tile_w_log2;  // a warp's tile is (1 << tile_w_log2) x (32 >> tile_w_log2) pixels
+  uint32_t _pad[2];
   float proj_inv[16];
   float wv_inv[16];
 };
@@ -104,6 +105,8 @@ struct Tuning {
   int variant = 0;          // render kernel: 0 = one ray per lane (while-while), 1 = warp packet traversal
   int block_warps = 4;      // warps per block
   int stage = 0;            // packet kernel: 1 = stage each brick in shared memory, 0 = read corners from global
+  int tile_w = 8;           // warp tile width in pixels (4, 8, 16 or 32; height 32 / tile_w)
+  int stack = 64;           // per-ray traversal stack entries (32 or 64; 32 only for shallow trees)
 };
 
 cudaError_t launch_render(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st, bool count,

@@ -14,13 +14,13 @@
 namespace lrt {
 namespace dev {
 
-template <bool COUNT>
+template <bool COUNT, int STACK>
 __device__ __forceinline__ void visit_node(const DevScene &s, uint32_t ref, float3 rp, float3 inv, float tNear,
                                            float hit_t, uint32_t *st_ref, float *st_t, int &sp, Counters &cnt);
 
 // RayQuery_NearestHit (BVH/BVH2Common.cpp:3490-3559) over the 4-wide BVH.
 // stopOnFirstHit (tFar <= 0) returns the first hit found (RayQuery_AnyHit).
-template <int TYPE, bool COUNT, int MODE = -1>
+template <int TYPE, bool COUNT, int MODE = -1, int STACK = kStackSize>
 __device__ void trace(const DevScene &s, float3 pos, float tNear, float3 dir, float tFar, Hit &hit, Counters &cnt) {
   const bool stop_first = (tFar <= 0.0f);
   if (stop_first) tFar *= -1.0f;
@@ -40,8 +40,8 @@ __device__ void trace(const DevScene &s, float3 pos, float tNear, float3 dir, fl
   const float3 inv = safe_inverse(rd);
   const float tNearSdf = mx(tNear, 0.1f);   // SDF bias passed to every leaf type (:3472-3476)
 
-  uint32_t st_ref[kStackSize];
-  float st_t[kStackSize];
+  uint32_t st_ref[STACK];
+  float st_t[STACK];
   int sp = 0;
   st_ref[sp] = 0;            // root wide node
   st_t[sp] = -3.4e38f;
@@ -62,7 +62,7 @@ __device__ void trace(const DevScene &s, float3 pos, float tNear, float3 dir, fl
         have_leaf = true;
         break;
       }
-      visit_node<COUNT>(s, ref, rp, inv, tNear, hit.t, st_ref, st_t, sp, cnt);
+      visit_node<COUNT, STACK>(s, ref, rp, inv, tNear, hit.t, st_ref, st_t, sp, cnt);
     }
     if (!have_leaf) break;
     const float t_before = hit.t;
@@ -78,7 +78,7 @@ __device__ void trace(const DevScene &s, float3 pos, float tNear, float3 dir, fl
 
 // One inner node of the per-ray traversal: test the four child boxes with the
 // reference slab test and push the entered ones far-to-near.
-template <bool COUNT>
+template <bool COUNT, int STACK>
 __device__ __forceinline__ void visit_node(const DevScene &s, uint32_t ref, float3 rp, float3 inv, float tNear,
                                            float hit_t, uint32_t *st_ref, float *st_t, int &sp, Counters &cnt) {
   {
@@ -116,14 +116,15 @@ __device__ __forceinline__ void visit_node(const DevScene &s, uint32_t ref, floa
     // The host rejects trees deeper than the stack allows ((W-1)*depth + 1 entries),
     // so this bound never drops an entry.
     for (int i = 0; i < nk; i++) {
-      if (sp < kStackSize) { st_ref[sp] = kr[i]; st_t[sp] = kt[i]; sp++; }
+      if (sp < STACK) { st_ref[sp] = kr[i]; st_t[sp] = kt[i]; sp++; }
     }
   }
 }
 
-// Persistent render kernel: each warp pulls 8x4-pixel tiles of the flattened
-// multi-view tile space from a global queue head and traces one ray per lane.
-template <int TYPE, bool COUNT, int MODE>
+// Persistent render kernel: each warp pulls 32-pixel tiles (8x4 by default, the
+// shape is tunable) of the flattened multi-view tile space from a global queue
+// head and traces one ray per lane.
+template <int TYPE, bool COUNT, int MODE, int STACK>
 __global__ void __launch_bounds__(128, 5) render_kernel(DevScene s, RenderLaunch L) {
   const uint32_t lane = threadIdx.x & 31u;
   Counters cnt = {0, 0, 0, 0};
@@ -138,8 +139,9 @@ __global__ void __launch_bounds__(128, 5) render_kernel(DevScene s, RenderLaunch
     uint32_t v = 0;
     while (v + 1 < L.n_views && L.views[v + 1].tile_offset <= tile) v++;
     const DevView &V = L.views[v];
-    const uint32_t lt = tile - V.tile_offset;
-    const uint32_t x = (lt % V.tiles_x) * 8u + (lane & 7u), y = (lt / V.tiles_x) * 4u + (lane >> 3);
+    const uint32_t lt = tile - V.tile_offset, lw = V.tile_w_log2;
+    const uint32_t x = (lt % V.tiles_x) * (1u << lw) + (lane & ((1u << lw) - 1u));
+    const uint32_t y = (lt / V.tiles_x) * (32u >> lw) + (lane >> lw);
     if (x >= V.width || y >= V.height) continue;   // all lanes meet again at the queue shuffle
     float4 acc = make_float4(0, 0, 0, 0);
     Hit first;
@@ -149,7 +151,7 @@ __global__ void __launch_bounds__(128, 5) render_kernel(DevScene s, RenderLaunch
       float3 pos, dir;
       eye_ray(x, y, V.width, V.height, dx, dy, V.proj_inv, V.wv_inv, pos, dir);
       Hit hit;
-      trace<TYPE, COUNT, MODE>(s, pos, 0.0f, dir, 1e9f, hit, cnt);
+      trace<TYPE, COUNT, MODE, STACK>(s, pos, 0.0f, dir, 1e9f, hit, cnt);
       if (si == 0) first = hit;
       if (L.rgba || L.rgba8) {
         const float4 c = shade(s, hit, dir);
@@ -203,33 +205,40 @@ __global__ void __launch_bounds__(128) query_kernel(DevScene s, const float4 *po
 
 }  // namespace dev
 
-template <int TYPE, bool COUNT, int MODE>
+template <int TYPE, bool COUNT, int MODE, int STACK>
 static cudaError_t launch_render_m(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st) {
   int per_sm = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::render_kernel<TYPE, COUNT, MODE>, 128, 0);
+  cudaError_t e =
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::render_kernel<TYPE, COUNT, MODE, STACK>, 128, 0);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   uint32_t blocks = uint32_t(num_sms) * uint32_t(per_sm);
   const uint32_t max_blocks = (L.total_tiles + 3) / 4;
   if (blocks > max_blocks) blocks = max_blocks;
   if (blocks == 0) blocks = 1;
-  dev::render_kernel<TYPE, COUNT, MODE><<<blocks, 128, 0, st>>>(s, L);
+  dev::render_kernel<TYPE, COUNT, MODE, STACK><<<blocks, 128, 0, st>>>(s, L);
   return cudaGetLastError();
 }
 
 template <int TYPE, bool COUNT>
-static cudaError_t launch_render_c(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st) {
-  if (TYPE == LRT_TYPE_MESH_TRIANGLE) return launch_render_m<TYPE, COUNT, -1>(s, L, num_sms, st);
+static cudaError_t launch_render_c(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st,
+                                   const Tuning &tu) {
+  if (TYPE == LRT_TYPE_MESH_TRIANGLE) return launch_render_m<TYPE, COUNT, -1, kStackSize>(s, L, num_sms, st);
   switch (s.preset.sdf_node_intersect) {
-    case LRT_INTERSECT_NEWTON: return launch_render_m<TYPE, COUNT, LRT_INTERSECT_NEWTON>(s, L, num_sms, st);
-    case LRT_INTERSECT_ST: return launch_render_m<TYPE, COUNT, LRT_INTERSECT_ST>(s, L, num_sms, st);
-    default: return launch_render_m<TYPE, COUNT, -1>(s, L, num_sms, st);
+    case LRT_INTERSECT_NEWTON:
+      // the headline configuration also comes with a 32-entry stack for shallow trees
+      if (TYPE == LRT_TYPE_SDF_SBS && !COUNT && tu.stack == 32)
+        return launch_render_m<TYPE, COUNT, LRT_INTERSECT_NEWTON, 32>(s, L, num_sms, st);
+      return launch_render_m<TYPE, COUNT, LRT_INTERSECT_NEWTON, kStackSize>(s, L, num_sms, st);
+    case LRT_INTERSECT_ST: return launch_render_m<TYPE, COUNT, LRT_INTERSECT_ST, kStackSize>(s, L, num_sms, st);
+    default: return launch_render_m<TYPE, COUNT, -1, kStackSize>(s, L, num_sms, st);
   }
 }
 
 template <int TYPE>
-static cudaError_t launch_render_t(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st, bool count) {
-  return count ? launch_render_c<TYPE, true>(s, L, num_sms, st) : launch_render_c<TYPE, false>(s, L, num_sms, st);
+static cudaError_t launch_render_t(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st, bool count,
+                                   const Tuning &tu) {
+  return count ? launch_render_c<TYPE, true>(s, L, num_sms, st, tu) : launch_render_c<TYPE, false>(s, L, num_sms, st, tu);
 }
 
 cudaError_t launch_render(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st, bool count,
@@ -237,9 +246,9 @@ cudaError_t launch_render(const DevScene &s, const RenderLaunch &L, int num_sms,
   const bool sbs = s.type == LRT_TYPE_SDF_SBS || s.type == LRT_TYPE_SDF_SBS_COL;
   if (sbs && tu.variant == 1) return launch_render_packet(s, L, num_sms, st, count, tu);
   switch (s.type) {
-    case LRT_TYPE_MESH_TRIANGLE: return launch_render_t<LRT_TYPE_MESH_TRIANGLE>(s, L, num_sms, st, count);
-    case LRT_TYPE_SDF_SVS: return launch_render_t<LRT_TYPE_SDF_SVS>(s, L, num_sms, st, count);
-    default: return launch_render_t<LRT_TYPE_SDF_SBS>(s, L, num_sms, st, count);
+    case LRT_TYPE_MESH_TRIANGLE: return launch_render_t<LRT_TYPE_MESH_TRIANGLE>(s, L, num_sms, st, count, tu);
+    case LRT_TYPE_SDF_SVS: return launch_render_t<LRT_TYPE_SDF_SVS>(s, L, num_sms, st, count, tu);
+    default: return launch_render_t<LRT_TYPE_SDF_SBS>(s, L, num_sms, st, count, tu);
   }
 }
 

@@ -99,7 +99,9 @@ __global__ void __launch_bounds__(256) render_packet_kernel(DevScene s, RenderLa
     while (v + 1 < L.n_views && L.views[v + 1].tile_offset <= tile) v++;
     const DevView &V = L.views[v];
     const uint32_t lt = tile - V.tile_offset;
-    const uint32_t x = (lt % V.tiles_x) * 8u + (lane & 7u), y = (lt / V.tiles_x) * 4u + (lane >> 3);
+    const uint32_t lw = V.tile_w_log2;
+    const uint32_t x = (lt % V.tiles_x) * (1u << lw) + (lane & ((1u << lw) - 1u));
+    const uint32_t y = (lt / V.tiles_x) * (32u >> lw) + (lane >> lw);
     const bool in_img = x < V.width && y < V.height;
     float4 acc = make_float4(0, 0, 0, 0);
     Hit first;

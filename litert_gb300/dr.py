@@ -52,6 +52,7 @@ def _lib():
             "lrt_dr_optimize": (I, [P, U32, U32, VP]),
             "lrt_dr_get": (I, [P, U32, U32, VP, C.c_uint64]),
             "lrt_dr_last_launch_count": (U32, [P]),
+            "lrt_dr_query_rays": (I, [P, U32, VP, VP, U32, VP]),
             "lrt_dr_grid_sbs": (I, [U32, U32, C.POINTER(lrt.SdfDesc), VP, C.POINTER(lrt.SbsHeader), C.POINTER(VP),
                                     C.POINTER(U32), C.POINTER(VP), C.POINTER(C.c_uint64), C.POINTER(VP),
                                     C.POINTER(U32)]),
@@ -210,6 +211,14 @@ class MultiRendererDR:
 
     def getLastdLoss_dS(self):
         return self.get(GET_GRAD)
+
+    def query_rays(self, flags, pos_near, dir_far):
+        """RayQuery_NearestHitWithGrad on a ray batch: (n, 32) uint32 records (see lrt_dr.h)."""
+        pos = np.ascontiguousarray(pos_near, np.float32).reshape(-1, 4)
+        d = np.ascontiguousarray(dir_far, np.float32).reshape(-1, 4)
+        out = np.zeros((pos.shape[0], 32), np.uint32)
+        self._chk(_lib().lrt_dr_query_rays(self._ctx, flags, lrt._ptr(pos), lrt._ptr(d), pos.shape[0], lrt._ptr(out)))
+        return out
 
     def last_launch_count(self):
         return _lib().lrt_dr_last_launch_count(self._ctx)

@@ -53,6 +53,14 @@ class View(C.Structure):
                 ("proj", C.c_float * 16)]
 
 
+class TuningChoice(C.Structure):
+    _fields_ = [("variant", C.c_int), ("block_warps", C.c_int), ("stage", C.c_int), ("tile_w", C.c_int),
+                ("stack", C.c_int), ("ms", C.c_float)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class SdfDesc(C.Structure):
     _fields_ = [("n_spheres", C.c_uint32), ("spheres", C.POINTER(C.c_float)), ("n_boxes", C.c_uint32),
                 ("boxes", C.POINTER(C.c_float)), ("k", C.c_float)]
@@ -107,6 +115,11 @@ def lib():
             "lrt_free": (None, [VP]),
             "lrt_set_tuning": (I, [P, C.c_char_p, I]),
             "lrt_render_noalloc": (I, [P, VP, U32, VP, VP, VP, VP]),
+            "lrt_autotune": (I, [P, VP, U32, U32, C.POINTER(TuningChoice), VP, U32, C.POINTER(U32)]),
+            "lrt_render_graph_create": (I, [P, VP, U32, VP, VP, VP, C.POINTER(P)]),
+            "lrt_render_graph_launch": (I, [P, P, VP]),
+            "lrt_render_graph_set_views": (I, [P, P, VP, U32]),
+            "lrt_render_graph_destroy": (None, [P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -333,6 +346,36 @@ class Scene:
         """Asynchronous render into device buffers (e.g. torch tensors' data_ptr())."""
         self._chk(lib().lrt_render(self._ctx, C.cast(view_array, C.c_void_p), n_views, C.c_void_p(hits_ptr or None),
                                    C.c_void_p(rgba_ptr or None), C.c_void_p(rgba8_ptr or None), C.c_void_p(stream or None)))
+
+    def autotune(self, views, reps=3):
+        """lrt_autotune: returns (best choice dict, list of all candidates tried)."""
+        va = make_views(views)
+        best = TuningChoice()
+        allc = (TuningChoice * 64)()
+        n = C.c_uint32()
+        self._chk(lib().lrt_autotune(self._ctx, C.cast(va, C.c_void_p), len(views), reps, C.byref(best),
+                                     C.cast(allc, C.c_void_p), 64, C.byref(n)))
+        return best.as_dict(), [allc[i].as_dict() for i in range(n.value)]
+
+    def graph_create(self, views, hits_ptr=0, rgba_ptr=0, rgba8_ptr=0):
+        """lrt_render_graph_create over device output pointers; returns a handle."""
+        va = make_views(views)
+        g = C.c_void_p()
+        self._chk(lib().lrt_render_graph_create(self._ctx, C.cast(va, C.c_void_p), len(views), C.c_void_p(hits_ptr or None),
+                                                C.c_void_p(rgba_ptr or None), C.c_void_p(rgba8_ptr or None),
+                                                C.byref(g)))
+        return g
+
+    def graph_launch(self, g, stream=0):
+        self._chk(lib().lrt_render_graph_launch(self._ctx, g, C.c_void_p(stream or None)))
+
+    def graph_set_views(self, g, views):
+        va = make_views(views)
+        self._chk(lib().lrt_render_graph_set_views(self._ctx, g, C.cast(va, C.c_void_p), len(views)))
+
+    @staticmethod
+    def graph_destroy(g):
+        lib().lrt_render_graph_destroy(g)
 
     def last_launch_count(self):
         return lib().lrt_last_launch_count(self._ctx)

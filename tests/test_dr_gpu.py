@@ -242,3 +242,48 @@ def test_host_rejects_bad_input():
         R.render_grad(0)                 # no scene / reference yet
     assert e.value.status == 7
     R.close()
+
+
+@pytest.mark.parametrize("flags,render_mode", [(8, dr.RENDER_LAMBERT), (1 | 2 | 4, dr.RENDER_LAMBERT), (8, dr.RENDER_MASK),
+                                               (16, dr.RENDER_LINEAR_DEPTH)])
+@pytest.mark.parametrize("layout_in", [True, False])
+def test_query_rays_match_oracle(flags, render_mode, layout_in):
+    """Per-ray RayQuery_NearestHitWithGrad: the hit and the border relaxation
+    point (t, sdf, colour, normal, indices, dSDF/dtheta) bit for bit, on eye rays
+    of three views and rays from random points, with the exact empty-voxel skips
+    active on the GPU (the oracle walks every voxel)."""
+    hdr, nodes, values, target, init, views = _problem(n_views=3, w=96, h=96, layout_in=layout_in)
+    rng = np.random.default_rng(9)
+    params = target.copy()
+    nd = 25 ** 3
+    params[:nd] += rng.normal(0, 0.004, nd).astype(np.float32)
+    R = dr.MultiRendererDR()
+    R.SetScene(hdr, nodes, values, params)
+    R.SetPreset(dr.default_preset(render_mode=render_mode))
+    P, D = [], []
+    for (w, h, wv, pj) in views:
+        p_, d_ = orc.eye_rays(w, h, lrt.inverse4x4(pj), lrt.inverse4x4(wv), np.arange(w * h, dtype=np.uint32),
+                              0.37, 0.61)
+        P.append(p_)
+        D.append(d_)
+    n = 6000
+    rp = np.zeros((n, 4), np.float32)
+    rp[:, :3] = rng.uniform(-1.6, 1.6, (n, 3))
+    rd = np.zeros((n, 4), np.float32)
+    d = rng.normal(size=(n, 3))
+    rd[:, :3] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    rd[:, 3] = 1e9
+    P.append(rp)
+    D.append(rd)
+    P, D = np.concatenate(P), np.concatenate(D)
+    got = R.query_rays(flags, P, D)
+    osc = _oracle(hdr, nodes, values, params, R.bvh2(), need_normal=render_mode in (1, 4))
+    o = osc.query(params, flags, P, D).view(np.uint32).reshape(len(P), -1)
+    want = np.concatenate([o[:, [0, 1]], o[:, 4:7], o[:, 8:11], o[:, [14, 21]], o[:, 18:21], o[:, 22:25],
+                           o[:, 28:36], o[:, 36:44]], 1)
+    assert (want[:, 1] != 0xFFFFFFFF).sum() > 3000
+    if flags & 8:
+        assert (want[:, 9].view(np.float32) < 1e-3).sum() > 50
+    bad = np.nonzero((got != want).any(1))[0]
+    assert bad.size == 0, (bad.size, bad[:5], got[bad[:2]], want[bad[:2]])
+    R.close()

@@ -1,0 +1,83 @@
+"""GPU: launch-shape tuning, the autotuner and CUDA-graph replay of the batched
+render.  Every tile shape / stack depth / kernel variant gives the same hit
+records bit for bit; a replayed graph equals a direct render, also after its
+cameras change; the autotuner picks one of its candidates and leaves results
+unchanged."""
+import numpy as np
+import pytest
+import torch
+
+from litert_gb300 import lrt, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def scene():
+    h, n, v = lrt.sbs_from_sdf(lrt.Sdf(**scenes.union_params()), 5, 8)
+    s = lrt.Scene(0)
+    g = s.add_sbs(h, n, v)
+    s.add_instance(g)
+    s.commit_scene()
+    s.set_preset(render_mode=lrt.RENDER_MODE_NORMAL, sdf_node_intersect=lrt.INTERSECT_NEWTON)
+    yield s
+    s.close()
+
+
+def _views():
+    return scenes.union_views(n_views=5, lo=96, hi=300)
+
+
+def _render(s, views):
+    return s.render_host(views, hits=True)["hits"].view(np.uint32).copy()
+
+
+@pytest.mark.parametrize("tile_w,stack,variant", [(4, 64, 0), (16, 64, 0), (32, 64, 0), (8, 32, 0), (8, 64, 1),
+                                                  (16, 32, 0)])
+def test_launch_shapes_bit_identical(scene, tile_w, stack, variant):
+    views = _views()
+    ref = _render(scene, views)
+    scene.set_tuning("tile_w", tile_w)
+    scene.set_tuning("stack", stack)
+    scene.set_tuning("variant", variant)
+    try:
+        got = _render(scene, views)
+    finally:
+        scene.set_tuning("tile_w", 8)
+        scene.set_tuning("stack", 64)
+        scene.set_tuning("variant", 0)
+    assert np.array_equal(got, ref)
+
+
+def test_graph_replay_matches_render(scene):
+    views = _views()
+    n = sum(w * h for w, h, _, _ in views)
+    ref = _render(scene, views)
+    out = torch.zeros(n * 4, dtype=torch.float32, device="cuda")
+    g = scene.graph_create(views, hits_ptr=out.data_ptr())
+    try:
+        for _ in range(3):
+            out.zero_()
+            scene.graph_launch(g)
+            torch.cuda.synchronize()
+            assert np.array_equal(out.cpu().numpy().view(np.uint32), ref)
+        moved = scenes.union_views(n_views=5, lo=96, hi=300, cam_seed=11)
+        moved = [(w, h, mv[2], mv[3]) for (w, h, _, _), mv in zip(views, moved)]
+        scene.graph_set_views(g, moved)
+        scene.graph_launch(g)
+        torch.cuda.synchronize()
+        assert np.array_equal(out.cpu().numpy().view(np.uint32), _render(scene, moved))
+        with pytest.raises(lrt.LrtError):
+            scene.graph_set_views(g, moved[:4])
+    finally:
+        lrt.Scene.graph_destroy(g)
+
+
+def test_autotune_picks_a_candidate(scene):
+    views = _views()
+    ref = _render(scene, views)
+    best, tried = scene.autotune(views, reps=2)
+    assert len(tried) >= 6
+    assert best["ms"] == min(c["ms"] for c in tried)
+    assert best["tile_w"] in (4, 8, 16) and best["stack"] in (32, 64)
+    assert np.array_equal(_render(scene, views), ref)
