@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--no-configs", action="store_true", help="skip the sphere and triangle-mesh lines")
     ap.add_argument("--no-autotune", action="store_true", help="use --variant/--block-warps/--stage as given")
     ap.add_argument("--no-graph", action="store_true", help="launch directly instead of replaying a CUDA graph")
+    ap.add_argument("--no-proposal", action="store_true", help="skip the learned-proposal measurement")
+    ap.add_argument("--prop-steps", type=int, default=20000, help="proposal training steps (batch 8192)")
     return ap.parse_args()
 
 
@@ -225,6 +227,71 @@ def run_small_configs(args, dev, torch):
                                  "sample": "the 1920x1080 view"}})
     sc.close()
     return out
+
+
+def run_proposal(args, scene, dev, torch):
+    """Learned proposal on the large SBS scene: triples from 64 training views
+    (1024^2, seed 6), Adam training (lr 1e-3, batch 8192, seed 7), then plain vs
+    proposal Mrays/s on 16 held-out views (1024^2, seed 8), each as a replayed
+    CUDA graph, with the hit records compared bit for bit."""
+    from litert_gb300 import lrt, proposal as pp, scenes
+    train_views = scenes.proposal_views(64, 1024, seed=6)
+    eval_views = scenes.proposal_views(16, 1024, seed=8)
+    pp.set_weights(scene, pp.init_weights(7))
+    pp.clear(scene)
+    t0 = time.time()
+    n_trip = pp.collect(scene, train_views, capacity=50_000_000)
+    t_collect = time.time() - t0
+    t0 = time.time()
+    losses = pp.train(scene, args.prop_steps, batch=8192, lr=1e-3, seed=7)
+    t_train = time.time() - t0
+    n = sum(w * h for w, h, _, _ in eval_views)
+    hits = torch.empty(n * 4, dtype=torch.float32, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    out = {}
+    recs = {}
+    for mode in (0, 1):
+        scene.set_tuning("proposal", mode)
+        g = scene.graph_create(eval_views, hits_ptr=hits.data_ptr())
+        for _ in range(3):
+            scene.graph_launch(g, stream.cuda_stream)
+        torch.cuda.synchronize(dev)
+        if mode:
+            pp.stats(scene)
+        ts = []
+        for i in range(max(args.steps, 5)):
+            flush.fill_(float(i))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            scene.graph_launch(g, stream.cuda_stream)
+            b.record(stream)
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+        if mode:
+            st = pp.stats(scene)
+        lrt.Scene.graph_destroy(g)
+        ms = statistics.median(ts)
+        out["proposal" if mode else "plain"] = {"ms": ms, "mrays": n / (ms * 1e-3) / 1e6}
+        recs[mode] = hits.cpu().numpy().view(np.uint32).reshape(-1, 4).copy()
+    scene.set_tuning("proposal", 0)
+    a, b = recs[0], recs[1]
+    mask_same = np.array_equal(a[:, 1] != lrt.MISS, b[:, 1] != lrt.MISS)
+    both = (a[:, 1] != lrt.MISS) & (b[:, 1] != lrt.MISS)
+    dt = np.abs(a[both, 0].view(np.float32) - b[both, 0].view(np.float32))
+    return {"metric": "SBS Mrays/s plain vs proposal at equal depth error", "unit": UNIT,
+            "plain": out["plain"]["mrays"], "proposal": out["proposal"]["mrays"],
+            "speedup": out["proposal"]["mrays"] / out["plain"]["mrays"],
+            "ms_plain": out["plain"]["ms"], "ms_proposal": out["proposal"]["ms"],
+            "hit_mask_identical": bool(mask_same), "records_identical": bool(np.array_equal(a, b)),
+            "max_dt_over_extent": float(dt.max() / 2.0) if dt.size else 0.0,
+            "proposals_per_step": st["proposals"] // max(1, len(ts)), "acceptance": st["jumps"] / max(1, st["proposals"]),
+            "jump_hit_rate": st["jump_hits"] / max(1, st["jumps"]),
+            "triples": int(n_trip), "train_steps": args.prop_steps, "batch": 8192,
+            "loss_first": float(losses[:10].mean()), "loss_last": float(losses[-100:].mean()),
+            "collect_s": round(t_collect, 2), "train_s": round(t_train, 2),
+            "config": {"workload": "proposal-16view-1024", "rays_per_step": n, "eval_views": 16,
+                       "train_views": 64, "network": "16-32-32-1 ReLU, BF16 mma.sync m16n8k16, FP32 accumulation"}}
 
 
 def dr_setup(dev_index=0):
@@ -497,6 +564,8 @@ def main():
         if cpu:
             line["cpu_baseline"] = {"value": cpu["value"], "unit": UNIT, "cores": cpu["cores"], "kind": "port",
                                     "sample": f"{cpu['rays']} strided pixels of the 16 views ({cpu['seconds']:.1f} s)"}
+        if not args.no_proposal and world == 1:
+            line["proposal"] = run_proposal(args, scene, dev, torch)
         if not args.no_dr and world == 1:
             line["dr"] = run_dr(args, dev, torch)
         if world == 1 and not args.no_configs:

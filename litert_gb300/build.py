@@ -17,8 +17,8 @@ LIB = os.path.join(OUT, "liblrt_gb300.so")
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
-CU_SOURCES = ["trace.cu", "trace_pkt.cu", "dr.cu"]
-CPP_SOURCES = ["lrt_api.cpp", "scene_build.cpp", "bvh_build.cpp", "dr_api.cpp"]
+CU_SOURCES = ["trace.cu", "trace_pkt.cu", "dr.cu", "proposal.cu"]
+CPP_SOURCES = ["lrt_api.cpp", "scene_build.cpp", "bvh_build.cpp", "dr_api.cpp", "proposal_api.cpp"]
 
 
 def _nvcc():

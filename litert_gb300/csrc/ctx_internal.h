@@ -13,6 +13,10 @@
 namespace lrt {
 struct DrState;
 void dr_state_free(DrState *st);
+struct ProposalState;
+void proposal_state_free(ProposalState *st);
+// the batched render launch of the context's kernel choice (plain or proposal)
+cudaError_t dispatch_render(struct ::lrt_ctx *ctx, const RenderLaunch &L, cudaStream_t st, bool count);
 }  // namespace lrt
 
 namespace lrt {
@@ -93,6 +97,8 @@ struct lrt_ctx {
   uint32_t brick_stride = 0;   // device words per brick (16-byte multiple)
   Tuning tuning;
   lrt::DrState *dr = nullptr;  // differentiable-render state (dr_api.cpp)
+  lrt::ProposalState *prop = nullptr;   // learned proposal (proposal_api.cpp)
+  int use_proposal = 0;        // render SBS leaves with the proposal kernel
 };
 
 static inline lrt_status fail(lrt_ctx *ctx, lrt_status s, const std::string &msg) {

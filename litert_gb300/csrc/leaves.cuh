@@ -239,9 +239,14 @@ struct SharedLoader {
 // for each axis max(lo, hi) is the plane the ray direction points to, so the
 // value equals RayBoxIntersection2's.  The near planes are evaluated only in
 // occupied voxels.
+//
+// start_t (default: no effect) lets the walk begin at a later distance; the
+// proposal path passes the entry of a voxel it has shown every earlier voxel of
+// the segment to be empty, where the reference's walk would run no finder.
 template <bool COUNT, bool STAGED, int MODE = -1>
 __device__ void brick_intersect(const DevScene &s, float3 ray_pos, float3 ray_dir, float3 inv, float tNear,
-                                uint32_t brick, Hit &hit, Counters &cnt, const float *staged = nullptr) {
+                                uint32_t brick, Hit &hit, Counters &cnt, const float *staged = nullptr,
+                                float start_t = -3.4e38f) {
   const lrt_sbs_header &h = s.sbs_hdr;
   const lrt_preset &pr = s.preset;
   const uint32_t type = s.type;
@@ -256,6 +261,7 @@ __device__ void brick_intersect(const DevScene &s, float3 ray_pos, float3 ray_di
   const float3 bmin = add(f3(-1, -1, -1), scl(sz_inv, f3(px, py, pz)));
   const float3 bmax = add(bmin, scl(sz_inv, f3(1, 1, 1)));
   float2 bnf = ray_box(ray_pos, inv, bmin.x, bmin.y, bmin.z, bmax.x, bmax.y, bmax.z);
+  bnf.x = fmx(bnf.x, start_t);
   const float old_t = hit.t;
   const float scale = 0.5f * sz * bs;
   const uint32_t *occ = s.occ + size_t(brick) * s.occ_words;

@@ -136,6 +136,8 @@ extern "C" void lrt_destroy(lrt_ctx *ctx) {
   cudaSetDevice(ctx->device);
   lrt::dr_state_free(ctx->dr);
   ctx->dr = nullptr;
+  lrt::proposal_state_free(ctx->prop);
+  ctx->prop = nullptr;
   release_scene(ctx);
   ctx->d_tile_counter.release();
   ctx->d_views.release();
@@ -448,6 +450,9 @@ extern "C" lrt_status lrt_set_tuning(lrt_ctx *ctx, const char *key, int value) {
   } else if (k == "stack") {
     if (value != 32 && value != 64) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: stack is 32 or 64");
     ctx->tuning.stack = value;
+  } else if (k == "proposal") {
+    if (value < 0 || value > 1) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: proposal is 0 or 1");
+    ctx->use_proposal = value;
   } else {
     return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: unknown key " + k);
   }
@@ -524,7 +529,7 @@ static lrt_status render_impl(lrt_ctx *ctx, const lrt_view *views, uint32_t n_vi
   L.tile_counter = ctx->d_tile_counter.p;
   L.counters = counters;
   LRT_CUDA(ctx, cudaMemsetAsync(ctx->d_tile_counter.p, 0, sizeof(uint32_t), st));
-  LRT_CUDA(ctx, launch_render(ctx->dev, L, ctx->num_sms, st, counters != nullptr, ctx->tuning));
+  LRT_CUDA(ctx, dispatch_render(ctx, L, st, counters != nullptr));
   ctx->last_launches = 1;
   return LRT_OK;
 }
@@ -787,7 +792,7 @@ extern "C" lrt_status lrt_render_graph_create(lrt_ctx *ctx, const lrt_view *view
     e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed);
     if (e == cudaSuccess) {
       cudaError_t e1 = cudaMemsetAsync(g->d_head.p, 0, sizeof(uint32_t), cs);
-      cudaError_t e2 = e1 == cudaSuccess ? launch_render(ctx->dev, L, ctx->num_sms, cs, false, ctx->tuning) : e1;
+      cudaError_t e2 = e1 == cudaSuccess ? dispatch_render(ctx, L, cs, false) : e1;
       e = cudaStreamEndCapture(cs, &g->graph);
       if (e == cudaSuccess) e = e2;
     }

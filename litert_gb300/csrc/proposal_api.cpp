@@ -1,0 +1,302 @@
+// C ABI of the learned proposal: weights, triple collection, training and the
+// render dispatch between the plain and the proposal kernels.  Host code only;
+// kernels live in proposal.cu.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "ctx_internal.h"
+#include "lrt_proposal.h"
+#include "proposal_internal.h"
+
+namespace lrt {
+
+struct ProposalState {
+  DevBuf<float> master, grad, adam_m, adam_v, losses;
+  DevBuf<__nv_bfloat16> wbf;
+  DevBuf<unsigned int> ticket;
+  DevBuf<__nv_bfloat16> feat;
+  DevBuf<float> target;
+  DevBuf<unsigned long long> count, stats;
+  DevBuf<DevView> views;
+  uint64_t n = 0;
+  bool has_weights = false;
+};
+
+void proposal_state_free(ProposalState *st) {
+  if (!st) return;
+  for (auto *b : {&st->master, &st->grad, &st->adam_m, &st->adam_v, &st->losses, &st->target}) b->release();
+  st->wbf.release();
+  st->ticket.release();
+  st->feat.release();
+  st->count.release();
+  st->stats.release();
+  st->views.release();
+  delete st;
+}
+
+namespace {
+MlpState mlp_state(ProposalState &p, float *loss) {
+  MlpState m;
+  m.master = p.master.p;
+  m.wbf = p.wbf.p;
+  m.grad = p.grad.p;
+  m.adam_m = p.adam_m.p;
+  m.adam_v = p.adam_v.p;
+  m.ticket = p.ticket.p;
+  m.loss = loss;
+  return m;
+}
+
+// round to nearest even BF16 (the device's __float2bfloat16_rn for finite values)
+uint16_t f2bf(float x) {
+  uint32_t u;
+  std::memcpy(&u, &x, 4);
+  if ((u & 0x7F800000u) == 0x7F800000u) return uint16_t(u >> 16);
+  u += 0x7FFFu + ((u >> 16) & 1u);
+  return uint16_t(u >> 16);
+}
+float bf2f(uint16_t b) {
+  const uint32_t u = uint32_t(b) << 16;
+  float x;
+  std::memcpy(&x, &u, 4);
+  return x;
+}
+
+lrt_status ensure(lrt_ctx *ctx) {
+  if (!ctx) return LRT_ERR_INVALID;
+  if (ctx->prop) return LRT_OK;
+  ProposalState *p = new (std::nothrow) ProposalState();
+  if (!p) return fail(ctx, LRT_ERR_OOM, "proposal state allocation failed");
+  ctx->prop = p;
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  for (auto *b : {&p->master, &p->grad, &p->adam_m, &p->adam_v}) LRT_CUDA(ctx, b->ensure(LRT_MLP_PARAMS));
+  LRT_CUDA(ctx, p->wbf.ensure(1792));
+  LRT_CUDA(ctx, p->ticket.ensure(1));
+  LRT_CUDA(ctx, p->count.ensure(1));
+  LRT_CUDA(ctx, p->stats.ensure(4));
+  LRT_CUDA(ctx, cudaMemset(p->grad.p, 0, 4 * LRT_MLP_PARAMS));
+  LRT_CUDA(ctx, cudaMemset(p->ticket.p, 0, 4));
+  LRT_CUDA(ctx, cudaMemset(p->stats.p, 0, 32));
+  return LRT_OK;
+}
+}  // namespace
+
+// the plain kernels, or the proposal kernel for DX-layout SBS scenes with the
+// NEWTON finder when it is switched on and the network has weights
+cudaError_t dispatch_render(lrt_ctx *ctx, const RenderLaunch &L, cudaStream_t st, bool count) {
+  const DevScene &s = ctx->dev;
+  const uint32_t layout = s.sbs_hdr.aux_data & 0xFF000000u;
+  const bool dx = s.type == LRT_TYPE_SDF_SBS && layout != LRT_SBS_LAYOUT_ID32F_IRGB32F &&
+                  layout != LRT_SBS_LAYOUT_ID32F_IRGB32F_IN;
+  if (ctx->use_proposal && !count && dx && s.preset.sdf_node_intersect == LRT_INTERSECT_NEWTON && ctx->prop &&
+      ctx->prop->has_weights && s.preset.spp <= 1)
+    return launch_render_proposal(s, L, mlp_state(*ctx->prop, nullptr), ctx->prop->stats.p, ctx->num_sms, st);
+  return launch_render(s, L, ctx->num_sms, st, count, ctx->tuning);
+}
+
+}  // namespace lrt
+
+using lrt::ProposalState;
+
+extern "C" lrt_status lrt_proposal_set_weights(lrt_ctx *ctx, const float *params) {
+  lrt_status s = lrt::ensure(ctx);
+  if (s != LRT_OK) return s;
+  if (!params) return fail(ctx, LRT_ERR_INVALID, "null parameters");
+  for (int i = 0; i < LRT_MLP_PARAMS; i++)
+    if (!std::isfinite(params[i])) return fail(ctx, LRT_ERR_INVALID, "non-finite parameter");
+  ProposalState &p = *ctx->prop;
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  LRT_CUDA(ctx, cudaMemcpy(p.master.p, params, 4 * LRT_MLP_PARAMS, cudaMemcpyHostToDevice));
+  std::vector<uint16_t> bf(1792, 0);
+  for (int i = 0; i < 512; i++) bf[i] = lrt::f2bf(params[i]);                 // W1
+  for (int i = 0; i < 1024; i++) bf[512 + i] = lrt::f2bf(params[544 + i]);    // W2
+  for (int i = 0; i < 32; i++) bf[1536 + i] = lrt::f2bf(params[1600 + i]);    // W3 (row 0 of 8)
+  LRT_CUDA(ctx, cudaMemcpy(p.wbf.p, bf.data(), bf.size() * 2, cudaMemcpyHostToDevice));
+  LRT_CUDA(ctx, cudaMemset(p.adam_m.p, 0, 4 * LRT_MLP_PARAMS));
+  LRT_CUDA(ctx, cudaMemset(p.adam_v.p, 0, 4 * LRT_MLP_PARAMS));
+  LRT_CUDA(ctx, cudaMemset(p.grad.p, 0, 4 * LRT_MLP_PARAMS));
+  p.has_weights = true;
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_proposal_get_weights(lrt_ctx *ctx, float *params) {
+  if (!ctx || !ctx->prop || !ctx->prop->has_weights || !params) return fail(ctx, LRT_ERR_STATE, "no weights set");
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  LRT_CUDA(ctx, cudaMemcpy(params, ctx->prop->master.p, 4 * LRT_MLP_PARAMS, cudaMemcpyDeviceToHost));
+  return LRT_OK;
+}
+
+static lrt_status reserve(lrt_ctx *ctx, uint64_t capacity) {
+  ProposalState &p = *ctx->prop;
+  if (p.feat.cap >= capacity * 16 && p.target.cap >= capacity) return LRT_OK;
+  // grow, keeping what is held
+  lrt::DevBuf<__nv_bfloat16> nf;
+  lrt::DevBuf<float> nt;
+  LRT_CUDA(ctx, nf.ensure(size_t(capacity) * 16));
+  LRT_CUDA(ctx, nt.ensure(size_t(capacity)));
+  if (p.n) {
+    LRT_CUDA(ctx, cudaMemcpy(nf.p, p.feat.p, size_t(p.n) * 32, cudaMemcpyDeviceToDevice));
+    LRT_CUDA(ctx, cudaMemcpy(nt.p, p.target.p, size_t(p.n) * 4, cudaMemcpyDeviceToDevice));
+  }
+  p.feat.release();
+  p.target.release();
+  p.feat = nf;
+  p.target = nt;
+  nf.p = nullptr;
+  nt.p = nullptr;
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_proposal_collect(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, uint64_t capacity,
+                                           uint64_t *n_total) {
+  lrt_status s = lrt::ensure(ctx);
+  if (s != LRT_OK) return s;
+  if (!views || n_views == 0) return fail(ctx, LRT_ERR_INVALID, "no views");
+  if (!ctx->committed || ctx->dev.type != LRT_TYPE_SDF_SBS)
+    return fail(ctx, LRT_ERR_STATE, "collect needs a committed SBS scene");
+  const uint32_t layout = ctx->dev.sbs_hdr.aux_data & 0xFF000000u;
+  if (layout == LRT_SBS_LAYOUT_ID32F_IRGB32F || layout == LRT_SBS_LAYOUT_ID32F_IRGB32F_IN)
+    return fail(ctx, LRT_ERR_UNSUPPORTED, "the proposal reads DX-layout bricks");
+  ProposalState &p = *ctx->prop;
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  if (capacity > p.n) {
+    if ((s = reserve(ctx, capacity)) != LRT_OK) return s;
+  }
+  std::vector<DevView> hv(n_views);
+  uint64_t pix = 0;
+  for (uint32_t v = 0; v < n_views; v++) {
+    if (views[v].width == 0 || views[v].height == 0 || views[v].width > 65535 || views[v].height > 65535)
+      return fail(ctx, LRT_ERR_INVALID, "bad view size");
+    std::memset(&hv[v], 0, sizeof(DevView));
+    hv[v].width = views[v].width;
+    hv[v].height = views[v].height;
+    hv[v].pix_offset = uint32_t(pix);
+    lrt_inverse4x4(views[v].proj, hv[v].proj_inv);
+    lrt_inverse4x4(views[v].world_view, hv[v].wv_inv);
+    pix += uint64_t(views[v].width) * views[v].height;
+    if (pix >= (1ull << 32)) return fail(ctx, LRT_ERR_INVALID, "batch too large");
+  }
+  LRT_CUDA(ctx, p.views.ensure(n_views));
+  LRT_CUDA(ctx, cudaMemcpy(p.views.p, hv.data(), n_views * sizeof(DevView), cudaMemcpyHostToDevice));
+  const unsigned long long start = p.n;
+  LRT_CUDA(ctx, cudaMemcpy(p.count.p, &start, 8, cudaMemcpyHostToDevice));
+  lrt::TripleBuf out{p.feat.p, p.target.p, p.count.p, capacity};
+  LRT_CUDA(ctx, lrt::launch_gen_triples(ctx->dev, p.views.p, n_views, pix, out, nullptr));
+  unsigned long long cnt = 0;
+  LRT_CUDA(ctx, cudaMemcpy(&cnt, p.count.p, 8, cudaMemcpyDeviceToHost));
+  p.n = cnt < capacity ? cnt : capacity;
+  if (n_total) *n_total = p.n;
+  ctx->last_launches = 1;
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_proposal_clear(lrt_ctx *ctx) {
+  if (!ctx) return LRT_ERR_INVALID;
+  if (ctx->prop) ctx->prop->n = 0;
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_proposal_set_triples(lrt_ctx *ctx, const float *features, const float *targets, uint64_t n) {
+  lrt_status s = lrt::ensure(ctx);
+  if (s != LRT_OK) return s;
+  if (!features || !targets || n == 0) return fail(ctx, LRT_ERR_INVALID, "empty triples");
+  ProposalState &p = *ctx->prop;
+  p.n = 0;
+  if ((s = reserve(ctx, n)) != LRT_OK) return s;
+  std::vector<uint16_t> bf(size_t(n) * 16);
+  for (size_t i = 0; i < bf.size(); i++) bf[i] = lrt::f2bf(features[i]);
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  LRT_CUDA(ctx, cudaMemcpy(p.feat.p, bf.data(), bf.size() * 2, cudaMemcpyHostToDevice));
+  LRT_CUDA(ctx, cudaMemcpy(p.target.p, targets, size_t(n) * 4, cudaMemcpyHostToDevice));
+  p.n = n;
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_proposal_get_triples(lrt_ctx *ctx, uint64_t first, uint64_t n, float *features,
+                                               float *targets) {
+  if (!ctx || !ctx->prop || first + n > ctx->prop->n) return fail(ctx, LRT_ERR_INVALID, "triple range");
+  ProposalState &p = *ctx->prop;
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  if (features) {
+    std::vector<uint16_t> bf(size_t(n) * 16);
+    LRT_CUDA(ctx, cudaMemcpy(bf.data(), p.feat.p + size_t(first) * 16, bf.size() * 2, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < bf.size(); i++) features[i] = lrt::bf2f(bf[i]);
+  }
+  if (targets) LRT_CUDA(ctx, cudaMemcpy(targets, p.target.p + first, size_t(n) * 4, cudaMemcpyDeviceToHost));
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_proposal_train(lrt_ctx *ctx, uint32_t first_step, uint32_t steps, uint32_t batch, float lr,
+                                         uint32_t seed, float *losses) {
+  if (!ctx || !ctx->prop || !ctx->prop->has_weights) return fail(ctx, LRT_ERR_STATE, "set weights first");
+  ProposalState &p = *ctx->prop;
+  if (p.n == 0) return fail(ctx, LRT_ERR_STATE, "no triples");
+  if (batch == 0 || batch % 32 != 0 || batch > (1u << 20) || steps == 0)
+    return fail(ctx, LRT_ERR_INVALID, "batch must be a positive multiple of 32");
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  LRT_CUDA(ctx, p.losses.ensure(steps));
+  LRT_CUDA(ctx, cudaMemset(p.losses.p, 0, 4 * size_t(steps)));
+  const lrt::TripleView data{p.feat.p, p.target.p, p.n};
+  for (uint32_t k = 0; k < steps; k++) {
+    const lrt::MlpState m = lrt::mlp_state(p, p.losses.p + k);
+    LRT_CUDA(ctx, lrt::launch_mlp_step(data, m, batch, first_step + k, seed, true, true, lr, 0.9f, 0.999f, 1e-8f,
+                                       nullptr));
+  }
+  if (losses) LRT_CUDA(ctx, cudaMemcpy(losses, p.losses.p, 4 * size_t(steps), cudaMemcpyDeviceToHost));
+  else LRT_CUDA(ctx, cudaDeviceSynchronize());
+  ctx->last_launches = steps;
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_proposal_gradient(lrt_ctx *ctx, uint32_t n, float *grad, float *loss) {
+  if (!ctx || !ctx->prop || !ctx->prop->has_weights) return fail(ctx, LRT_ERR_STATE, "set weights first");
+  ProposalState &p = *ctx->prop;
+  if (n == 0 || n % 32 != 0 || n > p.n) return fail(ctx, LRT_ERR_INVALID, "n must be a multiple of 32 within the triples");
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  LRT_CUDA(ctx, p.losses.ensure(1));
+  LRT_CUDA(ctx, cudaMemset(p.losses.p, 0, 4));
+  LRT_CUDA(ctx, cudaMemset(p.grad.p, 0, 4 * LRT_MLP_PARAMS));
+  const lrt::TripleView data{p.feat.p, p.target.p, p.n};
+  const lrt::MlpState m = lrt::mlp_state(p, p.losses.p);
+  LRT_CUDA(ctx, lrt::launch_mlp_step(data, m, n, 0, 0, false, false, 0.0f, 0.9f, 0.999f, 1e-8f, nullptr));
+  if (grad) LRT_CUDA(ctx, cudaMemcpy(grad, p.grad.p, 4 * LRT_MLP_PARAMS, cudaMemcpyDeviceToHost));
+  if (loss) LRT_CUDA(ctx, cudaMemcpy(loss, p.losses.p, 4, cudaMemcpyDeviceToHost));
+  LRT_CUDA(ctx, cudaMemset(p.grad.p, 0, 4 * LRT_MLP_PARAMS));
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_proposal_infer(lrt_ctx *ctx, uint64_t first, uint64_t n, float *out) {
+  if (!ctx || !ctx->prop || !ctx->prop->has_weights) return fail(ctx, LRT_ERR_STATE, "set weights first");
+  ProposalState &p = *ctx->prop;
+  if (!out || n == 0 || first + n > p.n) return fail(ctx, LRT_ERR_INVALID, "triple range");
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  lrt::DevBuf<float> d;
+  LRT_CUDA(ctx, d.ensure(size_t(n)));
+  const lrt::TripleView data{p.feat.p + size_t(first) * 16, p.target.p + first, n};
+  cudaError_t e = lrt::launch_mlp_infer(data, lrt::mlp_state(p, nullptr), d.p, nullptr);
+  if (e == cudaSuccess) e = cudaMemcpy(out, d.p, size_t(n) * 4, cudaMemcpyDeviceToHost);
+  d.release();
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "lrt_proposal_infer");
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_proposal_stats(lrt_ctx *ctx, unsigned long long out[3]) {
+  if (!ctx || !out) return LRT_ERR_INVALID;
+  if (!ctx->prop) {
+    out[0] = out[1] = out[2] = 0;
+    return LRT_OK;
+  }
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  unsigned long long h[4];
+  LRT_CUDA(ctx, cudaMemcpy(h, ctx->prop->stats.p, 32, cudaMemcpyDeviceToHost));
+  LRT_CUDA(ctx, cudaMemset(ctx->prop->stats.p, 0, 32));
+  out[0] = h[0];
+  out[1] = h[1];
+  out[2] = h[2];
+  return LRT_OK;
+}

@@ -1,0 +1,43 @@
+// Device-side state of the learned proposal (proposal.cu), shared with the host
+// driver (proposal_api.cpp).
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "lrt_internal.h"
+
+namespace lrt {
+
+// Training triples: 16 bf16 features and the crossing fraction per sample.
+struct TripleBuf {
+  __nv_bfloat16 *feat;
+  float *target;
+  unsigned long long *count;   // samples written (may exceed capacity: extra ones are dropped)
+  unsigned long long capacity;
+};
+struct TripleView {
+  const __nv_bfloat16 *feat;
+  const float *target;
+  uint64_t n;
+};
+
+// Network parameters and optimiser state (device).
+struct MlpState {
+  float *master;            // 1633 FP32 parameters
+  __nv_bfloat16 *wbf;       // BF16 weight image (W1 | W2 | W3 padded to 8 rows)
+  float *grad;              // gradient accumulator
+  float *adam_m, *adam_v;
+  unsigned int *ticket;     // blocks finished in the current step
+  float *loss;              // where a step adds its mean loss (may be null)
+};
+
+cudaError_t launch_gen_triples(const DevScene &s, const DevView *views, uint32_t n_views, uint64_t total_pix,
+                               const TripleBuf &out, cudaStream_t st);
+cudaError_t launch_mlp_step(const TripleView &data, const MlpState &m, uint32_t batch, uint32_t step, uint32_t seed,
+                            bool random, bool update, float lr, float b1, float b2, float eps, cudaStream_t st);
+cudaError_t launch_mlp_infer(const TripleView &data, const MlpState &m, float *out, cudaStream_t st);
+cudaError_t launch_render_proposal(const DevScene &s, const RenderLaunch &L, const MlpState &m,
+                                   unsigned long long *stats, int num_sms, cudaStream_t st);
+
+}  // namespace lrt

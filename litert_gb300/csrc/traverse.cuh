@@ -1,0 +1,117 @@
+// BVH traversal shared by the render kernels (trace.cu) and the proposal
+// kernels (proposal.cu): the per-ray closest-hit walk over the 4-wide BVH.
+#pragma once
+#include "leaves.cuh"
+
+namespace lrt {
+namespace dev {
+
+template <bool COUNT, int STACK>
+__device__ __forceinline__ void visit_node(const DevScene &s, uint32_t ref, float3 rp, float3 inv, float tNear,
+                                           float hit_t, uint32_t *st_ref, float *st_t, int &sp, Counters &cnt);
+
+// RayQuery_NearestHit (BVH/BVH2Common.cpp:3490-3559) over the 4-wide BVH.
+// stopOnFirstHit (tFar <= 0) returns the first hit found (RayQuery_AnyHit).
+template <int TYPE, bool COUNT, int MODE = -1, int STACK = kStackSize>
+__device__ void trace(const DevScene &s, float3 pos, float tNear, float3 dir, float tFar, Hit &hit, Counters &cnt) {
+  const bool stop_first = (tFar <= 0.0f);
+  if (stop_first) tFar *= -1.0f;
+  hit.t = tFar;
+  hit.prim = kMiss;
+  hit.geom = kMiss;
+  hit.c0 = 1.0f;
+  hit.c1 = hit.c2 = hit.c3 = 0.0f;
+  {  // TLAS: one leaf node holding the instance box (:3508-3529)
+    const float3 invw = safe_inverse(dir);
+    const float2 bh = ray_box(pos, invw, s.inst_bmin[0], s.inst_bmin[1], s.inst_bmin[2], s.inst_bmax[0],
+                              s.inst_bmax[1], s.inst_bmax[2]);
+    if (!((bh.x <= bh.y) && (bh.y > tNear) && (bh.x < hit.t))) return;
+  }
+  const float3 rp = matmul4x3(s.inst_inv, pos);
+  const float3 rd = matmul3x3(s.inst_inv, dir);
+  const float3 inv = safe_inverse(rd);
+  const float tNearSdf = mx(tNear, 0.1f);   // SDF bias passed to every leaf type (:3472-3476)
+
+  uint32_t st_ref[STACK];
+  float st_t[STACK];
+  int sp = 0;
+  st_ref[sp] = 0;            // root wide node
+  st_t[sp] = -3.4e38f;
+  sp++;
+  // "while-while" structure: each lane walks inner nodes until it holds a leaf
+  // (or its stack is empty); the warp reconverges, and all lanes holding a leaf
+  // intersect it together.  Leaf work then runs with the lanes that need it at
+  // the same time instead of one lane per iteration of a mixed loop.
+  for (;;) {
+    uint32_t leaf = 0;
+    bool have_leaf = false;
+    while (sp > 0) {
+      sp--;
+      const uint32_t ref = st_ref[sp];
+      if (st_t[sp] > hit.t) continue;
+      if (ref & kLeafBit) {
+        leaf = ref & ~kLeafBit;
+        have_leaf = true;
+        break;
+      }
+      visit_node<COUNT, STACK>(s, ref, rp, inv, tNear, hit.t, st_ref, st_t, sp, cnt);
+    }
+    if (!have_leaf) break;
+    const float t_before = hit.t;
+    if (TYPE == LRT_TYPE_MESH_TRIANGLE)
+      tri_intersect<COUNT>(s, rp, rd, tNearSdf, leaf & 0x00FFFFFFu, (leaf >> 24) & 0x7Fu, hit, cnt);
+    else if (TYPE == LRT_TYPE_SDF_SVS)
+      svs_intersect<COUNT, MODE>(s, rp, rd, tNearSdf, leaf, hit, cnt);
+    else
+      brick_intersect<COUNT, false, MODE>(s, rp, rd, inv, tNearSdf, leaf, hit, cnt);
+    if (stop_first && hit.t < t_before) break;
+  }
+}
+
+// One inner node of the per-ray traversal: test the four child boxes with the
+// reference slab test and push the entered ones far-to-near.
+template <bool COUNT, int STACK>
+__device__ __forceinline__ void visit_node(const DevScene &s, uint32_t ref, float3 rp, float3 inv, float tNear,
+                                           float hit_t, uint32_t *st_ref, float *st_t, int &sp, Counters &cnt) {
+  {
+    const WNode4 *nd = s.nodes + ref;
+    if (COUNT) cnt.nodes++;
+    const float4 lx = __ldg(reinterpret_cast<const float4 *>(nd->lo_x));
+    const float4 hx = __ldg(reinterpret_cast<const float4 *>(nd->hi_x));
+    const float4 ly = __ldg(reinterpret_cast<const float4 *>(nd->lo_y));
+    const float4 hy = __ldg(reinterpret_cast<const float4 *>(nd->hi_y));
+    const float4 lz = __ldg(reinterpret_cast<const float4 *>(nd->lo_z));
+    const float4 hz = __ldg(reinterpret_cast<const float4 *>(nd->hi_z));
+    const uint4 ch = __ldg(reinterpret_cast<const uint4 *>(nd->child));
+    const float lxa[4] = {lx.x, lx.y, lx.z, lx.w}, hxa[4] = {hx.x, hx.y, hx.z, hx.w};
+    const float lya[4] = {ly.x, ly.y, ly.z, ly.w}, hya[4] = {hy.x, hy.y, hy.z, hy.w};
+    const float lza[4] = {lz.x, lz.y, lz.z, lz.w}, hza[4] = {hz.x, hz.y, hz.z, hz.w};
+    const uint32_t cha[4] = {ch.x, ch.y, ch.z, ch.w};
+    float kt[4];
+    uint32_t kr[4];
+    int nk = 0;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      const float2 tm = ray_box(rp, inv, lxa[i], lya[i], lza[i], hxa[i], hya[i], hza[i]);
+      const bool h = (tm.x <= tm.y) && (tm.y >= tNear) && (tm.x <= hit_t) && cha[i] != kEmptyChild;
+      if (h) { kt[nk] = tm.x; kr[nk] = cha[i]; nk++; }
+    }
+    // push far-to-near so the nearest child is popped first
+    for (int i = 1; i < nk; i++) {
+      const float tv = kt[i];
+      const uint32_t rv = kr[i];
+      int j = i - 1;
+      while (j >= 0 && kt[j] < tv) { kt[j + 1] = kt[j]; kr[j + 1] = kr[j]; j--; }
+      kt[j + 1] = tv;
+      kr[j + 1] = rv;
+    }
+    // The host rejects trees deeper than the stack allows ((W-1)*depth + 1 entries),
+    // so this bound never drops an entry.
+    for (int i = 0; i < nk; i++) {
+      if (sp < STACK) { st_ref[sp] = kr[i]; st_t[sp] = kt[i]; sp++; }
+    }
+  }
+}
+
+}  // namespace dev
+}  // namespace lrt

@@ -205,3 +205,11 @@ def dr_workload(target_bricks=32, target_brick_size=8, opt_bricks=32, opt_brick_
     init = list(dr.grid_sbs(opt_bricks, opt_brick_size, lrt.Sdf(spheres=np.array([[0, 0, 0, 0.5]], np.float32)),
                             [1.0, 0.0, 0.0]))
     return target, init, dr_views(n_views, size)
+
+
+# ---------------------------------------------------------------- config 4: learned proposal on the config-3 scene
+def proposal_views(n_views, size=1024, seed=6, fov=60.0):
+    """Square views from cameras uniform on the radius-3 sphere (training: seed 6,
+    64 views; evaluation: seed 8, 16 views)."""
+    cams = uniform_sphere_cameras(np.random.default_rng(seed), n_views, 3.0)
+    return [camera(e, c, u, fov, size, size) for e, c, u in cams]

@@ -1,0 +1,104 @@
+"""GPU: the learned proposal.
+
+The tensor-core training step's loss and gradient equal the numpy oracle's
+(same BF16 rounding points) to 1e-3 relative; inference equals the oracle's
+forward; training lowers the loss; triples collected from plain renders are
+well formed; and rendering with the proposal returns the plain kernel's hits
+bit for bit (the network only chooses where a brick's walk starts), trained or
+not, while the counters show walks that started at the predicted voxel."""
+import numpy as np
+import pytest
+
+from litert_gb300 import lrt, proposal as pp, scenes
+from oracle import mlp_oracle as mo
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def union_scene():
+    h, n, v = lrt.sbs_from_sdf(lrt.Sdf(**scenes.union_params()), 5, 8)
+    s = lrt.Scene(0)
+    g = s.add_sbs(h, n, v)
+    s.add_instance(g)
+    s.commit_scene()
+    s.set_preset(render_mode=lrt.RENDER_MODE_NORMAL, sdf_node_intersect=lrt.INTERSECT_NEWTON)
+    yield s
+    s.close()
+
+
+def _synthetic(n, seed=3):
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(0, 1, (n, 16)).astype(np.float32)
+    x[:, 6:14] = rng.normal(0, 0.5, (n, 8))
+    t = np.clip(0.3 * x[:, 0] + 0.5 * x[:, 4] - 0.2 * x[:, 8], 0, 1).astype(np.float32)
+    return x, t
+
+
+def test_gradient_matches_oracle(union_scene):
+    x, t = _synthetic(4096)
+    w = pp.init_weights(7)
+    pp.set_weights(union_scene, w)
+    pp.set_triples(union_scene, x, t)
+    loss, g = pp.gradient(union_scene, 4096)
+    lo, go = mo.loss_and_grad(w, x, t)
+    assert abs(loss - lo) <= 1e-4 * max(1.0, abs(lo))
+    assert np.linalg.norm(g - go) <= 1e-3 * np.linalg.norm(go), np.linalg.norm(g - go) / np.linalg.norm(go)
+    for a, b in ((0, 512), (512, 544), (544, 1568), (1568, 1600), (1600, 1633)):
+        assert np.linalg.norm(g[a:b] - go[a:b]) <= 2e-3 * np.linalg.norm(go[a:b]) + 1e-7, (a, b)
+
+
+def test_inference_matches_oracle(union_scene):
+    x, t = _synthetic(1000, seed=4)
+    w = pp.init_weights(8)
+    pp.set_weights(union_scene, w)
+    pp.set_triples(union_scene, x, t)
+    y = pp.infer(union_scene, 0, 1000)
+    _, _, _, yo = mo.forward(w, x)
+    assert np.linalg.norm(y - yo) <= 3e-3 * np.linalg.norm(yo)
+    assert np.abs(y - yo).max() <= 2e-2 * np.abs(yo).max()
+
+
+def test_training_lowers_loss(union_scene):
+    x, t = _synthetic(20000, seed=5)
+    pp.set_weights(union_scene, pp.init_weights(7))
+    pp.set_triples(union_scene, x, t)
+    losses = pp.train(union_scene, 400, batch=1024, lr=1e-3, seed=7)
+    assert np.isfinite(losses).all()
+    assert losses[-20:].mean() < 0.2 * losses[:20].mean(), (losses[:5], losses[-5:])
+
+
+def test_collect_triples(union_scene):
+    views = scenes.union_views(n_views=2, lo=128, hi=192, cam_seed=6)
+    pp.set_weights(union_scene, pp.init_weights(7))
+    pp.clear(union_scene)
+    n = pp.collect(union_scene, views, capacity=200000)
+    hits = union_scene.render_host(views, hits=True)["hits"]
+    assert n == int((hits["primId"] != lrt.MISS).sum())
+    f, t = pp.get_triples(union_scene, 0, n)
+    assert np.all((t >= -1e-6) & (t <= 1 + 1e-6))
+    assert np.all((f[:, :6] >= -1e-2) & (f[:, :6] <= 1 + 1e-2))
+    assert np.all(f[:, 14] > 0)
+
+
+@pytest.mark.parametrize("trained", [False, True])
+def test_proposal_render_equals_plain(union_scene, trained):
+    views = scenes.union_views(n_views=4, lo=160, hi=320, cam_seed=8)
+    plain = union_scene.render_host(views, hits=True)["hits"].view(np.uint32).copy()
+    pp.set_weights(union_scene, pp.init_weights(7))
+    if trained:
+        pp.clear(union_scene)
+        n = pp.collect(union_scene, scenes.union_views(n_views=6, lo=160, hi=320, cam_seed=6), capacity=1_000_000)
+        assert n > 10000
+        pp.train(union_scene, 600, batch=4096, lr=1e-3, seed=7)
+    pp.stats(union_scene)
+    union_scene.set_tuning("proposal", 1)
+    try:
+        got = union_scene.render_host(views, hits=True)["hits"].view(np.uint32).copy()
+        st = pp.stats(union_scene)
+    finally:
+        union_scene.set_tuning("proposal", 0)
+    assert np.array_equal(got, plain)
+    assert st["proposals"] > 1000
+    if trained:
+        assert st["jumps"] > 0.05 * st["proposals"], st
