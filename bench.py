@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--no-graph", action="store_true", help="launch directly instead of replaying a CUDA graph")
     ap.add_argument("--no-proposal", action="store_true", help="skip the learned-proposal measurement")
     ap.add_argument("--prop-steps", type=int, default=20000, help="proposal training steps (batch 8192)")
+    ap.add_argument("--prop-train-views", type=int, default=64, help="proposal training views (1024^2 each)")
     return ap.parse_args()
 
 
@@ -235,12 +236,12 @@ def run_proposal(args, scene, dev, torch):
     proposal Mrays/s on 16 held-out views (1024^2, seed 8), each as a replayed
     CUDA graph, with the hit records compared bit for bit."""
     from litert_gb300 import lrt, proposal as pp, scenes
-    train_views = scenes.proposal_views(64, 1024, seed=6)
+    train_views = scenes.proposal_views(args.prop_train_views, 1024, seed=6)
     eval_views = scenes.proposal_views(16, 1024, seed=8)
     pp.set_weights(scene, pp.init_weights(7))
     pp.clear(scene)
     t0 = time.time()
-    n_trip = pp.collect(scene, train_views, capacity=50_000_000)
+    n_trip = pp.collect(scene, train_views, capacity=min(50_000_000, len(train_views) * (1 << 20)))
     t_collect = time.time() - t0
     t0 = time.time()
     losses = pp.train(scene, args.prop_steps, batch=8192, lr=1e-3, seed=7)
@@ -291,7 +292,7 @@ def run_proposal(args, scene, dev, torch):
             "loss_first": float(losses[:10].mean()), "loss_last": float(losses[-100:].mean()),
             "collect_s": round(t_collect, 2), "train_s": round(t_train, 2),
             "config": {"workload": "proposal-16view-1024", "rays_per_step": n, "eval_views": 16,
-                       "train_views": 64, "network": "16-32-32-1 ReLU, BF16 mma.sync m16n8k16, FP32 accumulation"}}
+                       "train_views": len(train_views), "network": "16-32-32-1 ReLU, BF16 mma.sync m16n8k16, FP32 accumulation"}}
 
 
 def dr_setup(dev_index=0):
