@@ -41,7 +41,9 @@ def parse():
     ap.add_argument("--brick", type=int, default=8)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--variant", type=int, default=0, help="render kernel: 0 per-lane rays, 1 warp packet")
+    ap.add_argument("--variant", type=int, default=0,
+                    help="render kernel: 0 per-lane rays, 1 warp packet, 2 per-lane rays with refill")
+    ap.add_argument("--refill", type=int, default=8, help="variant 2: idle lanes that trigger a refill")
     ap.add_argument("--block-warps", type=int, default=4)
     ap.add_argument("--stage", type=int, default=0, help="packet kernel: stage bricks in shared memory")
     ap.add_argument("--no-dr", action="store_true", help="skip the differentiable-render measurement")
@@ -457,6 +459,7 @@ def main():
     scene.set_tuning("variant", args.variant)
     scene.set_tuning("block_warps", args.block_warps)
     scene.set_tuning("stage", args.stage)
+    scene.set_tuning("refill", args.refill)
     dev = torch.device("cuda", local if world > 1 else 0)
     n_rays = sum(w * hh for w, hh, _, _ in views)
     hits = torch.empty(n_rays * 4, dtype=torch.float32, device=dev)

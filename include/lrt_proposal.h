@@ -52,6 +52,14 @@ lrt_status lrt_proposal_train(lrt_ctx *ctx, uint32_t first_step, uint32_t steps,
 lrt_status lrt_proposal_gradient(lrt_ctx *ctx, uint32_t n, float *grad, float *loss);
 /* Network outputs for triples [first, first + n). */
 lrt_status lrt_proposal_infer(lrt_ctx *ctx, uint64_t first, uint64_t n, float *out);
+/* The same on a chosen tensor-core engine: LRT_MLP_ENGINE_MMA (warp-level
+ * mma.sync, 32 samples a warp) or LRT_MLP_ENGINE_TCGEN05 (128-sample tiles,
+ * single-thread tcgen05.mma into TMEM).  Both round to BF16 at the same points;
+ * FP32 accumulation order inside the tensor core may differ.  ms (may be NULL)
+ * receives the kernel's device time. */
+#define LRT_MLP_ENGINE_MMA 0
+#define LRT_MLP_ENGINE_TCGEN05 1
+lrt_status lrt_proposal_infer_ex(lrt_ctx *ctx, uint64_t first, uint64_t n, float *out, int engine, float *ms);
 /* Counters of the proposal renders since the last call: proposals made, walks
  * started at the predicted voxel, and of those the ones that ended in a hit. */
 lrt_status lrt_proposal_stats(lrt_ctx *ctx, unsigned long long out[3]);

@@ -435,7 +435,7 @@ extern "C" lrt_status lrt_set_tuning(lrt_ctx *ctx, const char *key, int value) {
   if (!ctx || !key) return LRT_ERR_INVALID;
   const std::string k(key);
   if (k == "variant") {
-    if (value < 0 || value > 1) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: variant is 0 or 1");
+    if (value < 0 || value > 2) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: variant is 0, 1 or 2");
     ctx->tuning.variant = value;
   } else if (k == "block_warps") {
     if (value < 1 || value > 8) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: block_warps in 1..8");
@@ -450,6 +450,9 @@ extern "C" lrt_status lrt_set_tuning(lrt_ctx *ctx, const char *key, int value) {
   } else if (k == "stack") {
     if (value != 32 && value != 64) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: stack is 32 or 64");
     ctx->tuning.stack = value;
+  } else if (k == "refill") {
+    if (value < 1 || value > 32) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: refill in 1..32");
+    ctx->tuning.refill = value;
   } else if (k == "proposal") {
     if (value < 0 || value > 1) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: proposal is 0 or 1");
     ctx->use_proposal = value;
@@ -846,6 +849,8 @@ extern "C" lrt_status lrt_autotune(lrt_ctx *ctx, const lrt_view *views, uint32_t
   std::vector<lrt_tuning_choice> cand;
   for (int tw : {4, 8, 16})
     for (int stk : {32, 64}) cand.push_back(lrt_tuning_choice{0, 4, 0, tw, stk, 0.0f});
+  for (int tw : {4, 8})
+    for (int stk : {32, 64}) cand.push_back(lrt_tuning_choice{2, 4, 0, tw, stk, 0.0f});
   if (sbs)
     for (int stage : {0, 1})
       for (int bw : {2, 4}) cand.push_back(lrt_tuning_choice{1, bw, stage, 8, 64, 0.0f});

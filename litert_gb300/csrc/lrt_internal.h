@@ -102,11 +102,13 @@ struct RenderLaunch {
 
 // Launch-shape and kernel choices (set through lrt_set_tuning).
 struct Tuning {
-  int variant = 0;          // render kernel: 0 = one ray per lane (while-while), 1 = warp packet traversal
+  int variant = 0;          // render kernel: 0 = one ray per lane (while-while), 1 = warp packet traversal,
+                            // 2 = one ray per lane with per-lane ray refill
   int block_warps = 4;      // warps per block
   int stage = 0;            // packet kernel: 1 = stage each brick in shared memory, 0 = read corners from global
   int tile_w = 8;           // warp tile width in pixels (4, 8, 16 or 32; height 32 / tile_w)
   int stack = 64;           // per-ray traversal stack entries (32 or 64; 32 only for shallow trees)
+  int refill = 8;           // variant 2: idle lanes of a warp that trigger fetching new rays
 };
 
 cudaError_t launch_render(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st, bool count,

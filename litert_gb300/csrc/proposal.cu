@@ -18,6 +18,7 @@
 // phase (the warp evaluates the network for all lanes holding a brick at once).
 #include "mlp.cuh"
 #include "proposal_internal.h"
+#include "tc05.cuh"
 #include "traverse.cuh"
 
 namespace lrt {
@@ -380,6 +381,137 @@ __global__ void __launch_bounds__(128) mlp_infer_kernel(TripleView data, MlpStat
   if (gid < data.n) out[gid] = y;
 }
 
+// ---------------------------------------------------------------- 128-sample tiles on tcgen05
+// The network on the fifth-generation tensor cores: a CTA of 4 warps owns 128
+// samples (one M = 128 tile), operands staged in shared memory in the K-major
+// canonical layout, accumulators in TMEM (layer 1 in columns 0-31, layer 2 in
+// 32-63, layer 3 -- N padded to 16 -- in 64-79), each layer one or two
+// single-thread tcgen05.mma (K = 16 each) committed to an mbarrier; warps read
+// their 32 TMEM lanes back with tcgen05.ld for bias, ReLU and BF16 rounding,
+// the same rounding points as the mma.sync path.  Waits are bounded: a timeout
+// sets status bit 1 and the CTA frees its TMEM and returns.
+constexpr uint32_t kTcLbo = 128;         // adjacent core matrices along K
+constexpr uint32_t kTcWait = 1u << 22;   // mbarrier polls before giving up
+
+__device__ __forceinline__ void stage_row16(uint8_t *tile, uint32_t row, uint32_t sbo, const uint4 &lo, const uint4 &hi) {
+  *reinterpret_cast<uint4 *>(tile + tc05::kmajor_offset(row, 0, kTcLbo, sbo)) = lo;
+  *reinterpret_cast<uint4 *>(tile + tc05::kmajor_offset(row, 8, kTcLbo, sbo)) = hi;
+}
+
+__global__ void __launch_bounds__(128) mlp_infer_tc_kernel(TripleView data, MlpState m, float *out,
+                                                           unsigned int *status) {
+  __shared__ __align__(128) uint8_t sX[128 * kIn * 2];
+  __shared__ __align__(128) uint8_t sH[128 * kHid * 2];
+  __shared__ __align__(128) uint8_t sW1[kHid * kIn * 2];
+  __shared__ __align__(128) uint8_t sW2[kHid * kHid * 2];
+  __shared__ __align__(128) uint8_t sW3[16 * kHid * 2];
+  __shared__ float sb1[kHid], sb2[kHid], sb3;
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tmem_slot;
+  const uint32_t tid = threadIdx.x, warp = tid >> 5;
+  // weights into the canonical layout (W stored [n][k] is K-major B)
+  for (uint32_t i = tid; i < kHid * kIn; i += 128)
+    *reinterpret_cast<__nv_bfloat16 *>(sW1 + tc05::kmajor_offset(i / kIn, i % kIn, kTcLbo, 256)) = m.wbf[kBfW1 + i];
+  for (uint32_t i = tid; i < kHid * kHid; i += 128)
+    *reinterpret_cast<__nv_bfloat16 *>(sW2 + tc05::kmajor_offset(i / kHid, i % kHid, kTcLbo, 512)) = m.wbf[kBfW2 + i];
+  for (uint32_t i = tid; i < 16 * kHid; i += 128)
+    *reinterpret_cast<__nv_bfloat16 *>(sW3 + tc05::kmajor_offset(i / kHid, i % kHid, kTcLbo, 512)) =
+        i < kHid ? m.wbf[kBfW3 + i] : __float2bfloat16_rn(0.0f);
+  if (tid < kHid) {
+    sb1[tid] = m.master[kOffB1 + tid];
+    sb2[tid] = m.master[kOffB2 + tid];
+  }
+  if (tid == 0) sb3 = m.master[kOffB3];
+  // this thread's sample row
+  const uint64_t gid = uint64_t(blockIdx.x) * 128 + tid;
+  uint4 lo = make_uint4(0, 0, 0, 0), hi = lo;
+  if (gid < data.n) {
+    const uint4 *src = reinterpret_cast<const uint4 *>(data.feat + gid * 16);
+    lo = src[0];
+    hi = src[1];
+  }
+  stage_row16(sX, tid, 256, lo, hi);
+  if (warp == 0) tc05::tmem_alloc(&tmem_slot, 128);
+  if (tid == 0) tc05::mbar_init(&mbar, 1);
+  tc05::fence_proxy_async();
+  tc05::fence_before_sync();
+  __syncthreads();
+  tc05::fence_after_sync();
+  const uint32_t tbase = tmem_slot, trow = tbase + ((warp * 32u) << 16);
+  bool ok;  // warp-uniform: the tcgen05.ld below are .sync.aligned
+  // layer 1: D1[128 x 32] = X W1^T
+  if (tid == 0) {
+    tc05::mma_bf16(tbase, tc05::smem_desc(tc05::smem_addr(sX), kTcLbo, 256), tc05::smem_desc(tc05::smem_addr(sW1), kTcLbo, 256),
+                   tc05::idesc_bf16_f32(128, 32), false);
+    tc05::mma_commit(&mbar);
+  }
+  ok = __all_sync(0xffffffffu, tc05::mbar_wait(&mbar, 0, kTcWait));
+  tc05::fence_after_sync();
+  float v[32];
+  if (ok) {
+    tc05::tmem_ld32(trow + 0, v);
+#pragma unroll
+    for (int j = 0; j < 32; j += 8) {
+      uint4 q;
+      q.x = pack_bf16(fmaxf(v[j] + sb1[j], 0.f), fmaxf(v[j + 1] + sb1[j + 1], 0.f));
+      q.y = pack_bf16(fmaxf(v[j + 2] + sb1[j + 2], 0.f), fmaxf(v[j + 3] + sb1[j + 3], 0.f));
+      q.z = pack_bf16(fmaxf(v[j + 4] + sb1[j + 4], 0.f), fmaxf(v[j + 5] + sb1[j + 5], 0.f));
+      q.w = pack_bf16(fmaxf(v[j + 6] + sb1[j + 6], 0.f), fmaxf(v[j + 7] + sb1[j + 7], 0.f));
+      *reinterpret_cast<uint4 *>(sH + tc05::kmajor_offset(tid, j, kTcLbo, 512)) = q;
+    }
+  }
+  tc05::fence_proxy_async();
+  tc05::fence_before_sync();
+  __syncthreads();
+  tc05::fence_after_sync();
+  // layer 2: D2[128 x 32] = H1 W2^T, two K = 16 steps (next K block: 2 core matrices = 2 * LBO bytes on)
+  if (tid == 0 && ok) {
+    const uint32_t a = tc05::smem_addr(sH), b = tc05::smem_addr(sW2);
+    tc05::mma_bf16(tbase + 32, tc05::smem_desc(a, kTcLbo, 512), tc05::smem_desc(b, kTcLbo, 512),
+                   tc05::idesc_bf16_f32(128, 32), false);
+    tc05::mma_bf16(tbase + 32, tc05::smem_desc(a + 2 * kTcLbo, kTcLbo, 512), tc05::smem_desc(b + 2 * kTcLbo, kTcLbo, 512),
+                   tc05::idesc_bf16_f32(128, 32), true);
+    tc05::mma_commit(&mbar);
+  }
+  if (ok) ok = __all_sync(0xffffffffu, tc05::mbar_wait(&mbar, 1, kTcWait));
+  tc05::fence_after_sync();
+  if (ok) {
+    tc05::tmem_ld32(trow + 32, v);
+#pragma unroll
+    for (int j = 0; j < 32; j += 8) {
+      uint4 q;
+      q.x = pack_bf16(fmaxf(v[j] + sb2[j], 0.f), fmaxf(v[j + 1] + sb2[j + 1], 0.f));
+      q.y = pack_bf16(fmaxf(v[j + 2] + sb2[j + 2], 0.f), fmaxf(v[j + 3] + sb2[j + 3], 0.f));
+      q.z = pack_bf16(fmaxf(v[j + 4] + sb2[j + 4], 0.f), fmaxf(v[j + 5] + sb2[j + 5], 0.f));
+      q.w = pack_bf16(fmaxf(v[j + 6] + sb2[j + 6], 0.f), fmaxf(v[j + 7] + sb2[j + 7], 0.f));
+      *reinterpret_cast<uint4 *>(sH + tc05::kmajor_offset(tid, j, kTcLbo, 512)) = q;
+    }
+  }
+  tc05::fence_proxy_async();
+  tc05::fence_before_sync();
+  __syncthreads();
+  tc05::fence_after_sync();
+  // layer 3: D3[128 x 16] = H2 W3pad^T (column 0 is the output)
+  if (tid == 0 && ok) {
+    const uint32_t a = tc05::smem_addr(sH), b = tc05::smem_addr(sW3);
+    tc05::mma_bf16(tbase + 64, tc05::smem_desc(a, kTcLbo, 512), tc05::smem_desc(b, kTcLbo, 512),
+                   tc05::idesc_bf16_f32(128, 16), false);
+    tc05::mma_bf16(tbase + 64, tc05::smem_desc(a + 2 * kTcLbo, kTcLbo, 512), tc05::smem_desc(b + 2 * kTcLbo, kTcLbo, 512),
+                   tc05::idesc_bf16_f32(128, 16), true);
+    tc05::mma_commit(&mbar);
+  }
+  if (ok) ok = __all_sync(0xffffffffu, tc05::mbar_wait(&mbar, 0, kTcWait));
+  tc05::fence_after_sync();
+  if (ok) {
+    tc05::tmem_ld32(trow + 64, v);
+    if (gid < data.n) out[gid] = v[0] + sb3;
+  }
+  tc05::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc05::tmem_dealloc(tbase, 128);
+  if (!ok && tid == 0) atomicOr(status, 2u);
+}
+
 // ---------------------------------------------------------------- render with the proposal
 // The plain persistent kernel's structure (render_kernel, trace.cu) with the
 // leaf phase made warp-synchronous: every lane searches for its next brick,
@@ -514,6 +646,13 @@ cudaError_t launch_mlp_step(const TripleView &data, const MlpState &m, uint32_t 
 cudaError_t launch_mlp_infer(const TripleView &data, const MlpState &m, float *out, cudaStream_t st) {
   const uint64_t blocks = (data.n + 127) / 128;
   dev::mlp_infer_kernel<<<unsigned(blocks), 128, 0, st>>>(data, m, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_infer_tc(const TripleView &data, const MlpState &m, float *out, unsigned int *status,
+                                cudaStream_t st) {
+  const uint64_t blocks = (data.n + 127) / 128;
+  dev::mlp_infer_tc_kernel<<<unsigned(blocks), 128, 0, st>>>(data, m, out, status);
   return cudaGetLastError();
 }
 

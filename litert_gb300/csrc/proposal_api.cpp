@@ -270,19 +270,47 @@ extern "C" lrt_status lrt_proposal_gradient(lrt_ctx *ctx, uint32_t n, float *gra
   return LRT_OK;
 }
 
-extern "C" lrt_status lrt_proposal_infer(lrt_ctx *ctx, uint64_t first, uint64_t n, float *out) {
+extern "C" lrt_status lrt_proposal_infer_ex(lrt_ctx *ctx, uint64_t first, uint64_t n, float *out, int engine,
+                                            float *ms) {
   if (!ctx || !ctx->prop || !ctx->prop->has_weights) return fail(ctx, LRT_ERR_STATE, "set weights first");
   ProposalState &p = *ctx->prop;
   if (!out || n == 0 || first + n > p.n) return fail(ctx, LRT_ERR_INVALID, "triple range");
+  if (engine != LRT_MLP_ENGINE_MMA && engine != LRT_MLP_ENGINE_TCGEN05) return fail(ctx, LRT_ERR_INVALID, "engine");
+  if ((n + 127) / 128 > 0x7FFFFFFFull) return fail(ctx, LRT_ERR_INVALID, "too many triples for one launch");
   LRT_CUDA(ctx, cudaSetDevice(ctx->device));
   lrt::DevBuf<float> d;
+  lrt::DevBuf<unsigned int> status;
   LRT_CUDA(ctx, d.ensure(size_t(n)));
+  LRT_CUDA(ctx, status.ensure(1));
+  LRT_CUDA(ctx, cudaMemset(status.p, 0, 4));
   const lrt::TripleView data{p.feat.p + size_t(first) * 16, p.target.p + first, n};
-  cudaError_t e = lrt::launch_mlp_infer(data, lrt::mlp_state(p, nullptr), d.p, nullptr);
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  cudaError_t e = cudaSuccess;
+  if (ms) {
+    e = cudaEventCreate(&ev[0]);
+    if (e == cudaSuccess) e = cudaEventCreate(&ev[1]);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[0], nullptr);
+  }
+  if (e == cudaSuccess)
+    e = engine == LRT_MLP_ENGINE_TCGEN05 ? lrt::launch_mlp_infer_tc(data, lrt::mlp_state(p, nullptr), d.p, status.p, nullptr)
+                                         : lrt::launch_mlp_infer(data, lrt::mlp_state(p, nullptr), d.p, nullptr);
+  if (e == cudaSuccess && ms) e = cudaEventRecord(ev[1], nullptr);
+  if (e == cudaSuccess) e = ms ? cudaEventSynchronize(ev[1]) : cudaStreamSynchronize(nullptr);
+  if (e == cudaSuccess && ms) e = cudaEventElapsedTime(ms, ev[0], ev[1]);
+  unsigned int st = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&st, status.p, 4, cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(out, d.p, size_t(n) * 4, cudaMemcpyDeviceToHost);
+  for (cudaEvent_t x : ev)
+    if (x) cudaEventDestroy(x);
   d.release();
+  status.release();
   if (e != cudaSuccess) return cuda_fail(ctx, e, "lrt_proposal_infer");
+  if (st) return fail(ctx, LRT_ERR_CUDA, "tensor-core wait timed out");
   return LRT_OK;
+}
+
+extern "C" lrt_status lrt_proposal_infer(lrt_ctx *ctx, uint64_t first, uint64_t n, float *out) {
+  return lrt_proposal_infer_ex(ctx, first, n, out, LRT_MLP_ENGINE_MMA, nullptr);
 }
 
 extern "C" lrt_status lrt_proposal_stats(lrt_ctx *ctx, unsigned long long out[3]) {

@@ -74,6 +74,108 @@ __global__ void __launch_bounds__(128, 5) render_kernel(DevScene s, RenderLaunch
   }
 }
 
+// Persistent render kernel with per-lane ray refill: a lane whose ray has
+// finished takes the next ray of the global ray sequence (ray r = lane r % 32 of
+// tile r / 32, so consecutive rays stay neighbours) as soon as `refill` lanes of
+// its warp are idle, instead of waiting for the whole warp's tile.  Each ray is
+// traced exactly as by render_kernel (spp 1), so results are identical; only
+// the assignment of rays to lanes changes.
+template <int TYPE, int MODE, int STACK>
+__global__ void __launch_bounds__(128, 5) render_refill_kernel(DevScene s, RenderLaunch L, uint32_t refill) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint64_t total = uint64_t(L.total_tiles) * 32u;
+  Counters cnt = {0, 0, 0, 0};
+  bool live = false, exhausted = false;
+  uint32_t pix_out = 0;
+  float3 dir = f3(0, 0, 1), rp = f3(0, 0, 0), rd = f3(0, 0, 1), inv = f3(0, 0, 0);
+  Hit hit;
+  hit.t = 1e9f; hit.prim = kMiss; hit.geom = kMiss; hit.c0 = 1.0f; hit.c1 = hit.c2 = hit.c3 = 0.0f;
+  uint32_t st_ref[STACK];
+  float st_t[STACK];
+  int sp = 0;
+  const float tNearSdf = 0.1f;
+  for (;;) {
+    const unsigned idle = __ballot_sync(0xffffffffu, !live);
+    if (!exhausted && __popc(idle) >= int(refill)) {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(L.tile_counter, uint32_t(__popc(idle)));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (uint64_t(base) + __popc(idle) >= total) exhausted = true;
+      if (!live) {
+        const uint64_t r = uint64_t(base) + __popc(idle & ((1u << lane) - 1u));
+        if (r < total) {
+          const uint32_t tile = uint32_t(r >> 5), tl = uint32_t(r & 31u);
+          uint32_t v = 0;
+          while (v + 1 < L.n_views && L.views[v + 1].tile_offset <= tile) v++;
+          const DevView &V = L.views[v];
+          const uint32_t lt = tile - V.tile_offset, lw = V.tile_w_log2;
+          const uint32_t x = (lt % V.tiles_x) * (1u << lw) + (tl & ((1u << lw) - 1u));
+          const uint32_t y = (lt / V.tiles_x) * (32u >> lw) + (tl >> lw);
+          if (x < V.width && y < V.height) {
+            float3 pos;
+            eye_ray(x, y, V.width, V.height, 0.5f, 0.5f, V.proj_inv, V.wv_inv, pos, dir);
+            pix_out = V.pix_offset + y * V.width + x;
+            hit.t = 1e9f; hit.prim = kMiss; hit.geom = kMiss; hit.c0 = 1.0f; hit.c1 = hit.c2 = hit.c3 = 0.0f;
+            live = true;
+            sp = 0;
+            const float3 invw = safe_inverse(dir);   // TLAS leaf box of the single instance
+            const float2 bh = ray_box(pos, invw, s.inst_bmin[0], s.inst_bmin[1], s.inst_bmin[2], s.inst_bmax[0],
+                                      s.inst_bmax[1], s.inst_bmax[2]);
+            if ((bh.x <= bh.y) && (bh.y > 0.0f) && (bh.x < hit.t)) {
+              rp = matmul4x3(s.inst_inv, pos);
+              rd = matmul3x3(s.inst_inv, dir);
+              inv = safe_inverse(rd);
+              st_ref[0] = 0;
+              st_t[0] = -3.4e38f;
+              sp = 1;
+            }
+          }
+        }
+      }
+    }
+    if (exhausted && !__any_sync(0xffffffffu, live)) break;
+    uint32_t leaf = 0;
+    bool have_leaf = false;
+    if (live) {
+      while (sp > 0) {
+        sp--;
+        const uint32_t ref = st_ref[sp];
+        if (st_t[sp] > hit.t) continue;
+        if (ref & kLeafBit) {
+          leaf = ref & ~kLeafBit;
+          have_leaf = true;
+          break;
+        }
+        visit_node<false, STACK>(s, ref, rp, inv, 0.0f, hit.t, st_ref, st_t, sp, cnt);
+      }
+    }
+    if (have_leaf) {
+      if (TYPE == LRT_TYPE_MESH_TRIANGLE)
+        tri_intersect<false>(s, rp, rd, tNearSdf, leaf & 0x00FFFFFFu, (leaf >> 24) & 0x7Fu, hit, cnt);
+      else if (TYPE == LRT_TYPE_SDF_SVS)
+        svs_intersect<false, MODE>(s, rp, rd, tNearSdf, leaf, hit, cnt);
+      else
+        brick_intersect<false, false, MODE>(s, rp, rd, inv, tNearSdf, leaf, hit, cnt);
+    } else if (live) {   // stack empty: the ray is done
+      if (L.hits16) {
+        lrt_hit16 o;
+        o.t = hit.t;
+        o.primId = (hit.prim != kMiss && (hit.geom >> 24) == LRT_TYPE_MESH_TRIANGLE) ? s.prim_indices[hit.prim]
+                                                                                    : hit.prim;
+        o.nx = hit.c2;
+        o.ny = hit.c3;
+        reinterpret_cast<float4 *>(L.hits16)[pix_out] = *reinterpret_cast<const float4 *>(&o);
+      }
+      if (L.rgba || L.rgba8) {
+        const float4 c = shade(s, hit, dir);
+        if (L.rgba) L.rgba[pix_out] = c;
+        if (L.rgba8) L.rgba8[pix_out] = encode_rgba8(c);
+      }
+      live = false;
+    }
+  }
+}
+
 // Batched RayQuery_NearestHit: one thread per ray, full CRT_Hit output.
 template <int TYPE>
 __global__ void __launch_bounds__(128) query_kernel(DevScene s, const float4 *pos_near, const float4 *dir_far,
@@ -134,10 +236,41 @@ static cudaError_t launch_render_t(const DevScene &s, const RenderLaunch &L, int
   return count ? launch_render_c<TYPE, true>(s, L, num_sms, st, tu) : launch_render_c<TYPE, false>(s, L, num_sms, st, tu);
 }
 
+template <int TYPE, int MODE, int STACK>
+static cudaError_t launch_refill_m(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st,
+                                   uint32_t refill) {
+  int per_sm = 0;
+  cudaError_t e =
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::render_refill_kernel<TYPE, MODE, STACK>, 128, 0);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  uint32_t blocks = uint32_t(num_sms) * uint32_t(per_sm);
+  const uint32_t max_blocks = (L.total_tiles + 3) / 4;
+  if (blocks > max_blocks) blocks = max_blocks;
+  if (blocks == 0) blocks = 1;
+  dev::render_refill_kernel<TYPE, MODE, STACK><<<blocks, 128, 0, st>>>(s, L, refill);
+  return cudaGetLastError();
+}
+
+// the refill kernel for the SBS and triangle configurations (spp 1)
+static cudaError_t launch_refill(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st,
+                                 const Tuning &tu) {
+  const uint32_t refill = uint32_t(tu.refill < 1 ? 1 : (tu.refill > 32 ? 32 : tu.refill));
+  if (s.type == LRT_TYPE_MESH_TRIANGLE)
+    return launch_refill_m<LRT_TYPE_MESH_TRIANGLE, -1, kStackSize>(s, L, num_sms, st, refill);
+  if (tu.stack == 32)
+    return launch_refill_m<LRT_TYPE_SDF_SBS, LRT_INTERSECT_NEWTON, 32>(s, L, num_sms, st, refill);
+  return launch_refill_m<LRT_TYPE_SDF_SBS, LRT_INTERSECT_NEWTON, kStackSize>(s, L, num_sms, st, refill);
+}
+
 cudaError_t launch_render(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st, bool count,
                           const Tuning &tu) {
   const bool sbs = s.type == LRT_TYPE_SDF_SBS || s.type == LRT_TYPE_SDF_SBS_COL;
   if (sbs && tu.variant == 1) return launch_render_packet(s, L, num_sms, st, count, tu);
+  const bool refill_ok = (s.type == LRT_TYPE_MESH_TRIANGLE ||
+                          (s.type == LRT_TYPE_SDF_SBS && s.preset.sdf_node_intersect == LRT_INTERSECT_NEWTON)) &&
+                         s.preset.spp <= 1 && !count && uint64_t(L.total_tiles) * 32u < (1ull << 31);
+  if (tu.variant == 2 && refill_ok) return launch_refill(s, L, num_sms, st, tu);
   switch (s.type) {
     case LRT_TYPE_MESH_TRIANGLE: return launch_render_t<LRT_TYPE_MESH_TRIANGLE>(s, L, num_sms, st, count, tu);
     case LRT_TYPE_SDF_SVS: return launch_render_t<LRT_TYPE_SDF_SVS>(s, L, num_sms, st, count, tu);

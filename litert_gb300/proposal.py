@@ -33,6 +33,7 @@ def _lib():
             "lrt_proposal_train": (I, [P, U32, U32, U32, C.c_float, U32, VP]),
             "lrt_proposal_gradient": (I, [P, U32, VP, VP]),
             "lrt_proposal_infer": (I, [P, U64, U64, VP]),
+            "lrt_proposal_infer_ex": (I, [P, U64, U64, VP, I, VP]),
             "lrt_proposal_stats": (I, [P, VP]),
         }
         for name, (res, args) in sig.items():
@@ -108,10 +109,22 @@ def gradient(scene, n):
     return float(loss[0]), g
 
 
-def infer(scene, first, n):
+ENGINE_MMA = 0
+ENGINE_TCGEN05 = 1
+
+
+def infer(scene, first, n, engine=None, timed=False):
+    """Network outputs for triples [first, first + n); `engine` picks the
+    tensor-core path (ENGINE_MMA or ENGINE_TCGEN05).  With timed=True returns
+    (outputs, kernel milliseconds)."""
     out = np.zeros(n, np.float32)
-    _chk(scene, _lib().lrt_proposal_infer(scene._ctx, first, n, lrt._ptr(out)))
-    return out
+    if engine is None and not timed:
+        _chk(scene, _lib().lrt_proposal_infer(scene._ctx, first, n, lrt._ptr(out)))
+        return out
+    ms = np.zeros(1, np.float32)
+    _chk(scene, _lib().lrt_proposal_infer_ex(scene._ctx, first, n, lrt._ptr(out),
+                                             ENGINE_MMA if engine is None else engine, lrt._ptr(ms)))
+    return (out, float(ms[0])) if timed else out
 
 
 def stats(scene):

@@ -59,6 +59,42 @@ def test_inference_matches_oracle(union_scene):
     assert np.abs(y - yo).max() <= 2e-2 * np.abs(yo).max()
 
 
+@pytest.mark.parametrize("n", [1, 127, 128, 1000, 70000])
+def test_tcgen05_inference_matches(union_scene, n):
+    """The 128-sample tcgen05/TMEM tiles give the warp-level mma.sync outputs
+    (same BF16 rounding points; FP32 sums in the tensor core may be ordered
+    differently) and the oracle's forward, including a ragged last tile."""
+    x, t = _synthetic(n, seed=11)
+    w = pp.init_weights(9)
+    pp.set_weights(union_scene, w)
+    pp.set_triples(union_scene, x, t)
+    y_mma = pp.infer(union_scene, 0, n, engine=pp.ENGINE_MMA)
+    y_tc = pp.infer(union_scene, 0, n, engine=pp.ENGINE_TCGEN05)
+    _, _, _, yo = mo.forward(w, x)
+    scale = max(np.abs(yo).max(), 1e-6)
+    assert np.abs(y_tc - y_mma).max() <= 1e-2 * scale, np.abs(y_tc - y_mma).max() / scale
+    assert np.linalg.norm(y_tc - yo) <= 3e-3 * np.linalg.norm(yo) + 1e-6
+    # an offset window reads the right rows
+    if n > 256:
+        y_off = pp.infer(union_scene, 100, n - 200, engine=pp.ENGINE_TCGEN05)
+        assert np.abs(y_off - y_tc[100:n - 100]).max() <= 1e-2 * scale
+
+
+def test_tcgen05_inference_trained(union_scene):
+    """After training (weights of varied sign and size), the two engines still agree."""
+    x, t = _synthetic(20000, seed=12)
+    pp.set_weights(union_scene, pp.init_weights(7))
+    pp.set_triples(union_scene, x, t)
+    pp.train(union_scene, 200, batch=1024, lr=1e-3, seed=3)
+    w = pp.get_weights(union_scene)
+    y_mma = pp.infer(union_scene, 0, 20000, engine=pp.ENGINE_MMA)
+    y_tc = pp.infer(union_scene, 0, 20000, engine=pp.ENGINE_TCGEN05)
+    _, _, _, yo = mo.forward(w, x)
+    scale = np.abs(yo).max()
+    assert np.abs(y_tc - y_mma).max() <= 1e-2 * scale
+    assert np.linalg.norm(y_tc - yo) <= 3e-3 * np.linalg.norm(yo)
+
+
 def test_training_lowers_loss(union_scene):
     x, t = _synthetic(20000, seed=5)
     pp.set_weights(union_scene, pp.init_weights(7))

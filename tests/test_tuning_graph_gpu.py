@@ -33,7 +33,7 @@ def _render(s, views):
 
 
 @pytest.mark.parametrize("tile_w,stack,variant", [(4, 64, 0), (16, 64, 0), (32, 64, 0), (8, 32, 0), (8, 64, 1),
-                                                  (16, 32, 0)])
+                                                  (16, 32, 0), (8, 64, 2), (4, 32, 2), (16, 64, 2)])
 def test_launch_shapes_bit_identical(scene, tile_w, stack, variant):
     views = _views()
     ref = _render(scene, views)
@@ -47,6 +47,36 @@ def test_launch_shapes_bit_identical(scene, tile_w, stack, variant):
         scene.set_tuning("stack", 64)
         scene.set_tuning("variant", 0)
     assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("refill", [1, 4, 16, 32])
+def test_refill_variant_bit_identical(scene, refill):
+    views = _views()
+    ref = _render(scene, views)
+    scene.set_tuning("variant", 2)
+    scene.set_tuning("refill", refill)
+    try:
+        got = _render(scene, views)
+    finally:
+        scene.set_tuning("variant", 0)
+        scene.set_tuning("refill", 8)
+    assert np.array_equal(got, ref)
+
+
+def test_refill_variant_triangles():
+    verts, faces = scenes.displaced_icosphere(subdiv=4)
+    s = lrt.Scene(0)
+    g = s.add_triangles(verts, faces)
+    s.add_instance(g)
+    s.commit_scene()
+    s.set_preset(render_mode=lrt.RENDER_MODE_NORMAL)
+    view = [scenes.mesh_view(width=320, height=200)]
+    a = s.render_host(view, hits=True, rgba=True)
+    s.set_tuning("variant", 2)
+    b = s.render_host(view, hits=True, rgba=True)
+    s.close()
+    assert np.array_equal(a["hits"].view(np.uint32), b["hits"].view(np.uint32))
+    assert np.array_equal(a["rgba"].view(np.uint32), b["rgba"].view(np.uint32))
 
 
 def test_graph_replay_matches_render(scene):
