@@ -54,6 +54,9 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true", help="use --variant/--block-warps/--stage as given")
     ap.add_argument("--no-graph", action="store_true", help="launch directly instead of replaying a CUDA graph")
     ap.add_argument("--no-proposal", action="store_true", help="skip the learned-proposal measurement")
+    ap.add_argument("--fma", type=int, default=1, choices=(0, 1),
+                    help="headline kernel: 1 = compiled with FP contraction (within the forward parity tolerance), "
+                         "0 = bit-exact; the other one is timed beside it")
     ap.add_argument("--prop-steps", type=int, default=20000, help="proposal training steps (batch 8192)")
     ap.add_argument("--prop-train-views", type=int, default=64, help="proposal training views (1024^2 each)")
     return ap.parse_args()
@@ -248,12 +251,25 @@ def run_proposal(args, scene, dev, torch):
     t0 = time.time()
     losses = pp.train(scene, args.prop_steps, batch=8192, lr=1e-3, seed=7)
     t_train = time.time() - t0
+    # batched inference over the collected triples on both tensor-core engines
+    n_inf = int(min(n_trip, 8 << 20))
+    infer = {"samples": n_inf}
+    if n_inf:
+        ys = {}
+        for name, eng in (("mma_sync", pp.ENGINE_MMA), ("tcgen05", pp.ENGINE_TCGEN05)):
+            pp.infer(scene, 0, n_inf, engine=eng, timed=True)
+            y, t_ms = pp.infer(scene, 0, n_inf, engine=eng, timed=True)
+            ys[name] = y
+            infer[name + "_ms"] = t_ms
+            infer[name + "_gsamples_s"] = n_inf / (t_ms * 1e-3) / 1e9
+        infer["max_abs_diff"] = float(np.abs(ys["mma_sync"] - ys["tcgen05"]).max())
     n = sum(w * h for w, h, _, _ in eval_views)
     hits = torch.empty(n * 4, dtype=torch.float32, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
     out = {}
     recs = {}
+    scene.set_tuning("fma", 0)   # the proposal kernel is compiled without contraction: compare like with like
     for mode in (0, 1):
         scene.set_tuning("proposal", mode)
         g = scene.graph_create(eval_views, hits_ptr=hits.data_ptr())
@@ -278,6 +294,7 @@ def run_proposal(args, scene, dev, torch):
         out["proposal" if mode else "plain"] = {"ms": ms, "mrays": n / (ms * 1e-3) / 1e6}
         recs[mode] = hits.cpu().numpy().view(np.uint32).reshape(-1, 4).copy()
     scene.set_tuning("proposal", 0)
+    scene.set_tuning("fma", args.fma)
     a, b = recs[0], recs[1]
     mask_same = np.array_equal(a[:, 1] != lrt.MISS, b[:, 1] != lrt.MISS)
     both = (a[:, 1] != lrt.MISS) & (b[:, 1] != lrt.MISS)
@@ -292,7 +309,7 @@ def run_proposal(args, scene, dev, torch):
             "jump_hit_rate": st["jump_hits"] / max(1, st["jumps"]),
             "triples": int(n_trip), "train_steps": args.prop_steps, "batch": 8192,
             "loss_first": float(losses[:10].mean()), "loss_last": float(losses[-100:].mean()),
-            "collect_s": round(t_collect, 2), "train_s": round(t_train, 2),
+            "collect_s": round(t_collect, 2), "train_s": round(t_train, 2), "inference": infer,
             "config": {"workload": "proposal-16view-1024", "rays_per_step": n, "eval_views": 16,
                        "train_views": len(train_views), "network": "16-32-32-1 ReLU, BF16 mma.sync m16n8k16, FP32 accumulation"}}
 
@@ -460,6 +477,7 @@ def main():
     scene.set_tuning("block_warps", args.block_warps)
     scene.set_tuning("stage", args.stage)
     scene.set_tuning("refill", args.refill)
+    scene.set_tuning("fma", args.fma)
     dev = torch.device("cuda", local if world > 1 else 0)
     n_rays = sum(w * hh for w, hh, _, _ in views)
     hits = torch.empty(n_rays * 4, dtype=torch.float32, device=dev)
@@ -519,6 +537,28 @@ def main():
             e2e_times.append(time.perf_counter() - t0)
     e2e = world * n_rays / statistics.median(e2e_times) / 1e6
 
+    # the other floating-point form of the same kernel, same launch shape, timed the same way
+    other_fp = None
+    if world == 1:
+        scene.set_tuning("fma", 1 - args.fma)
+        g2 = scene.graph_create(views, hits_ptr=hits.data_ptr())
+        for _ in range(args.warmup):
+            flush.fill_(1.0)
+            scene.graph_launch(g2, stream.cuda_stream)
+        ts2 = []
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            scene.graph_launch(g2, stream.cuda_stream)
+            b.record(stream)
+            b.synchronize()
+            ts2.append(a.elapsed_time(b))
+        lrt.Scene.graph_destroy(g2)
+        scene.set_tuning("fma", args.fma)
+        ms2 = sum(ts2) / len(ts2)
+        other_fp = {"fma": 1 - args.fma, "ms": ms2, "value": n_rays / (ms2 * 1e-3) / 1e6}
+
     line = None
     if rank == 0:
         # algorithmic bytes per ray (64 B per BVH2 fat pair, 16 B per brick node, 32 B per voxel's
@@ -539,6 +579,8 @@ def main():
             pass
         peak = peaks.get("hbm_gbs", 6800.0)
         achieved = (b_ray * n_rays / (ms * 1e-3) / 1e9) if b_ray else None
+        if other_fp is not None and b_ray:
+            other_fp["roofline_frac"] = b_ray * n_rays / (other_fp["ms"] * 1e-3) / 1e9 / peak
         traffic = None
         tp = os.path.join(ROOT, "profiles", "render_kernel_sbs_batched16.md")
         if os.path.exists(tp):   # dram read+write of one launch, from the committed ncu summary
@@ -555,7 +597,10 @@ def main():
                        "l2": "256 MiB write between timed steps; scene data 623 MB > L2",
                        "scene_build_s": round(t_build, 2), "parallelism": f"replicas{world}",
                        "launch": "CUDA graph replay" if graph is not None else "direct",
-                       "tuning": tuned, "autotune_candidates": len(tried)},
+                       "tuning": tuned, "autotune_candidates": len(tried),
+                       "fp": ("FP32 with contraction (FMA); forward parity tolerance" if args.fma
+                              else "FP32 without contraction; bit-exact to the reference x86-64 build")},
+            "other_fp": other_fp,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(len(views) * 136),
                     "d2h_bytes_per_step": int(n_rays * 16)},
             "gpu_launches": launches,

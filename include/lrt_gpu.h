@@ -60,11 +60,17 @@ lrt_status lrt_set_preset(lrt_ctx *ctx, const lrt_preset *preset);
 
 /* Launch-shape and kernel choices; no reference counterpart (the reference's
  * device path is generated by kernel_slicer).  Keys: "variant" (0 = one ray per
- * lane, default; 1 = warp packet traversal), "stage" (packet kernel: 1 = stage
- * each brick in shared memory), "block_warps" (1..8), "tile_w" (a warp's pixel
- * tile is tile_w x 32/tile_w: 4, 8 (default), 16, 32), "stack" (traversal stack
- * entries: 64 (default) or 32, which renders refuse for trees too deep for it).
- * Results do not depend on these. */
+ * lane, default; 1 = warp packet traversal; 2 = one ray per lane with per-lane
+ * ray refill), "refill" (variant 2: idle lanes that trigger a refill, 1..32),
+ * "stage" (packet kernel: 1 = stage each brick in shared memory), "block_warps"
+ * (1..8), "tile_w" (a warp's pixel tile is tile_w x 32/tile_w: 4, 8 (default),
+ * 16, 32), "stack" (traversal stack entries: 64 (default) or 32, which renders
+ * refuse for trees too deep for it).  Results do not depend on these.
+ * "fma" (0 = default; 1 = variant-0 renders of SBS and SVS scenes run kernels compiled with
+ * floating-point contraction: faster, no longer bit-identical to the reference's
+ * x86-64 build, within the forward parity tolerance: same hit mask, depth within
+ * 1e-4 of the scene extent, normals within 1e-3, apart from grazing and crease
+ * pixels).  "proposal": see lrt_proposal.h. */
 lrt_status lrt_set_tuning(lrt_ctx *ctx, const char *key, int value);
 
 /* One launch shape and its median time. */

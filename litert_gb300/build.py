@@ -3,7 +3,7 @@
 Output: litert_gb300/_build/liblrt_gb300.so.  Translation units compile in
 parallel; the whole build takes well under a minute.  Kernels are compiled with
 --fmad=false so their float arithmetic follows the reference's evaluation order
-exactly; host code with -ffp-contract=off so x86-64 and aarch64 hosts agree.
+exactly (except trace_fused.cu, the opt-in contracted render kernels); host code with -ffp-contract=off so x86-64 and aarch64 hosts agree.
 """
 import os
 import subprocess
@@ -17,7 +17,9 @@ LIB = os.path.join(OUT, "liblrt_gb300.so")
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
-CU_SOURCES = ["trace.cu", "trace_pkt.cu", "dr.cu", "proposal.cu"]
+CU_SOURCES = ["trace.cu", "trace_fused.cu", "trace_pkt.cu", "dr.cu", "proposal.cu"]
+# translation units compiled with floating-point contraction (the opt-in "fma" kernels)
+CONTRACTED = {"trace_fused.cu"}
 CPP_SOURCES = ["lrt_api.cpp", "scene_build.cpp", "bvh_build.cpp", "dr_api.cpp", "proposal_api.cpp"]
 
 
@@ -33,7 +35,8 @@ def _cmds():
     for src in CU_SOURCES:
         obj = os.path.join(OUT, src.replace(".cu", ".o"))
         objs.append(obj)
-        cmds.append([_nvcc(), GENCODE, "-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xptxas", "-v",
+        fmad = "--fmad=true" if src in CONTRACTED else "--fmad=false"
+        cmds.append([_nvcc(), GENCODE, "-O3", "-lineinfo", fmad, "-std=c++17", "-Xptxas", "-v",
                      "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", *inc, "-c",
                      os.path.join(CSRC, src), "-o", obj])
     for src in CPP_SOURCES:

@@ -453,6 +453,9 @@ extern "C" lrt_status lrt_set_tuning(lrt_ctx *ctx, const char *key, int value) {
   } else if (k == "refill") {
     if (value < 1 || value > 32) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: refill in 1..32");
     ctx->tuning.refill = value;
+  } else if (k == "fma") {
+    if (value < 0 || value > 1) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: fma is 0 or 1");
+    ctx->tuning.fma = value;
   } else if (k == "proposal") {
     if (value < 0 || value > 1) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: proposal is 0 or 1");
     ctx->use_proposal = value;

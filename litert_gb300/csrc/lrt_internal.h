@@ -109,10 +109,14 @@ struct Tuning {
   int tile_w = 8;           // warp tile width in pixels (4, 8, 16 or 32; height 32 / tile_w)
   int stack = 64;           // per-ray traversal stack entries (32 or 64; 32 only for shallow trees)
   int refill = 8;           // variant 2: idle lanes of a warp that trigger fetching new rays
+  int fma = 0;              // 1: variant 0 without counters runs the kernels compiled with FP contraction
 };
 
 cudaError_t launch_render(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st, bool count,
                           const Tuning &tu);
+// The variant-0 render kernel compiled with FP contraction (trace_fused.cu).
+cudaError_t launch_render_fused(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st,
+                                const Tuning &tu);
 // Warp-packet SBS render kernel (trace_pkt.cu).
 cudaError_t launch_render_packet(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st, bool count,
                                  const Tuning &tu);
