@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--refill", type=int, default=8, help="variant 2: idle lanes that trigger a refill")
     ap.add_argument("--block-warps", type=int, default=4)
     ap.add_argument("--stage", type=int, default=0, help="packet kernel: stage bricks in shared memory")
+    ap.add_argument("--tile-w", type=int, default=8, choices=(4, 8, 16, 32), help="warp pixel tile width (no autotune)")
+    ap.add_argument("--stack", type=int, default=64, choices=(32, 64), help="traversal stack entries (no autotune)")
     ap.add_argument("--no-dr", action="store_true", help="skip the differentiable-render measurement")
     ap.add_argument("--dr-iters", type=int, default=200, help="reconstruction iterations (the first 10 untimed)")
     ap.add_argument("--dr-aggregate", type=int, default=1, help="warp-aggregated gradient atomics")
@@ -478,6 +480,8 @@ def main():
     scene.set_tuning("stage", args.stage)
     scene.set_tuning("refill", args.refill)
     scene.set_tuning("fma", args.fma)
+    scene.set_tuning("tile_w", args.tile_w)
+    scene.set_tuning("stack", args.stack)
     dev = torch.device("cuda", local if world > 1 else 0)
     n_rays = sum(w * hh for w, hh, _, _ in views)
     hits = torch.empty(n_rays * 4, dtype=torch.float32, device=dev)
@@ -582,7 +586,8 @@ def main():
         if other_fp is not None and b_ray:
             other_fp["roofline_frac"] = b_ray * n_rays / (other_fp["ms"] * 1e-3) / 1e9 / peak
         traffic = None
-        tp = os.path.join(ROOT, "profiles", "render_kernel_sbs_batched16.md")
+        tp = os.path.join(ROOT, "profiles", "render_kernel_fused_sbs_batched16.md" if args.fma
+                          else "render_kernel_sbs_batched16.md")
         if os.path.exists(tp):   # dram read+write of one launch, from the committed ncu summary
             for ln in open(tp):
                 if ln.startswith("traffic_bytes_per_launch:"):

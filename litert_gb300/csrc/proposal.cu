@@ -382,34 +382,68 @@ __global__ void __launch_bounds__(128) mlp_infer_kernel(TripleView data, MlpStat
 }
 
 // ---------------------------------------------------------------- 128-sample tiles on tcgen05
-// The network on the fifth-generation tensor cores: a CTA of 4 warps owns 128
-// samples (one M = 128 tile), operands staged in shared memory in the K-major
-// canonical layout, accumulators in TMEM (layer 1 in columns 0-31, layer 2 in
-// 32-63, layer 3 -- N padded to 16 -- in 64-79), each layer one or two
-// single-thread tcgen05.mma (K = 16 each) committed to an mbarrier; warps read
-// their 32 TMEM lanes back with tcgen05.ld for bias, ReLU and BF16 rounding,
-// the same rounding points as the mma.sync path.  Waits are bounded: a timeout
-// sets status bit 1 and the CTA frees its TMEM and returns.
+// The network on the fifth-generation tensor cores.  A persistent CTA of 4 warps
+// stages the BF16 weights once in shared memory (K-major canonical layout:
+// 8-row x 16-byte core matrices), allocates 32 TMEM columns once, and then walks
+// 128-sample tiles (one M = 128 MMA tile each): per layer one elected thread
+// issues tcgen05.mma (K = 16 per instruction) into the same 32 accumulator
+// columns and commits to an mbarrier; each warp reads its 32 TMEM lanes back with
+// tcgen05.ld for bias, ReLU and BF16 rounding (the rounding points of the
+// mma.sync path) and writes the next layer's A operand to shared memory.  The
+// next tile's features are loaded into registers while the current tile's chain
+// runs.  Eight CTAs per SM keep eight chains in flight.  Waits are bounded: a
+// timeout sets status bit 1, the CTA leaves its loop at the next barrier, waits
+// once more (bounded) for its MMAs and frees its TMEM.
 constexpr uint32_t kTcLbo = 128;         // adjacent core matrices along K
 constexpr uint32_t kTcWait = 1u << 22;   // mbarrier polls before giving up
+constexpr int kTcBlocksPerSm = 8;
 
 __device__ __forceinline__ void stage_row16(uint8_t *tile, uint32_t row, uint32_t sbo, const uint4 &lo, const uint4 &hi) {
   *reinterpret_cast<uint4 *>(tile + tc05::kmajor_offset(row, 0, kTcLbo, sbo)) = lo;
   *reinterpret_cast<uint4 *>(tile + tc05::kmajor_offset(row, 8, kTcLbo, sbo)) = hi;
 }
 
-__global__ void __launch_bounds__(128) mlp_infer_tc_kernel(TripleView data, MlpState m, float *out,
-                                                           unsigned int *status) {
+// bias + ReLU + BF16 of one 32-wide accumulator row into the A operand of the next layer
+__device__ __forceinline__ void hidden_to_smem(const float v[32], const float *bias, uint8_t *sH, uint32_t row) {
+#pragma unroll
+  for (int j = 0; j < 32; j += 8) {
+    uint4 q;
+    q.x = pack_bf16_relu(v[j] + bias[j], v[j + 1] + bias[j + 1]);
+    q.y = pack_bf16_relu(v[j + 2] + bias[j + 2], v[j + 3] + bias[j + 3]);
+    q.z = pack_bf16_relu(v[j + 4] + bias[j + 4], v[j + 5] + bias[j + 5]);
+    q.w = pack_bf16_relu(v[j + 6] + bias[j + 6], v[j + 7] + bias[j + 7]);
+    *reinterpret_cast<uint4 *>(sH + tc05::kmajor_offset(row, j, kTcLbo, 512)) = q;
+  }
+}
+
+__device__ __forceinline__ void load_row16(const TripleView &data, uint64_t gid, uint4 &lo, uint4 &hi) {
+  lo = make_uint4(0, 0, 0, 0);
+  hi = lo;
+  if (gid < data.n) {
+    const uint4 *src = reinterpret_cast<const uint4 *>(data.feat + gid * 16);
+    lo = __ldg(src);
+    hi = __ldg(src + 1);
+  }
+}
+
+__global__ void __launch_bounds__(128, kTcBlocksPerSm) mlp_infer_tc_kernel(TripleView data, MlpState m, float *out,
+                                                                           unsigned int *status) {
   __shared__ __align__(128) uint8_t sX[128 * kIn * 2];
   __shared__ __align__(128) uint8_t sH[128 * kHid * 2];
   __shared__ __align__(128) uint8_t sW1[kHid * kIn * 2];
   __shared__ __align__(128) uint8_t sW2[kHid * kHid * 2];
   __shared__ __align__(128) uint8_t sW3[16 * kHid * 2];
-  __shared__ float sb1[kHid], sb2[kHid], sb3;
+  __shared__ __align__(16) float sb1[kHid];
+  __shared__ __align__(16) float sb2[kHid];
+  __shared__ float sb3;
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t tmem_slot;
   const uint32_t tid = threadIdx.x, warp = tid >> 5;
-  // weights into the canonical layout (W stored [n][k] is K-major B)
+  const uint64_t n_tiles = (data.n + 127) / 128;
+  uint64_t tile = blockIdx.x;
+  uint4 lo, hi;
+  load_row16(data, tile * 128 + tid, lo, hi);
+  // weights into the canonical layout (W stored [n][k] is the K-major B operand)
   for (uint32_t i = tid; i < kHid * kIn; i += 128)
     *reinterpret_cast<__nv_bfloat16 *>(sW1 + tc05::kmajor_offset(i / kIn, i % kIn, kTcLbo, 256)) = m.wbf[kBfW1 + i];
   for (uint32_t i = tid; i < kHid * kHid; i += 128)
@@ -422,94 +456,90 @@ __global__ void __launch_bounds__(128) mlp_infer_tc_kernel(TripleView data, MlpS
     sb2[tid] = m.master[kOffB2 + tid];
   }
   if (tid == 0) sb3 = m.master[kOffB3];
-  // this thread's sample row
-  const uint64_t gid = uint64_t(blockIdx.x) * 128 + tid;
-  uint4 lo = make_uint4(0, 0, 0, 0), hi = lo;
-  if (gid < data.n) {
-    const uint4 *src = reinterpret_cast<const uint4 *>(data.feat + gid * 16);
-    lo = src[0];
-    hi = src[1];
-  }
-  stage_row16(sX, tid, 256, lo, hi);
-  if (warp == 0) tc05::tmem_alloc(&tmem_slot, 128);
+  if (warp == 0) tc05::tmem_alloc(&tmem_slot, 32);
   if (tid == 0) tc05::mbar_init(&mbar, 1);
-  tc05::fence_proxy_async();
   tc05::fence_before_sync();
   __syncthreads();
   tc05::fence_after_sync();
   const uint32_t tbase = tmem_slot, trow = tbase + ((warp * 32u) << 16);
-  bool ok;  // warp-uniform: the tcgen05.ld below are .sync.aligned
-  // layer 1: D1[128 x 32] = X W1^T
-  if (tid == 0) {
-    tc05::mma_bf16(tbase, tc05::smem_desc(tc05::smem_addr(sX), kTcLbo, 256), tc05::smem_desc(tc05::smem_addr(sW1), kTcLbo, 256),
-                   tc05::idesc_bf16_f32(128, 32), false);
-    tc05::mma_commit(&mbar);
-  }
-  ok = __all_sync(0xffffffffu, tc05::mbar_wait(&mbar, 0, kTcWait));
-  tc05::fence_after_sync();
+  const uint32_t aX = tc05::smem_addr(sX), aH = tc05::smem_addr(sH);
+  const uint32_t aW1 = tc05::smem_addr(sW1), aW2 = tc05::smem_addr(sW2), aW3 = tc05::smem_addr(sW3);
+  constexpr uint32_t kId32 = tc05::idesc_bf16_f32(128, 32), kId16 = tc05::idesc_bf16_f32(128, 16);
+  uint32_t phase = 0;
+  bool ok = true;
   float v[32];
-  if (ok) {
-    tc05::tmem_ld32(trow + 0, v);
-#pragma unroll
-    for (int j = 0; j < 32; j += 8) {
-      uint4 q;
-      q.x = pack_bf16(fmaxf(v[j] + sb1[j], 0.f), fmaxf(v[j + 1] + sb1[j + 1], 0.f));
-      q.y = pack_bf16(fmaxf(v[j + 2] + sb1[j + 2], 0.f), fmaxf(v[j + 3] + sb1[j + 3], 0.f));
-      q.z = pack_bf16(fmaxf(v[j + 4] + sb1[j + 4], 0.f), fmaxf(v[j + 5] + sb1[j + 5], 0.f));
-      q.w = pack_bf16(fmaxf(v[j + 6] + sb1[j + 6], 0.f), fmaxf(v[j + 7] + sb1[j + 7], 0.f));
-      *reinterpret_cast<uint4 *>(sH + tc05::kmajor_offset(tid, j, kTcLbo, 512)) = q;
+  for (; tile < n_tiles; tile += gridDim.x) {
+    // this tile's features to shared memory (the previous tile's layer-1 MMA has completed)
+    stage_row16(sX, tid, 256, lo, hi);
+    tc05::fence_proxy_async();
+    tc05::fence_before_sync();
+    __syncthreads();
+    tc05::fence_after_sync();
+    const uint64_t row = tile * 128 + tid;
+    load_row16(data, (tile + gridDim.x) * 128 + tid, lo, hi);   // next tile, in flight during this one
+    // layer 1: D[128 x 32] = X W1^T
+    if (tid == 0) {
+      tc05::mma_bf16(tbase, tc05::smem_desc(aX, kTcLbo, 256), tc05::smem_desc(aW1, kTcLbo, 256), kId32, false);
+      tc05::mma_commit(&mbar);
     }
-  }
-  tc05::fence_proxy_async();
-  tc05::fence_before_sync();
-  __syncthreads();
-  tc05::fence_after_sync();
-  // layer 2: D2[128 x 32] = H1 W2^T, two K = 16 steps (next K block: 2 core matrices = 2 * LBO bytes on)
-  if (tid == 0 && ok) {
-    const uint32_t a = tc05::smem_addr(sH), b = tc05::smem_addr(sW2);
-    tc05::mma_bf16(tbase + 32, tc05::smem_desc(a, kTcLbo, 512), tc05::smem_desc(b, kTcLbo, 512),
-                   tc05::idesc_bf16_f32(128, 32), false);
-    tc05::mma_bf16(tbase + 32, tc05::smem_desc(a + 2 * kTcLbo, kTcLbo, 512), tc05::smem_desc(b + 2 * kTcLbo, kTcLbo, 512),
-                   tc05::idesc_bf16_f32(128, 32), true);
-    tc05::mma_commit(&mbar);
-  }
-  if (ok) ok = __all_sync(0xffffffffu, tc05::mbar_wait(&mbar, 1, kTcWait));
-  tc05::fence_after_sync();
-  if (ok) {
-    tc05::tmem_ld32(trow + 32, v);
-#pragma unroll
-    for (int j = 0; j < 32; j += 8) {
-      uint4 q;
-      q.x = pack_bf16(fmaxf(v[j] + sb2[j], 0.f), fmaxf(v[j + 1] + sb2[j + 1], 0.f));
-      q.y = pack_bf16(fmaxf(v[j + 2] + sb2[j + 2], 0.f), fmaxf(v[j + 3] + sb2[j + 3], 0.f));
-      q.z = pack_bf16(fmaxf(v[j + 4] + sb2[j + 4], 0.f), fmaxf(v[j + 5] + sb2[j + 5], 0.f));
-      q.w = pack_bf16(fmaxf(v[j + 6] + sb2[j + 6], 0.f), fmaxf(v[j + 7] + sb2[j + 7], 0.f));
-      *reinterpret_cast<uint4 *>(sH + tc05::kmajor_offset(tid, j, kTcLbo, 512)) = q;
+    bool w_ok = __all_sync(0xffffffffu, tc05::mbar_wait(&mbar, phase, kTcWait));
+    phase ^= 1u;
+    tc05::fence_after_sync();
+    if (w_ok) {
+      tc05::tmem_ld32(trow, v);
+      hidden_to_smem(v, sb1, sH, tid);
     }
+    tc05::fence_proxy_async();
+    tc05::fence_before_sync();
+    ok = __syncthreads_and(w_ok);
+    tc05::fence_after_sync();
+    if (!ok) break;
+    // layer 2: D = H1 W2^T, two K = 16 steps (the next K block starts 2 core matrices on)
+    if (tid == 0) {
+      tc05::mma_bf16(tbase, tc05::smem_desc(aH, kTcLbo, 512), tc05::smem_desc(aW2, kTcLbo, 512), kId32, false);
+      tc05::mma_bf16(tbase, tc05::smem_desc(aH + 2 * kTcLbo, kTcLbo, 512), tc05::smem_desc(aW2 + 2 * kTcLbo, kTcLbo, 512),
+                     kId32, true);
+      tc05::mma_commit(&mbar);
+    }
+    w_ok = __all_sync(0xffffffffu, tc05::mbar_wait(&mbar, phase, kTcWait));
+    phase ^= 1u;
+    tc05::fence_after_sync();
+    if (w_ok) {
+      tc05::tmem_ld32(trow, v);
+      hidden_to_smem(v, sb2, sH, tid);
+    }
+    tc05::fence_proxy_async();
+    tc05::fence_before_sync();
+    ok = __syncthreads_and(w_ok);
+    tc05::fence_after_sync();
+    if (!ok) break;
+    // layer 3: D[:, 0:16] = H2 W3pad^T (column 0 is the output)
+    if (tid == 0) {
+      tc05::mma_bf16(tbase, tc05::smem_desc(aH, kTcLbo, 512), tc05::smem_desc(aW3, kTcLbo, 512), kId16, false);
+      tc05::mma_bf16(tbase, tc05::smem_desc(aH + 2 * kTcLbo, kTcLbo, 512), tc05::smem_desc(aW3 + 2 * kTcLbo, kTcLbo, 512),
+                     kId16, true);
+      tc05::mma_commit(&mbar);
+    }
+    w_ok = __all_sync(0xffffffffu, tc05::mbar_wait(&mbar, phase, kTcWait));
+    phase ^= 1u;
+    tc05::fence_after_sync();
+    if (w_ok) {
+      tc05::tmem_ld32(trow, v);
+      if (row < data.n) out[row] = v[0] + sb3;
+    }
+    tc05::fence_before_sync();
+    ok = __syncthreads_and(w_ok);   // every lane has read D before the next tile's MMA overwrites it
+    tc05::fence_after_sync();
+    if (!ok) break;
   }
-  tc05::fence_proxy_async();
+  if (!ok) {
+    tc05::mbar_wait(&mbar, phase ^ 1u, kTcWait);   // the MMAs of the step that timed out, if they finish
+    if (tid == 0) atomicOr(status, 2u);
+  }
   tc05::fence_before_sync();
   __syncthreads();
   tc05::fence_after_sync();
-  // layer 3: D3[128 x 16] = H2 W3pad^T (column 0 is the output)
-  if (tid == 0 && ok) {
-    const uint32_t a = tc05::smem_addr(sH), b = tc05::smem_addr(sW3);
-    tc05::mma_bf16(tbase + 64, tc05::smem_desc(a, kTcLbo, 512), tc05::smem_desc(b, kTcLbo, 512),
-                   tc05::idesc_bf16_f32(128, 16), false);
-    tc05::mma_bf16(tbase + 64, tc05::smem_desc(a + 2 * kTcLbo, kTcLbo, 512), tc05::smem_desc(b + 2 * kTcLbo, kTcLbo, 512),
-                   tc05::idesc_bf16_f32(128, 16), true);
-    tc05::mma_commit(&mbar);
-  }
-  if (ok) ok = __all_sync(0xffffffffu, tc05::mbar_wait(&mbar, 0, kTcWait));
-  tc05::fence_after_sync();
-  if (ok) {
-    tc05::tmem_ld32(trow + 64, v);
-    if (gid < data.n) out[gid] = v[0] + sb3;
-  }
-  tc05::fence_before_sync();
-  __syncthreads();
-  if (warp == 0) tc05::tmem_dealloc(tbase, 128);
-  if (!ok && tid == 0) atomicOr(status, 2u);
+  if (warp == 0) tc05::tmem_dealloc(tbase, 32);
 }
 
 // ---------------------------------------------------------------- render with the proposal
@@ -651,7 +681,14 @@ cudaError_t launch_mlp_infer(const TripleView &data, const MlpState &m, float *o
 
 cudaError_t launch_mlp_infer_tc(const TripleView &data, const MlpState &m, float *out, unsigned int *status,
                                 cudaStream_t st) {
-  const uint64_t blocks = (data.n + 127) / 128;
+  int device = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  if (e != cudaSuccess) return e;
+  const uint64_t tiles = (data.n + 127) / 128;
+  uint64_t blocks = uint64_t(sms) * dev::kTcBlocksPerSm;
+  if (blocks > tiles) blocks = tiles;
+  if (blocks == 0) return cudaSuccess;
   dev::mlp_infer_tc_kernel<<<unsigned(blocks), 128, 0, st>>>(data, m, out, status);
   return cudaGetLastError();
 }
