@@ -34,7 +34,7 @@ L2_FLUSH_BYTES = 256 << 20
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--depth", type=int, default=7)
@@ -191,8 +191,8 @@ def run_small_configs(args, dev, torch):
         ms = statistics.median(ts)
         return n, ms, n / (ms * 1e-3) / 1e6
 
-    def cpu_rate(osc, views):
-        cores = os.cpu_count() or 1
+    def cpu_rate(osc, views, threads=None):
+        cores = threads or os.cpu_count() or 1
         t0 = time.perf_counter()
         rays = 0
         for w, h, wv, pj in views[:1]:
@@ -211,12 +211,15 @@ def run_small_configs(args, dev, torch):
     osc = orc.Scene("sbs", sbs=(orc.SbsHeader(h.brick_size, h.brick_pad, h.bytes_per_value, h.aux_data), nodes, values),
                     intersect=2, render_mode=8)
     cpu, cores = cpu_rate(osc, v1)
+    cpu1, _ = cpu_rate(osc, v1, threads=1)   # the reference's Render path is single-threaded
     for name, views in (("sphere-sbs-256", v1), ("sphere-sbs-256-x16", v1 * 16)):
         n, ms, mr = timed(sc, views, max(args.steps, 10))
         out.append({"workload": name, "value": mr, "unit": UNIT, "ms_per_step": ms, "rays_per_step": n,
                     "bricks": int(nodes.shape[0]),
                     "cpu_baseline": {"value": cpu, "unit": UNIT, "cores": cores, "kind": "port",
-                                     "sample": "the 256x256 view"}})
+                                     "sample": "the 256x256 view"},
+                    "cpu_single_thread": {"value": cpu1, "unit": UNIT, "cores": 1, "kind": "port",
+                                          "sample": "the 256x256 view"}})
     sc.close()
     # config 2: triangles
     verts, faces = scenes.displaced_icosphere(subdiv=7)

@@ -40,6 +40,11 @@ struct DrState {
   lrt_dr_preset preset{};
   bool has_scene = false, has_ref = false;
   uint32_t last_launches = 0;
+  // summed batches: views run concurrently on side streams forked from and joined
+  // back into the caller's stream, so one view's tail overlaps the next one's work
+  static constexpr int kSide = 4;
+  cudaStream_t side[kSide] = {};
+  cudaEvent_t fork = nullptr, join[kSide] = {};
 };
 
 void dr_state_free(DrState *st) {
@@ -57,6 +62,11 @@ void dr_state_free(DrState *st) {
   st->d_border_list.release();
   st->d_border_count.release();
   st->d_status.release();
+  for (int k = 0; k < DrState::kSide; k++) {
+    if (st->side[k]) cudaStreamDestroy(st->side[k]);
+    if (st->join[k]) cudaEventDestroy(st->join[k]);
+  }
+  if (st->fork) cudaEventDestroy(st->fork);
   st->d_loss.release();
   delete st;
 }
@@ -164,7 +174,7 @@ drk::DevView dev_view(DrState &st, uint32_t v) {
   d.img = st.d_img.p + st.off[v];
   d.depth = st.d_depth.p + st.off[v];
   d.border_mask = st.d_border_mask.p + st.off[v];
-  d.border_list = st.d_border_list.p;
+  d.border_list = st.d_border_list.p + st.off[v];
   d.border_count = st.d_border_count.p + v;
   d.loss = st.d_loss.p + v;
   return d;
@@ -348,7 +358,7 @@ extern "C" lrt_status lrt_dr_set_reference(lrt_ctx *ctx, uint32_t n_views, const
   LRT_CUDA(ctx, st.d_img.ensure(n));
   LRT_CUDA(ctx, st.d_depth.ensure(n));
   LRT_CUDA(ctx, st.d_border_mask.ensure(n));
-  LRT_CUDA(ctx, st.d_border_list.ensure(mx));
+  LRT_CUDA(ctx, st.d_border_list.ensure(n));   // one region per view: views may run concurrently
   LRT_CUDA(ctx, st.d_border_count.ensure(n_views));
   LRT_CUDA(ctx, st.d_loss.ensure(n_views));
   LRT_CUDA(ctx, cudaMemset(st.d_img.p, 0, n * sizeof(float4)));
@@ -415,10 +425,30 @@ extern "C" lrt_status lrt_dr_step(lrt_ctx *ctx, uint32_t iter, double *losses) {
   if (st.preset.accumulate_batch) LRT_CUDA(ctx, cudaMemsetAsync(st.d_grad.p, 0, sizeof(float) * st.n_params, 0));
   drk::launch_brick_bounds(dev_scene(ctx), st.n_nodes, st.d_bounds.p, 0);
   st.last_launches += 1;
-  for (uint32_t v = 0; v < nv; v++) {
-    // the reference refills its gradient buffer for every image of the batch (:412)
-    if (!st.preset.accumulate_batch) LRT_CUDA(ctx, cudaMemsetAsync(st.d_grad.p, 0, sizeof(float) * st.n_params, 0));
-    if ((s = render_view(ctx, v, 0)) != LRT_OK) return s;
+  if (st.preset.accumulate_batch && nv > 1) {
+    // summed batch: the views are independent until Adam; fork them over side streams
+    if (!st.fork) {
+      LRT_CUDA(ctx, cudaEventCreateWithFlags(&st.fork, cudaEventDisableTiming));
+      for (int k = 0; k < DrState::kSide; k++) {
+        LRT_CUDA(ctx, cudaStreamCreateWithFlags(&st.side[k], cudaStreamNonBlocking));
+        LRT_CUDA(ctx, cudaEventCreateWithFlags(&st.join[k], cudaEventDisableTiming));
+      }
+    }
+    LRT_CUDA(ctx, cudaEventRecord(st.fork, 0));
+    const int used = int(std::min<uint32_t>(nv, DrState::kSide));
+    for (int k = 0; k < used; k++) LRT_CUDA(ctx, cudaStreamWaitEvent(st.side[k], st.fork, 0));
+    for (uint32_t v = 0; v < nv; v++)
+      if ((s = render_view(ctx, v, st.side[v % DrState::kSide])) != LRT_OK) return s;
+    for (int k = 0; k < used; k++) {
+      LRT_CUDA(ctx, cudaEventRecord(st.join[k], st.side[k]));
+      LRT_CUDA(ctx, cudaStreamWaitEvent(0, st.join[k], 0));
+    }
+  } else {
+    for (uint32_t v = 0; v < nv; v++) {
+      // the reference refills its gradient buffer for every image of the batch (:412)
+      if (!st.preset.accumulate_batch) LRT_CUDA(ctx, cudaMemsetAsync(st.d_grad.p, 0, sizeof(float) * st.n_params, 0));
+      if ((s = render_view(ctx, v, 0)) != LRT_OK) return s;
+    }
   }
   const lrt_dr_preset &p = st.preset;
   const double c1 = 1.0 - std::pow(double(p.opt_beta_1), double(iter + 1));
