@@ -87,28 +87,37 @@ __device__ __forceinline__ void visit_node(const DevScene &s, uint32_t ref, floa
     const float lya[4] = {ly.x, ly.y, ly.z, ly.w}, hya[4] = {hy.x, hy.y, hy.z, hy.w};
     const float lza[4] = {lz.x, lz.y, lz.z, lz.w}, hza[4] = {hz.x, hz.y, hz.z, hz.w};
     const uint32_t cha[4] = {ch.x, ch.y, ch.z, ch.w};
+    // child entry distances and refs; a missed child sorts last (key -inf)
     float kt[4];
-    uint32_t kr[4];
+    uint32_t kr[4], ki[4];
     int nk = 0;
 #pragma unroll
     for (int i = 0; i < 4; i++) {
       const float2 tm = ray_box(rp, inv, lxa[i], lya[i], lza[i], hxa[i], hya[i], hza[i]);
       const bool h = (tm.x <= tm.y) && (tm.y >= tNear) && (tm.x <= hit_t) && cha[i] != kEmptyChild;
-      if (h) { kt[nk] = tm.x; kr[nk] = cha[i]; nk++; }
+      kt[i] = h ? tm.x : -__int_as_float(0x7f800000);
+      kr[i] = cha[i];
+      ki[i] = uint32_t(i);
+      nk += h ? 1 : 0;
     }
-    // push far-to-near so the nearest child is popped first
-    for (int i = 1; i < nk; i++) {
-      const float tv = kt[i];
-      const uint32_t rv = kr[i];
-      int j = i - 1;
-      while (j >= 0 && kt[j] < tv) { kt[j + 1] = kt[j]; kr[j + 1] = kr[j]; j--; }
-      kt[j + 1] = tv;
-      kr[j + 1] = rv;
+    // far-to-near order (the nearest child is popped first) by a 5-exchange sorting
+    // network on registers: descending entry distance, equal distances in child
+    // order -- the order a stable insertion sort gives
+#define LRT_CE(a, b)                                                                        \
+    {                                                                                       \
+      const bool sw = kt[b] > kt[a] || (kt[b] == kt[a] && ki[b] < ki[a]);                   \
+      const float t0 = sw ? kt[b] : kt[a], t1 = sw ? kt[a] : kt[b];                         \
+      const uint32_t r0 = sw ? kr[b] : kr[a], r1 = sw ? kr[a] : kr[b];                      \
+      const uint32_t i0 = sw ? ki[b] : ki[a], i1 = sw ? ki[a] : ki[b];                      \
+      kt[a] = t0; kt[b] = t1; kr[a] = r0; kr[b] = r1; ki[a] = i0; ki[b] = i1;               \
     }
+    LRT_CE(0, 1) LRT_CE(2, 3) LRT_CE(0, 2) LRT_CE(1, 3) LRT_CE(1, 2)
+#undef LRT_CE
     // The host rejects trees deeper than the stack allows ((W-1)*depth + 1 entries),
     // so this bound never drops an entry.
-    for (int i = 0; i < nk; i++) {
-      if (sp < STACK) { st_ref[sp] = kr[i]; st_t[sp] = kt[i]; sp++; }
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      if (i < nk && sp < STACK) { st_ref[sp] = kr[i]; st_t[sp] = kt[i]; sp++; }
     }
   }
 }
