@@ -111,7 +111,9 @@ lrt_status lrt_query_rays(lrt_ctx *ctx, const float *pos_near, const float *dir_
  * are device memory; asynchronous on `stream`. */
 lrt_status lrt_render(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, lrt_hit16 *hits16,
                       float *rgba, uint32_t *rgba8, void *stream);
-/* Same, with host output buffers: copies views in and results out, synchronous. */
+/* Same, with host output buffers, synchronous.  Page-locked buffers (cudaHostAlloc,
+ * cudaHostRegister) are written by the render kernel directly across the host
+ * link while it runs; pageable ones receive a copy of device buffers afterwards. */
 lrt_status lrt_render_host(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, lrt_hit16 *hits16,
                            float *rgba, uint32_t *rgba8);
 /* Rendering that allocates nothing.  No counterpart in the reference.

@@ -546,6 +546,20 @@ extern "C" lrt_status lrt_render(lrt_ctx *ctx, const lrt_view *views, uint32_t n
   return render_impl(ctx, views, n_views, hits16, rgba, rgba8, static_cast<cudaStream_t>(stream), nullptr);
 }
 
+// Device address of a page-locked host buffer (cudaHostAlloc / cudaHostRegister,
+// mapped under unified addressing), or null for pageable memory.
+static void *mapped_host(const void *host) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// Outputs in page-locked host memory are written by the kernel itself across the
+// host link while it renders (no staging buffer, no copy after the launch);
+// pageable outputs are rendered into device buffers and copied back.
 extern "C" lrt_status lrt_render_host(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, lrt_hit16 *hits16,
                                       float *rgba, uint32_t *rgba8) {
   if (!ctx) return LRT_ERR_INVALID;
@@ -553,17 +567,23 @@ extern "C" lrt_status lrt_render_host(lrt_ctx *ctx, const lrt_view *views, uint3
   uint64_t pix = 0;
   for (uint32_t v = 0; v < n_views; v++) pix += uint64_t(views[v].width) * views[v].height;
   LRT_CUDA(ctx, cudaSetDevice(ctx->device));
-  if (hits16) LRT_CUDA(ctx, ctx->d_out_hits.ensure(pix));
-  if (rgba) LRT_CUDA(ctx, ctx->d_out_rgba.ensure(pix));
-  if (rgba8) LRT_CUDA(ctx, ctx->d_out_rgba8.ensure(pix));
+  lrt_hit16 *m_hits = hits16 ? static_cast<lrt_hit16 *>(mapped_host(hits16)) : nullptr;
+  float *m_rgba = rgba ? static_cast<float *>(mapped_host(rgba)) : nullptr;
+  uint32_t *m_rgba8 = rgba8 ? static_cast<uint32_t *>(mapped_host(rgba8)) : nullptr;
+  if (hits16 && !m_hits) LRT_CUDA(ctx, ctx->d_out_hits.ensure(pix));
+  if (rgba && !m_rgba) LRT_CUDA(ctx, ctx->d_out_rgba.ensure(pix));
+  if (rgba8 && !m_rgba8) LRT_CUDA(ctx, ctx->d_out_rgba8.ensure(pix));
   const cudaStream_t st = nullptr;
-  lrt_status s = render_impl(ctx, views, n_views, hits16 ? ctx->d_out_hits.p : nullptr,
-                             rgba ? reinterpret_cast<float *>(ctx->d_out_rgba.p) : nullptr,
-                             rgba8 ? ctx->d_out_rgba8.p : nullptr, st, nullptr);
+  lrt_status s = render_impl(ctx, views, n_views, hits16 ? (m_hits ? m_hits : ctx->d_out_hits.p) : nullptr,
+                             rgba ? (m_rgba ? m_rgba : reinterpret_cast<float *>(ctx->d_out_rgba.p)) : nullptr,
+                             rgba8 ? (m_rgba8 ? m_rgba8 : ctx->d_out_rgba8.p) : nullptr, st, nullptr);
   if (s != LRT_OK) return s;
-  if (hits16) LRT_CUDA(ctx, cudaMemcpyAsync(hits16, ctx->d_out_hits.p, pix * sizeof(lrt_hit16), cudaMemcpyDeviceToHost, st));
-  if (rgba) LRT_CUDA(ctx, cudaMemcpyAsync(rgba, ctx->d_out_rgba.p, pix * sizeof(float4), cudaMemcpyDeviceToHost, st));
-  if (rgba8) LRT_CUDA(ctx, cudaMemcpyAsync(rgba8, ctx->d_out_rgba8.p, pix * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  if (hits16 && !m_hits)
+    LRT_CUDA(ctx, cudaMemcpyAsync(hits16, ctx->d_out_hits.p, pix * sizeof(lrt_hit16), cudaMemcpyDeviceToHost, st));
+  if (rgba && !m_rgba)
+    LRT_CUDA(ctx, cudaMemcpyAsync(rgba, ctx->d_out_rgba.p, pix * sizeof(float4), cudaMemcpyDeviceToHost, st));
+  if (rgba8 && !m_rgba8)
+    LRT_CUDA(ctx, cudaMemcpyAsync(rgba8, ctx->d_out_rgba8.p, pix * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   LRT_CUDA(ctx, cudaStreamSynchronize(st));
   return LRT_OK;
 }

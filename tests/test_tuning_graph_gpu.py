@@ -111,3 +111,28 @@ def test_autotune_picks_a_candidate(scene):
     assert best["ms"] == min(c["ms"] for c in tried)
     assert best["tile_w"] in (4, 8, 16) and best["stack"] in (32, 64)
     assert np.array_equal(_render(scene, views), ref)
+
+
+@pytest.mark.parametrize("fma", [0, 1])
+def test_render_into_page_locked_host_memory(scene, fma):
+    """lrt_render_host writes page-locked outputs from the kernel directly; the
+    records, colours and packed colours equal those of the copy path
+    (pageable numpy buffers)."""
+    scene.set_tuning("fma", fma)
+    try:
+        views = _views()
+        n = sum(w * h for w, h, _, _ in views)
+        ref = scene.render_host(views, hits=True, rgba=True, rgba8=True)
+        hits = torch.full((n * 4,), -1.0, dtype=torch.float32, pin_memory=True)
+        rgba = torch.full((n * 4,), -1.0, dtype=torch.float32, pin_memory=True)
+        rgba8 = torch.zeros((n,), dtype=torch.int32, pin_memory=True)
+        va = lrt.make_views(views)
+        st = lrt.lib().lrt_render_host(scene._ctx, lrt.C.cast(va, lrt.C.c_void_p), len(views),
+                                       lrt.C.c_void_p(hits.data_ptr()), lrt.C.c_void_p(rgba.data_ptr()),
+                                       lrt.C.c_void_p(rgba8.data_ptr()))
+        assert st == 0
+        assert np.array_equal(hits.numpy().view(np.uint32), ref["hits"].view(np.uint32))
+        assert np.array_equal(rgba.numpy().view(np.uint32), ref["rgba"].view(np.uint32).reshape(-1))
+        assert np.array_equal(rgba8.numpy().view(np.uint32), ref["rgba8"])
+    finally:
+        scene.set_tuning("fma", 0)
