@@ -183,8 +183,14 @@ __device__ float intersect(const float values[8], float d, float qFar, float3 st
   if (BORDER) {
     float t_min = qFar + EPS;
     if (fabsf(aa) > EPS) {
-      const float root1 = -0.5f * (b + sqrtf(D)) / aa, root2 = -0.5f * (b - sqrtf(D)) / aa;
-      t_min = (signf(aa) > 0) == (root1 < root2) ? root1 : root2;
+      // with D < 0 the reference's roots are NaN, so t_min is NaN and nothing below
+      // updates; that case is taken without evaluating them
+      if (D >= 0.0f) {
+        const float root1 = -0.5f * (b + sqrtf(D)) / aa, root2 = -0.5f * (b - sqrtf(D)) / aa;
+        t_min = (signf(aa) > 0) == (root1 < root2) ? root1 : root2;
+      } else {
+        t_min = __int_as_float(0x7fffffff);
+      }
     } else if (b < -EPS) {
       t_min = -c / b;
     }
