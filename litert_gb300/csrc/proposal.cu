@@ -385,34 +385,41 @@ __global__ void __launch_bounds__(128) mlp_infer_kernel(TripleView data, MlpStat
 // The network on the fifth-generation tensor cores.  A persistent CTA of 4 warps
 // stages the BF16 weights once in shared memory (K-major canonical layout:
 // 8-row x 16-byte core matrices), allocates 32 TMEM columns once, and then walks
-// 128-sample tiles (one M = 128 MMA tile each): per layer one elected thread
+// 128-sample tiles (one M = 128 MMA tile each).  Per layer one elected thread
 // issues tcgen05.mma (K = 16 per instruction) into the same 32 accumulator
-// columns and commits to an mbarrier; each warp reads its 32 TMEM lanes back with
-// tcgen05.ld for bias, ReLU and BF16 rounding (the rounding points of the
-// mma.sync path) and writes the next layer's A operand to shared memory.  The
-// next tile's features are loaded into registers while the current tile's chain
-// runs.  Eight CTAs per SM keep eight chains in flight.  Waits are bounded: a
-// timeout sets status bit 1, the CTA leaves its loop at the next barrier, waits
+// columns, commits to an mbarrier and waits on it; after a CTA barrier each warp
+// reads its 32 TMEM lanes with tcgen05.ld, adds the bias and applies ReLU and
+// BF16 rounding (the rounding points of the mma.sync path), writing the next
+// layer's A operand to shared memory.  A tile's features are staged while the
+// previous tile is still in layers 2-3, and loaded into registers one tile
+// earlier still.  Ten CTAs per SM keep ten chains in flight.  Waits are bounded:
+// a timeout sets status bit 1, the CTA leaves its loop at the next barrier, waits
 // once more (bounded) for its MMAs and frees its TMEM.
 constexpr uint32_t kTcLbo = 128;         // adjacent core matrices along K
 constexpr uint32_t kTcWait = 1u << 22;   // mbarrier polls before giving up
-constexpr int kTcBlocksPerSm = 8;
+constexpr int kTcBlocksPerSm = 10;
 
 __device__ __forceinline__ void stage_row16(uint8_t *tile, uint32_t row, uint32_t sbo, const uint4 &lo, const uint4 &hi) {
   *reinterpret_cast<uint4 *>(tile + tc05::kmajor_offset(row, 0, kTcLbo, sbo)) = lo;
   *reinterpret_cast<uint4 *>(tile + tc05::kmajor_offset(row, 8, kTcLbo, sbo)) = hi;
 }
 
-// bias + ReLU + BF16 of one 32-wide accumulator row into the A operand of the next layer
-__device__ __forceinline__ void hidden_to_smem(const float v[32], const float *bias, uint8_t *sH, uint32_t row) {
+// bias + ReLU + BF16 of one 32-wide accumulator row (this lane's TMEM lane, read in
+// two 16-column halves to keep registers low) into the A operand of the next layer
+__device__ __forceinline__ void hidden_to_smem(uint32_t trow, const float *bias, uint8_t *sH, uint32_t row) {
 #pragma unroll
-  for (int j = 0; j < 32; j += 8) {
-    uint4 q;
-    q.x = pack_bf16_relu(v[j] + bias[j], v[j + 1] + bias[j + 1]);
-    q.y = pack_bf16_relu(v[j + 2] + bias[j + 2], v[j + 3] + bias[j + 3]);
-    q.z = pack_bf16_relu(v[j + 4] + bias[j + 4], v[j + 5] + bias[j + 5]);
-    q.w = pack_bf16_relu(v[j + 6] + bias[j + 6], v[j + 7] + bias[j + 7]);
-    *reinterpret_cast<uint4 *>(sH + tc05::kmajor_offset(row, j, kTcLbo, 512)) = q;
+  for (int h = 0; h < 32; h += 16) {
+    float v[16];
+    tc05::tmem_ld16(trow + uint32_t(h), v);
+#pragma unroll
+    for (int j = 0; j < 16; j += 8) {
+      uint4 q;
+      q.x = pack_bf16_relu(v[j] + bias[h + j], v[j + 1] + bias[h + j + 1]);
+      q.y = pack_bf16_relu(v[j + 2] + bias[h + j + 2], v[j + 3] + bias[h + j + 3]);
+      q.z = pack_bf16_relu(v[j + 4] + bias[h + j + 4], v[j + 5] + bias[h + j + 5]);
+      q.w = pack_bf16_relu(v[j + 6] + bias[h + j + 6], v[j + 7] + bias[h + j + 7]);
+      *reinterpret_cast<uint4 *>(sH + tc05::kmajor_offset(row, uint32_t(h + j), kTcLbo, 512)) = q;
+    }
   }
 }
 
@@ -467,74 +474,80 @@ __global__ void __launch_bounds__(128, kTcBlocksPerSm) mlp_infer_tc_kernel(Tripl
   constexpr uint32_t kId32 = tc05::idesc_bf16_f32(128, 32), kId16 = tc05::idesc_bf16_f32(128, 16);
   uint32_t phase = 0;
   bool ok = true;
-  float v[32];
+  // One thread issues each layer's MMAs and waits for their commit; the CTA barrier
+  // that follows carries the completion (and a timeout) to the other warps, which
+  // do not poll.  The first tile's features go to shared memory here, each later
+  // tile's as soon as the previous tile's layer 1 has consumed them.
+  stage_row16(sX, tid, 256, lo, hi);
+  load_row16(data, (tile + gridDim.x) * 128 + tid, lo, hi);
+  tc05::fence_proxy_async();
+  tc05::fence_before_sync();
+  __syncthreads();
+  tc05::fence_after_sync();
   for (; tile < n_tiles; tile += gridDim.x) {
-    // this tile's features to shared memory (the previous tile's layer-1 MMA has completed)
-    stage_row16(sX, tid, 256, lo, hi);
+    const uint64_t row = tile * 128 + tid;
+    // layer 1: D[128 x 32] = X W1^T
+    bool t_ok = true;
+    if (tid == 0) {
+      tc05::mma_bf16(tbase, tc05::smem_desc(aX, kTcLbo, 256), tc05::smem_desc(aW1, kTcLbo, 256), kId32, false);
+      tc05::mma_commit(&mbar);
+      t_ok = tc05::mbar_wait(&mbar, phase, kTcWait);
+    }
+    phase ^= 1u;
+    tc05::fence_before_sync();
+    ok = __syncthreads_and(t_ok);
+    tc05::fence_after_sync();
+    if (!ok) break;
+    hidden_to_smem(trow, sb1, sH, tid);
+    stage_row16(sX, tid, 256, lo, hi);                              // next tile's features
+    load_row16(data, (tile + 2 * uint64_t(gridDim.x)) * 128 + tid, lo, hi);   // and the one after, in flight
     tc05::fence_proxy_async();
     tc05::fence_before_sync();
     __syncthreads();
     tc05::fence_after_sync();
-    const uint64_t row = tile * 128 + tid;
-    load_row16(data, (tile + gridDim.x) * 128 + tid, lo, hi);   // next tile, in flight during this one
-    // layer 1: D[128 x 32] = X W1^T
-    if (tid == 0) {
-      tc05::mma_bf16(tbase, tc05::smem_desc(aX, kTcLbo, 256), tc05::smem_desc(aW1, kTcLbo, 256), kId32, false);
-      tc05::mma_commit(&mbar);
-    }
-    bool w_ok = __all_sync(0xffffffffu, tc05::mbar_wait(&mbar, phase, kTcWait));
-    phase ^= 1u;
-    tc05::fence_after_sync();
-    if (w_ok) {
-      tc05::tmem_ld32(trow, v);
-      hidden_to_smem(v, sb1, sH, tid);
-    }
-    tc05::fence_proxy_async();
-    tc05::fence_before_sync();
-    ok = __syncthreads_and(w_ok);
-    tc05::fence_after_sync();
-    if (!ok) break;
     // layer 2: D = H1 W2^T, two K = 16 steps (the next K block starts 2 core matrices on)
     if (tid == 0) {
       tc05::mma_bf16(tbase, tc05::smem_desc(aH, kTcLbo, 512), tc05::smem_desc(aW2, kTcLbo, 512), kId32, false);
       tc05::mma_bf16(tbase, tc05::smem_desc(aH + 2 * kTcLbo, kTcLbo, 512), tc05::smem_desc(aW2 + 2 * kTcLbo, kTcLbo, 512),
                      kId32, true);
       tc05::mma_commit(&mbar);
+      t_ok = tc05::mbar_wait(&mbar, phase, kTcWait);
     }
-    w_ok = __all_sync(0xffffffffu, tc05::mbar_wait(&mbar, phase, kTcWait));
     phase ^= 1u;
-    tc05::fence_after_sync();
-    if (w_ok) {
-      tc05::tmem_ld32(trow, v);
-      hidden_to_smem(v, sb2, sH, tid);
-    }
-    tc05::fence_proxy_async();
     tc05::fence_before_sync();
-    ok = __syncthreads_and(w_ok);
+    ok = __syncthreads_and(t_ok);
     tc05::fence_after_sync();
     if (!ok) break;
+    hidden_to_smem(trow, sb2, sH, tid);
+    tc05::fence_proxy_async();
+    tc05::fence_before_sync();
+    __syncthreads();
+    tc05::fence_after_sync();
     // layer 3: D[:, 0:16] = H2 W3pad^T (column 0 is the output)
     if (tid == 0) {
       tc05::mma_bf16(tbase, tc05::smem_desc(aH, kTcLbo, 512), tc05::smem_desc(aW3, kTcLbo, 512), kId16, false);
       tc05::mma_bf16(tbase, tc05::smem_desc(aH + 2 * kTcLbo, kTcLbo, 512), tc05::smem_desc(aW3 + 2 * kTcLbo, kTcLbo, 512),
                      kId16, true);
       tc05::mma_commit(&mbar);
+      t_ok = tc05::mbar_wait(&mbar, phase, kTcWait);
     }
-    w_ok = __all_sync(0xffffffffu, tc05::mbar_wait(&mbar, phase, kTcWait));
     phase ^= 1u;
+    tc05::fence_before_sync();
+    ok = __syncthreads_and(t_ok);
     tc05::fence_after_sync();
-    if (w_ok) {
-      tc05::tmem_ld32(trow, v);
+    if (!ok) break;
+    {
+      float v[16];
+      tc05::tmem_ld16(trow, v);
       if (row < data.n) out[row] = v[0] + sb3;
     }
     tc05::fence_before_sync();
-    ok = __syncthreads_and(w_ok);   // every lane has read D before the next tile's MMA overwrites it
+    __syncthreads();   // every lane has read D before the next tile's MMA overwrites it
     tc05::fence_after_sync();
-    if (!ok) break;
   }
-  if (!ok) {
+  if (!ok && tid == 0) {
     tc05::mbar_wait(&mbar, phase ^ 1u, kTcWait);   // the MMAs of the step that timed out, if they finish
-    if (tid == 0) atomicOr(status, 2u);
+    atomicOr(status, 2u);
   }
   tc05::fence_before_sync();
   __syncthreads();
