@@ -116,6 +116,19 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def job_rate(ms_local, rays_per_rank, world, device=None):
+    """Whole-job throughput of `world` replicas: the slowest rank's time (MAX
+    all-reduce over the process group when world > 1) and the rays of all ranks
+    over it.  Returns (ms, Mrays/s)."""
+    ms = float(ms_local)
+    if world > 1:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, world * rays_per_rank / (ms * 1e-3) / 1e6
+
+
 def build_workload(args):
     from litert_gb300 import lrt, scenes
     t0 = time.time()
@@ -525,12 +538,7 @@ def main():
         torch.distributed.barrier()
     clk = clocks.stop()
     times = [a.elapsed_time(b) for a, b in evs]
-    ms = sum(times) / len(times)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * n_rays / (ms * 1e-3) / 1e6
+    ms, value = job_rate(sum(times) / len(times), n_rays, world, dev)
 
     # end to end through the C ABI with host buffers (views in, hit buffer out, pinned host memory)
     host_hits = torch.empty(n_rays * 4, dtype=torch.float32, pin_memory=True)
@@ -542,7 +550,7 @@ def main():
                                   lrt.C.c_void_p(host_hits.data_ptr()), None, None)
         if i >= args.warmup:
             e2e_times.append(time.perf_counter() - t0)
-    e2e = world * n_rays / statistics.median(e2e_times) / 1e6
+    _, e2e = job_rate(statistics.median(e2e_times) * 1e3, n_rays, world, dev)
 
     # the other floating-point form of the same kernel, same launch shape, timed the same way
     other_fp = None
