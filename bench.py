@@ -287,8 +287,13 @@ def run_proposal(args, scene, dev, torch):
     stream = torch.cuda.current_stream(dev)
     out = {}
     recs = {}
+    stats = {}
+    trained_w = pp.get_weights(scene)
     scene.set_tuning("fma", 0)   # the proposal kernel is compiled without contraction: compare like with like
-    for mode in (0, 1):
+    # plain; the proposal with the untrained (initial) network; the proposal with the trained one
+    for name, mode, w in (("plain", 0, None), ("untrained", 1, pp.init_weights(7)), ("proposal", 1, trained_w)):
+        if w is not None:
+            pp.set_weights(scene, w)
         scene.set_tuning("proposal", mode)
         g = scene.graph_create(eval_views, hits_ptr=hits.data_ptr())
         for _ in range(3):
@@ -306,14 +311,19 @@ def run_proposal(args, scene, dev, torch):
             b.synchronize()
             ts.append(a.elapsed_time(b))
         if mode:
-            st = pp.stats(scene)
+            stats[name] = pp.stats(scene)
         lrt.Scene.graph_destroy(g)
         ms = statistics.median(ts)
-        out["proposal" if mode else "plain"] = {"ms": ms, "mrays": n / (ms * 1e-3) / 1e6}
-        recs[mode] = hits.cpu().numpy().view(np.uint32).reshape(-1, 4).copy()
+        out[name] = {"ms": ms, "mrays": n / (ms * 1e-3) / 1e6}
+        recs[name] = hits.cpu().numpy().view(np.uint32).reshape(-1, 4).copy()
     scene.set_tuning("proposal", 0)
     scene.set_tuning("fma", args.fma)
-    a, b = recs[0], recs[1]
+    st = stats["proposal"]
+    reps = max(args.steps, 5)
+
+    def per_step(d):
+        return {k: v // reps for k, v in d.items()}
+    a, b = recs["plain"], recs["proposal"]
     mask_same = np.array_equal(a[:, 1] != lrt.MISS, b[:, 1] != lrt.MISS)
     both = (a[:, 1] != lrt.MISS) & (b[:, 1] != lrt.MISS)
     dt = np.abs(a[both, 0].view(np.float32) - b[both, 0].view(np.float32))
@@ -325,6 +335,9 @@ def run_proposal(args, scene, dev, torch):
             "max_dt_over_extent": float(dt.max() / 2.0) if dt.size else 0.0,
             "proposals_per_step": st["proposals"] // max(1, len(ts)), "acceptance": st["jumps"] / max(1, st["proposals"]),
             "jump_hit_rate": st["jump_hits"] / max(1, st["jumps"]),
+            "trained": per_step(stats["proposal"]), "untrained": per_step(stats["untrained"]),
+            "untrained_mrays": out["untrained"]["mrays"],
+            "untrained_records_identical": bool(np.array_equal(recs["plain"], recs["untrained"])),
             "triples": int(n_trip), "train_steps": args.prop_steps, "batch": 8192,
             "loss_first": float(losses[:10].mean()), "loss_last": float(losses[-100:].mean()),
             "collect_s": round(t_collect, 2), "train_s": round(t_train, 2), "inference": infer,

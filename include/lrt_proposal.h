@@ -61,8 +61,10 @@ lrt_status lrt_proposal_infer(lrt_ctx *ctx, uint64_t first, uint64_t n, float *o
 #define LRT_MLP_ENGINE_TCGEN05 1
 lrt_status lrt_proposal_infer_ex(lrt_ctx *ctx, uint64_t first, uint64_t n, float *out, int engine, float *ms);
 /* Counters of the proposal renders since the last call: proposals made, walks
- * started at the predicted voxel, and of those the ones that ended in a hit. */
-lrt_status lrt_proposal_stats(lrt_ctx *ctx, unsigned long long out[3]);
+ * started at the predicted voxel, of those the ones that ended in a hit, and the
+ * voxel steps those jumps skipped (voxel faces between the entry voxel and the
+ * predicted one) -- the work the network saves. */
+lrt_status lrt_proposal_stats(lrt_ctx *ctx, unsigned long long out[4]);
 
 #ifdef __cplusplus
 }

@@ -69,8 +69,9 @@ __device__ __forceinline__ int3 walk_voxel(float3 rp, float3 rd, float t, float3
 // the predicted voxel's entry distance if every other voxel of the box spanned
 // with the entry voxel is empty, else -inf (walk from the brick entry).
 __device__ float proposal_start(const DevScene &s, uint32_t brick, float3 rp, float3 rd, float3 inv, float t0,
-                                float t1, float u, bool &jumped) {
+                                float t1, float u, bool &jumped, uint32_t &skipped) {
   jumped = false;
+  skipped = 0;
   const float none = -3.4e38f;
   const uint32_t bsz = s.sbs_hdr.brick_size;
   // z rows of the occupancy mask stay inside one word for power-of-two bricks up to 32
@@ -100,6 +101,7 @@ __device__ float proposal_start(const DevScene &s, uint32_t brick, float3 rp, fl
   const float ny = inv.y * ((inv.y > 0.0f ? mp.y : mp.y + d) - rp.y);
   const float nz = inv.z * ((inv.z > 0.0f ? mp.z : mp.z + d) - rp.z);
   jumped = true;
+  skipped = uint32_t(abs(vh.x - v0.x) + abs(vh.y - v0.y) + abs(vh.z - v0.z));   // voxel faces crossed
   return fmx(fmx(nx, ny), nz);
 }
 
@@ -569,7 +571,7 @@ __global__ void __launch_bounds__(128, 4) render_proposal_kernel(DevScene s, Ren
   __syncthreads();
   const uint32_t lane = threadIdx.x & 31u, wi = threadIdx.x >> 5;
   Counters cnt = {0, 0, 0, 0};
-  unsigned long long n_prop = 0, n_jump = 0, n_hit_jump = 0;
+  unsigned long long n_prop = 0, n_jump = 0, n_hit_jump = 0, n_skip = 0;
   for (;;) {
     uint32_t tile = 0;
     if (lane == 0) tile = atomicAdd(L.tile_counter, 1u);
@@ -636,7 +638,9 @@ __global__ void __launch_bounds__(128, 4) render_proposal_kernel(DevScene s, Ren
       if (have_leaf) {
         n_prop++;
         bool jumped = false;
-        const float start = proposal_start(s, leaf, rp, rd, inv, t0, t1, u, jumped);
+        uint32_t skipped = 0;
+        const float start = proposal_start(s, leaf, rp, rd, inv, t0, t1, u, jumped, skipped);
+        n_skip += skipped;
         const float before = hit.t;
         brick_intersect<false, false, LRT_INTERSECT_NEWTON>(s, rp, rd, inv, tNearSdf, leaf, hit, cnt, nullptr, start);
         if (jumped) {
@@ -666,6 +670,7 @@ __global__ void __launch_bounds__(128, 4) render_proposal_kernel(DevScene s, Ren
     atomicAdd(&stats[0], n_prop);
     atomicAdd(&stats[1], n_jump);
     atomicAdd(&stats[2], n_hit_jump);
+    atomicAdd(&stats[3], n_skip);
   }
 }
 

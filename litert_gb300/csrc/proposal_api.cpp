@@ -313,10 +313,10 @@ extern "C" lrt_status lrt_proposal_infer(lrt_ctx *ctx, uint64_t first, uint64_t 
   return lrt_proposal_infer_ex(ctx, first, n, out, LRT_MLP_ENGINE_MMA, nullptr);
 }
 
-extern "C" lrt_status lrt_proposal_stats(lrt_ctx *ctx, unsigned long long out[3]) {
+extern "C" lrt_status lrt_proposal_stats(lrt_ctx *ctx, unsigned long long out[4]) {
   if (!ctx || !out) return LRT_ERR_INVALID;
   if (!ctx->prop) {
-    out[0] = out[1] = out[2] = 0;
+    out[0] = out[1] = out[2] = out[3] = 0;
     return LRT_OK;
   }
   LRT_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -326,5 +326,6 @@ extern "C" lrt_status lrt_proposal_stats(lrt_ctx *ctx, unsigned long long out[3]
   out[0] = h[0];
   out[1] = h[1];
   out[2] = h[2];
+  out[3] = h[3];
   return LRT_OK;
 }

@@ -128,6 +128,6 @@ def infer(scene, first, n, engine=None, timed=False):
 
 
 def stats(scene):
-    out = np.zeros(3, np.uint64)
+    out = np.zeros(4, np.uint64)
     _chk(scene, _lib().lrt_proposal_stats(scene._ctx, lrt._ptr(out)))
-    return {"proposals": int(out[0]), "jumps": int(out[1]), "jump_hits": int(out[2])}
+    return {"proposals": int(out[0]), "jumps": int(out[1]), "jump_hits": int(out[2]), "steps_skipped": int(out[3])}
