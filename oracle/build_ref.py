@@ -7,7 +7,8 @@ oracle/ref_driver.cpp, against the project's shims for the reference's missing
 dependencies (oracle/ref_shim/: a LiteMath stand-in and the CrossRT
 ISceneObject interface).  Leaf types off the path are compiled out with the
 reference's own DISABLE_* switches.  Runs only where the reference tree exists
-(this build container); the GPU machine never has it and never needs this library.
+(LRT_REFERENCE_TREE); machines without it skip this step, nothing in the engine,
+the benchmark or the GPU tests needs this library.
 """
 import os
 import subprocess

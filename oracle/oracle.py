@@ -1,7 +1,8 @@
 """ctypes binding of the CPU oracle (oracle/_build/liblrt_oracle.so).
 
 TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and bench.py's
-CPU baseline legs as the checker.  The product never imports this module.
+CPU baseline legs to verify the GPU engine against.  The product never imports
+this module.
 """
 import ctypes as C
 import os

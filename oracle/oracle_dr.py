@@ -1,8 +1,9 @@
 """ctypes binding of the differentiable-render part of the CPU oracle
 (oracle/lrt_oracle_dr.c in oracle/_build/liblrt_oracle.so).
 
-TEST INFRASTRUCTURE ONLY: used by tests/ and bench.py's CPU legs as the checker
-of the GPU DR kernels.  The product never imports this module.
+TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and bench.py's
+CPU legs to verify and time against the GPU DR kernels.  The product never
+imports this module.
 """
 import ctypes as C
 

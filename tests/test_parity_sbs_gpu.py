@@ -4,7 +4,7 @@ Bar: bit-exact hit records (t, primId, octahedral normal) and hit mask on every
 pixel, because both sides evaluate the reference's FP32 expressions in the same
 order without contraction.  The ANALYTIC finder calls acosf/cosf/powf whose
 last-ulp results differ between CUDA and glibc; there the bar is the
-spec tolerance: identical mask except <0.01% of pixels, |dt| <= 1e-4 of
+forward tolerance of the path: identical mask except <0.01% of pixels, |dt| <= 1e-4 of
 the scene extent (2), normals within 1e-3.
 """
 import numpy as np
