@@ -602,12 +602,10 @@ __global__ void __launch_bounds__(128, 4) render_proposal_kernel(DevScene s, Ren
     const float3 rp = matmul4x3(s.inst_inv, pos), rd = matmul3x3(s.inst_inv, dir);
     const float3 inv = safe_inverse(rd);
     const float tNearSdf = 0.1f;
-    uint32_t st_ref[kStackSize];
-    float st_t[kStackSize];
+    uint2 st[kStackSize];
     int sp = 0;
     if (active) {
-      st_ref[0] = 0;
-      st_t[0] = -3.4e38f;
+      st[0] = make_uint2(0u, __float_as_uint(-3.4e38f));
       sp = 1;
     }
     for (;;) {
@@ -615,14 +613,15 @@ __global__ void __launch_bounds__(128, 4) render_proposal_kernel(DevScene s, Ren
       bool have_leaf = false;
       while (sp > 0) {
         sp--;
-        const uint32_t ref = st_ref[sp];
-        if (st_t[sp] > hit.t) continue;
+        const uint2 top = st[sp];
+        const uint32_t ref = top.x;
+        if (__uint_as_float(top.y) > hit.t) continue;
         if (ref & kLeafBit) {
           leaf = ref & ~kLeafBit;
           have_leaf = true;
           break;
         }
-        visit_node<false, kStackSize>(s, ref, rp, inv, 0.0f, hit.t, st_ref, st_t, sp, cnt);
+        visit_node<false, kStackSize>(s, ref, rp, inv, 0.0f, hit.t, st, sp, cnt);
       }
       if (!__any_sync(0xffffffffu, have_leaf)) break;
       float f[16], t0 = 0.0f, t1 = 0.0f;

@@ -30,8 +30,7 @@ __global__ void __launch_bounds__(128, 5) render_refill_kernel(DevScene s, Rende
   float3 dir = f3(0, 0, 1), rp = f3(0, 0, 0), rd = f3(0, 0, 1), inv = f3(0, 0, 0);
   Hit hit;
   hit.t = 1e9f; hit.prim = kMiss; hit.geom = kMiss; hit.c0 = 1.0f; hit.c1 = hit.c2 = hit.c3 = 0.0f;
-  uint32_t st_ref[STACK];
-  float st_t[STACK];
+  uint2 st[STACK];
   int sp = 0;
   const float tNearSdf = 0.1f;
   for (;;) {
@@ -65,8 +64,7 @@ __global__ void __launch_bounds__(128, 5) render_refill_kernel(DevScene s, Rende
               rp = matmul4x3(s.inst_inv, pos);
               rd = matmul3x3(s.inst_inv, dir);
               inv = safe_inverse(rd);
-              st_ref[0] = 0;
-              st_t[0] = -3.4e38f;
+              st[0] = make_uint2(0u, __float_as_uint(-3.4e38f));
               sp = 1;
             }
           }
@@ -79,14 +77,15 @@ __global__ void __launch_bounds__(128, 5) render_refill_kernel(DevScene s, Rende
     if (live) {
       while (sp > 0) {
         sp--;
-        const uint32_t ref = st_ref[sp];
-        if (st_t[sp] > hit.t) continue;
+        const uint2 top = st[sp];
+        const uint32_t ref = top.x;
+        if (__uint_as_float(top.y) > hit.t) continue;
         if (ref & kLeafBit) {
           leaf = ref & ~kLeafBit;
           have_leaf = true;
           break;
         }
-        visit_node<false, STACK>(s, ref, rp, inv, 0.0f, hit.t, st_ref, st_t, sp, cnt);
+        visit_node<false, STACK>(s, ref, rp, inv, 0.0f, hit.t, st, sp, cnt);
       }
     }
     if (have_leaf) {

@@ -8,7 +8,7 @@ namespace dev {
 
 template <bool COUNT, int STACK>
 __device__ __forceinline__ void visit_node(const DevScene &s, uint32_t ref, float3 rp, float3 inv, float tNear,
-                                           float hit_t, uint32_t *st_ref, float *st_t, int &sp, Counters &cnt);
+                                           float hit_t, uint2 *st, int &sp, Counters &cnt);
 
 // RayQuery_NearestHit (BVH/BVH2Common.cpp:3490-3559) over the 4-wide BVH.
 // stopOnFirstHit (tFar <= 0) returns the first hit found (RayQuery_AnyHit).
@@ -32,11 +32,10 @@ __device__ void trace(const DevScene &s, float3 pos, float tNear, float3 dir, fl
   const float3 inv = safe_inverse(rd);
   const float tNearSdf = mx(tNear, 0.1f);   // SDF bias passed to every leaf type (:3472-3476)
 
-  uint32_t st_ref[STACK];
-  float st_t[STACK];
+  // per-ray stack of (node ref, entry distance as float bits), one 8-byte entry each
+  uint2 st[STACK];
   int sp = 0;
-  st_ref[sp] = 0;            // root wide node
-  st_t[sp] = -3.4e38f;
+  st[sp] = make_uint2(0u, __float_as_uint(-3.4e38f));   // root wide node
   sp++;
   // "while-while" structure: each lane walks inner nodes until it holds a leaf
   // (or its stack is empty); the warp reconverges, and all lanes holding a leaf
@@ -47,14 +46,15 @@ __device__ void trace(const DevScene &s, float3 pos, float tNear, float3 dir, fl
     bool have_leaf = false;
     while (sp > 0) {
       sp--;
-      const uint32_t ref = st_ref[sp];
-      if (st_t[sp] > hit.t) continue;
+      const uint2 top = st[sp];
+      const uint32_t ref = top.x;
+      if (__uint_as_float(top.y) > hit.t) continue;
       if (ref & kLeafBit) {
         leaf = ref & ~kLeafBit;
         have_leaf = true;
         break;
       }
-      visit_node<COUNT, STACK>(s, ref, rp, inv, tNear, hit.t, st_ref, st_t, sp, cnt);
+      visit_node<COUNT, STACK>(s, ref, rp, inv, tNear, hit.t, st, sp, cnt);
     }
     if (!have_leaf) break;
     const float t_before = hit.t;
@@ -72,7 +72,7 @@ __device__ void trace(const DevScene &s, float3 pos, float tNear, float3 dir, fl
 // reference slab test and push the entered ones far-to-near.
 template <bool COUNT, int STACK>
 __device__ __forceinline__ void visit_node(const DevScene &s, uint32_t ref, float3 rp, float3 inv, float tNear,
-                                           float hit_t, uint32_t *st_ref, float *st_t, int &sp, Counters &cnt) {
+                                           float hit_t, uint2 *st, int &sp, Counters &cnt) {
   {
     const WNode4 *nd = s.nodes + ref;
     if (COUNT) cnt.nodes++;
@@ -117,7 +117,7 @@ __device__ __forceinline__ void visit_node(const DevScene &s, uint32_t ref, floa
     // so this bound never drops an entry.
 #pragma unroll
     for (int i = 0; i < 4; i++) {
-      if (i < nk && sp < STACK) { st_ref[sp] = kr[i]; st_t[sp] = kt[i]; sp++; }
+      if (i < nk && sp < STACK) { st[sp] = make_uint2(kr[i], __float_as_uint(kt[i])); sp++; }
     }
   }
 }
