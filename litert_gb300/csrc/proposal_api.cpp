@@ -305,7 +305,7 @@ extern "C" lrt_status lrt_proposal_infer_ex(lrt_ctx *ctx, uint64_t first, uint64
   d.release();
   status.release();
   if (e != cudaSuccess) return cuda_fail(ctx, e, "lrt_proposal_infer");
-  if (st) return fail(ctx, LRT_ERR_CUDA, "tensor-core wait timed out");
+  if (st) return fail(ctx, LRT_ERR_TIMEOUT, "tensor-core wait timed out");
   return LRT_OK;
 }
 
