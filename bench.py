@@ -137,6 +137,18 @@ def build_workload(args):
     return h, nodes, values, views, time.time() - t0
 
 
+def gpu_build(args, host):
+    """The same scene from the GPU builder: wall time (after one warm-up build)
+    and whether it equals the host builder's output."""
+    from litert_gb300 import lrt, scenes
+    lrt.sbs_from_sdf(scenes.union_sdf(), 4, args.brick, gpu=0)   # context and module load
+    t0 = time.time()
+    h, nodes, values = lrt.sbs_from_sdf(scenes.union_sdf(), args.depth, args.brick, gpu=0)
+    dt = time.time() - t0
+    same = bool(np.array_equal(nodes, host[1]) and np.array_equal(values, host[2]))
+    return dt, same
+
+
 def cpu_sample(views, n_target, seed=0):
     """A strided pixel sample over all views: list of (view index, pixel ids)."""
     total = sum(w * h for w, h, _, _ in views)
@@ -499,6 +511,7 @@ def main():
     from oracle import oracle as orc
 
     h, nodes, values, views, t_build = build_workload(args)
+    t_gbuild, gbuild_same = gpu_build(args, (h, nodes, values)) if world == 1 else (None, None)
     scene = lrt.Scene(local if world > 1 else 0)
     g = scene.add_sbs(h, nodes, values)
     scene.add_instance(g)
@@ -624,7 +637,9 @@ def main():
                        "depth": args.depth, "brick": args.brick, "bricks": int(nodes.shape[0]),
                        "brick_bytes": int(values.nbytes), "finder": "NEWTON", "render_mode": "NORMAL",
                        "l2": "256 MiB write between timed steps; scene data 623 MB > L2",
-                       "scene_build_s": round(t_build, 2), "parallelism": f"replicas{world}",
+                       "scene_build_s": round(t_build, 2),
+                       "scene_build_gpu_s": None if t_gbuild is None else round(t_gbuild, 3),
+                       "scene_build_gpu_identical": gbuild_same, "parallelism": f"replicas{world}",
                        "launch": "CUDA graph replay" if graph is not None else "direct",
                        "tuning": tuned, "autotune_candidates": len(tried),
                        "fp": ("FP32 with contraction (FMA); forward parity tolerance" if args.fma

@@ -173,6 +173,16 @@ void       lrt_sbs_free(lrt_sbs *sbs);
 lrt_status lrt_svs_build_from_sdf(const lrt_sdf_desc *sdf, uint32_t depth, int threads, lrt_svs **out);
 lrt_status lrt_svs_data(const lrt_svs *svs, const lrt_svs_node **nodes, uint32_t *n_nodes);
 void       lrt_svs_free(lrt_svs *svs);
+/* The same two builders on GPU `device`: the same frame octree, bricks and voxels
+ * in the same order, bit for bit (the octree grows level by level, one thread per
+ * node; brick values one block per leaf).  depth >= 4 (shallower sets are a few
+ * thousand nodes: use the host builders); results in host memory as above.
+ * lrt_build_last_error() describes the last failure of these calls on the calling
+ * thread. */
+lrt_status lrt_sbs_build_from_sdf_gpu(int device, const lrt_sdf_desc *sdf, uint32_t depth, const lrt_sbs_header *hdr,
+                                      lrt_sbs **out);
+lrt_status lrt_svs_build_from_sdf_gpu(int device, const lrt_sdf_desc *sdf, uint32_t depth, lrt_svs **out);
+const char *lrt_build_last_error(void);
 
 /* ---- camera helpers (LiteMath::perspectiveMatrix / lookAt / inverse4x4 as used
  *      by tests/tests.cpp:29-41 and Renderer/eye_ray_host.cpp:59-65) ---- */

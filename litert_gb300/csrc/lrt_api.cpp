@@ -726,6 +726,56 @@ extern "C" lrt_status lrt_svs_build_from_sdf(const lrt_sdf_desc *sdf, uint32_t d
   return LRT_OK;
 }
 
+// The GPU builders report errors through their return code only (no context);
+// the message of the last failure on this thread is kept for lrt_build_last_error.
+static thread_local std::string g_build_error;
+
+extern "C" const char *lrt_build_last_error(void) { return g_build_error.c_str(); }
+
+static bool sdf_args_ok(const lrt_sdf_desc *sdf) {
+  if (!sdf || (sdf->n_spheres + sdf->n_boxes) == 0) return false;
+  if ((sdf->n_spheres && !sdf->spheres) || (sdf->n_boxes && !sdf->boxes)) return false;
+  return true;
+}
+
+extern "C" lrt_status lrt_sbs_build_from_sdf_gpu(int device, const lrt_sdf_desc *sdf, uint32_t depth,
+                                                 const lrt_sbs_header *hdr, lrt_sbs **out) {
+  g_build_error.clear();
+  if (!sdf_args_ok(sdf) || !hdr || !out) return LRT_ERR_INVALID;
+  if (hdr->brick_size < 1 || hdr->brick_size > 16 || hdr->brick_pad > 1 ||
+      !(hdr->bytes_per_value == 1 || hdr->bytes_per_value == 2 || hdr->bytes_per_value == 4) || depth > 15)
+    return LRT_ERR_INVALID;
+  if ((hdr->aux_data & 0xFF000000u) != LRT_SBS_LAYOUT_DX && (hdr->aux_data & 0xFF000000u) != LRT_SBS_LAYOUT_UNDEFINED)
+    return LRT_ERR_UNSUPPORTED;
+  if (depth < 4) {
+    g_build_error = "the GPU builder needs depth >= 4 (use lrt_sbs_build_from_sdf)";
+    return LRT_ERR_UNSUPPORTED;
+  }
+  if (cudaSetDevice(device) != cudaSuccess) return LRT_ERR_CUDA;
+  lrt_sbs *r = new (std::nothrow) lrt_sbs();
+  if (!r) return LRT_ERR_OOM;
+  lrt_status s = build_sbs_gpu(*sdf, depth, *hdr, r->d, g_build_error);
+  if (s != LRT_OK) { delete r; return s; }
+  *out = r;
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_svs_build_from_sdf_gpu(int device, const lrt_sdf_desc *sdf, uint32_t depth, lrt_svs **out) {
+  g_build_error.clear();
+  if (!sdf_args_ok(sdf) || !out || depth > 15) return LRT_ERR_INVALID;
+  if (depth < 4) {
+    g_build_error = "the GPU builder needs depth >= 4 (use lrt_svs_build_from_sdf)";
+    return LRT_ERR_UNSUPPORTED;
+  }
+  if (cudaSetDevice(device) != cudaSuccess) return LRT_ERR_CUDA;
+  lrt_svs *r = new (std::nothrow) lrt_svs();
+  if (!r) return LRT_ERR_OOM;
+  lrt_status s = build_svs_gpu(*sdf, depth, r->nodes, g_build_error);
+  if (s != LRT_OK) { delete r; return s; }
+  *out = r;
+  return LRT_OK;
+}
+
 extern "C" lrt_status lrt_svs_data(const lrt_svs *svs, const lrt_svs_node **nodes, uint32_t *n_nodes) {
   if (!svs) return LRT_ERR_INVALID;
   if (nodes) *nodes = svs->nodes.data();

@@ -1,6 +1,7 @@
 // Internal declarations shared by the host library (C++) and the CUDA kernels.
 #pragma once
 #include <cstdint>
+#include <string>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -42,6 +43,10 @@ struct BvhData {
 float sdf_eval(const lrt_sdf_desc &f, float x, float y, float z);
 lrt_status build_sbs(const lrt_sdf_desc &f, uint32_t depth, const lrt_sbs_header &hdr, int threads, SbsData &out);
 lrt_status build_svs(const lrt_sdf_desc &f, uint32_t depth, int threads, std::vector<lrt_svs_node> &out);
+// the same on the current device (build_gpu.cu); depth >= 4, arguments validated by the caller
+lrt_status build_sbs_gpu(const lrt_sdf_desc &f, uint32_t depth, const lrt_sbs_header &hdr, SbsData &out,
+                         std::string &err);
+lrt_status build_svs_gpu(const lrt_sdf_desc &f, uint32_t depth, std::vector<lrt_svs_node> &out, std::string &err);
 // Voxel occupancy of every brick: bit (i*bs + j)*bs + k of brick b is set when
 // the smallest of the voxel's 8 decoded corner values is <= 0 -- exactly the
 // voxel test of OctreeBrickIntersect (BVH/BVH2Common.cpp:821).

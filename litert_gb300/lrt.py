@@ -105,6 +105,9 @@ def lib():
             "lrt_sbs_data": (I, [P, C.POINTER(SbsHeader), C.POINTER(VP), C.POINTER(U32), C.POINTER(VP), C.POINTER(U32)]),
             "lrt_sbs_free": (None, [P]),
             "lrt_svs_build_from_sdf": (I, [C.POINTER(SdfDesc), U32, I, C.POINTER(P)]),
+            "lrt_sbs_build_from_sdf_gpu": (I, [I, C.POINTER(SdfDesc), U32, C.POINTER(SbsHeader), C.POINTER(P)]),
+            "lrt_svs_build_from_sdf_gpu": (I, [I, C.POINTER(SdfDesc), U32, C.POINTER(P)]),
+            "lrt_build_last_error": (C.c_char_p, []),
             "lrt_svs_data": (I, [P, C.POINTER(VP), C.POINTER(U32)]),
             "lrt_svs_free": (None, [P]),
             "lrt_perspective": (None, [C.c_float, C.c_float, C.c_float, C.c_float, VP]),
@@ -190,12 +193,23 @@ def _check(status, ctx=None, what=""):
         raise LrtError(status, msg or what)
 
 
-def sbs_from_sdf(sdf, depth, brick_size, brick_pad=0, bytes_per_value=4, threads=0):
-    """create_sdf_SBS (utils/sdf_converter.cpp:162-181): returns (header, nodes (n,4) u32, values u32)."""
+def _build_check(status, what):
+    if status != 0:
+        msg = lib().lrt_build_last_error()
+        raise LrtError(status, (msg.decode() if msg else "") or what)
+
+
+def sbs_from_sdf(sdf, depth, brick_size, brick_pad=0, bytes_per_value=4, threads=0, gpu=None):
+    """create_sdf_SBS (utils/sdf_converter.cpp:162-181): returns (header, nodes (n,4) u32, values u32).
+    gpu=<device index> builds on that GPU (depth >= 4; identical output)."""
     hdr = SbsHeader(brick_size, brick_pad, bytes_per_value, SBS_LAYOUT_DX)
     h = C.c_void_p()
-    _check(lib().lrt_sbs_build_from_sdf(C.byref(sdf.desc()), depth, C.byref(hdr), threads, C.byref(h)),
-           what="lrt_sbs_build_from_sdf")
+    if gpu is not None:
+        _build_check(lib().lrt_sbs_build_from_sdf_gpu(int(gpu), C.byref(sdf.desc()), depth, C.byref(hdr), C.byref(h)),
+                     "lrt_sbs_build_from_sdf_gpu")
+    else:
+        _check(lib().lrt_sbs_build_from_sdf(C.byref(sdf.desc()), depth, C.byref(hdr), threads, C.byref(h)),
+               what="lrt_sbs_build_from_sdf")
     try:
         oh, np_, nn, vp, nv = SbsHeader(), C.c_void_p(), C.c_uint32(), C.c_void_p(), C.c_uint32()
         _check(lib().lrt_sbs_data(h, C.byref(oh), C.byref(np_), C.byref(nn), C.byref(vp), C.byref(nv)))
@@ -206,10 +220,16 @@ def sbs_from_sdf(sdf, depth, brick_size, brick_pad=0, bytes_per_value=4, threads
     return oh, nodes, values
 
 
-def svs_from_sdf(sdf, depth, threads=0):
-    """create_sdf_SVS (utils/sdf_converter.cpp:118-134): returns nodes (n,4) u32."""
+def svs_from_sdf(sdf, depth, threads=0, gpu=None):
+    """create_sdf_SVS (utils/sdf_converter.cpp:118-134): returns nodes (n,4) u32.
+    gpu=<device index> builds on that GPU (depth >= 4; identical output)."""
     h = C.c_void_p()
-    _check(lib().lrt_svs_build_from_sdf(C.byref(sdf.desc()), depth, threads, C.byref(h)), what="lrt_svs_build_from_sdf")
+    if gpu is not None:
+        _build_check(lib().lrt_svs_build_from_sdf_gpu(int(gpu), C.byref(sdf.desc()), depth, C.byref(h)),
+                     "lrt_svs_build_from_sdf_gpu")
+    else:
+        _check(lib().lrt_svs_build_from_sdf(C.byref(sdf.desc()), depth, threads, C.byref(h)),
+               what="lrt_svs_build_from_sdf")
     try:
         np_, nn = C.c_void_p(), C.c_uint32()
         _check(lib().lrt_svs_data(h, C.byref(np_), C.byref(nn)))
