@@ -184,6 +184,17 @@ lrt_status lrt_sbs_build_from_sdf_gpu(int device, const lrt_sdf_desc *sdf, uint3
 lrt_status lrt_svs_build_from_sdf_gpu(int device, const lrt_sdf_desc *sdf, uint32_t depth, lrt_svs **out);
 const char *lrt_build_last_error(void);
 
+/* Files in the reference's binary layout (save_sdf_SBS / load_sdf_SBS /
+ * save_sdf_SVS / load_sdf_SVS, sdfScene/sdf_scene.cpp:121-175): SBS = header,
+ * u32 node count, nodes, u32 value count, values; SVS = u32 node count, nodes.
+ * Loads check every count against the file size (LRT_ERR_INVALID for a short or
+ * foreign file) and return the same objects as the builders. */
+lrt_status lrt_sbs_save(const char *path, const lrt_sbs_header *hdr, const lrt_sbs_node *nodes, uint32_t n_nodes,
+                        const uint32_t *values, uint32_t n_values);
+lrt_status lrt_sbs_load(const char *path, lrt_sbs **out);
+lrt_status lrt_svs_save(const char *path, const lrt_svs_node *nodes, uint32_t n_nodes);
+lrt_status lrt_svs_load(const char *path, lrt_svs **out);
+
 /* ---- camera helpers (LiteMath::perspectiveMatrix / lookAt / inverse4x4 as used
  *      by tests/tests.cpp:29-41 and Renderer/eye_ray_host.cpp:59-65) ---- */
 void lrt_perspective(float fov_deg, float aspect, float znear, float zfar, float out[16]);

@@ -689,8 +689,6 @@ extern "C" lrt_status lrt_build_bvh2(const float *boxes6, uint32_t n, uint32_t p
 extern "C" void lrt_free(void *p) { std::free(p); }
 
 // ---------------------------------------------------------------- scene construction
-struct lrt_sbs { SbsData d; };
-struct lrt_svs { std::vector<lrt_svs_node> nodes; };
 
 extern "C" lrt_status lrt_sbs_build_from_sdf(const lrt_sdf_desc *sdf, uint32_t depth, const lrt_sbs_header *hdr,
                                              int threads, lrt_sbs **out) {

@@ -133,3 +133,7 @@ cudaError_t launch_query(const DevScene &s, const float4 *pos_near, const float4
                          lrt_hit *out, cudaStream_t st);
 
 }  // namespace lrt
+
+// host-side results of the SBS / SVS builders and loaders (opaque in the C ABI)
+struct lrt_sbs { lrt::SbsData d; };
+struct lrt_svs { std::vector<lrt_svs_node> nodes; };

@@ -108,6 +108,10 @@ def lib():
             "lrt_sbs_build_from_sdf_gpu": (I, [I, C.POINTER(SdfDesc), U32, C.POINTER(SbsHeader), C.POINTER(P)]),
             "lrt_svs_build_from_sdf_gpu": (I, [I, C.POINTER(SdfDesc), U32, C.POINTER(P)]),
             "lrt_build_last_error": (C.c_char_p, []),
+            "lrt_sbs_save": (I, [C.c_char_p, C.POINTER(SbsHeader), VP, U32, VP, U32]),
+            "lrt_sbs_load": (I, [C.c_char_p, C.POINTER(P)]),
+            "lrt_svs_save": (I, [C.c_char_p, VP, U32]),
+            "lrt_svs_load": (I, [C.c_char_p, C.POINTER(P)]),
             "lrt_svs_data": (I, [P, C.POINTER(VP), C.POINTER(U32)]),
             "lrt_svs_free": (None, [P]),
             "lrt_perspective": (None, [C.c_float, C.c_float, C.c_float, C.c_float, VP]),
@@ -237,6 +241,54 @@ def svs_from_sdf(sdf, depth, threads=0, gpu=None):
     finally:
         lib().lrt_svs_free(h)
     return nodes
+
+
+def _sbs_arrays(h):
+    oh, np_, nn, vp, nv = SbsHeader(), C.c_void_p(), C.c_uint32(), C.c_void_p(), C.c_uint32()
+    _check(lib().lrt_sbs_data(h, C.byref(oh), C.byref(np_), C.byref(nn), C.byref(vp), C.byref(nv)))
+    nodes = (np.ctypeslib.as_array(C.cast(np_, C.POINTER(C.c_uint32)), (nn.value * 4,)).copy() if nn.value
+             else np.zeros(0, np.uint32))
+    values = (np.ctypeslib.as_array(C.cast(vp, C.POINTER(C.c_uint32)), (nv.value,)).copy() if nv.value
+              else np.zeros(0, np.uint32))
+    return oh, nodes.reshape(-1, 4), values
+
+
+def save_sbs(path, hdr, nodes, values):
+    """save_sdf_SBS (sdfScene/sdf_scene.cpp:148-158)."""
+    nodes = np.ascontiguousarray(nodes, np.uint32).reshape(-1, 4)
+    values = np.ascontiguousarray(values, np.uint32)
+    _check(lib().lrt_sbs_save(os.fsencode(path), C.byref(hdr), _ptr(nodes), nodes.shape[0], _ptr(values), values.size),
+           what="lrt_sbs_save")
+
+
+def load_sbs(path):
+    """load_sdf_SBS (sdfScene/sdf_scene.cpp:160-173): (header, nodes (n,4) u32, values u32)."""
+    h = C.c_void_p()
+    _check(lib().lrt_sbs_load(os.fsencode(path), C.byref(h)), what="lrt_sbs_load")
+    try:
+        return _sbs_arrays(h)
+    finally:
+        lib().lrt_sbs_free(h)
+
+
+def save_svs(path, nodes):
+    """save_sdf_SVS (sdfScene/sdf_scene.cpp:121-127)."""
+    nodes = np.ascontiguousarray(nodes, np.uint32).reshape(-1, 4)
+    _check(lib().lrt_svs_save(os.fsencode(path), _ptr(nodes), nodes.shape[0]), what="lrt_svs_save")
+
+
+def load_svs(path):
+    """load_sdf_SVS (sdfScene/sdf_scene.cpp:129-137): nodes (n,4) u32."""
+    h = C.c_void_p()
+    _check(lib().lrt_svs_load(os.fsencode(path), C.byref(h)), what="lrt_svs_load")
+    try:
+        np_, nn = C.c_void_p(), C.c_uint32()
+        _check(lib().lrt_svs_data(h, C.byref(np_), C.byref(nn)))
+        if nn.value == 0:
+            return np.zeros((0, 4), np.uint32)
+        return np.ctypeslib.as_array(C.cast(np_, C.POINTER(C.c_uint32)), (nn.value * 4,)).copy().reshape(-1, 4)
+    finally:
+        lib().lrt_svs_free(h)
 
 
 def build_bvh2(boxes6, prims_per_leaf):

@@ -52,3 +52,24 @@ def test_shallow_depth_is_refused():
         lrt.sbs_from_sdf(lrt.Sdf(**scenes.SPHERE_SDF), 3, 4, gpu=0)
     with pytest.raises(lrt.LrtError):
         lrt.svs_from_sdf(lrt.Sdf(**scenes.SPHERE_SDF), 3, gpu=0)
+
+
+def test_gpu_built_scene_through_a_file_renders_like_the_host_built_one(tmp_path):
+    """GPU build -> save (the reference's file layout) -> load -> render equals the
+    render of the host-built scene bit for bit."""
+    sdf = scenes.union_sdf()
+    h, n, v = lrt.sbs_from_sdf(sdf, 5, 8, gpu=0)
+    p = tmp_path / "union.sbs"
+    lrt.save_sbs(p, h, n, v)
+    h2, n2, v2 = lrt.load_sbs(p)
+    views = scenes.union_views(n_views=2, lo=128, hi=192, cam_seed=3)
+    out = []
+    for hh, nn, vv in ((h2, n2, v2), lrt.sbs_from_sdf(sdf, 5, 8)):
+        s = lrt.Scene(0)
+        s.add_instance(s.add_sbs(hh, nn, vv))
+        s.commit_scene()
+        s.set_preset(render_mode=lrt.RENDER_MODE_NORMAL, sdf_node_intersect=lrt.INTERSECT_NEWTON)
+        out.append(s.render_host(views, hits=True)["hits"].view(np.uint32).copy())
+        s.close()
+    assert (out[0].reshape(-1, 4)[:, 1] != lrt.MISS).sum() > 1000
+    assert np.array_equal(out[0], out[1])
