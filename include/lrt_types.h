@@ -73,7 +73,10 @@ enum {
 enum {
   LRT_RENDER_MODE_MASK = 0, LRT_RENDER_MODE_LAMBERT_NO_TEX = 1, LRT_RENDER_MODE_DEPTH = 2,
   LRT_RENDER_MODE_LINEAR_DEPTH = 3, LRT_RENDER_MODE_INVERSE_LINEAR_DEPTH = 4,
-  LRT_RENDER_MODE_NORMAL = 8, LRT_RENDER_MODE_LAMBERT = 17
+  LRT_RENDER_MODE_PRIMITIVE = 5, LRT_RENDER_MODE_TYPE = 6, LRT_RENDER_MODE_GEOM = 7,
+  LRT_RENDER_MODE_NORMAL = 8, LRT_RENDER_MODE_BARYCENTRIC = 9, LRT_RENDER_MODE_ST_ITERATIONS = 10,
+  LRT_RENDER_MODE_PHONG_NO_TEX = 12, LRT_RENDER_MODE_DIFFUSE = 16, LRT_RENDER_MODE_LAMBERT = 17,
+  LRT_RENDER_MODE_PHONG = 18, LRT_RENDER_MODE_HSV_DEPTH = 19
 };
 enum {
   LRT_INTERSECT_ST = 0, LRT_INTERSECT_ANALYTIC = 1, LRT_INTERSECT_NEWTON = 2,

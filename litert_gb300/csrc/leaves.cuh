@@ -403,7 +403,24 @@ __device__ void tri_intersect(const DevScene &s, float3 ray_pos, float3 ray_dir,
 
 // kernel_RayTrace shading, Renderer/eye_ray.cpp:162-489 (MASK, LAMBERT_NO_TEX,
 // LAMBERT for coloured bricks, DEPTH, LINEAR_DEPTH, INVERSE_LINEAR_DEPTH, NORMAL)
-__device__ inline float4 shade(const DevScene &s, const Hit &hit, float3 dir) {
+// MultiRenderer::m_palette (Renderer/eye_ray.h:235-241): the reference's 20 colours,
+// kept identical because PRIMITIVE / TYPE / GEOM images are compared with it
+__device__ __forceinline__ uint32_t palette_color(uint32_t i) {
+  constexpr uint32_t P[20] = {0xffe6194bu, 0xff3cb44bu, 0xffffe119u, 0xff0082c8u, 0xfff58231u, 0xff911eb4u, 0xff46f0f0u,
+                              0xfff032e6u, 0xffd2f53cu, 0xfffabebeu, 0xff008080u, 0xffe6beffu, 0xffaa6e28u, 0xfffffac8u,
+                              0xff800000u, 0xffaaffc3u, 0xff808000u, 0xffffd8b1u, 0xff000080u, 0xff808080u};
+  return P[i % 20u];
+}
+// decode_RGBA8, Renderer/eye_ray.cpp:15-19
+__device__ __forceinline__ float4 decode_rgba8(uint32_t c) {
+  return make_float4(float(c & 0xFF) * (1.0f / 255.0f), float((c >> 8) & 0xFF) * (1.0f / 255.0f),
+                     float((c >> 16) & 0xFF) * (1.0f / 255.0f), float((c >> 24) & 0xFF) * (1.0f / 255.0f));
+}
+
+// kernel_RayTrace, Renderer/eye_ray.cpp:162-489 (the geometry-based modes without
+// shadow rays; lights are the reference's defaults, Renderer/eye_ray_host.cpp:40;
+// geometry without brick colours takes the default material's texel (0, 1, 1))
+__device__ inline float4 shade(const DevScene &s, const Hit &hit, float3 pos, float3 dir) {
   if (hit.prim == kMiss) return make_float4(0, 0, 0, 1);
   const float z = hit.t, z_near = 0.1f, z_far = 10;
   const uint32_t type = hit.geom >> 24;
@@ -425,7 +442,9 @@ __device__ inline float4 shade(const DevScene &s, const Hit &hit, float3 dir) {
     case LRT_RENDER_MODE_NORMAL: return make_float4(fabsf(norm.x), fabsf(norm.y), fabsf(norm.z), 1);
     case LRT_RENDER_MODE_LAMBERT_NO_TEX:
     case LRT_RENDER_MODE_LAMBERT: {
-      float3 color = f3(1, 1, 1);
+      // LAMBERT_NO_TEX: white; LAMBERT: the brick colour, else the default textured
+      // material's constant texel (0, 1, 1) (Renderer/eye_ray_host.cpp:30-33)
+      float3 color = s.preset.render_mode == LRT_RENDER_MODE_LAMBERT ? f3(0, 1, 1) : f3(1, 1, 1);
       if (s.preset.render_mode == LRT_RENDER_MODE_LAMBERT && type == LRT_TYPE_SDF_SBS_COL) {
         color.x = roundf(hit.c0) / 255.0f;
         color.y = hit.c0 - floorf(hit.c0);
@@ -439,6 +458,49 @@ __device__ inline float4 shade(const DevScene &s, const Hit &hit, float3 dir) {
       fc = add(fc, scl(q, mul(f3(lc, lc, lc), color)));
       fc = add(fc, mul(f3(0.25f, 0.25f, 0.25f), color));
       return make_float4(fc.x, fc.y, fc.z, 1);
+    }
+    case LRT_RENDER_MODE_PRIMITIVE:   // the reference's primId: original triangle ids
+      return decode_rgba8(palette_color(type == LRT_TYPE_MESH_TRIANGLE ? s.prim_indices[hit.prim] : hit.prim));
+    case LRT_RENDER_MODE_TYPE: return decode_rgba8(palette_color(type));
+    case LRT_RENDER_MODE_GEOM: return decode_rgba8(palette_color(hit.geom & 0x00FFFFFFu));
+    case LRT_RENDER_MODE_BARYCENTRIC: return make_float4(hit.c0, hit.c1, 1 - hit.c0 - hit.c1, 1);
+    case LRT_RENDER_MODE_ST_ITERATIONS: {   // the finder stored its iteration count as primId
+      const uint32_t it = type == LRT_TYPE_MESH_TRIANGLE ? s.prim_indices[hit.prim] : hit.prim;
+      if (it == 0) return make_float4(0.5f, 0.5f, 0.5f, 1);
+      if (it <= 64) {
+        const float q = clampf(float(it) / 64, 0.0f, 1.0f), r = 1 - q;
+        return make_float4(q * 0.0f + r * 0.0f, q * 0.0f + r * 1.0f, q * 1.0f + r * 0.0f, q * 1.0f + r * 1.0f);
+      }
+      const float q = clampf(float(it - 64) / (256 - 64), 0.0f, 1.0f), r = 1 - q;
+      return make_float4(q * 1.0f + r * 0.0f, q * 0.0f + r * 0.0f, q * 0.0f + r * 1.0f, q * 1.0f + r * 1.0f);
+    }
+    case LRT_RENDER_MODE_DIFFUSE: {
+      float3 color = f3(0, 1, 1);
+      if (type == LRT_TYPE_SDF_SBS_COL) {
+        color.x = roundf(hit.c0) / 255.0f;
+        color.y = hit.c0 - floorf(hit.c0);
+        color.z = roundf(hit.c1) / 255.0f;
+      }
+      return make_float4(color.x, color.y, color.z, 1);
+    }
+    case LRT_RENDER_MODE_HSV_DEPTH: {
+      const float iz = pos.z + z * dir.z;
+      float zt = (iz + 1.f) * 2.f;
+      zt = zt - float(int(zt));
+      if (zt < 0.f) zt = 1.f + zt;
+      // HSV (zt, 1, 1) -> RGB; the two written channels are always distinct
+      const float vmin = (1.f - 1.f) * 1.0f;
+      float hi;
+      const float a = (1.0f - vmin) * modff(zt * 6.f, &hi);
+      uint32_t h = uint32_t(hi);
+      h = h <= 5u ? h : 5u;
+      const uint32_t i0 = (2u + (h >> 1)) % 3u;
+      const uint32_t i1 = (h & 1u) ? (h >> 1) : (1u + (h >> 1)) % 3u;
+      const float v1 = (h & 1u) ? 1.0f - a : vmin + a;
+      const float r = i1 == 0 ? v1 : (i0 == 0 ? vmin : 1.0f);
+      const float g = i1 == 1 ? v1 : (i0 == 1 ? vmin : 1.0f);
+      const float b = i1 == 2 ? v1 : (i0 == 2 ? vmin : 1.0f);
+      return make_float4(r, g, b, 1.f);
     }
     default: return make_float4(1, 0, 1, 1);
   }

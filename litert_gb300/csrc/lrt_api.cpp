@@ -426,6 +426,17 @@ extern "C" lrt_status lrt_set_preset(lrt_ctx *ctx, const lrt_preset *preset) {
     return fail(ctx, LRT_ERR_UNSUPPORTED, "lrt_set_preset: only trilinear interpolation is supported");
   if (preset->ray_gen_mode != 0) return fail(ctx, LRT_ERR_UNSUPPORTED, "lrt_set_preset: only regular ray generation");
   if (preset->spp == 0 || preset->spp > 1024) return fail(ctx, LRT_ERR_INVALID, "lrt_set_preset: bad spp");
+  switch (preset->render_mode) {   // kernel_RayTrace's modes for the geometry types of this path
+    case LRT_RENDER_MODE_MASK: case LRT_RENDER_MODE_LAMBERT_NO_TEX: case LRT_RENDER_MODE_DEPTH:
+    case LRT_RENDER_MODE_LINEAR_DEPTH: case LRT_RENDER_MODE_INVERSE_LINEAR_DEPTH: case LRT_RENDER_MODE_PRIMITIVE:
+    case LRT_RENDER_MODE_TYPE: case LRT_RENDER_MODE_GEOM: case LRT_RENDER_MODE_NORMAL:
+    case LRT_RENDER_MODE_BARYCENTRIC: case LRT_RENDER_MODE_ST_ITERATIONS: case LRT_RENDER_MODE_PHONG_NO_TEX:
+    case LRT_RENDER_MODE_DIFFUSE: case LRT_RENDER_MODE_LAMBERT: case LRT_RENDER_MODE_PHONG:
+    case LRT_RENDER_MODE_HSV_DEPTH:
+      break;
+    default:   // radiance-field, Gaussian-splat and texture-coordinate modes
+      return fail(ctx, LRT_ERR_UNSUPPORTED, "lrt_set_preset: render mode not supported");
+  }
   ctx->preset = *preset;
   ctx->dev.preset = *preset;
   return LRT_OK;

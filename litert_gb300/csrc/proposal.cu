@@ -659,7 +659,7 @@ __global__ void __launch_bounds__(128, 4) render_proposal_kernel(DevScene s, Ren
         reinterpret_cast<float4 *>(L.hits16)[pix] = *reinterpret_cast<const float4 *>(&o);
       }
       if (L.rgba || L.rgba8) {
-        const float4 c = shade(s, hit, dir);
+        const float4 c = shade(s, hit, pos, dir);
         if (L.rgba) L.rgba[pix] = c;
         if (L.rgba8) L.rgba8[pix] = encode_rgba8(c);
       }

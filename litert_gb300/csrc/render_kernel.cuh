@@ -10,10 +10,56 @@
 namespace lrt {
 namespace dev {
 
+// PHONG / PHONG_NO_TEX shading (Renderer/eye_ray.cpp:420-483) with the default
+// lights: the direct light adds an unshadowed Lambert term and a shadowed Phong
+// term (Kd = Ks = 0.25, exponent 32); ambient adds its colour.  The reference's
+// shadow ray is a nearest-hit query from just before the hit point towards the
+// light with the eye ray's tNear and tFar; only hit / miss is used, so an any-hit
+// query (the first leaf that reports a hit) decides the same.
+template <int TYPE, int MODE, int STACK>
+__device__ __noinline__ float4 shade_phong(const DevScene &s, const Hit &hit, float3 pos, float3 dir) {
+  if (hit.prim == kMiss) return make_float4(0, 0, 0, 1);
+  const uint32_t type = hit.geom >> 24;
+  float3 norm;
+  if (type == LRT_TYPE_MESH_TRIANGLE) {
+    const float4 a = s.tri_verts[3 * hit.prim + 0], b = s.tri_verts[3 * hit.prim + 1], c = s.tri_verts[3 * hit.prim + 2];
+    const float3 e1 = f3(b.x - a.x, b.y - a.y, b.z - a.z), e2 = f3(c.x - a.x, c.y - a.y, c.z - a.z);
+    norm = normalize(matmul4x3(s.inst_inv_t, cross(e1, e2)));
+  } else {
+    norm = decode_normal(hit.c2, hit.c3);
+  }
+  norm = scl(signf(dot(scl(-1.0f, dir), norm)), norm);
+  const float Kd = 0.25f, Ks = 0.25f, BIAS = 1e-6f;
+  float3 color = s.preset.render_mode == LRT_RENDER_MODE_PHONG_NO_TEX ? f3(1, 1, 1) : f3(0, 1, 1);
+  if (s.preset.render_mode == LRT_RENDER_MODE_PHONG && type == LRT_TYPE_SDF_SBS_COL) {
+    color.x = roundf(hit.c0) / 255.0f;
+    color.y = hit.c0 - floorf(hit.c0);
+    color.z = roundf(hit.c1) / 255.0f;
+  }
+  float3 fc = f3(0, 0, 0);
+  {  // direct light, normalize(1, 1, 1), colour 2/3
+    const float3 ld = normalize(f3(1, 1, 1));
+    const float l = 2.0f / 3.0f;
+    const float3 lc = f3(l, l, l);
+    const float3 surf = add(pos, scl(hit.t - BIAS, dir));
+    const float q = mx(0.0f, dot(norm, ld));
+    fc = add(fc, scl(q, mul(lc, color)));
+    Hit sh;
+    Counters cnt = {0, 0, 0, 0};
+    trace<TYPE, false, MODE, STACK>(s, surf, 0.0f, ld, -1e9f, sh, cnt);   // tFar <= 0: any hit
+    const float shade = (sh.prim == kMiss) ? 1.0f : 0.0f;
+    const float3 refl = add(scl(-1.0f, ld), scl(2.0f * dot(norm, ld), norm));
+    const float inner = Kd * mx(0.0f, dot(norm, ld)) + Ks * powf(mx(0.0f, dot(norm, refl)), 32.0f);
+    fc = add(fc, mul(scl(inner, scl(shade, lc)), color));
+  }
+  fc = add(fc, mul(f3(0.25f, 0.25f, 0.25f), color));   // ambient
+  return make_float4(fc.x, fc.y, fc.z, 1);
+}
+
 // Persistent render kernel: each warp pulls 32-pixel tiles (8x4 by default, the
 // shape is tunable) of the flattened multi-view tile space from a global queue
 // head and traces one ray per lane.
-template <int TYPE, bool COUNT, int MODE, int STACK, int FP>
+template <int TYPE, bool COUNT, int MODE, int STACK, int FP, bool PHONG = false>
 __global__ void __launch_bounds__(128, 5) render_kernel(DevScene s, RenderLaunch L) {
   const uint32_t lane = threadIdx.x & 31u;
   Counters cnt = {0, 0, 0, 0};
@@ -43,7 +89,7 @@ __global__ void __launch_bounds__(128, 5) render_kernel(DevScene s, RenderLaunch
       trace<TYPE, COUNT, MODE, STACK>(s, pos, 0.0f, dir, 1e9f, hit, cnt);
       if (si == 0) first = hit;
       if (L.rgba || L.rgba8) {
-        const float4 c = shade(s, hit, dir);
+        const float4 c = PHONG ? shade_phong<TYPE, MODE, STACK>(s, hit, pos, dir) : shade(s, hit, pos, dir);
         acc.x += c.x; acc.y += c.y; acc.z += c.z; acc.w += c.w;
       }
     }

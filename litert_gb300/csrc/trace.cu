@@ -27,7 +27,7 @@ __global__ void __launch_bounds__(128, 5) render_refill_kernel(DevScene s, Rende
   Counters cnt = {0, 0, 0, 0};
   bool live = false, exhausted = false;
   uint32_t pix_out = 0;
-  float3 dir = f3(0, 0, 1), rp = f3(0, 0, 0), rd = f3(0, 0, 1), inv = f3(0, 0, 0);
+  float3 dir = f3(0, 0, 1), org = f3(0, 0, 0), rp = f3(0, 0, 0), rd = f3(0, 0, 1), inv = f3(0, 0, 0);
   Hit hit;
   hit.t = 1e9f; hit.prim = kMiss; hit.geom = kMiss; hit.c0 = 1.0f; hit.c1 = hit.c2 = hit.c3 = 0.0f;
   uint2 st[STACK];
@@ -53,6 +53,7 @@ __global__ void __launch_bounds__(128, 5) render_refill_kernel(DevScene s, Rende
           if (x < V.width && y < V.height) {
             float3 pos;
             eye_ray(x, y, V.width, V.height, 0.5f, 0.5f, V.proj_inv, V.wv_inv, pos, dir);
+            org = pos;
             pix_out = V.pix_offset + y * V.width + x;
             hit.t = 1e9f; hit.prim = kMiss; hit.geom = kMiss; hit.c0 = 1.0f; hit.c1 = hit.c2 = hit.c3 = 0.0f;
             live = true;
@@ -106,7 +107,7 @@ __global__ void __launch_bounds__(128, 5) render_refill_kernel(DevScene s, Rende
         reinterpret_cast<float4 *>(L.hits16)[pix_out] = *reinterpret_cast<const float4 *>(&o);
       }
       if (L.rgba || L.rgba8) {
-        const float4 c = shade(s, hit, dir);
+        const float4 c = shade(s, hit, org, dir);
         if (L.rgba) L.rgba[pix_out] = c;
         if (L.rgba8) L.rgba8[pix_out] = encode_rgba8(c);
       }
@@ -202,8 +203,43 @@ static cudaError_t launch_refill(const DevScene &s, const RenderLaunch &L, int n
   return launch_refill_m<LRT_TYPE_SDF_SBS, LRT_INTERSECT_NEWTON, kStackSize>(s, L, num_sms, st, refill);
 }
 
+// PHONG / PHONG_NO_TEX with colour outputs: kernels whose shading traces shadow rays
+// (variant 0, no counters: the counters of these renders stay zero)
+template <int TYPE, int MODE>
+static cudaError_t launch_phong_m(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st) {
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &per_sm, dev::render_kernel<TYPE, false, MODE, kStackSize, 0, true>, 128, 0);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  uint32_t blocks = uint32_t(num_sms) * uint32_t(per_sm);
+  const uint32_t max_blocks = (L.total_tiles + 3) / 4;
+  if (blocks > max_blocks) blocks = max_blocks;
+  if (blocks == 0) blocks = 1;
+  dev::render_kernel<TYPE, false, MODE, kStackSize, 0, true><<<blocks, 128, 0, st>>>(s, L);
+  return cudaGetLastError();
+}
+
+template <int TYPE>
+static cudaError_t launch_phong_t(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st) {
+  if (TYPE == LRT_TYPE_MESH_TRIANGLE) return launch_phong_m<TYPE, -1>(s, L, num_sms, st);
+  switch (s.preset.sdf_node_intersect) {
+    case LRT_INTERSECT_NEWTON: return launch_phong_m<TYPE, LRT_INTERSECT_NEWTON>(s, L, num_sms, st);
+    case LRT_INTERSECT_ST: return launch_phong_m<TYPE, LRT_INTERSECT_ST>(s, L, num_sms, st);
+    default: return launch_phong_m<TYPE, -1>(s, L, num_sms, st);
+  }
+}
+
 cudaError_t launch_render(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st, bool count,
                           const Tuning &tu) {
+  const uint32_t rm = s.preset.render_mode;
+  if ((rm == LRT_RENDER_MODE_PHONG || rm == LRT_RENDER_MODE_PHONG_NO_TEX) && (L.rgba || L.rgba8)) {
+    switch (s.type) {
+      case LRT_TYPE_MESH_TRIANGLE: return launch_phong_t<LRT_TYPE_MESH_TRIANGLE>(s, L, num_sms, st);
+      case LRT_TYPE_SDF_SVS: return launch_phong_t<LRT_TYPE_SDF_SVS>(s, L, num_sms, st);
+      default: return launch_phong_t<LRT_TYPE_SDF_SBS>(s, L, num_sms, st);
+    }
+  }
   const bool sbs = s.type == LRT_TYPE_SDF_SBS || s.type == LRT_TYPE_SDF_SBS_COL;
   if (sbs && tu.variant == 1) return launch_render_packet(s, L, num_sms, st, count, tu);
   const bool refill_ok = (s.type == LRT_TYPE_MESH_TRIANGLE ||

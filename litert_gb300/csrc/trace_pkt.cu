@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(256) render_packet_kernel(DevScene s, RenderLa
       }
       if (si == 0) first = hit;
       if (L.rgba || L.rgba8) {
-        const float4 c = shade(s, hit, dir);
+        const float4 c = shade(s, hit, pos, dir);
         acc.x += c.x; acc.y += c.y; acc.z += c.z; acc.w += c.w;
       }
     }

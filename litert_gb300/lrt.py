@@ -20,6 +20,9 @@ LIB_PATH = os.path.join(_HERE, "_build", "liblrt_gb300.so")
 TYPE_MESH_TRIANGLE, TYPE_SDF_SVS, TYPE_SDF_SBS, TYPE_SDF_SBS_COL = 0, 5, 6, 11
 RENDER_MODE_MASK, RENDER_MODE_LAMBERT_NO_TEX, RENDER_MODE_DEPTH, RENDER_MODE_LINEAR_DEPTH = 0, 1, 2, 3
 RENDER_MODE_INVERSE_LINEAR_DEPTH, RENDER_MODE_NORMAL, RENDER_MODE_LAMBERT = 4, 8, 17
+RENDER_MODE_PRIMITIVE, RENDER_MODE_TYPE, RENDER_MODE_GEOM, RENDER_MODE_BARYCENTRIC = 5, 6, 7, 9
+RENDER_MODE_ST_ITERATIONS, RENDER_MODE_PHONG_NO_TEX, RENDER_MODE_DIFFUSE = 10, 12, 16
+RENDER_MODE_PHONG, RENDER_MODE_HSV_DEPTH = 18, 19
 INTERSECT_ST, INTERSECT_ANALYTIC, INTERSECT_NEWTON, INTERSECT_BBOX, INTERSECT_IT = 0, 1, 2, 3, 4
 SBS_LAYOUT_DX = 1 << 24
 SBS_LAYOUT_ID32F_IRGB32F = 4 << 24

@@ -483,6 +483,19 @@ static f3 decode_normal(float ex, float ey) {
   return normalize3(v);
 }
 
+/* MultiRenderer::m_palette (Renderer/eye_ray.h:235-241) and decode_RGBA8
+ * (Renderer/eye_ray.cpp:15-19) */
+static const uint32_t orc_palette[20] = {0xffe6194bu, 0xff3cb44bu, 0xffffe119u, 0xff0082c8u, 0xfff58231u,
+                                         0xff911eb4u, 0xff46f0f0u, 0xfff032e6u, 0xffd2f53cu, 0xfffabebeu,
+                                         0xff008080u, 0xffe6beffu, 0xffaa6e28u, 0xfffffac8u, 0xff800000u,
+                                         0xffaaffc3u, 0xff808000u, 0xffffd8b1u, 0xff000080u, 0xff808080u};
+static void decode_rgba8(uint32_t c, float out[4]) {
+  out[0] = (float)(c & 0xFF) * (1.0f / 255.0f);
+  out[1] = (float)((c >> 8) & 0xFF) * (1.0f / 255.0f);
+  out[2] = (float)((c >> 16) & 0xFF) * (1.0f / 255.0f);
+  out[3] = (float)((c >> 24) & 0xFF) * (1.0f / 255.0f);
+}
+
 void orc_shade(const orc_scene *s, const orc_hit *hit, const float pos_near[4], const float dir_far[4], float out[4]) {
   /* kernel_RayTrace, Renderer/eye_ray.cpp:162-489 */
   if (hit->prim_id == 0xFFFFFFFFu) { out[0] = 0; out[1] = 0; out[2] = 0; out[3] = 1; return; }
@@ -509,7 +522,9 @@ void orc_shade(const orc_scene *s, const orc_hit *hit, const float pos_near[4], 
     case 4: { float d = 1 - ((z - z_near) / (z_far - z_near)); out[0] = out[1] = out[2] = d; out[3] = 1; } break;
     case 8: out[0] = fabsf(norm.x); out[1] = fabsf(norm.y); out[2] = fabsf(norm.z); out[3] = 1; break;
     case 1: case 17: {
-      f3 color = mk3(1, 1, 1);
+      /* LAMBERT_NO_TEX: white; LAMBERT: the brick colour, else the default textured
+       * material's constant texel (0, 1, 1) (Renderer/eye_ray_host.cpp:30-33) */
+      f3 color = s->preset.render_mode == 17 ? mk3(0, 1, 1) : mk3(1, 1, 1);
       if (s->preset.render_mode == 17 && type == ORC_TYPE_SDF_SBS_COL) {
         color.x = roundf(hit->coords[0]) / 255.0f;
         color.y = hit->coords[0] - floorf(hit->coords[0]);
@@ -523,6 +538,81 @@ void orc_shade(const orc_scene *s, const orc_hit *hit, const float pos_near[4], 
       fc = add3(fc, scl3(q, mul3(mk3(lc, lc, lc), color)));
       fc = add3(fc, mul3(mk3(0.25f, 0.25f, 0.25f), color));
       out[0] = fc.x; out[1] = fc.y; out[2] = fc.z; out[3] = 1;
+    } break;
+    case 5: decode_rgba8(orc_palette[hit->prim_id % 20u], out); break;               /* PRIMITIVE */
+    case 6: decode_rgba8(orc_palette[type % 20u], out); break;                        /* TYPE */
+    case 7: decode_rgba8(orc_palette[(hit->geom_id & 0x00FFFFFFu) % 20u], out); break; /* GEOM */
+    case 9:                                                                           /* BARYCENTRIC */
+      out[0] = hit->coords[0]; out[1] = hit->coords[1]; out[2] = 1 - hit->coords[0] - hit->coords[1]; out[3] = 1;
+      break;
+    case 10: {                                                                        /* ST_ITERATIONS */
+      const uint32_t it = hit->prim_id;
+      if (it == 0) { out[0] = out[1] = out[2] = 0.5f; out[3] = 1; }
+      else if (it <= 64) {
+        float q = (float)it / 64; q = q < 0.0f ? 0.0f : (q > 1.0f ? 1.0f : q);
+        const float r = 1 - q;
+        out[0] = q * 0.0f + r * 0.0f; out[1] = q * 0.0f + r * 1.0f; out[2] = q * 1.0f + r * 0.0f; out[3] = q * 1.0f + r * 1.0f;
+      } else {
+        float q = (float)(it - 64) / (256 - 64); q = q < 0.0f ? 0.0f : (q > 1.0f ? 1.0f : q);
+        const float r = 1 - q;
+        out[0] = q * 1.0f + r * 0.0f; out[1] = q * 0.0f + r * 0.0f; out[2] = q * 0.0f + r * 1.0f; out[3] = q * 1.0f + r * 1.0f;
+      }
+    } break;
+    case 16: {                                                                        /* DIFFUSE */
+      f3 color = mk3(0, 1, 1);
+      if (type == ORC_TYPE_SDF_SBS_COL) {
+        color.x = roundf(hit->coords[0]) / 255.0f;
+        color.y = hit->coords[0] - floorf(hit->coords[0]);
+        color.z = roundf(hit->coords[1]) / 255.0f;
+      }
+      out[0] = color.x; out[1] = color.y; out[2] = color.z; out[3] = 1;
+    } break;
+    case 12: case 18: {                                                               /* PHONG(_NO_TEX) */
+      /* Renderer/eye_ray.cpp:420-483 with the default lights: the direct light adds an
+       * unshadowed Lambert term and a shadowed Phong term; the shadow ray is a nearest-hit
+       * query from just before the hit point towards the light */
+      const float Kd = 0.25f, Ks = 0.25f, BIAS = 1e-6f;
+      f3 color = s->preset.render_mode == 12 ? mk3(1, 1, 1) : mk3(0, 1, 1);
+      if (s->preset.render_mode == 18 && type == ORC_TYPE_SDF_SBS_COL) {
+        color.x = roundf(hit->coords[0]) / 255.0f;
+        color.y = hit->coords[0] - floorf(hit->coords[0]);
+        color.z = roundf(hit->coords[1]) / 255.0f;
+      }
+      f3 fc = mk3(0, 0, 0);
+      {
+        const f3 ld = normalize3(mk3(1, 1, 1));
+        const float l = 2.0f / 3.0f;
+        const f3 lc = mk3(l, l, l);
+        const f3 surf = add3(mk3(pos_near[0], pos_near[1], pos_near[2]), scl3(hit->t - BIAS, rd));
+        const float q = fmaxf_(0.0f, dot3(norm, ld));
+        fc = add3(fc, scl3(q, mul3(lc, color)));
+        const float sp[4] = {surf.x, surf.y, surf.z, pos_near[3]}, sd[4] = {ld.x, ld.y, ld.z, dir_far[3]};
+        orc_counters cc;
+        memset(&cc, 0, sizeof(cc));
+        const orc_hit sh = orc_ray_query_nearest(s, sp, sd, &cc);
+        const float shade = (sh.prim_id == 0xFFFFFFFFu) ? 1.0f : 0.0f;
+        const f3 refl = add3(scl3(-1.0f, ld), scl3(2.0f * dot3(norm, ld), norm));
+        const float inner = Kd * fmaxf_(0.0f, dot3(norm, ld)) + Ks * powf(fmaxf_(0.0f, dot3(norm, refl)), 32.0f);
+        fc = add3(fc, mul3(scl3(inner, scl3(shade, lc)), color));
+      }
+      fc = add3(fc, mul3(mk3(0.25f, 0.25f, 0.25f), color));   /* ambient */
+      out[0] = fc.x; out[1] = fc.y; out[2] = fc.z; out[3] = 1;
+    } break;
+    case 19: {                                                                        /* HSV_DEPTH */
+      const float iz = pos_near[2] + z * dir_far[2];
+      float zt = (iz + 1.f) * 2.f;
+      zt = zt - (float)(int)zt;
+      if (zt < 0.f) zt = 1.f + zt;
+      float c[4] = {1.0f, 1.0f, 1.0f, 1.0f};
+      const float vmin = (1.f - 1.f) * 1.0f;
+      float hi;
+      const float a = (1.0f - vmin) * modff(zt * 6.f, &hi);
+      uint32_t h = (uint32_t)hi;
+      h = h <= 5u ? h : 5u;
+      c[(2u + (h >> 1)) % 3u] = vmin;
+      if ((h & 1u) != 0u) c[h >> 1] = 1.0f - a;
+      else c[(1u + (h >> 1)) % 3u] = vmin + a;
+      out[0] = c[0]; out[1] = c[1]; out[2] = c[2]; out[3] = 1.f;
     } break;
     default: out[0] = 1; out[1] = 0; out[2] = 1; out[3] = 1; break;
   }
