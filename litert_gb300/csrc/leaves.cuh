@@ -327,6 +327,41 @@ __device__ void brick_intersect(const DevScene &s, float3 ray_pos, float3 ray_di
                clampf(floorf(255.0f * col.z + 0.5f), 0.0f, 255.0f));
       hit.c0 = col.x + col.y / 256.0f;
       hit.c1 = col.z;
+    } else if (layout == LRT_SBS_LAYOUT_DX_UV16 || layout == LRT_SBS_LAYOUT_DX_RGB8) {
+      // 8 words after the packed distances: 16-bit texture coordinates or RGB8 colours
+      const float3 pos = add(ray_pos, scl(hit.t, ray_dir));
+      const float3 dp = scr(sub(pos, bmin), 0.5f * sz);
+      const uint32_t vpi = 4u / h.bytes_per_value;
+      const uint32_t *tw = s.values + nd.z + (v_size * v_size * v_size + vpi - 1) / vpi;
+      const float w[8] = {(1 - dp.x) * (1 - dp.y) * (1 - dp.z), (1 - dp.x) * (1 - dp.y) * (dp.z),
+                          (1 - dp.x) * (dp.y) * (1 - dp.z),     (1 - dp.x) * (dp.y) * (dp.z),
+                          (dp.x) * (1 - dp.y) * (1 - dp.z),     (dp.x) * (1 - dp.y) * (dp.z),
+                          (dp.x) * (dp.y) * (1 - dp.z),         (dp.x) * (dp.y) * (dp.z)};
+      if (layout == LRT_SBS_LAYOUT_DX_UV16) {
+        float u = 0, v = 0;
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+          const uint32_t q = __ldg(&tw[i]);
+          const float ui = w[i] * (1.5259022e-5f * float(q >> 16));
+          const float vi = w[i] * (1.5259022e-5f * float(q & 0xFFFFu));
+          u = i == 0 ? ui : u + ui;
+          v = i == 0 ? vi : v + vi;
+        }
+        hit.c0 = u;
+        hit.c1 = v;
+      } else {
+        float3 col = f3(0, 0, 0);
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+          const uint32_t q = __ldg(&tw[i]);
+          const float3 ci = f3(w[i] * float(q & 0xFFu), w[i] * float((q >> 8) & 0xFFu), w[i] * float((q >> 16) & 0xFFu));
+          col = i == 0 ? ci : add(col, ci);
+        }
+        col = f3(clampf(floorf(col.x + 0.5f), 0.0f, 255.0f), clampf(floorf(col.y + 0.5f), 0.0f, 255.0f),
+                 clampf(floorf(col.z + 0.5f), 0.0f, 255.0f));
+        hit.c0 = col.x + col.y / 256.0f;
+        hit.c1 = col.z;
+      }
     }
   }
 }

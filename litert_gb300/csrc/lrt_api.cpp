@@ -177,15 +177,18 @@ extern "C" lrt_status lrt_add_sbs(lrt_ctx *ctx, const lrt_sbs_header *hdr, const
   const uint32_t layout = hdr->aux_data & 0xFF000000u;
   uint32_t type;
   const bool indexed = layout == LRT_SBS_LAYOUT_ID32F_IRGB32F || layout == LRT_SBS_LAYOUT_ID32F_IRGB32F_IN;
+  const bool extra8 = layout == LRT_SBS_LAYOUT_DX_UV16 || layout == LRT_SBS_LAYOUT_DX_RGB8;   // + 8 words per brick
+  // AddGeom_SdfSBS, BVH/BVH2Common_host.cpp:572-592
   if (layout == LRT_SBS_LAYOUT_UNDEFINED || layout == LRT_SBS_LAYOUT_DX) type = LRT_TYPE_SDF_SBS;
-  else if (indexed) type = LRT_TYPE_SDF_SBS_COL;
-  else return fail(ctx, LRT_ERR_UNSUPPORTED, "lrt_add_sbs: only DX and ID32F_IRGB32F(_IN) layouts are supported");
+  else if (layout == LRT_SBS_LAYOUT_DX_UV16) type = LRT_TYPE_SDF_SBS_TEX;
+  else if (indexed || layout == LRT_SBS_LAYOUT_DX_RGB8) type = LRT_TYPE_SDF_SBS_COL;
+  else return fail(ctx, LRT_ERR_UNSUPPORTED, "lrt_add_sbs: unknown node layout");
   if (indexed && (!values_f || n_values_f == 0))
     return fail(ctx, LRT_ERR_INVALID, "lrt_add_sbs: indexed layout needs values_f");
   // every brick's data must lie inside `values`
   const uint32_t v_size = hdr->brick_size + 2 * hdr->brick_pad + 1, v3 = v_size * v_size * v_size;
   const uint32_t words = indexed ? v3 + 8 + (layout == LRT_SBS_LAYOUT_ID32F_IRGB32F_IN ? 27 : 0)
-                                 : (v3 + 4 / hdr->bytes_per_value - 1) / (4 / hdr->bytes_per_value);
+                                 : (v3 + 4 / hdr->bytes_per_value - 1) / (4 / hdr->bytes_per_value) + (extra8 ? 8 : 0);
   for (uint32_t i = 0; i < n_nodes; i++) {
     if (uint64_t(nodes[i].data_offset) + words > n_values)
       return fail(ctx, LRT_ERR_INVALID, "lrt_add_sbs: brick data_offset out of range");
@@ -376,7 +379,9 @@ extern "C" lrt_status lrt_commit_scene(lrt_ctx *ctx) {
     const uint32_t v_size = hd.brick_size + 2 * hd.brick_pad + 1, v3 = v_size * v_size * v_size;
     const bool indexed = layout == LRT_SBS_LAYOUT_ID32F_IRGB32F || layout == LRT_SBS_LAYOUT_ID32F_IRGB32F_IN;
     const uint32_t vpi = 4 / hd.bytes_per_value;
-    const uint32_t words = indexed ? v3 + 8 + (layout == LRT_SBS_LAYOUT_ID32F_IRGB32F_IN ? 27 : 0) : (v3 + vpi - 1) / vpi;
+    const bool extra8 = layout == LRT_SBS_LAYOUT_DX_UV16 || layout == LRT_SBS_LAYOUT_DX_RGB8;
+    const uint32_t words = indexed ? v3 + 8 + (layout == LRT_SBS_LAYOUT_ID32F_IRGB32F_IN ? 27 : 0)
+                                   : (v3 + vpi - 1) / vpi + (extra8 ? 8 : 0);
     const uint32_t stride = (words + 3u) & ~3u;
     const size_t nb = g.sbs.nodes.size();
     if (uint64_t(nb) * stride >= (1ull << 32))
@@ -927,7 +932,8 @@ extern "C" lrt_status lrt_autotune(lrt_ctx *ctx, const lrt_view *views, uint32_t
   uint64_t pix = 0;
   for (uint32_t v = 0; v < n_views; v++) pix += uint64_t(views[v].width) * views[v].height;
   LRT_CUDA(ctx, ctx->d_out_hits.ensure(size_t(pix)));
-  const bool sbs = ctx->dev.type == LRT_TYPE_SDF_SBS || ctx->dev.type == LRT_TYPE_SDF_SBS_COL;
+  const bool sbs = ctx->dev.type == LRT_TYPE_SDF_SBS || ctx->dev.type == LRT_TYPE_SDF_SBS_COL ||
+                   ctx->dev.type == LRT_TYPE_SDF_SBS_TEX;
   std::vector<lrt_tuning_choice> cand;
   for (int tw : {4, 8, 16})
     for (int stk : {32, 64}) cand.push_back(lrt_tuning_choice{0, 4, 0, tw, stk, 0.0f});

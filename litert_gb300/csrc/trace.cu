@@ -240,7 +240,7 @@ cudaError_t launch_render(const DevScene &s, const RenderLaunch &L, int num_sms,
       default: return launch_phong_t<LRT_TYPE_SDF_SBS>(s, L, num_sms, st);
     }
   }
-  const bool sbs = s.type == LRT_TYPE_SDF_SBS || s.type == LRT_TYPE_SDF_SBS_COL;
+  const bool sbs = s.type == LRT_TYPE_SDF_SBS || s.type == LRT_TYPE_SDF_SBS_COL || s.type == LRT_TYPE_SDF_SBS_TEX;
   if (sbs && tu.variant == 1) return launch_render_packet(s, L, num_sms, st, count, tu);
   const bool refill_ok = (s.type == LRT_TYPE_MESH_TRIANGLE ||
                           (s.type == LRT_TYPE_SDF_SBS && s.preset.sdf_node_intersect == LRT_INTERSECT_NEWTON)) &&

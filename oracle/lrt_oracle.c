@@ -292,6 +292,37 @@ static void brick_intersect(const orc_scene *s, uint32_t type, f3 ray_pos, f3 ra
                 clampf_(floorf(255.0f * col.z + 0.5f), 0.0f, 255.0f));
       hit->coords[0] = col.x + col.y / 256.0f;
       hit->coords[1] = col.z;
+    } else if (layout == (2u << 24) || layout == (3u << 24)) {   /* DX_UV16 / DX_RGB8: 8 words after the distances */
+      f3 pos = add3(ray_pos, scl3(hit->t, ray_dir));
+      f3 dp = mul3s(sub3(pos, brick_min), 0.5f * sz);
+      const uint32_t vpi = 4 / h->bytes_per_value;
+      const uint32_t *tw = s->sbs_values + nd->data_offset + (v_size * v_size * v_size + vpi - 1) / vpi;
+      float w[8] = {(1 - dp.x) * (1 - dp.y) * (1 - dp.z), (1 - dp.x) * (1 - dp.y) * (dp.z),
+                    (1 - dp.x) * (dp.y) * (1 - dp.z), (1 - dp.x) * (dp.y) * (dp.z),
+                    (dp.x) * (1 - dp.y) * (1 - dp.z), (dp.x) * (1 - dp.y) * (dp.z),
+                    (dp.x) * (dp.y) * (1 - dp.z), (dp.x) * (dp.y) * (dp.z)};
+      if (layout == (2u << 24)) {   /* texture coordinates, 16 bits each */
+        float u = 0, v = 0;
+        for (int i = 0; i < 8; i++) {
+          const float ui = w[i] * (1.5259022e-5f * (float)(tw[i] >> 16));
+          const float vi = w[i] * (1.5259022e-5f * (float)(tw[i] & 0xFFFF));
+          u = i == 0 ? ui : u + ui;
+          v = i == 0 ? vi : v + vi;
+        }
+        hit->coords[0] = u;
+        hit->coords[1] = v;
+      } else {                      /* RGB8 colours */
+        f3 col = mk3(0, 0, 0);
+        for (int i = 0; i < 8; i++) {
+          f3 ci = mk3(w[i] * (float)((tw[i] >> 0) & 0xFF), w[i] * (float)((tw[i] >> 8) & 0xFF),
+                      w[i] * (float)((tw[i] >> 16) & 0xFF));
+          col = i == 0 ? ci : add3(col, ci);
+        }
+        col = mk3(clampf_(floorf(col.x + 0.5f), 0.0f, 255.0f), clampf_(floorf(col.y + 0.5f), 0.0f, 255.0f),
+                  clampf_(floorf(col.z + 0.5f), 0.0f, 255.0f));
+        hit->coords[0] = col.x + col.y / 256.0f;
+        hit->coords[1] = col.z;
+      }
     }
   }
 }

@@ -169,7 +169,8 @@ class Scene:
             nodes = np.ascontiguousarray(nodes, np.uint32)
             values = np.ascontiguousarray(values, np.uint32)
             layout = hdr.aux_data & 0xFF000000
-            s.type = 11 if layout in (4 << 24, 5 << 24) else 6
+            # AddGeom_SdfSBS, BVH/BVH2Common_host.cpp:572-592
+            s.type = 11 if layout in (3 << 24, 4 << 24, 5 << 24) else (10 if layout == 2 << 24 else 6)
             s.sbs_hdr = SbsHeader(hdr.brick_size, hdr.brick_pad, hdr.bytes_per_value, hdr.aux_data)
             s.sbs_nodes, s.n_sbs_nodes, s.sbs_values = _p(nodes), nodes.shape[0], _p(values)
             self.keep += [nodes, values]

@@ -80,9 +80,11 @@ void *ref_make_sbs(const SdfSBSHeader *hdr, const SdfSBSNode *nodes, uint32_t n_
   RefScene *s = new RefScene();
   BVHRT &rt = s->rt;
   const uint32_t layout = hdr->aux_data & SDF_SBS_NODE_LAYOUT_MASK;
-  uint32_t type = TYPE_SDF_SBS;
-  if (layout == SDF_SBS_NODE_LAYOUT_DX_RGB8 || layout == SDF_SBS_NODE_LAYOUT_ID32F_IRGB32F ||
-      layout == SDF_SBS_NODE_LAYOUT_ID32F_IRGB32F_IN)
+  uint32_t type = TYPE_SDF_SBS;   // BVH/BVH2Common_host.cpp:572-592
+  if (layout == SDF_SBS_NODE_LAYOUT_DX_UV16)
+    type = TYPE_SDF_SBS_TEX;
+  else if (layout == SDF_SBS_NODE_LAYOUT_DX_RGB8 || layout == SDF_SBS_NODE_LAYOUT_ID32F_IRGB32F ||
+           layout == SDF_SBS_NODE_LAYOUT_ID32F_IRGB32F_IN)
     type = TYPE_SDF_SBS_COL;
   place_object<GeomDataSdfBrick>(rt);
   rt.m_SdfSBSRoots.assign(1, 0u);
