@@ -229,6 +229,84 @@ struct SharedLoader {
   }
 };
 
+// eval_dist_trilinear_diff, BVH/BVH2Common.cpp:656-686 (a + -(b) is a - b exactly)
+__device__ __forceinline__ float3 tri_diff(const float v[8], float3 dp) {
+  const float dx = -(1 - dp.y) * (1 - dp.z) * v[0] - (1 - dp.y) * (dp.z) * v[1] - (dp.y) * (1 - dp.z) * v[2] -
+                   (dp.y) * (dp.z) * v[3] + (1 - dp.y) * (1 - dp.z) * v[4] + (1 - dp.y) * (dp.z) * v[5] +
+                   (dp.y) * (1 - dp.z) * v[6] + (dp.y) * (dp.z) * v[7];
+  const float dy = -(1 - dp.x) * (1 - dp.z) * v[0] - (1 - dp.x) * (dp.z) * v[1] + (1 - dp.x) * (1 - dp.z) * v[2] +
+                   (1 - dp.x) * (dp.z) * v[3] - (dp.x) * (1 - dp.z) * v[4] - (dp.x) * (dp.z) * v[5] +
+                   (dp.x) * (1 - dp.z) * v[6] + (dp.x) * (dp.z) * v[7];
+  const float dz = -(1 - dp.x) * (1 - dp.y) * v[0] + (1 - dp.x) * (1 - dp.y) * v[1] - (1 - dp.x) * (dp.y) * v[2] +
+                   (1 - dp.x) * (dp.y) * v[3] - (dp.x) * (1 - dp.y) * v[4] + (dp.x) * (1 - dp.y) * v[5] -
+                   (dp.x) * (dp.y) * v[6] + (dp.x) * (dp.y) * v[7];
+  return f3(dx, dy, dz);
+}
+
+// NORMAL_MODE_SDF_SMOOTHED on the ID32F_IRGB32F_IN layout (BVH/BVH2Common.cpp:838-905):
+// the normals of the 8 voxels around the hit, read across brick borders through the
+// brick's 27-neighbour table, blended with weights that switch over +-beta of the
+// voxel centre.  Compiled only into the kernels instantiated for this layout and mode.
+__device__ __forceinline__ void smooth_normal(const DevScene &s, uint32_t node, float3 vox, float3 start_q, float fnear,
+                                           float d, float3 ray_dir, uint32_t v_size, Hit &hit) {
+  const lrt_sbs_header &h = s.sbs_hdr;
+  const float beta = 0.5f;
+  const float3 dp = add(start_q, scl((hit.t - fnear) / d, ray_dir));
+  auto step01 = [](float e0, float e1, float x) { return clampf((x - e0) / (e1 - e0), 0.0f, 1.0f); };
+  const float3 nmq = f3(dp.x < 0.5f ? step01(-beta, beta, dp.x) : step01(-beta, beta, dp.x - 1.0f),
+                        dp.y < 0.5f ? step01(-beta, beta, dp.y) : step01(-beta, beta, dp.y - 1.0f),
+                        dp.z < 0.5f ? step01(-beta, beta, dp.z) : step01(-beta, beta, dp.z - 1.0f));
+  const int v0x = int(dp.x < 0.5f ? vox.x - 1 : vox.x), v0y = int(dp.y < 0.5f ? vox.y - 1 : vox.y),
+            v0z = int(dp.z < 0.5f ? vox.z - 1 : vox.z);
+  const int bsz = int(h.brick_size);
+  const float bsf = float(h.brick_size);
+  const uint32_t v3 = v_size * v_size * v_size;
+  float3 sm = f3(0, 0, 0);
+#pragma unroll 1
+  for (int i = 0; i < 8; i++) {
+    const int vx = v0x + ((i & 4) >> 2), vy = v0y + ((i & 2) >> 1), vz = v0z + (i & 1);
+    const int bx = vx >= 0 ? (vx < bsz ? 0 : 1) : -1, by = vy >= 0 ? (vy < bsz ? 0 : 1) : -1,
+              bz = vz >= 0 ? (vz < bsz ? 0 : 1) : -1;
+    const uint32_t nb = uint32_t(9 * (bx + 1) + 3 * (by + 1) + (bz + 1));
+    const float3 dvox = sub(f3(float(vx), float(vy), float(vz)), vox);
+    uint32_t nid;
+    float3 nvp;
+    if (nb == 9 + 3 + 1) {
+      nid = node;
+      nvp = f3(float(vx), float(vy), float(vz));
+    } else {
+      nid = __ldg(&s.values[__ldg(&s.bricks[node].data_offset) + v3 + 8 + nb]);
+      nvp = sub(f3(float(vx), float(vy), float(vz)), f3(bsf * float(bx), bsf * float(by), bsf * float(bz)));
+    }
+    float3 n = f3(0, 0, 0);
+    if (nid != 0x80000000u) {
+      const uint32_t off = __ldg(&s.bricks[nid].data_offset);
+      float vals[8];
+#pragma unroll
+      for (int c = 0; c < 8; c++) {
+        const uint32_t vId = (uint32_t(nvp.x) + ((c & 4) >> 2) + h.brick_pad) * v_size * v_size +
+                             (uint32_t(nvp.y) + ((c & 2) >> 1) + h.brick_pad) * v_size +
+                             (uint32_t(nvp.z) + (c & 1) + h.brick_pad);
+        vals[c] = __ldg(&s.values_f[__ldg(&s.values[off + vId])]);
+      }
+      n = normalize(tri_diff(vals, sub(dp, dvox)));
+    }
+    const float w = i == 0 ? (1 - nmq.x) * (1 - nmq.y) * (1 - nmq.z)
+                  : i == 1 ? (1 - nmq.x) * (1 - nmq.y) * (nmq.z)
+                  : i == 2 ? (1 - nmq.x) * (nmq.y) * (1 - nmq.z)
+                  : i == 3 ? (1 - nmq.x) * (nmq.y) * (nmq.z)
+                  : i == 4 ? (nmq.x) * (1 - nmq.y) * (1 - nmq.z)
+                  : i == 5 ? (nmq.x) * (1 - nmq.y) * (nmq.z)
+                  : i == 6 ? (nmq.x) * (nmq.y) * (1 - nmq.z)
+                           : (nmq.x) * (nmq.y) * (nmq.z);
+    const float3 wn = scl(w, n);
+    sm = i == 0 ? wn : add(sm, wn);
+  }
+  const float2 en = encode_normal(normalize(sm));
+  hit.c2 = en.x;
+  hit.c3 = en.y;
+}
+
 // OctreeBrickIntersect, BVH/BVH2Common.cpp:764-984 (trilinear, colour for indexed
 // layouts).  The voxel walk is the reference's: the voxel is recomputed from the
 // current entry distance, the distance advances past the voxel's exit plane by
@@ -243,7 +321,7 @@ struct SharedLoader {
 // start_t (default: no effect) lets the walk begin at a later distance; the
 // proposal path passes the entry of a voxel it has shown every earlier voxel of
 // the segment to be empty, where the reference's walk would run no finder.
-template <bool COUNT, bool STAGED, int MODE = -1>
+template <bool COUNT, bool STAGED, int MODE = -1, bool SMOOTH = false>
 __device__ void brick_intersect(const DevScene &s, float3 ray_pos, float3 ray_dir, float3 inv, float tNear,
                                 uint32_t brick, Hit &hit, Counters &cnt, const float *staged = nullptr,
                                 float start_t = -3.4e38f) {
@@ -301,6 +379,8 @@ __device__ void brick_intersect(const DevScene &s, float3 ray_pos, float3 ray_di
           const float3 start_q = scr(sub(start_pos, min_pos), scale);
           const float qFar = (fnf.y - fnf.x) * scale;
           local_surface<COUNT, MODE>(pr, s, type, ray_dir, values, brick, d, 0.0f, qFar, fnf, start_q, hit, cnt);
+          if (SMOOTH && hit.t != old_t)
+            smooth_normal(s, brick, vp, start_q, fnf.x, d, ray_dir, v_size, hit);
         }
       }
     }

@@ -119,6 +119,14 @@ struct Tuning {
 
 cudaError_t launch_render(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st, bool count,
                           const Tuning &tu);
+// NORMAL_MODE_SDF_SMOOTHED applies: the neighbour layout and a mode that needs normals
+// (BVH/BVH2Common.cpp:838-840; trilinear interpolation is the only one supported)
+inline bool smoothed_normals(const DevScene &s) {
+  const uint32_t m = s.preset.render_mode;
+  return s.type != LRT_TYPE_MESH_TRIANGLE && s.type != LRT_TYPE_SDF_SVS &&
+         s.sbs_hdr.aux_data == LRT_SBS_LAYOUT_ID32F_IRGB32F_IN && s.preset.normal_mode == 2 &&
+         (m == 1 || m == 8 || m == 12 || m == 17 || m == 18);
+}
 // The variant-0 render kernel compiled with FP contraction (trace_fused.cu).
 cudaError_t launch_render_fused(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st,
                                 const Tuning &tu);

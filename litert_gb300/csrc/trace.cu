@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(128, 5) render_refill_kernel(DevScene s, Rende
 }
 
 // Batched RayQuery_NearestHit: one thread per ray, full CRT_Hit output.
-template <int TYPE>
+template <int TYPE, bool SMOOTH = false>
 __global__ void __launch_bounds__(128) query_kernel(DevScene s, const float4 *pos_near, const float4 *dir_far,
                                                    uint32_t n, lrt_hit *out) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(128) query_kernel(DevScene s, const float4 *po
   const float4 p = pos_near[i], d = dir_far[i];
   Counters cnt = {0, 0, 0, 0};
   Hit hit;
-  trace<TYPE, false>(s, f3(p.x, p.y, p.z), p.w, f3(d.x, d.y, d.z), d.w, hit, cnt);
+  trace<TYPE, false, -1, kStackSize, SMOOTH>(s, f3(p.x, p.y, p.z), p.w, f3(d.x, d.y, d.z), d.w, hit, cnt);
   lrt_hit o;
   o.t = hit.t;
   o.primId = (hit.prim != kMiss && (hit.geom >> 24) == LRT_TYPE_MESH_TRIANGLE) ? s.prim_indices[hit.prim] : hit.prim;
@@ -203,37 +203,48 @@ static cudaError_t launch_refill(const DevScene &s, const RenderLaunch &L, int n
   return launch_refill_m<LRT_TYPE_SDF_SBS, LRT_INTERSECT_NEWTON, kStackSize>(s, L, num_sms, st, refill);
 }
 
-// PHONG / PHONG_NO_TEX with colour outputs: kernels whose shading traces shadow rays
-// (variant 0, no counters: the counters of these renders stay zero)
-template <int TYPE, int MODE>
-static cudaError_t launch_phong_m(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st) {
+// Kernels with the less common features, variant 0 and no counters (the counters of
+// these renders stay zero): PHONG / PHONG_NO_TEX with colour outputs, whose shading
+// traces shadow rays, and smoothed SDF normals (NORMAL_MODE_SDF_SMOOTHED on the
+// neighbour layout).  Separate instantiations keep both out of the other kernels.
+template <int TYPE, int MODE, bool PHONG, bool SMOOTH>
+static cudaError_t launch_feature_m(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st) {
   int per_sm = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      &per_sm, dev::render_kernel<TYPE, false, MODE, kStackSize, 0, true>, 128, 0);
+      &per_sm, dev::render_kernel<TYPE, false, MODE, kStackSize, 0, PHONG, SMOOTH>, 128, 0);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   uint32_t blocks = uint32_t(num_sms) * uint32_t(per_sm);
   const uint32_t max_blocks = (L.total_tiles + 3) / 4;
   if (blocks > max_blocks) blocks = max_blocks;
   if (blocks == 0) blocks = 1;
-  dev::render_kernel<TYPE, false, MODE, kStackSize, 0, true><<<blocks, 128, 0, st>>>(s, L);
+  dev::render_kernel<TYPE, false, MODE, kStackSize, 0, PHONG, SMOOTH><<<blocks, 128, 0, st>>>(s, L);
   return cudaGetLastError();
+}
+
+template <int TYPE, bool PHONG, bool SMOOTH>
+static cudaError_t launch_feature_t(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st) {
+  if (TYPE == LRT_TYPE_MESH_TRIANGLE) return launch_feature_m<TYPE, -1, PHONG, false>(s, L, num_sms, st);
+  switch (s.preset.sdf_node_intersect) {
+    case LRT_INTERSECT_NEWTON: return launch_feature_m<TYPE, LRT_INTERSECT_NEWTON, PHONG, SMOOTH>(s, L, num_sms, st);
+    case LRT_INTERSECT_ST: return launch_feature_m<TYPE, LRT_INTERSECT_ST, PHONG, SMOOTH>(s, L, num_sms, st);
+    default: return launch_feature_m<TYPE, -1, PHONG, SMOOTH>(s, L, num_sms, st);
+  }
 }
 
 template <int TYPE>
 static cudaError_t launch_phong_t(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st) {
-  if (TYPE == LRT_TYPE_MESH_TRIANGLE) return launch_phong_m<TYPE, -1>(s, L, num_sms, st);
-  switch (s.preset.sdf_node_intersect) {
-    case LRT_INTERSECT_NEWTON: return launch_phong_m<TYPE, LRT_INTERSECT_NEWTON>(s, L, num_sms, st);
-    case LRT_INTERSECT_ST: return launch_phong_m<TYPE, LRT_INTERSECT_ST>(s, L, num_sms, st);
-    default: return launch_phong_m<TYPE, -1>(s, L, num_sms, st);
-  }
+  return launch_feature_t<TYPE, true, false>(s, L, num_sms, st);
 }
 
 cudaError_t launch_render(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st, bool count,
                           const Tuning &tu) {
   const uint32_t rm = s.preset.render_mode;
-  if ((rm == LRT_RENDER_MODE_PHONG || rm == LRT_RENDER_MODE_PHONG_NO_TEX) && (L.rgba || L.rgba8)) {
+  const bool phong = (rm == LRT_RENDER_MODE_PHONG || rm == LRT_RENDER_MODE_PHONG_NO_TEX) && (L.rgba || L.rgba8);
+  if (smoothed_normals(s))   // SBS only (the neighbour layout)
+    return phong ? launch_feature_t<LRT_TYPE_SDF_SBS, true, true>(s, L, num_sms, st)
+                 : launch_feature_t<LRT_TYPE_SDF_SBS, false, true>(s, L, num_sms, st);
+  if (phong) {
     switch (s.type) {
       case LRT_TYPE_MESH_TRIANGLE: return launch_phong_t<LRT_TYPE_MESH_TRIANGLE>(s, L, num_sms, st);
       case LRT_TYPE_SDF_SVS: return launch_phong_t<LRT_TYPE_SDF_SVS>(s, L, num_sms, st);
@@ -263,7 +274,12 @@ cudaError_t launch_query(const DevScene &s, const float4 *pos_near, const float4
   switch (s.type) {
     case LRT_TYPE_MESH_TRIANGLE: dev::query_kernel<LRT_TYPE_MESH_TRIANGLE><<<blocks, 128, 0, st>>>(s, pos_near, dir_far, n, out); break;
     case LRT_TYPE_SDF_SVS: dev::query_kernel<LRT_TYPE_SDF_SVS><<<blocks, 128, 0, st>>>(s, pos_near, dir_far, n, out); break;
-    default: dev::query_kernel<LRT_TYPE_SDF_SBS><<<blocks, 128, 0, st>>>(s, pos_near, dir_far, n, out); break;
+    default:
+      if (smoothed_normals(s))
+        dev::query_kernel<LRT_TYPE_SDF_SBS, true><<<blocks, 128, 0, st>>>(s, pos_near, dir_far, n, out);
+      else
+        dev::query_kernel<LRT_TYPE_SDF_SBS><<<blocks, 128, 0, st>>>(s, pos_near, dir_far, n, out);
+      break;
   }
   return cudaGetLastError();
 }

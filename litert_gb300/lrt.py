@@ -374,10 +374,13 @@ class Scene:
     def commit_scene(self):
         self._chk(lib().lrt_commit_scene(self._ctx))
 
-    def set_preset(self, render_mode=None, sdf_node_intersect=None, spp=None, representation_mode=None):
+    def set_preset(self, render_mode=None, sdf_node_intersect=None, spp=None, representation_mode=None,
+                   normal_mode=None):
         p = self.preset
         if render_mode is not None:
             p.render_mode = render_mode
+        if normal_mode is not None:
+            p.normal_mode = normal_mode
         if sdf_node_intersect is not None:
             p.sdf_node_intersect = sdf_node_intersect
         if spp is not None:

@@ -227,6 +227,72 @@ static float load_distance_values(const orc_scene *s, uint32_t node_id, f3 voxel
   return vmin;
 }
 
+/* eval_dist_trilinear_diff (BVH/BVH2Common.cpp:656-686); a + -(b) is a - b exactly */
+static f3 tri_diff(const float v[8], f3 dp) {
+  float dx = -(1 - dp.y) * (1 - dp.z) * v[0] - (1 - dp.y) * (dp.z) * v[1] - (dp.y) * (1 - dp.z) * v[2] -
+             (dp.y) * (dp.z) * v[3] + (1 - dp.y) * (1 - dp.z) * v[4] + (1 - dp.y) * (dp.z) * v[5] +
+             (dp.y) * (1 - dp.z) * v[6] + (dp.y) * (dp.z) * v[7];
+  float dy = -(1 - dp.x) * (1 - dp.z) * v[0] - (1 - dp.x) * (dp.z) * v[1] + (1 - dp.x) * (1 - dp.z) * v[2] +
+             (1 - dp.x) * (dp.z) * v[3] - (dp.x) * (1 - dp.z) * v[4] - (dp.x) * (dp.z) * v[5] +
+             (dp.x) * (1 - dp.z) * v[6] + (dp.x) * (dp.z) * v[7];
+  float dz = -(1 - dp.x) * (1 - dp.y) * v[0] + (1 - dp.x) * (1 - dp.y) * v[1] - (1 - dp.x) * (dp.y) * v[2] +
+             (1 - dp.x) * (dp.y) * v[3] - (dp.x) * (1 - dp.y) * v[4] + (dp.x) * (1 - dp.y) * v[5] -
+             (dp.x) * (dp.y) * v[6] + (dp.x) * (dp.y) * v[7];
+  return mk3(dx, dy, dz);
+}
+/* step (BVH/BVH2Common.cpp:689-694) */
+static float step01(float e0, float e1, float x) { return clampf_((x - e0) / (e1 - e0), 0.0f, 1.0f); }
+
+/* NORMAL_MODE_SDF_SMOOTHED for the ID32F_IRGB32F_IN layout (BVH/BVH2Common.cpp:838-905):
+ * the normals of the 8 voxels around the hit, read across brick borders through the
+ * 27-neighbour table, blended with weights that switch over +-beta of the voxel centre */
+static void smooth_normal(const orc_scene *s, uint32_t node_id, f3 voxelPos, f3 start_q, float fnear, float d,
+                          f3 ray_dir, uint32_t v_size, float sz_inv, orc_hit *hit) {
+  const orc_sbs_header *h = &s->sbs_hdr;
+  const float beta = 0.5f;
+  const f3 dp = add3(start_q, scl3((hit->t - fnear) / d, ray_dir));
+  f3 normals[8];
+  float values_n[8];
+  for (int i = 0; i < 8; i++) normals[i] = mk3(0, 0, 0);
+  const f3 nmq = mk3(dp.x < 0.5f ? step01(-beta, beta, dp.x) : step01(-beta, beta, dp.x - 1.0f),
+                     dp.y < 0.5f ? step01(-beta, beta, dp.y) : step01(-beta, beta, dp.y - 1.0f),
+                     dp.z < 0.5f ? step01(-beta, beta, dp.z) : step01(-beta, beta, dp.z - 1.0f));
+  const int v0[3] = {(int)(dp.x < 0.5f ? voxelPos.x - 1 : voxelPos.x), (int)(dp.y < 0.5f ? voxelPos.y - 1 : voxelPos.y),
+                     (int)(dp.z < 0.5f ? voxelPos.z - 1 : voxelPos.z)};
+  const int bsz = (int)h->brick_size;
+  for (int i = 0; i < 8; i++) {
+    const int vi[3] = {v0[0] + ((i & 4) >> 2), v0[1] + ((i & 2) >> 1), v0[2] + (i & 1)};
+    int bp[3];
+    for (int a = 0; a < 3; a++) bp[a] = vi[a] >= 0 ? (vi[a] < bsz ? 0 : 1) : -1;
+    const uint32_t nb = (uint32_t)(9 * (bp[0] + 1) + 3 * (bp[1] + 1) + (bp[2] + 1));
+    const f3 dvox = sub3(mk3((float)vi[0], (float)vi[1], (float)vi[2]), voxelPos);
+    uint32_t nid;
+    f3 nvp;
+    if (nb == 9 + 3 + 1) {
+      nid = node_id;
+      nvp = mk3((float)vi[0], (float)vi[1], (float)vi[2]);
+    } else {
+      const uint32_t v_off = s->sbs_nodes[node_id].data_offset;
+      nid = s->sbs_values[v_off + v_size * v_size * v_size + 8 + nb];
+      const float b = (float)h->brick_size;
+      nvp = sub3(mk3((float)vi[0], (float)vi[1], (float)vi[2]), mk3(b * (float)bp[0], b * (float)bp[1], b * (float)bp[2]));
+    }
+    if (nid != 0x80000000u) {
+      load_distance_values(s, nid, nvp, v_size, sz_inv, values_n);
+      normals[i] = normalize3(tri_diff(values_n, sub3(dp, dvox)));
+    }
+  }
+  const float w[8] = {(1 - nmq.x) * (1 - nmq.y) * (1 - nmq.z), (1 - nmq.x) * (1 - nmq.y) * (nmq.z),
+                      (1 - nmq.x) * (nmq.y) * (1 - nmq.z),     (1 - nmq.x) * (nmq.y) * (nmq.z),
+                      (nmq.x) * (1 - nmq.y) * (1 - nmq.z),     (nmq.x) * (1 - nmq.y) * (nmq.z),
+                      (nmq.x) * (nmq.y) * (1 - nmq.z),         (nmq.x) * (nmq.y) * (nmq.z)};
+  f3 sm = scl3(w[0], normals[0]);
+  for (int i = 1; i < 8; i++) sm = add3(sm, scl3(w[i], normals[i]));
+  const f2 en = encode_normal(normalize3(sm));
+  hit->coords[2] = en.x;
+  hit->coords[3] = en.y;
+}
+
 /* OctreeBrickIntersect, BVH/BVH2Common.cpp:764-984 (trilinear; COL-layout colour) */
 static void brick_intersect(const orc_scene *s, uint32_t type, f3 ray_pos, f3 ray_dir, float tNear,
                             uint32_t geom_id, uint32_t bvh_node_id, orc_hit *hit, orc_counters *cnt) {
@@ -268,6 +334,8 @@ static void brick_intersect(const orc_scene *s, uint32_t type, f3 ray_pos, f3 ra
       f3 start_q = mul3s(sub3(start_pos, min_pos), scale);
       float qFar = (fnf.y - fnf.x) * scale;
       local_surface_intersection(s, type, ray_dir, geom_id, values, prim_id, d, 0.0f, qFar, fnf, start_q, hit, cnt);
+      if (h->aux_data == (5u << 24) && s->preset.normal_mode == 2 && need_normal(&s->preset) && hit->t != old_t)
+        smooth_normal(s, node_id, voxelPos, start_q, fnf.x, d, ray_dir, v_size, sz_inv, hit);
     }
     bnf.x += fmaxf_(0.0f, fnf.y - bnf.x) + 1e-6f;
   }

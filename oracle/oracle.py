@@ -156,7 +156,7 @@ class Scene:
     """One geometry + identity-or-given instance, as the oracle sees it."""
 
     def __init__(self, kind, *, sbs=None, svs=None, mesh=None, pairs=None, matrix=None, closest_hit=True,
-                 render_mode=1, intersect=2, representation_mode=1, spp=1):
+                 render_mode=1, intersect=2, representation_mode=1, spp=1, normal_mode=0):
         self.keep = []
         s = OrcScene()
         m = np.eye(4, dtype=np.float32) if matrix is None else np.asarray(matrix, np.float32)
@@ -221,7 +221,7 @@ class Scene:
         tc = corners @ m.T
         s.inst_bmin[:] = tc[:, :3].min(0).tolist()
         s.inst_bmax[:] = tc[:, :3].max(0).tolist()
-        s.preset = Preset(render_mode, intersect, 0, 0, 0, representation_mode, spp)
+        s.preset = Preset(render_mode, intersect, normal_mode, 0, 0, representation_mode, spp)
         s.closest_hit = 1 if closest_hit else 0
         self.s = s
 

@@ -1,5 +1,6 @@
 """Generate tests/golden/ref_layouts.npz from the reference's own code: the
-coloured (DX_RGB8) and textured (DX_UV16) brick layouts.
+coloured (DX_RGB8) and textured (DX_UV16) brick layouts, and smoothed normals
+(NORMAL_MODE_SDF_SMOOTHED) on the neighbour layout (ID32F_IRGB32F_IN).
 
 Runs where the reference tree is present (oracle/_ref, the reference's
 BVH/BVH2Common.cpp compiled in place).  Each case is a DX brick set of the
@@ -66,6 +67,15 @@ def main():
         oh = orc.SbsHeader(*[int(x) for x in hdr])
         out[name + "_hdr"], out[name + "_nodes"], out[name + "_values"], out[name + "_pairs"] = hdr, n, v, pairs
         out[name + "_hits"] = ref.RefScene("sbs", (oh, n, v), pairs, (8, 2, 0, 0, 0, 1, 1)).query(P, D)
+    # NORMAL_MODE_SDF_SMOOTHED on the neighbour layout (ID32F_IRGB32F_IN, create_grid_sbs)
+    from litert_gb300 import dr
+    hd, n, v, vf = dr.grid_sbs(6, 4, lrt.Sdf(**scenes.union_params()), None)
+    pairs, _, _ = lrt.build_bvh2(orc.node_boxes(n), 1)
+    oh = orc.SbsHeader(hd.brick_size, hd.brick_pad, hd.bytes_per_value, hd.aux_data)
+    out["smooth_hdr"] = np.array([hd.brick_size, hd.brick_pad, hd.bytes_per_value, hd.aux_data], np.uint32)
+    out["smooth_nodes"], out["smooth_values"], out["smooth_values_f"], out["smooth_pairs"] = n, v, vf, pairs
+    for nm in (0, 2):
+        out[f"smooth_hits_n{nm}"] = ref.RefScene("sbs", (oh, n, v, vf), pairs, (8, 2, nm, 0, 0, 1, 1)).query(P, D)
     np.savez_compressed(OUT, **out)
     print("wrote", OUT, {k: v.shape for k, v in out.items() if k.endswith("_hits")})
 

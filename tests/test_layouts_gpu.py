@@ -59,3 +59,33 @@ def test_layout_images(name, mode):
     assert (out["hits"]["primId"] != lrt.MISS).sum() > 1000
     assert np.array_equal(canon_bits(out["rgba"]), canon_bits(col))
     assert len(np.unique(out["rgba"][:, 0])) > 20   # the colours / coordinates vary
+
+
+@pytest.mark.parametrize("normal_mode", [0, 2])
+def test_smoothed_normals(normal_mode):
+    """NORMAL_MODE_SDF_SMOOTHED on the neighbour layout: query records and NORMAL /
+    LAMBERT images equal the oracle's (which equals the reference's) bit for bit."""
+    g = np.load(GOLD)
+    r = np.load(RAYS)
+    hdr = [int(x) for x in g["smooth_hdr"]]
+    h, oh = lrt.SbsHeader(*hdr), orc.SbsHeader(*hdr)
+    n, v, vf = g["smooth_nodes"], g["smooth_values"], g["smooth_values_f"]
+    s = lrt.Scene(0)
+    s.add_instance(s.add_sbs(h, n, v, vf))
+    s.commit_scene()
+    s.set_preset(render_mode=lrt.RENDER_MODE_NORMAL, sdf_node_intersect=lrt.INTERSECT_NEWTON, normal_mode=normal_mode)
+    got = s.query_rays(r["rays_pos"], r["rays_dir"])
+    osc = orc.Scene("sbs", sbs=(oh, n, v, vf), intersect=2, render_mode=8, normal_mode=normal_mode)
+    want = osc.query_rays(r["rays_pos"], r["rays_dir"])
+    hit = want["primId"] != lrt.MISS
+    assert hit.sum() > 300
+    assert np.array_equal(got["primId"], want["primId"]) and np.array_equal(got["t"], want["t"])
+    assert np.array_equal(canon_bits(got["coords"][hit]), canon_bits(want["coords"][hit]))
+    for mode in (lrt.RENDER_MODE_NORMAL, lrt.RENDER_MODE_LAMBERT):
+        s.set_preset(render_mode=mode, sdf_node_intersect=lrt.INTERSECT_NEWTON, normal_mode=normal_mode)
+        view = scenes.union_views(n_views=1, lo=128, hi=160, cam_seed=5)[0]
+        out = s.render_host([view], hits=True, rgba=True)
+        _, col, _ = oracle_render(orc.Scene("sbs", sbs=(oh, n, v, vf), intersect=2, render_mode=mode,
+                                            normal_mode=normal_mode), view)
+        assert np.array_equal(canon_bits(out["rgba"]), canon_bits(col))
+    s.close()
