@@ -307,6 +307,70 @@ __device__ __forceinline__ void smooth_normal(const DevScene &s, uint32_t node, 
   hit.c3 = en.y;
 }
 
+// The hit's colour or texture coordinates for the layouts that carry them
+// (OctreeBrickIntersect, BVH/BVH2Common.cpp:912-982), out of line: the plain DX
+// layout never reaches it, so the leaf loop of every kernel stays small.
+static __device__ __noinline__ void brick_colour(const DevScene &s, uint4 nd, float3 bmin, float sz, uint32_t v_size,
+                                                 float3 ray_pos, float3 ray_dir, Hit &hit) {
+  const lrt_sbs_header &h = s.sbs_hdr;
+  const uint32_t layout = h.aux_data & 0xFF000000u;
+  if (layout == LRT_SBS_LAYOUT_ID32F_IRGB32F || layout == LRT_SBS_LAYOUT_ID32F_IRGB32F_IN) {
+    const float3 pos = add(ray_pos, scl(hit.t, ray_dir));
+    const float3 dp = scr(sub(pos, bmin), 0.5f * sz);
+    const uint32_t t_off = nd.z + v_size * v_size * v_size;
+    const float w[8] = {(1 - dp.x) * (1 - dp.y) * (1 - dp.z), (1 - dp.x) * (1 - dp.y) * (dp.z),
+                        (1 - dp.x) * (dp.y) * (1 - dp.z),     (1 - dp.x) * (dp.y) * (dp.z),
+                        (dp.x) * (1 - dp.y) * (1 - dp.z),     (dp.x) * (1 - dp.y) * (dp.z),
+                        (dp.x) * (dp.y) * (1 - dp.z),         (dp.x) * (dp.y) * (dp.z)};
+    float3 col = f3(0, 0, 0);
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      const float *c = &s.values_f[__ldg(&s.values[t_off + i])];
+      const float3 ci = f3(w[i] * c[0], w[i] * c[1], w[i] * c[2]);
+      col = i == 0 ? ci : add(col, ci);
+    }
+    col = f3(clampf(floorf(255.0f * col.x + 0.5f), 0.0f, 255.0f), clampf(floorf(255.0f * col.y + 0.5f), 0.0f, 255.0f),
+             clampf(floorf(255.0f * col.z + 0.5f), 0.0f, 255.0f));
+    hit.c0 = col.x + col.y / 256.0f;
+    hit.c1 = col.z;
+  } else if (layout == LRT_SBS_LAYOUT_DX_UV16 || layout == LRT_SBS_LAYOUT_DX_RGB8) {
+    // 8 words after the packed distances: 16-bit texture coordinates or RGB8 colours
+    const float3 pos = add(ray_pos, scl(hit.t, ray_dir));
+    const float3 dp = scr(sub(pos, bmin), 0.5f * sz);
+    const uint32_t vpi = 4u / h.bytes_per_value;
+    const uint32_t *tw = s.values + nd.z + (v_size * v_size * v_size + vpi - 1) / vpi;
+    const float w[8] = {(1 - dp.x) * (1 - dp.y) * (1 - dp.z), (1 - dp.x) * (1 - dp.y) * (dp.z),
+                        (1 - dp.x) * (dp.y) * (1 - dp.z),     (1 - dp.x) * (dp.y) * (dp.z),
+                        (dp.x) * (1 - dp.y) * (1 - dp.z),     (dp.x) * (1 - dp.y) * (dp.z),
+                        (dp.x) * (dp.y) * (1 - dp.z),         (dp.x) * (dp.y) * (dp.z)};
+    if (layout == LRT_SBS_LAYOUT_DX_UV16) {
+      float u = 0, v = 0;
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        const uint32_t q = __ldg(&tw[i]);
+        const float ui = w[i] * (1.5259022e-5f * float(q >> 16));
+        const float vi = w[i] * (1.5259022e-5f * float(q & 0xFFFFu));
+        u = i == 0 ? ui : u + ui;
+        v = i == 0 ? vi : v + vi;
+      }
+      hit.c0 = u;
+      hit.c1 = v;
+    } else {
+      float3 col = f3(0, 0, 0);
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        const uint32_t q = __ldg(&tw[i]);
+        const float3 ci = f3(w[i] * float(q & 0xFFu), w[i] * float((q >> 8) & 0xFFu), w[i] * float((q >> 16) & 0xFFu));
+        col = i == 0 ? ci : add(col, ci);
+      }
+      col = f3(clampf(floorf(col.x + 0.5f), 0.0f, 255.0f), clampf(floorf(col.y + 0.5f), 0.0f, 255.0f),
+               clampf(floorf(col.z + 0.5f), 0.0f, 255.0f));
+      hit.c0 = col.x + col.y / 256.0f;
+      hit.c1 = col.z;
+    }
+  }
+}
+
 // OctreeBrickIntersect, BVH/BVH2Common.cpp:764-984 (trilinear, colour for indexed
 // layouts).  The voxel walk is the reference's: the voxel is recomputed from the
 // current entry distance, the distance advances past the voxel's exit plane by
@@ -321,7 +385,12 @@ __device__ __forceinline__ void smooth_normal(const DevScene &s, uint32_t node, 
 // start_t (default: no effect) lets the walk begin at a later distance; the
 // proposal path passes the entry of a voxel it has shown every earlier voxel of
 // the segment to be empty, where the reference's walk would run no finder.
-template <bool COUNT, bool STAGED, int MODE = -1, bool SMOOTH = false>
+// FEAT: bit 0 smoothed SDF normals (NORMAL_MODE_SDF_SMOOTHED), bit 1 the hit
+// colour computed in this brick as the reference does (kept for ST_ITERATIONS,
+// where primId no longer names the brick; otherwise hit_colour computes it once
+// for the final hit, which gives the same values: the last brick that reports a
+// hit is the hit brick).
+template <bool COUNT, bool STAGED, int MODE = -1, int FEAT = 0>
 __device__ void brick_intersect(const DevScene &s, float3 ray_pos, float3 ray_dir, float3 inv, float tNear,
                                 uint32_t brick, Hit &hit, Counters &cnt, const float *staged = nullptr,
                                 float start_t = -3.4e38f) {
@@ -379,71 +448,31 @@ __device__ void brick_intersect(const DevScene &s, float3 ray_pos, float3 ray_di
           const float3 start_q = scr(sub(start_pos, min_pos), scale);
           const float qFar = (fnf.y - fnf.x) * scale;
           local_surface<COUNT, MODE>(pr, s, type, ray_dir, values, brick, d, 0.0f, qFar, fnf, start_q, hit, cnt);
-          if (SMOOTH && hit.t != old_t)
+          if ((FEAT & 1) && hit.t != old_t)
             smooth_normal(s, brick, vp, start_q, fnf.x, d, ray_dir, v_size, hit);
         }
       }
     }
     bnf.x += fmx(0.0f, exit_t - bnf.x) + 1e-6f;
   }
-  if (hit.t < old_t) {
-    const uint32_t layout = h.aux_data & 0xFF000000u;
-    if (layout == LRT_SBS_LAYOUT_ID32F_IRGB32F || layout == LRT_SBS_LAYOUT_ID32F_IRGB32F_IN) {
-      const float3 pos = add(ray_pos, scl(hit.t, ray_dir));
-      const float3 dp = scr(sub(pos, bmin), 0.5f * sz);
-      const uint32_t t_off = nd.z + v_size * v_size * v_size;
-      const float w[8] = {(1 - dp.x) * (1 - dp.y) * (1 - dp.z), (1 - dp.x) * (1 - dp.y) * (dp.z),
-                          (1 - dp.x) * (dp.y) * (1 - dp.z),     (1 - dp.x) * (dp.y) * (dp.z),
-                          (dp.x) * (1 - dp.y) * (1 - dp.z),     (dp.x) * (1 - dp.y) * (dp.z),
-                          (dp.x) * (dp.y) * (1 - dp.z),         (dp.x) * (dp.y) * (dp.z)};
-      float3 col = f3(0, 0, 0);
-#pragma unroll
-      for (int i = 0; i < 8; i++) {
-        const float *c = &s.values_f[__ldg(&s.values[t_off + i])];
-        const float3 ci = f3(w[i] * c[0], w[i] * c[1], w[i] * c[2]);
-        col = i == 0 ? ci : add(col, ci);
-      }
-      col = f3(clampf(floorf(255.0f * col.x + 0.5f), 0.0f, 255.0f), clampf(floorf(255.0f * col.y + 0.5f), 0.0f, 255.0f),
-               clampf(floorf(255.0f * col.z + 0.5f), 0.0f, 255.0f));
-      hit.c0 = col.x + col.y / 256.0f;
-      hit.c1 = col.z;
-    } else if (layout == LRT_SBS_LAYOUT_DX_UV16 || layout == LRT_SBS_LAYOUT_DX_RGB8) {
-      // 8 words after the packed distances: 16-bit texture coordinates or RGB8 colours
-      const float3 pos = add(ray_pos, scl(hit.t, ray_dir));
-      const float3 dp = scr(sub(pos, bmin), 0.5f * sz);
-      const uint32_t vpi = 4u / h.bytes_per_value;
-      const uint32_t *tw = s.values + nd.z + (v_size * v_size * v_size + vpi - 1) / vpi;
-      const float w[8] = {(1 - dp.x) * (1 - dp.y) * (1 - dp.z), (1 - dp.x) * (1 - dp.y) * (dp.z),
-                          (1 - dp.x) * (dp.y) * (1 - dp.z),     (1 - dp.x) * (dp.y) * (dp.z),
-                          (dp.x) * (1 - dp.y) * (1 - dp.z),     (dp.x) * (1 - dp.y) * (dp.z),
-                          (dp.x) * (dp.y) * (1 - dp.z),         (dp.x) * (dp.y) * (dp.z)};
-      if (layout == LRT_SBS_LAYOUT_DX_UV16) {
-        float u = 0, v = 0;
-#pragma unroll
-        for (int i = 0; i < 8; i++) {
-          const uint32_t q = __ldg(&tw[i]);
-          const float ui = w[i] * (1.5259022e-5f * float(q >> 16));
-          const float vi = w[i] * (1.5259022e-5f * float(q & 0xFFFFu));
-          u = i == 0 ? ui : u + ui;
-          v = i == 0 ? vi : v + vi;
-        }
-        hit.c0 = u;
-        hit.c1 = v;
-      } else {
-        float3 col = f3(0, 0, 0);
-#pragma unroll
-        for (int i = 0; i < 8; i++) {
-          const uint32_t q = __ldg(&tw[i]);
-          const float3 ci = f3(w[i] * float(q & 0xFFu), w[i] * float((q >> 8) & 0xFFu), w[i] * float((q >> 16) & 0xFFu));
-          col = i == 0 ? ci : add(col, ci);
-        }
-        col = f3(clampf(floorf(col.x + 0.5f), 0.0f, 255.0f), clampf(floorf(col.y + 0.5f), 0.0f, 255.0f),
-                 clampf(floorf(col.z + 0.5f), 0.0f, 255.0f));
-        hit.c0 = col.x + col.y / 256.0f;
-        hit.c1 = col.z;
-      }
-    }
-  }
+  if ((FEAT & 2) && hit.t < old_t && (h.aux_data & 0xFF000000u) != LRT_SBS_LAYOUT_DX &&
+      (h.aux_data & 0xFF000000u) != LRT_SBS_LAYOUT_UNDEFINED)
+    brick_colour(s, nd, bmin, sz, v_size, ray_pos, ray_dir, hit);
+}
+
+// The colour / texture coordinates of the final hit of an SBS with a layout that
+// carries them, from its brick (hit.prim) -- once per ray instead of in the leaf
+// loop.  pos / dir: the world-space ray, taken to object space as the traversal does.
+__device__ __forceinline__ void hit_colour(const DevScene &s, float3 pos, float3 dir, Hit &hit) {
+  const uint32_t layout = s.sbs_hdr.aux_data & 0xFF000000u;
+  if (hit.prim == kMiss || layout == LRT_SBS_LAYOUT_DX || layout == LRT_SBS_LAYOUT_UNDEFINED) return;
+  const float3 ray_pos = matmul4x3(s.inst_inv, pos), ray_dir = matmul3x3(s.inst_inv, dir);
+  const lrt_sbs_header &h = s.sbs_hdr;
+  const uint4 nd = __ldg(reinterpret_cast<const uint4 *>(s.bricks) + hit.prim);
+  const float px = float(nd.x >> 16), py = float(nd.x & 0x0000FFFF);
+  const float pz = float(nd.y >> 16), sz = float(nd.y & 0x0000FFFF);
+  const float3 bmin = add(f3(-1, -1, -1), scl(2.0f / sz, f3(px, py, pz)));
+  brick_colour(s, nd, bmin, sz, h.brick_size + 2 * h.brick_pad + 1, ray_pos, ray_dir, hit);
 }
 
 // SVS voxel: OctreeNodeIntersect + RayNodeIntersection, BVH/BVH2Common.cpp:126-153, 633-655
@@ -532,48 +561,11 @@ __device__ __forceinline__ float4 decode_rgba8(uint32_t c) {
                      float((c >> 16) & 0xFF) * (1.0f / 255.0f), float((c >> 24) & 0xFF) * (1.0f / 255.0f));
 }
 
-// kernel_RayTrace, Renderer/eye_ray.cpp:162-489 (the geometry-based modes without
-// shadow rays; lights are the reference's defaults, Renderer/eye_ray_host.cpp:40;
-// geometry without brick colours takes the default material's texel (0, 1, 1))
-__device__ inline float4 shade(const DevScene &s, const Hit &hit, float3 pos, float3 dir) {
-  if (hit.prim == kMiss) return make_float4(0, 0, 0, 1);
-  const float z = hit.t, z_near = 0.1f, z_far = 10;
-  const uint32_t type = hit.geom >> 24;
-  float3 norm;
-  if (type == LRT_TYPE_MESH_TRIANGLE) {
-    const float4 a = s.tri_verts[3 * hit.prim + 0], b = s.tri_verts[3 * hit.prim + 1], c = s.tri_verts[3 * hit.prim + 2];
-    const float3 e1 = f3(b.x - a.x, b.y - a.y, b.z - a.z), e2 = f3(c.x - a.x, c.y - a.y, c.z - a.z);
-    norm = normalize(matmul4x3(s.inst_inv_t, cross(e1, e2)));
-  } else {
-    norm = decode_normal(hit.c2, hit.c3);
-  }
-  const float ns = signf(dot(scl(-1.0f, dir), norm));
-  norm = scl(ns, norm);
+// The less common shading modes of kernel_RayTrace, out of line so that the
+// render kernels carry only a call for them.
+static __device__ __noinline__ float4 shade_extra(const DevScene &s, const Hit &hit, uint32_t type, float z,
+                                                  float3 pos, float3 dir) {
   switch (s.preset.render_mode) {
-    case LRT_RENDER_MODE_MASK: return make_float4(1, 1, 1, 1);
-    case LRT_RENDER_MODE_DEPTH: { const float d = (1 / z - 1 / z_near) / (1 / z_far - 1 / z_near); return make_float4(d, d, d, 1); }
-    case LRT_RENDER_MODE_LINEAR_DEPTH: { const float d = ((z - z_near) / (z_far - z_near)); return make_float4(d, d, d, 1); }
-    case LRT_RENDER_MODE_INVERSE_LINEAR_DEPTH: { const float d = 1 - ((z - z_near) / (z_far - z_near)); return make_float4(d, d, d, 1); }
-    case LRT_RENDER_MODE_NORMAL: return make_float4(fabsf(norm.x), fabsf(norm.y), fabsf(norm.z), 1);
-    case LRT_RENDER_MODE_LAMBERT_NO_TEX:
-    case LRT_RENDER_MODE_LAMBERT: {
-      // LAMBERT_NO_TEX: white; LAMBERT: the brick colour, else the default textured
-      // material's constant texel (0, 1, 1) (Renderer/eye_ray_host.cpp:30-33)
-      float3 color = s.preset.render_mode == LRT_RENDER_MODE_LAMBERT ? f3(0, 1, 1) : f3(1, 1, 1);
-      if (s.preset.render_mode == LRT_RENDER_MODE_LAMBERT && type == LRT_TYPE_SDF_SBS_COL) {
-        color.x = roundf(hit.c0) / 255.0f;
-        color.y = hit.c0 - floorf(hit.c0);
-        color.z = roundf(hit.c1) / 255.0f;
-      }
-      // default lights, Renderer/eye_ray_host.cpp:40
-      const float3 ldir = normalize(f3(1, 1, 1));
-      const float lc = 2.0f / 3.0f;
-      float3 fc = f3(0, 0, 0);
-      const float q = mx(0.0f, dot(norm, ldir));
-      fc = add(fc, scl(q, mul(f3(lc, lc, lc), color)));
-      fc = add(fc, mul(f3(0.25f, 0.25f, 0.25f), color));
-      return make_float4(fc.x, fc.y, fc.z, 1);
-    }
     case LRT_RENDER_MODE_PRIMITIVE:   // the reference's primId: original triangle ids
       return decode_rgba8(palette_color(type == LRT_TYPE_MESH_TRIANGLE ? s.prim_indices[hit.prim] : hit.prim));
     case LRT_RENDER_MODE_TYPE: return decode_rgba8(palette_color(type));
@@ -617,6 +609,56 @@ __device__ inline float4 shade(const DevScene &s, const Hit &hit, float3 pos, fl
       const float b = i1 == 2 ? v1 : (i0 == 2 ? vmin : 1.0f);
       return make_float4(r, g, b, 1.f);
     }
+    default: return make_float4(1, 0, 1, 1);
+  }
+}
+
+// kernel_RayTrace, Renderer/eye_ray.cpp:162-489 (the geometry-based modes without
+// shadow rays; lights are the reference's defaults, Renderer/eye_ray_host.cpp:40;
+// geometry without brick colours takes the default material's texel (0, 1, 1))
+static __device__ __noinline__ float4 shade(const DevScene &s, const Hit &hit, float3 pos, float3 dir) {
+  if (hit.prim == kMiss) return make_float4(0, 0, 0, 1);
+  const float z = hit.t, z_near = 0.1f, z_far = 10;
+  const uint32_t type = hit.geom >> 24;
+  float3 norm;
+  if (type == LRT_TYPE_MESH_TRIANGLE) {
+    const float4 a = s.tri_verts[3 * hit.prim + 0], b = s.tri_verts[3 * hit.prim + 1], c = s.tri_verts[3 * hit.prim + 2];
+    const float3 e1 = f3(b.x - a.x, b.y - a.y, b.z - a.z), e2 = f3(c.x - a.x, c.y - a.y, c.z - a.z);
+    norm = normalize(matmul4x3(s.inst_inv_t, cross(e1, e2)));
+  } else {
+    norm = decode_normal(hit.c2, hit.c3);
+  }
+  const float ns = signf(dot(scl(-1.0f, dir), norm));
+  norm = scl(ns, norm);
+  switch (s.preset.render_mode) {
+    case LRT_RENDER_MODE_MASK: return make_float4(1, 1, 1, 1);
+    case LRT_RENDER_MODE_DEPTH: { const float d = (1 / z - 1 / z_near) / (1 / z_far - 1 / z_near); return make_float4(d, d, d, 1); }
+    case LRT_RENDER_MODE_LINEAR_DEPTH: { const float d = ((z - z_near) / (z_far - z_near)); return make_float4(d, d, d, 1); }
+    case LRT_RENDER_MODE_INVERSE_LINEAR_DEPTH: { const float d = 1 - ((z - z_near) / (z_far - z_near)); return make_float4(d, d, d, 1); }
+    case LRT_RENDER_MODE_NORMAL: return make_float4(fabsf(norm.x), fabsf(norm.y), fabsf(norm.z), 1);
+    case LRT_RENDER_MODE_LAMBERT_NO_TEX:
+    case LRT_RENDER_MODE_LAMBERT: {
+      // LAMBERT_NO_TEX: white; LAMBERT: the brick colour, else the default textured
+      // material's constant texel (0, 1, 1) (Renderer/eye_ray_host.cpp:30-33)
+      float3 color = s.preset.render_mode == LRT_RENDER_MODE_LAMBERT ? f3(0, 1, 1) : f3(1, 1, 1);
+      if (s.preset.render_mode == LRT_RENDER_MODE_LAMBERT && type == LRT_TYPE_SDF_SBS_COL) {
+        color.x = roundf(hit.c0) / 255.0f;
+        color.y = hit.c0 - floorf(hit.c0);
+        color.z = roundf(hit.c1) / 255.0f;
+      }
+      // default lights, Renderer/eye_ray_host.cpp:40
+      const float3 ldir = normalize(f3(1, 1, 1));
+      const float lc = 2.0f / 3.0f;
+      float3 fc = f3(0, 0, 0);
+      const float q = mx(0.0f, dot(norm, ldir));
+      fc = add(fc, scl(q, mul(f3(lc, lc, lc), color)));
+      fc = add(fc, mul(f3(0.25f, 0.25f, 0.25f), color));
+      return make_float4(fc.x, fc.y, fc.z, 1);
+    }
+    case LRT_RENDER_MODE_PRIMITIVE: case LRT_RENDER_MODE_TYPE: case LRT_RENDER_MODE_GEOM:
+    case LRT_RENDER_MODE_BARYCENTRIC: case LRT_RENDER_MODE_ST_ITERATIONS: case LRT_RENDER_MODE_DIFFUSE:
+    case LRT_RENDER_MODE_HSV_DEPTH:
+      return shade_extra(s, hit, type, z, pos, dir);
     default: return make_float4(1, 0, 1, 1);
   }
 }

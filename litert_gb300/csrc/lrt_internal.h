@@ -127,6 +127,17 @@ inline bool smoothed_normals(const DevScene &s) {
          s.sbs_hdr.aux_data == LRT_SBS_LAYOUT_ID32F_IRGB32F_IN && s.preset.normal_mode == 2 &&
          (m == 1 || m == 8 || m == 12 || m == 17 || m == 18);
 }
+// Kernel features an SBS scene needs: 1 smoothed normals; 2 brick colours computed in
+// the leaf loop (ST_ITERATIONS stores the iteration count in primId, so the final
+// hit no longer names its brick); 0 neither.
+inline int render_features(const DevScene &s) {
+  if (smoothed_normals(s)) return 1;
+  const uint32_t layout = s.sbs_hdr.aux_data & 0xFF000000u;
+  if (s.type != LRT_TYPE_MESH_TRIANGLE && s.type != LRT_TYPE_SDF_SVS && s.preset.render_mode == 10 &&
+      layout != LRT_SBS_LAYOUT_DX && layout != LRT_SBS_LAYOUT_UNDEFINED)
+    return 2;
+  return 0;
+}
 // The variant-0 render kernel compiled with FP contraction (trace_fused.cu).
 cudaError_t launch_render_fused(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st,
                                 const Tuning &tu);

@@ -59,7 +59,7 @@ __device__ __noinline__ float4 shade_phong(const DevScene &s, const Hit &hit, fl
 // Persistent render kernel: each warp pulls 32-pixel tiles (8x4 by default, the
 // shape is tunable) of the flattened multi-view tile space from a global queue
 // head and traces one ray per lane.
-template <int TYPE, bool COUNT, int MODE, int STACK, int FP, bool PHONG = false, bool SMOOTH = false>
+template <int TYPE, bool COUNT, int MODE, int STACK, int FP, bool PHONG = false, int FEAT = 0>
 __global__ void __launch_bounds__(128, 5) render_kernel(DevScene s, RenderLaunch L) {
   const uint32_t lane = threadIdx.x & 31u;
   Counters cnt = {0, 0, 0, 0};
@@ -86,7 +86,8 @@ __global__ void __launch_bounds__(128, 5) render_kernel(DevScene s, RenderLaunch
       float3 pos, dir;
       eye_ray(x, y, V.width, V.height, dx, dy, V.proj_inv, V.wv_inv, pos, dir);
       Hit hit;
-      trace<TYPE, COUNT, MODE, STACK, SMOOTH>(s, pos, 0.0f, dir, 1e9f, hit, cnt);
+      trace<TYPE, COUNT, MODE, STACK, FEAT>(s, pos, 0.0f, dir, 1e9f, hit, cnt);
+      if (TYPE == LRT_TYPE_SDF_SBS && !(FEAT & 2)) hit_colour(s, pos, dir, hit);
       if (si == 0) first = hit;
       if (L.rgba || L.rgba8) {
         const float4 c = PHONG ? shade_phong<TYPE, MODE, STACK>(s, hit, pos, dir) : shade(s, hit, pos, dir);

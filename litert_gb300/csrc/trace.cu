@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(128, 5) render_refill_kernel(DevScene s, Rende
 }
 
 // Batched RayQuery_NearestHit: one thread per ray, full CRT_Hit output.
-template <int TYPE, bool SMOOTH = false>
+template <int TYPE, int FEAT = 0>
 __global__ void __launch_bounds__(128) query_kernel(DevScene s, const float4 *pos_near, const float4 *dir_far,
                                                    uint32_t n, lrt_hit *out) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -125,7 +125,8 @@ __global__ void __launch_bounds__(128) query_kernel(DevScene s, const float4 *po
   const float4 p = pos_near[i], d = dir_far[i];
   Counters cnt = {0, 0, 0, 0};
   Hit hit;
-  trace<TYPE, false, -1, kStackSize, SMOOTH>(s, f3(p.x, p.y, p.z), p.w, f3(d.x, d.y, d.z), d.w, hit, cnt);
+  trace<TYPE, false, -1, kStackSize, FEAT>(s, f3(p.x, p.y, p.z), p.w, f3(d.x, d.y, d.z), d.w, hit, cnt);
+  if (TYPE == LRT_TYPE_SDF_SBS && !(FEAT & 2)) hit_colour(s, f3(p.x, p.y, p.z), f3(d.x, d.y, d.z), hit);
   lrt_hit o;
   o.t = hit.t;
   o.primId = (hit.prim != kMiss && (hit.geom >> 24) == LRT_TYPE_MESH_TRIANGLE) ? s.prim_indices[hit.prim] : hit.prim;
@@ -207,43 +208,47 @@ static cudaError_t launch_refill(const DevScene &s, const RenderLaunch &L, int n
 // these renders stay zero): PHONG / PHONG_NO_TEX with colour outputs, whose shading
 // traces shadow rays, and smoothed SDF normals (NORMAL_MODE_SDF_SMOOTHED on the
 // neighbour layout).  Separate instantiations keep both out of the other kernels.
-template <int TYPE, int MODE, bool PHONG, bool SMOOTH>
+template <int TYPE, int MODE, bool PHONG, int FEAT>
 static cudaError_t launch_feature_m(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st) {
   int per_sm = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      &per_sm, dev::render_kernel<TYPE, false, MODE, kStackSize, 0, PHONG, SMOOTH>, 128, 0);
+      &per_sm, dev::render_kernel<TYPE, false, MODE, kStackSize, 0, PHONG, FEAT>, 128, 0);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   uint32_t blocks = uint32_t(num_sms) * uint32_t(per_sm);
   const uint32_t max_blocks = (L.total_tiles + 3) / 4;
   if (blocks > max_blocks) blocks = max_blocks;
   if (blocks == 0) blocks = 1;
-  dev::render_kernel<TYPE, false, MODE, kStackSize, 0, PHONG, SMOOTH><<<blocks, 128, 0, st>>>(s, L);
+  dev::render_kernel<TYPE, false, MODE, kStackSize, 0, PHONG, FEAT><<<blocks, 128, 0, st>>>(s, L);
   return cudaGetLastError();
 }
 
-template <int TYPE, bool PHONG, bool SMOOTH>
+template <int TYPE, bool PHONG, int FEAT>
 static cudaError_t launch_feature_t(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st) {
-  if (TYPE == LRT_TYPE_MESH_TRIANGLE) return launch_feature_m<TYPE, -1, PHONG, false>(s, L, num_sms, st);
+  if (TYPE == LRT_TYPE_MESH_TRIANGLE) return launch_feature_m<TYPE, -1, PHONG, 0>(s, L, num_sms, st);
   switch (s.preset.sdf_node_intersect) {
-    case LRT_INTERSECT_NEWTON: return launch_feature_m<TYPE, LRT_INTERSECT_NEWTON, PHONG, SMOOTH>(s, L, num_sms, st);
-    case LRT_INTERSECT_ST: return launch_feature_m<TYPE, LRT_INTERSECT_ST, PHONG, SMOOTH>(s, L, num_sms, st);
-    default: return launch_feature_m<TYPE, -1, PHONG, SMOOTH>(s, L, num_sms, st);
+    case LRT_INTERSECT_NEWTON: return launch_feature_m<TYPE, LRT_INTERSECT_NEWTON, PHONG, FEAT>(s, L, num_sms, st);
+    case LRT_INTERSECT_ST: return launch_feature_m<TYPE, LRT_INTERSECT_ST, PHONG, FEAT>(s, L, num_sms, st);
+    default: return launch_feature_m<TYPE, -1, PHONG, FEAT>(s, L, num_sms, st);
   }
 }
 
 template <int TYPE>
 static cudaError_t launch_phong_t(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st) {
-  return launch_feature_t<TYPE, true, false>(s, L, num_sms, st);
+  return launch_feature_t<TYPE, true, 0>(s, L, num_sms, st);
 }
 
 cudaError_t launch_render(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st, bool count,
                           const Tuning &tu) {
   const uint32_t rm = s.preset.render_mode;
   const bool phong = (rm == LRT_RENDER_MODE_PHONG || rm == LRT_RENDER_MODE_PHONG_NO_TEX) && (L.rgba || L.rgba8);
-  if (smoothed_normals(s))   // SBS only (the neighbour layout)
-    return phong ? launch_feature_t<LRT_TYPE_SDF_SBS, true, true>(s, L, num_sms, st)
-                 : launch_feature_t<LRT_TYPE_SDF_SBS, false, true>(s, L, num_sms, st);
+  switch (render_features(s)) {   // SBS only; smoothed normals need a normal mode, so never with ST_ITERATIONS
+    case 1:
+      return phong ? launch_feature_t<LRT_TYPE_SDF_SBS, true, 1>(s, L, num_sms, st)
+                   : launch_feature_t<LRT_TYPE_SDF_SBS, false, 1>(s, L, num_sms, st);
+    case 2: return launch_feature_t<LRT_TYPE_SDF_SBS, false, 2>(s, L, num_sms, st);
+    default: break;
+  }
   if (phong) {
     switch (s.type) {
       case LRT_TYPE_MESH_TRIANGLE: return launch_phong_t<LRT_TYPE_MESH_TRIANGLE>(s, L, num_sms, st);
@@ -275,10 +280,11 @@ cudaError_t launch_query(const DevScene &s, const float4 *pos_near, const float4
     case LRT_TYPE_MESH_TRIANGLE: dev::query_kernel<LRT_TYPE_MESH_TRIANGLE><<<blocks, 128, 0, st>>>(s, pos_near, dir_far, n, out); break;
     case LRT_TYPE_SDF_SVS: dev::query_kernel<LRT_TYPE_SDF_SVS><<<blocks, 128, 0, st>>>(s, pos_near, dir_far, n, out); break;
     default:
-      if (smoothed_normals(s))
-        dev::query_kernel<LRT_TYPE_SDF_SBS, true><<<blocks, 128, 0, st>>>(s, pos_near, dir_far, n, out);
-      else
-        dev::query_kernel<LRT_TYPE_SDF_SBS><<<blocks, 128, 0, st>>>(s, pos_near, dir_far, n, out);
+      switch (render_features(s)) {
+        case 1: dev::query_kernel<LRT_TYPE_SDF_SBS, 1><<<blocks, 128, 0, st>>>(s, pos_near, dir_far, n, out); break;
+        case 2: dev::query_kernel<LRT_TYPE_SDF_SBS, 2><<<blocks, 128, 0, st>>>(s, pos_near, dir_far, n, out); break;
+        default: dev::query_kernel<LRT_TYPE_SDF_SBS><<<blocks, 128, 0, st>>>(s, pos_near, dir_far, n, out); break;
+      }
       break;
   }
   return cudaGetLastError();

@@ -199,6 +199,7 @@ __global__ void __launch_bounds__(256) render_packet_kernel(DevScene s, RenderLa
         }
         __syncwarp();
       }
+      hit_colour(s, pos, dir, hit);   // a lane outside the image holds no hit
       if (si == 0) first = hit;
       if (L.rgba || L.rgba8) {
         const float4 c = shade(s, hit, pos, dir);

@@ -12,7 +12,9 @@ __device__ __forceinline__ void visit_node(const DevScene &s, uint32_t ref, floa
 
 // RayQuery_NearestHit (BVH/BVH2Common.cpp:3490-3559) over the 4-wide BVH.
 // stopOnFirstHit (tFar <= 0) returns the first hit found (RayQuery_AnyHit).
-template <int TYPE, bool COUNT, int MODE = -1, int STACK = kStackSize, bool SMOOTH = false>
+// SBS brick colours are added by the caller (hit_colour) unless FEAT bit 1 has
+// them computed in the leaf loop.
+template <int TYPE, bool COUNT, int MODE = -1, int STACK = kStackSize, int FEAT = 0>
 __device__ void trace(const DevScene &s, float3 pos, float tNear, float3 dir, float tFar, Hit &hit, Counters &cnt) {
   const bool stop_first = (tFar <= 0.0f);
   if (stop_first) tFar *= -1.0f;
@@ -63,7 +65,7 @@ __device__ void trace(const DevScene &s, float3 pos, float tNear, float3 dir, fl
     else if (TYPE == LRT_TYPE_SDF_SVS)
       svs_intersect<COUNT, MODE>(s, rp, rd, tNearSdf, leaf, hit, cnt);
     else
-      brick_intersect<COUNT, false, MODE, SMOOTH>(s, rp, rd, inv, tNearSdf, leaf, hit, cnt);
+      brick_intersect<COUNT, false, MODE, FEAT>(s, rp, rd, inv, tNearSdf, leaf, hit, cnt);
     if (stop_first && hit.t < t_before) break;
   }
 }
