@@ -51,6 +51,14 @@ typedef struct {
   uint32_t accumulate_batch;
   /* 1: warp-aggregated gradient atomics (default), 0: one atomic per contribution */
   uint32_t warp_aggregate;
+  /* Regularization (diff_render/MultiRendererDR.cpp:1933-2055): reg_function != 0
+   * adds reg_lambda * reg_power * sign(d) * |d|^(reg_power-1) per brick value and
+   * in-brick neighbour to the batch gradient (defaults 0, 0.25, 2) */
+  uint32_t reg_function;
+  float reg_lambda, reg_power;
+  /* Redistance (:2122-2330) of the dense distance grid every redistancing_interval
+   * iterations when enabled (defaults off, 1); needs a cubic create_grid_sbs set */
+  uint32_t redistancing_enable, redistancing_interval;
 } lrt_dr_preset;
 
 /* getDefaultPresetDR (diff_render/MultiRendererDR.h:12-66) with the colour+geometry

@@ -1147,6 +1147,147 @@ void launch_border(const DevScene &s, const DevPreset &p, const DevView &v, uint
   dr_border_kernel<<<blocks, 128, 0, st>>>(s, p, v);
 }
 
+// Regularization (diff_render/MultiRendererDR.cpp:1933-2055): one thread per brick
+// value (brick_size + 1 per axis, the reference's v_size), its in-brick neighbours
+__global__ void dr_regularize_kernel(DevScene s, uint32_t n_nodes, float lambda, float power) {
+  const uint32_t v = s.brick_size + 1, v3 = v * v * v;
+  const uint64_t gid = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (gid >= uint64_t(n_nodes) * v3) return;
+  const uint32_t node = uint32_t(gid / v3), r = uint32_t(gid % v3);
+  const uint32_t i0 = r / (v * v), j0 = (r / v) % v, k0 = r % v;
+  const uint32_t idx = s.nodes[node].z + r;
+  const uint32_t own = __ldg(&s.values[idx]);
+  const float pv = __ldg(&s.P[own]);
+  const bool has[6] = {i0 > 0, i0 < v - 1, j0 > 0, j0 < v - 1, k0 > 0, k0 < v - 1};
+  const int step[6] = {-int(v * v), int(v * v), -int(v), int(v), -1, 1};
+  float acc = 0.0f;
+  bool first = true;
+#pragma unroll
+  for (int n = 0; n < 6; n++) {
+    if (!has[n]) continue;
+    float d = pv - __ldg(&s.P[__ldg(&s.values[int64_t(idx) + step[n]])]);
+    const float sgn_d = d > 0.0f ? 1.0f : -1.0f;
+    d = fabsf(d);
+    const float c = lambda * power * sgn_d * powf(d, power - 1);
+    acc = first ? c : acc + c;
+    first = false;
+  }
+  if (!first) atomicAdd(&s.grad[own], acc);
+}
+
+// SolveEikonal (:2058-2120), f = 1
+__device__ float solve_eikonal(float m0, float m1, float m2, float h) {
+  float m[3] = {m0, m1, m2}, t;
+  if (m[0] > m[1]) { t = m[0]; m[0] = m[1]; m[1] = t; }
+  if (m[0] > m[2]) { t = m[0]; m[0] = m[2]; m[2] = t; }
+  if (m[1] > m[2]) { t = m[1]; m[1] = m[2]; m[2] = t; }
+  float dist_new = m[0] + h;
+  if (dist_new > m[1]) {
+    const float h_2 = h * h;
+    float m_sum = m[0] + m[1], c_2 = (m[0] - m[1]) * (m[0] - m[1]);
+    dist_new = (m_sum + sqrtf(2 * h_2 - c_2)) * 0.5f;
+    if (dist_new > m[2]) {
+      const float one_third = 1.f / 3;
+      m_sum += m[2];
+      c_2 = 3.f * (m[0] * m[0] + m[1] * m[1] + m[2] * m[2] - h_2);
+      dist_new = (m_sum + sqrtf(m_sum * m_sum - c_2)) * one_third;
+    }
+  }
+  return dist_new;
+}
+
+constexpr float kRedistBig = 99999.f;
+
+// Redistance initialisation (:2170-2227): frozen surface nodes keep their values
+__global__ void dr_redist_init_kernel(const float *dist, uint32_t n, float *b0, float *b1, uint8_t *frozen) {
+  const uint64_t li = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const uint64_t N = uint64_t(n) * n * n;
+  if (li >= N) return;
+  const int ix[3] = {int(li / (uint64_t(n) * n)), int((li / n) % n), int(li % n)};
+  const int64_t off[3] = {int64_t(n) * n, int64_t(n), 1};
+  bool fr = false;
+  float v0 = kRedistBig;
+  const float dv = dist[li];
+  if (dv == 0.f) { fr = true; v0 = 0.f; }
+  if (!fr)
+    for (int dim = 0; dim < 3; dim++)
+      for (int sg = -1; sg < 2; sg += 2) {
+        const int q = ix[dim] + sg;
+        if (q >= 0 && q < int(n) && dist[int64_t(li) + sg * off[dim]] * dv < 0) { v0 = dv; fr = true; }
+      }
+  b0[li] = v0;
+  b1[li] = v0;
+  frozen[li] = fr ? 1 : 0;
+}
+
+// One Jacobi update of all nodes (each iteration of the reference reads only the
+// previous iteration's array, so its 8 sweep orderings compute these values)
+__global__ void dr_redist_step_kernel(const float *old, float *nw, const uint8_t *frozen, uint32_t n, float h) {
+  const uint64_t li = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const uint64_t N = uint64_t(n) * n * n;
+  if (li >= N) return;
+  const float ov = old[li];
+  if (frozen[li]) { nw[li] = ov; return; }
+  const int ix[3] = {int(li / (uint64_t(n) * n)), int((li / n) % n), int(li % n)};
+  const int64_t off[3] = {int64_t(n) * n, int64_t(n), 1};
+  float am[3] = {kRedistBig, kRedistBig, kRedistBig};
+#pragma unroll
+  for (int dim = 0; dim < 3; dim++) {
+    if (ix[dim] > 0 && ix[dim] < int(n) - 1) {
+      am[dim] = old[int64_t(li) - off[dim]];
+      const float tmp = old[int64_t(li) + off[dim]];
+      if (fabsf(tmp) < fabsf(am[dim])) am[dim] = tmp;
+    } else if (ix[dim] > 0 && ix[dim] == int(n) - 1) {
+      am[dim] = old[int64_t(li) - off[dim]];
+    } else if (ix[dim] == 0 && ix[dim] < int(n) - 1) {
+      am[dim] = old[int64_t(li) + off[dim]];
+    }
+  }
+  float r = ov;
+  if (am[0] < kRedistBig || am[1] < kRedistBig || am[2] < kRedistBig) {
+    if (am[0] >= 0.f && am[1] >= 0.f && am[2] >= 0.f) {
+      const float e = solve_eikonal(am[0], am[1], am[2], h);
+      r = e < ov ? e : ov;                              // std::min
+    } else {
+      for (int k = 0; k < 3; k++) if (am[k] < 0.f) am[k] = -am[k];
+      const float e = -solve_eikonal(am[0], am[1], am[2], h), o = -fabsf(ov);
+      r = e < o ? o : e;                                // std::max
+    }
+  }
+  nw[li] = r;
+}
+
+void launch_regularize(const DevScene &s, uint32_t n_nodes, float lambda, float power, cudaStream_t st) {
+  const uint64_t total = uint64_t(n_nodes) * (s.brick_size + 1) * (s.brick_size + 1) * (s.brick_size + 1);
+  if (total == 0) return;
+  dr_regularize_kernel<<<unsigned((total + 255) / 256), 256, 0, st>>>(s, n_nodes, lambda, power);
+}
+
+cudaError_t launch_redistance(float *dist, uint32_t n, float h, uint32_t n_iters, cudaStream_t st) {
+  const uint64_t N = uint64_t(n) * n * n;
+  if (N == 0) return cudaSuccess;
+  float *b[2] = {nullptr, nullptr};
+  uint8_t *frozen = nullptr;
+  cudaError_t e = cudaMallocAsync(&b[0], N * 4, st);
+  if (e == cudaSuccess) e = cudaMallocAsync(&b[1], N * 4, st);
+  if (e == cudaSuccess) e = cudaMallocAsync(&frozen, N, st);
+  const unsigned grid = unsigned((N + 255) / 256);
+  if (e == cudaSuccess) {
+    dr_redist_init_kernel<<<grid, 256, 0, st>>>(dist, n, b[0], b[1], frozen);
+    int cur = 0;
+    for (uint32_t it = 0; it < n_iters; it++) {
+      dr_redist_step_kernel<<<grid, 256, 0, st>>>(b[1 - cur], b[cur], frozen, n, h);
+      cur = 1 - cur;
+    }
+    e = cudaMemcpyAsync(dist, b[1 - cur], N * 4, cudaMemcpyDeviceToDevice, st);
+  }
+  if (e == cudaSuccess) e = cudaGetLastError();
+  for (float *p : b)
+    if (p) cudaFreeAsync(p, st);
+  if (frozen) cudaFreeAsync(frozen, st);
+  return e;
+}
+
 void launch_adam(float *x, float *V, float *S, const float *g, uint32_t n, float batch, float lr, float b1, float b2,
                  float eps, double c1, double c2, cudaStream_t st) {
   dr_adam_kernel<<<(n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096, 256, 0, st>>>(x, V, S, g, n, batch, lr, b1, b2,

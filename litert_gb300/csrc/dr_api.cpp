@@ -240,6 +240,11 @@ extern "C" void lrt_dr_default_preset(lrt_dr_preset *p) {
   p->opt_eps = 1e-8f;
   p->accumulate_batch = 0;
   p->warp_aggregate = 1;
+  p->reg_function = 0;            // getDefaultPresetDR, diff_render/MultiRendererDR.h:42-47
+  p->reg_lambda = 0.25f;
+  p->reg_power = 2.0f;
+  p->redistancing_enable = 0;
+  p->redistancing_interval = 1;
 }
 
 extern "C" lrt_status lrt_dr_set_scene(lrt_ctx *ctx, const lrt_sbs_header *hdr, const lrt_sbs_node *nodes,
@@ -451,6 +456,17 @@ extern "C" lrt_status lrt_dr_step(lrt_ctx *ctx, uint32_t iter, double *losses) {
     }
   }
   const lrt_dr_preset &p = st.preset;
+  if (p.reg_function != 0) {   // :453-456, into the batch gradient before the division
+    drk::launch_regularize(dev_scene(ctx), st.n_nodes, p.reg_lambda, p.reg_power, 0);
+    st.last_launches += 1;
+  }
+  if (p.redistancing_enable && p.redistancing_interval && iter % p.redistancing_interval == 0) {   // :459-466
+    const uint32_t bc = uint32_t(std::cbrt(double(st.n_nodes)));
+    const uint32_t pc = bc * st.hdr.brick_size + 1;
+    if (uint64_t(pc) * pc * pc > st.n_params) return fail(ctx, LRT_ERR_INVALID, "redistancing needs a cubic grid set");
+    LRT_CUDA(ctx, drk::launch_redistance(st.d_params.p, pc, 2.f / float(pc), pc, 0));
+    st.last_launches += pc + 1;
+  }
   const double c1 = 1.0 - std::pow(double(p.opt_beta_1), double(iter + 1));
   const double c2 = 1.0 - std::pow(double(p.opt_beta_2), double(iter + 1));
   drk::launch_adam(st.d_params.p, st.d_adam.p, st.d_adam.p + st.n_params, st.d_grad.p, st.n_params, float(nv),

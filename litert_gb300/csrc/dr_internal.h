@@ -58,6 +58,10 @@ void launch_pixels(const DevScene &s, const DevPreset &p, const DevView &v, cuda
 void launch_border_detect(const DevPreset &p, const DevView &v, cudaStream_t st);
 void launch_border(const DevScene &s, const DevPreset &p, const DevView &v, uint32_t max_pixels, int n_sm,
                    cudaStream_t st);
+// Regularization (diff_render/MultiRendererDR.cpp:1933-2055) into s.grad
+void launch_regularize(const DevScene &s, uint32_t n_nodes, float lambda, float power, cudaStream_t st);
+// Redistance (:2122-2330) of the dense n^3 grid at the start of dist, in place
+cudaError_t launch_redistance(float *dist, uint32_t n, float h, uint32_t n_iters, cudaStream_t st);
 void launch_adam(float *x, float *V, float *S, const float *g, uint32_t n, float inv_batch, float lr, float b1,
                  float b2, float eps, double c1, double c2, cudaStream_t st);
 void launch_scale(float *g, uint32_t n, float s, cudaStream_t st);

@@ -29,7 +29,9 @@ class DrPreset(C.Structure):
                 ("loss_function", C.c_uint32), ("spp", C.c_uint32), ("border_spp", C.c_uint32),
                 ("border_relax_eps", C.c_float), ("seed", C.c_uint32), ("n_lights", C.c_uint32),
                 ("lights", Light * 4), ("opt_lr", C.c_float), ("opt_beta_1", C.c_float), ("opt_beta_2", C.c_float),
-                ("opt_eps", C.c_float), ("accumulate_batch", C.c_uint32), ("warp_aggregate", C.c_uint32)]
+                ("opt_eps", C.c_float), ("accumulate_batch", C.c_uint32), ("warp_aggregate", C.c_uint32),
+                ("reg_function", C.c_uint32), ("reg_lambda", C.c_float), ("reg_power", C.c_float),
+                ("redistancing_enable", C.c_uint32), ("redistancing_interval", C.c_uint32)]
 
 
 _bound = False

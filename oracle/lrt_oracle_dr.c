@@ -467,6 +467,12 @@ void orc_dr_step(const orc_dr_scene *s, float *params, const orc_dr_preset *p, c
     free(img); free(dep);
     off += n;
   }
+  if (p->reg_function != 0) orc_dr_regularize(s, params, p, acc);               /* :453-456 */
+  if (p->redistancing_enable && p->redistancing_interval && iter % p->redistancing_interval == 0) {   /* :459-466 */
+    const uint32_t bc = (uint32_t)cbrt((double)s->n_nodes);
+    const uint32_t pc = bc * s->hdr.brick_size + 1;
+    orc_dr_redistance(params, pc, 2.f / pc, pc);
+  }
   for (uint32_t j = 0; j < np; j++) acc[j] /= (float)n_images;
   if (grad_out) memcpy(grad_out, acc, sizeof(float) * np);
   orc_dr_adam(iter, acc, params, adam_state, np, p->lr, p->beta1, p->beta2, p->eps);
@@ -606,4 +612,115 @@ uint32_t orc_dr_grid_sbs(uint32_t bc, uint32_t bs, const orc_sdf *f, const float
   free(adj);
   *nodes_out = nodes; *values_out = vals; *n_values = nn * per_new; *params_out = P; *n_params = np;
   return nn;
+}
+
+
+/* Regularization, diff_render/MultiRendererDR.cpp:1933-2055 (the reference sums
+ * per-thread slices afterwards; here one pass in node order) */
+void orc_dr_regularize(const orc_dr_scene *s, const float *params, const orc_dr_preset *p, float *grad) {
+  const uint32_t v = s->hdr.brick_size + 1;
+  const float power = p->reg_power, lambda = p->reg_lambda;
+  for (uint32_t node = 0; node < s->n_nodes; node++) {
+    const uint32_t off = s->nodes[node].data_offset;
+    for (uint32_t i0 = 0; i0 < v; i0++)
+      for (uint32_t j0 = 0; j0 < v; j0++)
+        for (uint32_t k0 = 0; k0 < v; k0++) {
+          const uint32_t idx = off + i0 * v * v + j0 * v + k0;
+          const int has[6] = {i0 > 0, i0 < v - 1, j0 > 0, j0 < v - 1, k0 > 0, k0 < v - 1};
+          const int64_t step[6] = {-(int64_t)(v * v), (int64_t)(v * v), -(int64_t)v, (int64_t)v, -1, 1};
+          for (int n = 0; n < 6; n++) {
+            if (!has[n]) continue;
+            float d = params[s->values[idx]] - params[s->values[(int64_t)idx + step[n]]];
+            const float sgn_d = d > 0.0f ? 1.0f : -1.0f;
+            d = fabsf(d);
+            grad[s->values[idx]] += lambda * power * sgn_d * powf(d, power - 1);
+          }
+        }
+  }
+}
+
+/* SolveEikonal, :2058-2120 (f = 1) */
+static float solve_eikonal(float m0, float m1, float m2, float h) {
+  float m[3] = {m0, m1, m2}, t;
+  if (m[0] > m[1]) { t = m[0]; m[0] = m[1]; m[1] = t; }
+  if (m[0] > m[2]) { t = m[0]; m[0] = m[2]; m[2] = t; }
+  if (m[1] > m[2]) { t = m[1]; m[1] = m[2]; m[2] = t; }
+  float dist_new = m[0] + h;
+  if (dist_new > m[1]) {
+    const float h_2 = h * h;
+    float m_sum = m[0] + m[1], c_2 = (m[0] - m[1]) * (m[0] - m[1]);
+    float x2 = (m_sum + sqrtf(2 * h_2 - c_2)) * 0.5f;
+    dist_new = x2;
+    if (dist_new > m[2]) {
+      const float one_third = 1.f / 3;
+      m_sum += m[2];
+      c_2 = 3.f * (m[0] * m[0] + m[1] * m[1] + m[2] * m[2] - h_2);
+      x2 = (m_sum + sqrtf(m_sum * m_sum - c_2)) * one_third;
+      dist_new = x2;
+    }
+  }
+  return dist_new;
+}
+
+/* Redistance, :2122-2330.  Every update of an iteration reads the previous
+ * iteration's array, so the reference's 8 sweep orderings all compute the same
+ * values: one Jacobi update per iteration. */
+void orc_dr_redistance(float *dist, uint32_t n, float h, uint32_t n_iters) {
+  const size_t N = (size_t)n * n * n;
+  const int64_t off[3] = {(int64_t)n * n, (int64_t)n, 1};
+  const float big = 99999.f;
+  float *b[2] = {(float *)malloc(4 * N), (float *)malloc(4 * N)};
+  uint8_t *frozen = (uint8_t *)malloc(N);
+  for (size_t li = 0; li < N; li++) {
+    const int ix[3] = {(int)(li / ((size_t)n * n)), (int)((li / n) % n), (int)(li % n)};
+    frozen[li] = 0;
+    b[0][li] = b[1][li] = big;
+    const float dv = dist[li];
+    if (dv == 0.f) { frozen[li] = 1; b[0][li] = b[1][li] = 0.f; }
+    if (!frozen[li])
+      for (int dim = 0; dim < 3; dim++)
+        for (int sg = -1; sg < 2; sg += 2) {
+          const int q = ix[dim] + sg;
+          if (q >= 0 && q < (int)n) {
+            const float nv = dist[(int64_t)li + sg * off[dim]];
+            if (nv * dv < 0) { b[0][li] = b[1][li] = dv; frozen[li] = 1; }
+          }
+        }
+  }
+  int cur = 0;
+  for (uint32_t it = 0; it < n_iters; it++) {
+    const float *old = b[1 - cur];
+    float *nw = b[cur];
+    for (size_t li = 0; li < N; li++) {
+      nw[li] = old[li];
+      if (frozen[li]) continue;
+      const int ix[3] = {(int)(li / ((size_t)n * n)), (int)((li / n) % n), (int)(li % n)};
+      float am[3] = {big, big, big};
+      for (int dim = 0; dim < 3; dim++) {
+        if (ix[dim] > 0 && ix[dim] < (int)n - 1) {
+          am[dim] = old[(int64_t)li - off[dim]];
+          const float tmp = old[(int64_t)li + off[dim]];
+          if (fabsf(tmp) < fabsf(am[dim])) am[dim] = tmp;
+        } else if (ix[dim] > 0 && ix[dim] == (int)n - 1) {
+          am[dim] = old[(int64_t)li - off[dim]];
+        } else if (ix[dim] == 0 && ix[dim] < (int)n - 1) {
+          am[dim] = old[(int64_t)li + off[dim]];
+        }
+      }
+      if (am[0] < big || am[1] < big || am[2] < big) {
+        const int pos_part = am[0] >= 0.f && am[1] >= 0.f && am[2] >= 0.f;
+        if (pos_part) {
+          const float e = solve_eikonal(am[0], am[1], am[2], h);
+          nw[li] = e < old[li] ? e : old[li];                          /* std::min */
+        } else {
+          for (int k = 0; k < 3; k++) if (am[k] < 0.f) am[k] = -am[k];
+          const float e = -solve_eikonal(am[0], am[1], am[2], h), o = -fabsf(old[li]);
+          nw[li] = e < o ? o : e;                                      /* std::max */
+        }
+      }
+    }
+    cur = 1 - cur;
+  }
+  memcpy(dist, b[1 - cur], 4 * N);
+  free(b[0]); free(b[1]); free(frozen);
 }

@@ -56,6 +56,9 @@ typedef struct {
   orc_dr_light lights[4];
   float lr, beta1, beta2, eps;          /* Adam */
   uint32_t accumulate_batch;            /* 0: the reference's per-image zeroing; 1: sum over the batch */
+  uint32_t reg_function;                /* DR_REG_FUNCTION_NONE = 0, else Regularization runs */
+  float reg_lambda, reg_power;
+  uint32_t redistancing_enable, redistancing_interval;
 } orc_dr_preset;
 
 typedef struct {
@@ -89,6 +92,17 @@ double orc_dr_loss_f64(const orc_dr_scene *s, const double *params, const orc_dr
 void orc_dr_step(const orc_dr_scene *s, float *params, const orc_dr_preset *p, const orc_dr_view *views,
                  const float *images, uint32_t n_images, uint32_t iter, float *adam_state, float *grad_out,
                  double *losses, float *images_out, int threads);
+
+/* Regularization (diff_render/MultiRendererDR.cpp:1933-2055): for every brick
+ * value and each of its 6 neighbours inside the brick (brick_size + 1 values per
+ * axis), adds reg_lambda * reg_power * sign(d) * |d|^(reg_power - 1) to grad at the
+ * value's parameter index, d = own value - neighbour value. */
+void orc_dr_regularize(const orc_dr_scene *s, const float *params, const orc_dr_preset *p, float *grad);
+
+/* Redistance (:2122-2330) with SolveEikonal (:2058-2120): n_iters Jacobi updates of
+ * the dense n^3 distance grid dist (in place), grid spacing h; nodes next to a sign
+ * change or on the surface keep their values. */
+void orc_dr_redistance(float *dist, uint32_t n, float h, uint32_t n_iters);
 
 /* OptimizeStepAdam (:828-853). */
 void orc_dr_adam(uint32_t iter, const float *g, float *x, float *state, uint32_t n, float lr, float b1, float b2,

@@ -43,7 +43,9 @@ class DrPreset(C.Structure):
                 ("loss_function", C.c_uint32), ("spp", C.c_uint32), ("border_spp", C.c_uint32),
                 ("border_relax_eps", C.c_float), ("seed", C.c_uint32), ("n_lights", C.c_uint32),
                 ("lights", Light * 4), ("lr", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float),
-                ("eps", C.c_float), ("accumulate_batch", C.c_uint32)]
+                ("eps", C.c_float), ("accumulate_batch", C.c_uint32), ("reg_function", C.c_uint32),
+                ("reg_lambda", C.c_float), ("reg_power", C.c_float), ("redistancing_enable", C.c_uint32),
+                ("redistancing_interval", C.c_uint32)]
 
 
 class DrView(C.Structure):
@@ -67,6 +69,8 @@ def _lib():
         L.orc_dr_step.argtypes = [C.POINTER(DrScene_), VP, C.POINTER(DrPreset), VP, VP, C.c_uint32, C.c_uint32, VP,
                                   VP, VP, VP, C.c_int]
         L.orc_dr_adam.argtypes = [C.c_uint32, VP, VP, VP, C.c_uint32, C.c_float, C.c_float, C.c_float, C.c_float]
+        L.orc_dr_regularize.argtypes = [C.POINTER(DrScene_), VP, C.POINTER(DrPreset), VP]
+        L.orc_dr_redistance.argtypes = [VP, C.c_uint32, C.c_float, C.c_uint32]
         L.orc_dr_grid_sbs.restype = C.c_uint32
         L.orc_dr_grid_sbs.argtypes = [C.c_uint32, C.c_uint32, C.c_void_p, VP, C.POINTER(SbsHeader), C.POINTER(VP),
                                       C.POINTER(VP), C.POINTER(C.c_uint32), C.POINTER(VP), C.POINTER(C.c_uint32)]
@@ -85,7 +89,8 @@ def default_lights():
 
 def make_preset(render_mode=RENDER_LAMBERT, reconstruction=RECON_COLOR | RECON_GEOMETRY, input_type=0, loss=0,
                 spp=1, border_spp=256, border_relax_eps=1e-3, seed=1, lights=None, lr=3e-3, beta1=0.9, beta2=0.999,
-                eps=1e-8, accumulate_batch=0):
+                eps=1e-8, accumulate_batch=0, reg_function=0, reg_lambda=0.25, reg_power=2.0,
+                redistancing_enable=0, redistancing_interval=1):
     p = DrPreset()
     p.render_mode, p.reconstruction_flags, p.input_type, p.loss_function = render_mode, reconstruction, input_type, loss
     p.spp, p.border_spp, p.border_relax_eps, p.seed = spp, border_spp, border_relax_eps, seed
@@ -96,6 +101,8 @@ def make_preset(render_mode=RENDER_LAMBERT, reconstruction=RECON_COLOR | RECON_G
         p.lights[i].dir[:] = [float(x) for x in np.asarray(d, np.float32)]
         p.lights[i].color[:] = [float(x) for x in np.asarray(c, np.float32)]
     p.lr, p.beta1, p.beta2, p.eps, p.accumulate_batch = lr, beta1, beta2, eps, accumulate_batch
+    p.reg_function, p.reg_lambda, p.reg_power = reg_function, reg_lambda, reg_power
+    p.redistancing_enable, p.redistancing_interval = redistancing_enable, redistancing_interval
     return p
 
 
@@ -179,6 +186,13 @@ class DrScene:
         loss = _lib().orc_dr_loss_f64(C.byref(self.s), _p(P), C.byref(preset), C.byref(view), _p(ref), _p(hc))
         return loss, hc
 
+    def regularize(self, params, preset):
+        """Regularization's gradient alone (diff_render/MultiRendererDR.cpp:1933-2055)."""
+        params = np.ascontiguousarray(params, np.float32)
+        g = np.zeros(params.size, np.float32)
+        _lib().orc_dr_regularize(C.byref(self.s), _p(params), C.byref(preset), _p(g))
+        return g
+
     def step(self, params, preset, views, images, it, adam_state, threads=0):
         """One OptimizeFixedStructure iteration; params and adam_state are updated in place."""
         assert params.dtype == np.float32 and params.flags.c_contiguous
@@ -197,3 +211,10 @@ class DrScene:
 def adam(it, g, x, state, lr, b1=0.9, b2=0.999, eps=1e-8):
     g = np.ascontiguousarray(g, np.float32)
     _lib().orc_dr_adam(it, _p(g), _p(x), _p(state), x.size, lr, b1, b2, eps)
+
+
+def redistance(dist, n, h, iters):
+    """Redistance (diff_render/MultiRendererDR.cpp:2122-2330) of a dense n^3 grid; returns a copy."""
+    d = np.ascontiguousarray(dist, np.float32).copy()
+    _lib().orc_dr_redistance(_p(d), n, h, iters)
+    return d
