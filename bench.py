@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true", help="use --variant/--block-warps/--stage as given")
     ap.add_argument("--no-graph", action="store_true", help="launch directly instead of replaying a CUDA graph")
     ap.add_argument("--no-proposal", action="store_true", help="skip the learned-proposal measurement")
+    ap.add_argument("--no-device-bvh", action="store_true", help="skip the device BVH build measurement")
     ap.add_argument("--fma", type=int, default=1, choices=(0, 1),
                     help="headline kernel: 1 = compiled with FP contraction (within the forward parity tolerance), "
                          "0 = bit-exact; the other one is timed beside it")
@@ -147,6 +148,52 @@ def gpu_build(args, host):
     dt = time.time() - t0
     same = bool(np.array_equal(nodes, host[1]) and np.array_equal(values, host[2]))
     return dt, same
+
+
+def run_device_bvh(args, h, nodes, values, views, tuned, hits, flush, stream, torch):
+    """Scene commit wall time with the host binned-SAH BVH and with the device
+    linear BVH (second commit of each, after a warm-up commit), and the headline
+    render through the device-built tree with the same launch shape, timed like
+    the headline (CUDA events, L2 flush between steps)."""
+    from litert_gb300 import lrt
+    out = {}
+    n_rays = sum(w * hh for w, hh, _, _ in views)
+    for builder in (0, 1):
+        s = lrt.Scene(0)
+        s.set_tuning("bvh_builder", builder)
+        gid = s.add_sbs(h, nodes, values)
+        s.add_instance(gid)
+        s.commit_scene()
+        t0 = time.perf_counter()
+        s.commit_scene()
+        out["commit_s_host_bvh" if builder == 0 else "commit_s_device_bvh"] = round(time.perf_counter() - t0, 3)
+        if builder == 0:
+            s.close()
+            continue
+        s.set_preset(render_mode=lrt.RENDER_MODE_NORMAL, sdf_node_intersect=lrt.INTERSECT_NEWTON)
+        s.set_tuning("fma", args.fma)
+        if tuned:
+            for k in ("variant", "block_warps", "stage", "tile_w", "stack"):
+                s.set_tuning(k, tuned[k])
+        g = s.graph_create(views, hits_ptr=hits.data_ptr())
+        for _ in range(args.warmup):
+            flush.fill_(1.0)
+            s.graph_launch(g, stream.cuda_stream)
+        ts = []
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            s.graph_launch(g, stream.cuda_stream)
+            b.record(stream)
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+        lrt.Scene.graph_destroy(g)
+        s.close()
+        ms = sum(ts) / len(ts)
+        out["render_ms"] = ms
+        out["render_value"] = n_rays / (ms * 1e-3) / 1e6
+    return out
 
 
 def cpu_sample(views, n_target, seed=0):
@@ -659,6 +706,8 @@ def main():
                                     "sample": f"{cpu['rays']} strided pixels of the 16 views ({cpu['seconds']:.1f} s)"}
         if not args.no_proposal and world == 1:
             line["proposal"] = run_proposal(args, scene, dev, torch)
+        if not args.no_device_bvh and world == 1:
+            line["device_bvh"] = run_device_bvh(args, h, nodes, values, views, tuned, hits, flush, stream, torch)
         if not args.no_dr and world == 1:
             line["dr"] = run_dr(args, dev, torch)
         if world == 1 and not args.no_configs:

@@ -70,8 +70,22 @@ lrt_status lrt_set_preset(lrt_ctx *ctx, const lrt_preset *preset);
  * floating-point contraction: faster, no longer bit-identical to the reference's
  * x86-64 build, within the forward parity tolerance: same hit mask, depth within
  * 1e-4 of the scene extent, normals within 1e-3, apart from grazing and crease
- * pixels).  "proposal": see lrt_proposal.h. */
+ * pixels).  "proposal": see lrt_proposal.h.
+ * "bvh_builder" (read by lrt_commit_scene: 0 = host binned-SAH build, default,
+ * the reference's Embree build restated (BVH/cbvh.cpp:591-657); 1 = the BVH is
+ * built on the device: Morton codes of the primitive centroids, a radix sort,
+ * a binary radix tree and the same 4-wide collapse, one primitive per leaf.
+ * Hits are the same apart from exact ties between primitives; traversal cost
+ * depends on the tree). */
 lrt_status lrt_set_tuning(lrt_ctx *ctx, const char *key, int value);
+
+/* New vertex positions for the committed triangle mesh (same vertex count and
+ * indices; n_vert positions, v_byte_stride bytes apart): the BVH keeps its
+ * topology and its boxes are refit on the device, deepest level first; the
+ * instance box follows the new geometry box.  No reference counterpart (the
+ * reference rebuilds).  Afterwards lrt_get_bvh2 fails (the fat pairs are made
+ * at commit only) and graphs captured earlier must be created again. */
+lrt_status lrt_refit_triangles(lrt_ctx *ctx, const float *vpos, size_t n_vert, size_t v_byte_stride);
 
 /* One launch shape and its median time. */
 typedef struct { int variant, block_warps, stage, tile_w, stack; float ms; } lrt_tuning_choice;
@@ -147,7 +161,9 @@ lrt_status lrt_render_counters(lrt_ctx *ctx, const lrt_view *views, uint32_t n_v
 
 /* The committed scene's BVH2 in the reference's fat-pair layout (root pair at 0),
  * as CreateFatTreeArray produces it (BVH/cbvh_fat.cpp:100-142).  Host pointer
- * owned by ctx, valid until the next commit. */
+ * owned by ctx, valid until the next commit.  A device-built BVH numbers pair i
+ * after internal node i of its radix tree and is copied from the device on the
+ * first call. */
 lrt_status lrt_get_bvh2(lrt_ctx *ctx, const lrt_bvh_pair **pairs, uint32_t *n_pairs);
 
 /* The BVH builder alone, no device needed: fat pairs for n boxes (n x 6 floats,

@@ -698,4 +698,8 @@ lrt_status build_svs_gpu(const lrt_sdf_desc &sd, uint32_t depth, std::vector<lrt
   return LRT_OK;
 }
 
+cudaError_t gpu_exclusive_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint64_t *total, cudaStream_t st) {
+  return exclusive_scan(in, out, n, total, st);
+}
+
 }  // namespace lrt

@@ -178,6 +178,7 @@ lrt_status build_bvh(const float *boxes6, uint32_t n, bool boxes, BvhData &out) 
   std::vector<uint32_t> wdepth(1, 0);
   std::vector<WNode4> &wn = out.wnodes;
   wn.clear();
+  out.level_start.assign(1, 0);
   uint32_t max_wdepth = 0;
   for (size_t wi = 0; wi < pend.size(); wi++) {
     const Node2 &root = B.nodes[pend[wi]];
@@ -210,6 +211,7 @@ lrt_status build_bvh(const float *boxes6, uint32_t n, bool boxes, BvhData &out) 
           w.child[i] = leaf_ref(c, B.order, boxes);
         } else {
           w.child[i] = uint32_t(pend.size());
+          if (wdepth[wi] + 1 == out.level_start.size()) out.level_start.push_back(uint32_t(pend.size()));
           pend.push_back(ch[i]);
           wdepth.push_back(wdepth[wi] + 1);
           max_wdepth = std::max(max_wdepth, wdepth[wi] + 1);

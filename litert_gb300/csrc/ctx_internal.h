@@ -81,6 +81,17 @@ struct lrt_ctx {
   DevBuf<lrt_svs_node> d_svs;
   DevBuf<float4> d_tri_verts;
   DevBuf<uint32_t> d_prim_indices;
+  // BVH built on the device (bvh_builder = 1) and triangle refit
+  DevBuf<float> d_boxes6;              // primitive boxes (build input / refit scratch)
+  DevBuf<lrt_bvh_pair> d_pairs;        // reference fat-pair layout of a device-built BVH
+  DevBuf<uint32_t> d_leaf_start_count;
+  DevBuf<float4> d_vpos;               // mesh vertices (refit)
+  DevBuf<uint32_t> d_tri_indices;      // mesh indices (refit)
+  int bvh_builder = 0;                 // 0: host binned SAH, 1: device linear BVH
+  bool bvh_on_device = false;          // the committed BVH was built on the device
+  bool bvh_refit = false;              // slot boxes refit since the commit (fat pairs not refit)
+  bool tri_indices_on_device = false;
+  uint32_t n_wnodes = 0, n_pairs = 0, n_leaf_start_count = 0;
   // per-call scratch
   DevBuf<uint32_t> d_tile_counter;
   DevBuf<DevView> d_views;

@@ -295,11 +295,30 @@ extern "C" lrt_status lrt_dr_set_scene(lrt_ctx *ctx, const lrt_sbs_header *hdr, 
         boxes[6 * i + 3 + k] = lo[k] + 2.0f * 1 / sz;
       }
     }
-    BvhData b;
-    s = build_bvh(boxes.data(), n_nodes, true, b);
-    if (s != LRT_OK) return fail(ctx, s, "BVH build failed");
-    st.pairs.assign(reinterpret_cast<const lrt_bvh_pair *>(b.pairs.data()),
-                    reinterpret_cast<const lrt_bvh_pair *>(b.pairs.data()) + b.pairs.size());
+    if (ctx->bvh_builder == 1) {   // device linear BVH (lrt_set_tuning "bvh_builder"), pairs fetched back
+      const uint32_t n_int = n_nodes > 1 ? n_nodes - 1 : 1;
+      DevBuf<float> d_boxes;
+      DevBuf<WNode4> d_wide;
+      DevBuf<lrt_bvh_pair> d_pairs;
+      cudaError_t e = upload(d_boxes, boxes.data(), boxes.size());
+      if (e == cudaSuccess) e = d_wide.ensure(n_int);
+      if (e == cudaSuccess) e = d_pairs.ensure(n_int);
+      GpuBvhInfo info;
+      if (e == cudaSuccess) e = build_bvh_gpu(d_boxes.p, n_nodes, true, d_wide.p, nullptr, d_pairs.p, nullptr, info, 0);
+      st.pairs.resize(n_int);
+      if (e == cudaSuccess)
+        e = cudaMemcpy(st.pairs.data(), d_pairs.p, size_t(n_int) * sizeof(lrt_bvh_pair), cudaMemcpyDeviceToHost);
+      d_boxes.release();
+      d_wide.release();
+      d_pairs.release();
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "lrt_dr_set_scene: device BVH build");
+    } else {
+      BvhData b;
+      s = build_bvh(boxes.data(), n_nodes, true, b);
+      if (s != LRT_OK) return fail(ctx, s, "BVH build failed");
+      st.pairs.assign(reinterpret_cast<const lrt_bvh_pair *>(b.pairs.data()),
+                      reinterpret_cast<const lrt_bvh_pair *>(b.pairs.data()) + b.pairs.size());
+    }
   }
   // every child reference of the BVH2 must be a pair index or a leaf of a valid brick
   for (const lrt_bvh_pair &p : st.pairs)

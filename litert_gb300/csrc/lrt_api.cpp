@@ -128,6 +128,12 @@ static void release_scene(lrt_ctx *ctx) {
   ctx->d_svs.release();
   ctx->d_tri_verts.release();
   ctx->d_prim_indices.release();
+  ctx->d_boxes6.release();
+  ctx->d_pairs.release();
+  ctx->d_leaf_start_count.release();
+  ctx->d_vpos.release();
+  ctx->d_tri_indices.release();
+  ctx->bvh_on_device = ctx->bvh_refit = ctx->tri_indices_on_device = false;
   ctx->committed = false;
 }
 
@@ -267,6 +273,17 @@ extern "C" lrt_status lrt_clear_scene(lrt_ctx *ctx) {
   return LRT_OK;
 }
 
+// transformed corners of the geometry box, BVH/BVH2Common_host.cpp:1460-1475
+static void instance_bounds(const Geom &g, Inst &in) {
+  for (int k = 0; k < 3; k++) { in.bmin[k] = 3.4e38f; in.bmax[k] = -3.4e38f; }
+  for (int c = 0; c < 8; c++) {
+    const float v[4] = {(c & 1) ? g.bmax[0] : g.bmin[0], (c & 2) ? g.bmax[1] : g.bmin[1], (c & 4) ? g.bmax[2] : g.bmin[2], 1.0f};
+    float r[4];
+    mat_mul_vec4(in.m, v, r);
+    for (int k = 0; k < 3; k++) { in.bmin[k] = std::min(in.bmin[k], r[k]); in.bmax[k] = std::max(in.bmax[k], r[k]); }
+  }
+}
+
 extern "C" lrt_status lrt_add_instance(lrt_ctx *ctx, uint32_t geom_id, const float matrix[16], uint32_t *inst_id) {
   if (!ctx) return LRT_ERR_INVALID;
   geom_id &= 0x7fffffffu;   // CRT_GEOM_MASK_AABB_BIT, BVH/BVH2Common_host.cpp:1452-1453
@@ -278,14 +295,7 @@ extern "C" lrt_status lrt_add_instance(lrt_ctx *ctx, uint32_t geom_id, const flo
   lrt_inverse4x4(matrix, in.inv);
   for (int i = 0; i < 4; i++)
     for (int j = 0; j < 4; j++) in.inv_t[i * 4 + j] = in.inv[j * 4 + i];
-  // transformed corners of the geometry box, BVH/BVH2Common_host.cpp:1460-1475
-  for (int k = 0; k < 3; k++) { in.bmin[k] = 3.4e38f; in.bmax[k] = -3.4e38f; }
-  for (int c = 0; c < 8; c++) {
-    const float v[4] = {(c & 1) ? g.bmax[0] : g.bmin[0], (c & 2) ? g.bmax[1] : g.bmin[1], (c & 4) ? g.bmax[2] : g.bmin[2], 1.0f};
-    float r[4];
-    mat_mul_vec4(matrix, v, r);
-    for (int k = 0; k < 3; k++) { in.bmin[k] = std::min(in.bmin[k], r[k]); in.bmax[k] = std::max(in.bmax[k], r[k]); }
-  }
+  instance_bounds(g, in);
   ctx->insts.push_back(in);
   if (inst_id) *inst_id = uint32_t(ctx->insts.size() - 1);
   ctx->committed = false;
@@ -297,6 +307,42 @@ static cudaError_t upload(DevBuf<T> &b, const T *src, size_t n) {
   cudaError_t e = b.ensure(n);
   if (e != cudaSuccess || n == 0) return e;
   return cudaMemcpy(b.p, src, n * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+// BVH of the committed geometry built on the device: wide nodes straight into
+// d_nodes, the sorted triangle order into d_prim_indices, the fat pairs kept on
+// the device until lrt_get_bvh2 asks for them.
+static lrt_status device_bvh(lrt_ctx *ctx, const std::vector<float> &boxes, bool tri) {
+  const Geom &g = ctx->geoms[ctx->insts[0].geom];
+  const uint32_t n = uint32_t(boxes.size() / 6);
+  if (n == 0) return fail(ctx, LRT_ERR_INVALID, "lrt_commit_scene: empty geometry");
+  if (!tri && n >= (1u << 31)) return fail(ctx, LRT_ERR_UNSUPPORTED, "lrt_commit_scene: too many boxes");
+  const uint32_t n_int = std::max<uint32_t>(1, n - 1);
+  cudaError_t e;
+  if ((e = upload(ctx->d_boxes6, boxes.data(), boxes.size())) != cudaSuccess) return cuda_fail(ctx, e, "upload boxes");
+  LRT_CUDA(ctx, ctx->d_nodes.ensure(n_int));
+  LRT_CUDA(ctx, ctx->d_pairs.ensure(n_int));
+  if (tri) {
+    LRT_CUDA(ctx, ctx->d_prim_indices.ensure(n));
+    LRT_CUDA(ctx, ctx->d_leaf_start_count.ensure(n));
+    if ((e = upload(ctx->d_vpos, reinterpret_cast<const float4 *>(g.vpos.data()), g.vpos.size() / 4)) != cudaSuccess)
+      return cuda_fail(ctx, e, "upload vertices");
+    if ((e = upload(ctx->d_tri_indices, g.indices.data(), g.indices.size())) != cudaSuccess)
+      return cuda_fail(ctx, e, "upload indices");
+    ctx->tri_indices_on_device = true;
+  }
+  GpuBvhInfo info;
+  e = build_bvh_gpu(ctx->d_boxes6.p, n, !tri, ctx->d_nodes.p, tri ? ctx->d_prim_indices.p : nullptr, ctx->d_pairs.p,
+                    tri ? ctx->d_leaf_start_count.p : nullptr, info, 0);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "lrt_commit_scene: device BVH build");
+  ctx->bvh = BvhData{};
+  ctx->bvh.max_depth = info.max_depth;
+  ctx->bvh.level_start = info.level_start;
+  ctx->n_wnodes = info.n_wnodes;
+  ctx->n_pairs = n_int;
+  ctx->n_leaf_start_count = tri ? n : 0;
+  ctx->bvh_on_device = true;
+  return LRT_OK;
 }
 
 extern "C" lrt_status lrt_commit_scene(lrt_ctx *ctx) {
@@ -327,7 +373,6 @@ extern "C" lrt_status lrt_commit_scene(lrt_ctx *ctx) {
         boxes[6 * t + k] = lo;
         boxes[6 * t + 3 + k] = hi;
       }
-    st = build_bvh(boxes.data(), uint32_t(nt), false, ctx->bvh);
   } else {
     // one AABB per brick / voxel, BVH/BVH2Common_host.cpp:546-555, 640-653
     const bool sbs = g.type != LRT_TYPE_SDF_SVS;
@@ -343,17 +388,32 @@ extern "C" lrt_status lrt_commit_scene(lrt_ctx *ctx) {
         boxes[6 * i + 3 + k] = lo[k] + 2.0f * 1 / sz;
       }
     }
-    st = build_bvh(boxes.data(), uint32_t(n), true, ctx->bvh);
   }
-  if (st != LRT_OK) return fail(ctx, st, "lrt_commit_scene: BVH build failed");
+  const bool tri = g.type == LRT_TYPE_MESH_TRIANGLE;
+  const uint32_t n_prims = uint32_t(boxes.size() / 6);
+  cudaError_t e;
+  if (ctx->bvh_builder == 1) {
+    if ((st = device_bvh(ctx, boxes, tri)) != LRT_OK) return st;
+  } else {
+    st = build_bvh(boxes.data(), n_prims, !tri, ctx->bvh);
+    if (st != LRT_OK) return fail(ctx, st, "lrt_commit_scene: BVH build failed");
+    ctx->n_wnodes = uint32_t(ctx->bvh.wnodes.size());
+  }
   if (3 * int(ctx->bvh.max_depth) + 4 > kStackSize)
     return fail(ctx, LRT_ERR_UNSUPPORTED, "lrt_commit_scene: BVH deeper than the traversal stack");
 
-  cudaError_t e;
-  if ((e = upload(ctx->d_nodes, ctx->bvh.wnodes.data(), ctx->bvh.wnodes.size())) != cudaSuccess)
+  if (!ctx->bvh_on_device && (e = upload(ctx->d_nodes, ctx->bvh.wnodes.data(), ctx->bvh.wnodes.size())) != cudaSuccess)
     return cuda_fail(ctx, e, "upload nodes");
   s.nodes = ctx->d_nodes.p;
-  if (g.type == LRT_TYPE_MESH_TRIANGLE) {
+  if (tri && ctx->bvh_on_device) {
+    const size_t nt = g.indices.size() / 3;
+    LRT_CUDA(ctx, ctx->d_tri_verts.ensure(3 * nt));
+    LRT_CUDA(ctx, gather_triangles_gpu(ctx->d_vpos.p, ctx->d_tri_indices.p, ctx->d_prim_indices.p, uint32_t(nt),
+                                       ctx->d_tri_verts.p, 0));
+    LRT_CUDA(ctx, cudaDeviceSynchronize());
+    s.tri_verts = ctx->d_tri_verts.p;
+    s.prim_indices = ctx->d_prim_indices.p;
+  } else if (tri) {
     const size_t nt = g.indices.size() / 3;
     std::vector<float4> tv(3 * nt);
     for (size_t r = 0; r < nt; r++) {
@@ -472,6 +532,9 @@ extern "C" lrt_status lrt_set_tuning(lrt_ctx *ctx, const char *key, int value) {
   } else if (k == "fma") {
     if (value < 0 || value > 1) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: fma is 0 or 1");
     ctx->tuning.fma = value;
+  } else if (k == "bvh_builder") {
+    if (value < 0 || value > 1) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: bvh_builder is 0 or 1");
+    ctx->bvh_builder = value;
   } else if (k == "proposal") {
     if (value < 0 || value > 1) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: proposal is 0 or 1");
     ctx->use_proposal = value;
@@ -481,9 +544,62 @@ extern "C" lrt_status lrt_set_tuning(lrt_ctx *ctx, const char *key, int value) {
   return LRT_OK;
 }
 
+extern "C" lrt_status lrt_refit_triangles(lrt_ctx *ctx, const float *vpos, size_t n_vert, size_t v_byte_stride) {
+  if (!ctx) return LRT_ERR_INVALID;
+  if (!ctx->committed) return fail(ctx, LRT_ERR_STATE, "lrt_refit_triangles: no committed scene");
+  Inst &in = ctx->insts[0];
+  Geom &g = ctx->geoms[in.geom];
+  if (g.type != LRT_TYPE_MESH_TRIANGLE)
+    return fail(ctx, LRT_ERR_UNSUPPORTED, "lrt_refit_triangles: the committed geometry is not a triangle mesh");
+  if (!vpos || v_byte_stride < 12 || v_byte_stride % 4 != 0 || n_vert != g.vpos.size() / 4)
+    return fail(ctx, LRT_ERR_INVALID, "lrt_refit_triangles: vertex count or stride differs from the mesh");
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  const size_t sv = v_byte_stride / 4;
+  for (int k = 0; k < 3; k++) { g.bmin[k] = 3.4e38f; g.bmax[k] = -3.4e38f; }
+  for (size_t i = 0; i < n_vert; i++)
+    for (int k = 0; k < 3; k++) {
+      const float v = vpos[i * sv + k];
+      g.vpos[4 * i + k] = v;
+      g.bmin[k] = std::min(g.bmin[k], v);
+      g.bmax[k] = std::max(g.bmax[k], v);
+    }
+  instance_bounds(g, in);
+  for (int k = 0; k < 3; k++) { ctx->dev.inst_bmin[k] = in.bmin[k]; ctx->dev.inst_bmax[k] = in.bmax[k]; }
+  cudaError_t e;
+  if ((e = upload(ctx->d_vpos, reinterpret_cast<const float4 *>(g.vpos.data()), n_vert)) != cudaSuccess)
+    return cuda_fail(ctx, e, "lrt_refit_triangles: upload vertices");
+  if (!ctx->tri_indices_on_device) {
+    if ((e = upload(ctx->d_tri_indices, g.indices.data(), g.indices.size())) != cudaSuccess)
+      return cuda_fail(ctx, e, "lrt_refit_triangles: upload indices");
+    ctx->tri_indices_on_device = true;
+  }
+  const uint32_t nt = uint32_t(g.indices.size() / 3);
+  LRT_CUDA(ctx, ctx->d_boxes6.ensure(6 * size_t(nt)));
+  LRT_CUDA(ctx, gather_triangles_gpu(ctx->d_vpos.p, ctx->d_tri_indices.p, ctx->d_prim_indices.p, nt,
+                                     ctx->d_tri_verts.p, 0));
+  LRT_CUDA(ctx, triangle_boxes_gpu(ctx->d_tri_verts.p, nt, ctx->d_boxes6.p, 0));
+  LRT_CUDA(ctx, refit_bvh_gpu(ctx->d_boxes6.p, false, nullptr, ctx->d_nodes.p, ctx->bvh.level_start, ctx->n_wnodes, 0));
+  LRT_CUDA(ctx, cudaDeviceSynchronize());
+  ctx->bvh_refit = true;
+  ctx->last_launches = 2 + uint32_t(ctx->bvh.level_start.size());
+  return LRT_OK;
+}
+
 extern "C" lrt_status lrt_get_bvh2(lrt_ctx *ctx, const lrt_bvh_pair **pairs, uint32_t *n_pairs) {
   if (!ctx || !pairs || !n_pairs) return LRT_ERR_INVALID;
   if (!ctx->committed) return fail(ctx, LRT_ERR_STATE, "lrt_get_bvh2: no committed scene");
+  if (ctx->bvh_refit)
+    return fail(ctx, LRT_ERR_STATE, "lrt_get_bvh2: the BVH was refit; the fat-pair layout is only made at commit");
+  if (ctx->bvh_on_device && ctx->bvh.pairs.empty()) {   // device-built: fetch once
+    LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+    ctx->bvh.pairs.resize(ctx->n_pairs);
+    ctx->bvh.leaf_start_count.resize(ctx->n_leaf_start_count);
+    LRT_CUDA(ctx, cudaMemcpy(ctx->bvh.pairs.data(), ctx->d_pairs.p, size_t(ctx->n_pairs) * sizeof(lrt_bvh_pair),
+                             cudaMemcpyDeviceToHost));
+    if (ctx->n_leaf_start_count)
+      LRT_CUDA(ctx, cudaMemcpy(ctx->bvh.leaf_start_count.data(), ctx->d_leaf_start_count.p,
+                               size_t(ctx->n_leaf_start_count) * 4, cudaMemcpyDeviceToHost));
+  }
   *pairs = ctx->bvh.pairs.data();
   *n_pairs = uint32_t(ctx->bvh.pairs.size());
   return LRT_OK;

@@ -38,6 +38,7 @@ struct BvhData {
   std::vector<lrt_bvh_pair> pairs;       // reference fat-pair layout
   std::vector<uint32_t> leaf_start_count;  // triangles: per fat-pair leaf
   uint32_t max_depth = 0;                // wide-node depth
+  std::vector<uint32_t> level_start;     // first wide node of each depth (nodes are breadth first)
 };
 
 float sdf_eval(const lrt_sdf_desc &f, float x, float y, float z);
@@ -55,6 +56,29 @@ void build_occupancy(const SbsData &sbs, const std::vector<float> &values_f, uin
 // boxes6: n x (min xyz, max xyz).  boxes=true: one box per leaf, payload = box
 // id; boxes=false: triangles, up to two per leaf, payload = range in `order`.
 lrt_status build_bvh(const float *boxes6, uint32_t n, bool boxes, BvhData &out);
+
+// The same wide BVH layout built on the device (bvh_gpu.cu): a linear BVH over
+// Morton codes, collapsed like build_bvh, one primitive per leaf.  All pointers
+// are device memory: d_boxes6 n x 6 floats; d_wnodes room for max(1, n-1)
+// nodes; optional outputs d_order (n: primitive of each sorted position),
+// d_pairs (max(1, n-1): the reference fat-pair layout) and, for triangles,
+// d_leaf_start_count (n).  Synchronises the stream.
+struct GpuBvhInfo {
+  uint32_t n_wnodes = 0, max_depth = 0;
+  std::vector<uint32_t> level_start;   // first wide node of each depth
+};
+cudaError_t build_bvh_gpu(const float *d_boxes6, uint32_t n, bool boxes, WNode4 *d_wnodes, uint32_t *d_order,
+                          lrt_bvh_pair *d_pairs, uint32_t *d_leaf_start_count, GpuBvhInfo &info, cudaStream_t st);
+// New slot boxes for an existing wide tree (host- or device-built) from new
+// primitive boxes; triangle leaf ranges index d_order (null: identity).
+cudaError_t refit_bvh_gpu(const float *d_boxes6, bool boxes, const uint32_t *d_order, WNode4 *d_wnodes,
+                          const std::vector<uint32_t> &level_start, uint32_t n_wnodes, cudaStream_t st);
+// boxes of the gathered triangles; gather of the triangles' vertices in BVH order
+cudaError_t triangle_boxes_gpu(const float4 *d_tri_verts, uint32_t n, float *d_boxes6, cudaStream_t st);
+cudaError_t gather_triangles_gpu(const float4 *d_vpos, const uint32_t *d_indices, const uint32_t *d_order, uint32_t n,
+                                 float4 *d_tri_verts, cudaStream_t st);
+// exclusive scan of n words on the device; *total (host, optional) receives the sum
+cudaError_t gpu_exclusive_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint64_t *total, cudaStream_t st);
 
 // ------------------------------------------------------------------ device side
 // Scene as the kernels see it (all pointers device memory).

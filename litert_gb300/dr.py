@@ -133,6 +133,10 @@ class MultiRendererDR:
         if s != 0:
             raise lrt.LrtError(s, lrt.lib().lrt_last_error(self._ctx).decode())
 
+    def set_tuning(self, key, value):
+        """lrt_set_tuning on this context ("bvh_builder" 1: SetScene builds the BVH on the device)."""
+        self._chk(lrt.lib().lrt_set_tuning(self._ctx, key.encode(), int(value)))
+
     # ---- scene / reference / preset
     def SetScene(self, hdr, nodes, values, params, pairs=None):
         nodes = np.ascontiguousarray(nodes, np.uint32).reshape(-1, 4)

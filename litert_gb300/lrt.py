@@ -124,6 +124,7 @@ def lib():
                                    C.POINTER(VP)]),
             "lrt_free": (None, [VP]),
             "lrt_set_tuning": (I, [P, C.c_char_p, I]),
+            "lrt_refit_triangles": (I, [P, VP, C.c_size_t, C.c_size_t]),
             "lrt_render_noalloc": (I, [P, VP, U32, VP, VP, VP, VP]),
             "lrt_autotune": (I, [P, VP, U32, U32, C.POINTER(TuningChoice), VP, U32, C.POINTER(U32)]),
             "lrt_render_graph_create": (I, [P, VP, U32, VP, VP, VP, C.POINTER(P)]),
@@ -361,6 +362,11 @@ class Scene:
         self._chk(lib().lrt_add_triangles(self._ctx, _ptr(vpos), vpos.shape[0], stride, _ptr(idx), idx.size,
                                           C.byref(gid)))
         return gid.value
+
+    def refit_triangles(self, vpos):
+        """Move the committed mesh's vertices (same count) and refit its BVH on the device."""
+        vpos = np.ascontiguousarray(vpos, np.float32)
+        self._chk(lib().lrt_refit_triangles(self._ctx, _ptr(vpos), vpos.shape[0], vpos.shape[1] * 4))
 
     def clear_scene(self):
         self._chk(lib().lrt_clear_scene(self._ctx))
