@@ -59,6 +59,17 @@ typedef struct {
   /* Redistance (:2122-2330) of the dense distance grid every redistancing_interval
    * iterations when enabled (defaults off, 1); needs a cubic create_grid_sbs set */
   uint32_t redistancing_enable, redistancing_interval;
+  /* dr_border_sampling (DR_common.h:123-124): 0 random (CastBorderRay), 1 SVM
+   * (CastBorderRaySVM, :1651-1931: a quarter of border_spp classifies the pixel's
+   * sub-samples by depth, a linear SVM fits the silhouette line and the rest
+   * sample a stripe around it; border_spp <= 1024).  The reference draws the
+   * stripe points from the process-wide rand(); here they come from the same
+   * per-sample hash as the other samples, so results are reproducible. */
+  uint32_t border_sampling;
+  /* dr_raycasting_mask (DR_common.h:86-87): 1 casts a view's interior rays only
+   * where its previous render hit (:1097-1100, :443-448); the masks start full
+   * at lrt_dr_set_reference, lrt_dr_set_scene and lrt_dr_set_preset. */
+  uint32_t raycasting_mask;
 } lrt_dr_preset;
 
 /* getDefaultPresetDR (diff_render/MultiRendererDR.h:12-66) with the colour+geometry
@@ -105,7 +116,8 @@ lrt_status lrt_dr_optimize(lrt_ctx *ctx, uint32_t first_iter, uint32_t iteration
  * LRT_DR_IMAGE (view's W*H float4 = getLastImage), LRT_DR_DEPTH (W*H floats,
  * depth-discontinuity thresholds), LRT_DR_BORDER (W*H bytes, border-pixel mask),
  * LRT_DR_ADAM (2*n_params floats: first then second moments).  bytes must match. */
-enum { LRT_DR_PARAMS = 0, LRT_DR_GRAD = 1, LRT_DR_IMAGE = 2, LRT_DR_DEPTH = 3, LRT_DR_BORDER = 4, LRT_DR_ADAM = 5 };
+enum { LRT_DR_PARAMS = 0, LRT_DR_GRAD = 1, LRT_DR_IMAGE = 2, LRT_DR_DEPTH = 3, LRT_DR_BORDER = 4, LRT_DR_ADAM = 5,
+       LRT_DR_CAST_MASK = 6 /* view's W*H bytes of ray-casting mask (raycasting_mask on) */ };
 lrt_status lrt_dr_get(lrt_ctx *ctx, uint32_t what, uint32_t view, void *out, uint64_t bytes);
 
 /* dr::BVHDR::RayQuery_NearestHitWithGrad (diff_render/BVH2DR.cpp:12-102) on n rays

@@ -828,7 +828,9 @@ __global__ void __launch_bounds__(128) dr_pixel_kernel(DevScene s, DevPreset p, 
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint32_t x = blockIdx.x * 16 + (w & 1) * 8 + (lane & 7);
   const uint32_t y = blockIdx.y * 8 + (w >> 1) * 4 + (lane >> 3);
-  const bool in = x < v.width && y < v.height;
+  // a pixel outside the ray-casting mask is not cast (CastRayWithGrad :1097-1100):
+  // no image, depth, loss or gradient; its mask entry stays 0
+  const bool in = x < v.width && y < v.height && (!v.cast_mask || v.cast_mask[(size_t)y * v.width + x]);
   const uint32_t spp = p.spp;
   float3 res = f3(0, 0, 0);
   uint32_t hit_count = 0;
@@ -857,6 +859,7 @@ __global__ void __launch_bounds__(128) dr_pixel_kernel(DevScene s, DevPreset p, 
   double loss = 0.0;
   if (in) {
     const size_t px = (size_t)y * v.width + x;
+    if (v.cast_mask) v.cast_mask[px] = hit_count > 0 ? 1 : 0;   // process_mask -> masks[image] (:443-448, :1164-1167)
     const float4 cm = make_float4(res.x, res.y, res.z, float(hit_count) / float(spp));
     v.img[px] = cm;
     v.depth[px] = hit_count == 0 ? 0.0f : t_threshold(samples, hit_count, 1e9f, spp - hit_count);
@@ -941,8 +944,181 @@ __device__ __forceinline__ float3 color_plain(const DevPreset &p, float t, float
   return color_grad(p, t, c, n, a, b);
 }
 
-// CastBorderRay + CalculateBorderRayDerivatives (:1319-1499): a warp per (border
-// pixel, 32 of its border_spp samples), grid-stride over the compacted list
+// SVM_fit (:1518-1546) on rows (x, y, 1) * label, scaled in place by etha
+__device__ float4 svm_fit(float *xs, float *ys, float *zs, uint32_t N) {
+  const float etha = 0.01f, alpha = 0.1f;
+  const int epochs = 200;
+  for (uint32_t i = 0; i < N; i++) { xs[i] = xs[i] * etha; ys[i] = ys[i] * etha; zs[i] = zs[i] * etha; }
+  uint32_t errors = N;
+  float w0 = -1.0f, w1 = 1.0f, w2 = 0.0f;
+  const float mult = 1.0f - etha * alpha / float(epochs);
+  for (int e = 0; e < epochs && errors > 0; e++) {
+    errors = 0;
+    for (uint32_t j = 0; j < N; j++) {
+      const float margin = w0 * xs[j] + w1 * ys[j] + w2 * zs[j];
+      w0 = w0 * mult; w1 = w1 * mult; w2 = w2 * mult;
+      if (margin < 0) {
+        w0 = w0 + xs[j]; w1 = w1 + ys[j]; w2 = w2 + zs[j];
+        errors++;
+      }
+    }
+  }
+  return make_float4(w0, w1, w2, float(errors) / float(N));
+}
+
+__device__ __forceinline__ uint32_t out_code(float x, float y) {   // ComputeOutCode (:1552-1578)
+  uint32_t c = 0;
+  if (x < 0.0f) c |= 1u; else if (x > 1.0f) c |= 2u;
+  if (y < 0.0f) c |= 4u; else if (y > 1.0f) c |= 8u;
+  return c;
+}
+
+// CohenSutherlandLineClip (:1580-1649) against [0,1]^2.  Each pass moves one end
+// onto a window edge, after which that end's code loses the bit it was moved
+// for; four passes settle every segment, eight bound the loop.
+__device__ bool line_clip(float &x0, float &y0, float &x1, float &y1) {
+  uint32_t c0 = out_code(x0, y0), c1 = out_code(x1, y1);
+  for (int it = 0; it < 8; it++) {
+    if (!(c0 | c1)) return true;
+    if (c0 & c1) return false;
+    float x = -1, y = -1;
+    const uint32_t co = c1 > c0 ? c1 : c0;
+    if (co & 8u) { x = x0 + (x1 - x0) * (1.0f - y0) / (y1 - y0); y = 1.0f; }
+    else if (co & 4u) { x = x0 + (x1 - x0) * (0.0f - y0) / (y1 - y0); y = 0.0f; }
+    else if (co & 2u) { y = y0 + (y1 - y0) * (1.0f - x0) / (x1 - x0); x = 1.0f; }
+    else if (co & 1u) { y = y0 + (y1 - y0) * (0.0f - x0) / (x1 - x0); x = 0.0f; }
+    if (co == c0) { x0 = x; y0 = y; c0 = out_code(x0, y0); }
+    else { x1 = x; y1 = y; c1 = out_code(x1, y1); }
+  }
+  return false;
+}
+
+__device__ __forceinline__ float2 w2s(const float pv[16], float3 q) {   // TransformWorldToScreenSpace (:1296-1301)
+  float r[4];
+  const float q4[4] = {q.x, q.y, q.z, 1.0f};
+  mat_vec4(pv, q4, r);
+  return make_float2(0.5f * (r[0] / r[3] + 1.0f), 1.0f - 0.5f * (r[1] / r[3] + 1.0f));
+}
+
+// The SVM stage of CastBorderRaySVM (:1651-1816) for every border pixel: a warp
+// casts the svm_spp classification rays, then one lane labels them by the depth
+// threshold, fits the SVM and derives the pixel's sampling line.
+__global__ void __launch_bounds__(128) dr_svm_kernel(DevScene s, DevPreset p, DevView v) {
+  __shared__ float sh_t[4][kMaxSvm], sh_x[4][kMaxSvm], sh_y[4][kMaxSvm], sh_z[4][kMaxSvm];
+  const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+  float *ts = sh_t[wl], *xs = sh_x[wl], *ys = sh_y[wl], *zs = sh_z[wl];
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t nb = *v.border_count;
+  const uint32_t W = v.width, H = v.height, N = p.svm_spp, sq = p.svm_sqrt;
+  const float isq = 1.0f / float(sq);
+  for (uint32_t b = warp; b < nb; b += n_warps) {
+    const uint32_t pix = v.border_list[b];
+    const uint32_t x = pix % W, y = pix / W;
+    for (uint32_t k = lane; k < N; k += 32) {
+      const float2 rnd = rand2(x, y, k, p.seed);
+      const float dx = isq * (float(k / sq) + rnd.x), dy = isq * (float(k % sq) + rnd.y);
+      float3 P, D;
+      eye_ray(x, y, W, H, dx, dy, v.proj_inv, v.wv_inv, P, D);
+      HitRec hr;
+      query<false>(s, P, D, 1e9f, hr, nullptr);
+      ts[k] = hr.t;
+      xs[k] = dx;
+      ys[k] = dy;
+    }
+    __syncwarp();
+    if (lane == 0) {
+      SvmLine L{};
+      // closest classification hit (first of equal t), from its recomputed ray
+      float closest_t = 1e6f;
+      uint32_t ck = N;
+      for (uint32_t k = 0; k < N; k++)
+        if (ts[k] < closest_t) { closest_t = ts[k]; ck = k; }
+      float3 closest = f3(1e6f, 1e6f, 1e6f);
+      if (ck < N) {
+        float3 P, D;
+        eye_ray(x, y, W, H, xs[ck], ys[ck], v.proj_inv, v.wv_inv, P, D);
+        closest = add(P, scl(ts[ck], D));
+      }
+      const float thr = t_threshold(ts, N, 0.0f, 0u);
+      uint32_t type0 = 0;
+      for (uint32_t k = 0; k < N; k++) {
+        const float lab = ts[k] <= thr ? -1.0f : 1.0f;
+        type0 += ts[k] <= thr ? 1u : 0u;
+        xs[k] *= lab; ys[k] *= lab; zs[k] = lab;   // (x, y, 1) * label
+      }
+      bool keep = !(type0 == N || type0 == 0);
+      if (keep) {
+        const float4 Wt = svm_fit(xs, ys, zs, N);
+        const float err = Wt.w;
+        const float f0 = float(type0) / float(N);
+        const float rare = mn(f0, 1.0f - f0);
+        float p0x = 0, p0y = 0, p1x = 0, p1y = 0, rx = 0, ry = 0, nx = 0, ny = 0, radius = 0, area = 0;
+        bool force = false;
+        if (err > 0.05f || 2 * err > rare) {
+          force = true;
+          area = 1.0f;
+        } else {
+          if (fabsf(Wt.y) > 1e-6f && fabsf(Wt.x) > 1e-6f) {
+            p0x = 0.0f; p0y = -Wt.z / Wt.y;
+            p1x = 1.0f; p1y = (-Wt.z - Wt.x) / Wt.y;
+            const float rY = p1y - p0y;
+            if (p0y < -1e-6f || p0y > 1 + 1e-6f) {
+              const float k1 = -p0y / rY, k2 = (1 - p0y) / rY, k = (fabsf(k1) < fabsf(k2)) ? k1 : k2;
+              p0x = p0x + k * 1.0f; p0y = p0y + k * rY;
+            }
+            if (p1y < -1e-6f || p1y > 1 + 1e-6f) {
+              const float k1 = -p1y / rY, k2 = (1 - p1y) / rY, k = (fabsf(k1) < fabsf(k2)) ? k1 : k2;
+              p1x = p1x + k * 1.0f; p1y = p1y + k * rY;
+            }
+          } else if (fabsf(Wt.x) > 1e-6f) {
+            p0x = -Wt.z / Wt.x; p0y = 0.0f;
+            p1x = -Wt.z / Wt.x; p1y = 1.0f;
+          } else {
+            force = true;
+          }
+          keep = line_clip(p0x, p0y, p1x, p1y);
+          if (keep) {
+            const float2 a = w2s(v.pv, closest);
+            const float2 c = w2s(v.pv, add(closest, scl(p.relax_eps, f3(v.up[0], v.up[1], v.up[2]))));
+            const float ddx = c.x - a.x, ddy = c.y - a.y;
+            const float thick = sqrtf(ddx * ddx + ddy * ddy) * float(W > H ? W : H);
+            radius = mx(0.15f, thick) + 2.0f * err;
+            rx = p1x - p0x; ry = p1y - p0y;
+            float l = sqrtf(rx * rx + ry * ry);
+            const float ux = rx / l, uy = ry / l;
+            p0x = p0x - radius * ux; p0y = p0y - radius * uy;
+            p1x = p1x + radius * ux; p1y = p1y + radius * uy;
+            rx = p1x - p0x; ry = p1y - p0y;
+            l = sqrtf(ry * ry + rx * rx);
+            nx = -ry / l; ny = rx / l;
+            area = 2 * radius * sqrtf(rx * rx + ry * ry);
+            keep = force || !(area < 0.005f);
+          }
+        }
+        if (keep) {
+          const float area_mult = mn(1.0f, 0.05f + 2.0f * area);
+          uint32_t cnt = (uint32_t)(area_mult * float(p.border_spp - N));
+          if (cnt < 1u) cnt = 1u;
+          L.count = cnt;
+          L.force = force ? 1u : 0u;
+          L.p0x = p0x; L.p0y = p0y; L.rx = rx; L.ry = ry; L.nx = nx; L.ny = ny;
+          L.radius = radius;
+          L.pdf = force ? 1.0f / float(cnt) : area / float(cnt);
+        }
+      }
+      v.svm[b] = L;
+    }
+    __syncwarp();
+  }
+}
+
+// CastBorderRay / CastBorderRaySVM + CalculateBorderRayDerivatives
+// (:1319-1499, :1816-1869): a warp per (border pixel, 32 of its samples),
+// grid-stride over the compacted list.  SVM: the samples of the pixel's line
+// (dr_svm_kernel), sample index svm_spp + j; the reference's urand() stream is
+// replaced by rand2 of the sample index (the oracle draws the same).
+template <bool SVM>
 __global__ void __launch_bounds__(128, 4) dr_border_kernel(DevScene s, DevPreset p, DevView v) {
   __shared__ float ws_all[4][32];
   float *ws = ws_all[threadIdx.x >> 5];
@@ -951,12 +1127,13 @@ __global__ void __launch_bounds__(128, 4) dr_border_kernel(DevScene s, DevPreset
   const uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
   const uint32_t nb = *v.border_count;
   const uint32_t W = v.width, H = v.height;
-  const float pdf = 1.0f / float(p.border_spp);
   // work item = (border pixel, chunk of 32 samples): a pixel's samples spread over
   // several warps so that the few border pixels still fill the GPU
-  const uint32_t chunks = (p.border_spp + 31) / 32;
+  const uint32_t n_max = SVM ? max(1u, p.border_spp - p.svm_spp) : p.border_spp;   // a line's count is at most this
+  const uint32_t chunks = (n_max + 31) / 32;
   for (uint32_t item = warp; item < nb * chunks; item += n_warps) {
-    const uint32_t pix = v.border_list[item / chunks];
+    const uint32_t bi = item / chunks;
+    const uint32_t pix = v.border_list[bi];
     const uint32_t x = pix % W, y = pix / W;
     {
       const uint32_t sid = (item % chunks) * 32 + lane;
@@ -964,7 +1141,24 @@ __global__ void __launch_bounds__(128, 4) dr_border_kernel(DevScene s, DevPreset
       Relax rl;
       bool br = false;
       float3 P = f3(0, 0, 0), D = f3(0, 0, 0);
-      if (sid < p.border_spp) {
+      float pdf = 1.0f / float(p.border_spp);
+      if (SVM) {
+        const SvmLine L = v.svm[bi];
+        pdf = L.pdf;
+        if (sid < L.count) {
+          const float2 u = rand2(x, y, p.svm_spp + sid, p.seed);
+          float2 d = u;
+          if (!L.force) {
+            const float a = u.x, br_ = (u.y * 2.0f - 1.0f) * L.radius;
+            d = make_float2((L.p0x + a * L.rx) + br_ * L.nx, (L.p0y + a * L.ry) + br_ * L.ny);
+          }
+          if (d.x > 0 && d.x < 1 && d.y > 0 && d.y < 1) {
+            eye_ray(x, y, W, H, d.x, d.y, v.proj_inv, v.wv_inv, P, D);
+            query<true>(s, P, D, 1e9f, hr, &rl);
+            br = rl.sdf < p.relax_eps;
+          }
+        }
+      } else if (sid < p.border_spp) {
         const float2 d = rand2(x, y, sid, p.seed);
         eye_ray(x, y, W, H, d.x, d.y, v.proj_inv, v.wv_inv, P, D);
         query<true>(s, P, D, 1e9f, hr, &rl);
@@ -1144,7 +1338,17 @@ void launch_border(const DevScene &s, const DevPreset &p, const DevView &v, uint
   const uint32_t cap = (uint32_t)n_sm * 16;
   if (blocks > cap) blocks = cap;
   if (blocks == 0) blocks = 1;
-  dr_border_kernel<<<blocks, 128, 0, st>>>(s, p, v);
+  if (p.svm) dr_border_kernel<true><<<blocks, 128, 0, st>>>(s, p, v);
+  else dr_border_kernel<false><<<blocks, 128, 0, st>>>(s, p, v);
+}
+
+void launch_svm_lines(const DevScene &s, const DevPreset &p, const DevView &v, uint32_t max_pixels, int n_sm,
+                      cudaStream_t st) {
+  uint32_t blocks = (max_pixels + 3) / 4;   // a warp per border pixel, grid-stride beyond the cap
+  const uint32_t cap = (uint32_t)n_sm * 8;
+  if (blocks > cap) blocks = cap;
+  if (blocks == 0) blocks = 1;
+  dr_svm_kernel<<<blocks, 128, 0, st>>>(s, p, v);
 }
 
 // Regularization (diff_render/MultiRendererDR.cpp:1933-2055): one thread per brick

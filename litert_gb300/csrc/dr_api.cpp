@@ -35,6 +35,8 @@ struct DrState {
   DevBuf<float4> d_ref, d_img;
   DevBuf<float> d_depth;
   DevBuf<uint8_t> d_border_mask;
+  DevBuf<uint8_t> d_cast_mask;  // ray-casting masks of all views (raycasting_mask)
+  DevBuf<drk::SvmLine> d_svm;   // SVM sampling lines of all views' border lists
   DevBuf<uint32_t> d_border_list, d_border_count, d_status;
   DevBuf<double> d_loss;
   lrt_dr_preset preset{};
@@ -59,6 +61,8 @@ void dr_state_free(DrState *st) {
   st->d_img.release();
   st->d_depth.release();
   st->d_border_mask.release();
+  st->d_cast_mask.release();
+  st->d_svm.release();
   st->d_border_list.release();
   st->d_border_count.release();
   st->d_status.release();
@@ -159,6 +163,13 @@ drk::DevPreset dev_preset(const DrState &st) {
   }
   d.agg = p.warp_aggregate;
   d.flags = pixel_flags(p);
+  d.svm = p.border_sampling;
+  if (d.svm) {   // svm_spp = max(1, 0.25 border_spp) rounded down to a square (:1675-1678)
+    uint32_t n = (uint32_t)(0.25f * float(p.border_spp));
+    if (n < 1u) n = 1u;
+    d.svm_sqrt = (uint32_t)std::sqrt(double(n));
+    d.svm_spp = d.svm_sqrt * d.svm_sqrt;
+  }
   return d;
 }
 
@@ -177,6 +188,9 @@ drk::DevView dev_view(DrState &st, uint32_t v) {
   d.border_list = st.d_border_list.p + st.off[v];
   d.border_count = st.d_border_count.p + v;
   d.loss = st.d_loss.p + v;
+  d.cast_mask = st.preset.raycasting_mask ? st.d_cast_mask.p + st.off[v] : nullptr;
+  d.svm = st.preset.border_sampling ? st.d_svm.p + st.off[v] : nullptr;
+  for (int k = 0; k < 3; k++) d.up[k] = lv.world_view[4 + k];
   return d;
 }
 
@@ -194,10 +208,28 @@ lrt_status render_view(lrt_ctx *ctx, uint32_t v, cudaStream_t stream) {
   drk::launch_border_detect(p, dv, stream);
   st.last_launches += 2;
   if ((st.preset.reconstruction_flags & LRT_DR_RECON_GEOMETRY) && st.preset.border_spp > 0) {
+    if (p.svm) {
+      drk::launch_svm_lines(s, p, dv, W * H, ctx->num_sms, stream);
+      st.last_launches += 1;
+    }
     drk::launch_border(s, p, dv, W * H, ctx->num_sms, stream);
     st.last_launches += 1;
   }
   LRT_CUDA(ctx, cudaGetLastError());
+  return LRT_OK;
+}
+
+// Buffers of the optional DR features for the current views; the ray-casting
+// masks restart full (OptimizeFixedStructure :369-383).
+lrt_status prepare_extras(lrt_ctx *ctx) {
+  DrState &st = *ctx->dr;
+  if (!st.has_ref || st.n_pix == 0) return LRT_OK;
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  if (st.preset.raycasting_mask) {
+    LRT_CUDA(ctx, st.d_cast_mask.ensure(st.n_pix));
+    LRT_CUDA(ctx, cudaMemset(st.d_cast_mask.p, 1, st.n_pix));
+  }
+  if (st.preset.border_sampling) LRT_CUDA(ctx, st.d_svm.ensure(st.n_pix));
   return LRT_OK;
 }
 
@@ -347,7 +379,7 @@ extern "C" lrt_status lrt_dr_set_scene(lrt_ctx *ctx, const lrt_sbs_header *hdr, 
   LRT_CUDA(ctx, st.d_bounds.ensure(n_nodes));
   LRT_CUDA(ctx, st.d_bvals.ensure(size_t(n_nodes) * v3));
   st.has_scene = true;
-  return LRT_OK;
+  return prepare_extras(ctx);
 }
 
 extern "C" lrt_status lrt_dr_get_bvh2(lrt_ctx *ctx, const lrt_bvh_pair **pairs, uint32_t *n_pairs) {
@@ -390,7 +422,7 @@ extern "C" lrt_status lrt_dr_set_reference(lrt_ctx *ctx, uint32_t n_views, const
   LRT_CUDA(ctx, cudaMemset(st.d_loss.p, 0, n_views * sizeof(double)));
   if (st.d_adam.p) LRT_CUDA(ctx, cudaMemset(st.d_adam.p, 0, sizeof(float) * 2 * size_t(st.n_params)));
   st.has_ref = true;
-  return LRT_OK;
+  return prepare_extras(ctx);
 }
 
 extern "C" lrt_status lrt_dr_set_preset(lrt_ctx *ctx, const lrt_dr_preset *preset) {
@@ -405,8 +437,12 @@ extern "C" lrt_status lrt_dr_set_preset(lrt_ctx *ctx, const lrt_dr_preset *prese
     if (preset->lights[i].type != LRT_DR_LIGHT_DIRECT && preset->lights[i].type != LRT_DR_LIGHT_AMBIENT)
       return fail(ctx, LRT_ERR_UNSUPPORTED, "only direct and ambient lights");
   if (!(preset->border_relax_eps > 0.0f)) return fail(ctx, LRT_ERR_INVALID, "border_relax_eps must be > 0");
+  if (preset->border_sampling > 1 || preset->raycasting_mask > 1)
+    return fail(ctx, LRT_ERR_INVALID, "border_sampling and raycasting_mask are 0 or 1");
+  if (preset->border_sampling == 1 && preset->border_spp > 4 * drk::kMaxSvm)
+    return fail(ctx, LRT_ERR_UNSUPPORTED, "SVM border sampling takes border_spp <= 1024");
   ctx->dr->preset = *preset;
-  return LRT_OK;
+  return prepare_extras(ctx);
 }
 
 extern "C" lrt_status lrt_dr_set_params(lrt_ctx *ctx, const float *params, uint32_t n_params) {
@@ -525,7 +561,11 @@ extern "C" lrt_status lrt_dr_get(lrt_ctx *ctx, uint32_t what, uint32_t view, voi
     if (what == LRT_DR_IMAGE) { src = st.d_img.p + st.off[view]; want = 16 * px; }
     else if (what == LRT_DR_DEPTH) { src = st.d_depth.p + st.off[view]; want = 4 * px; }
     else if (what == LRT_DR_BORDER) { src = st.d_border_mask.p + st.off[view]; want = px; }
-    else return fail(ctx, LRT_ERR_INVALID, "unknown item");
+    else if (what == LRT_DR_CAST_MASK) {
+      if (!st.preset.raycasting_mask || !st.d_cast_mask.p) return fail(ctx, LRT_ERR_STATE, "raycasting_mask is off");
+      src = st.d_cast_mask.p + st.off[view];
+      want = px;
+    } else return fail(ctx, LRT_ERR_INVALID, "unknown item");
   }
   if (bytes != want) return fail(ctx, LRT_ERR_INVALID, "output size mismatch");
   LRT_CUDA(ctx, cudaMemcpy(out, src, bytes, cudaMemcpyDeviceToHost));

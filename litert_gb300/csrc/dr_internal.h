@@ -40,7 +40,18 @@ struct DevPreset {
   float light_dir[4][3], light_col[4][3];
   uint32_t agg;              // 1: warp-aggregated gradient atomics, 0: one atomic per contribution
   uint32_t flags;            // DR_RAY_FLAG_* of CastRayWithGrad for this preset
+  uint32_t svm;              // border sampling: 0 random (CastBorderRay), 1 SVM (CastBorderRaySVM)
+  uint32_t svm_spp, svm_sqrt;   // the SVM stage's ray count (a square) and its side
 };
+
+// Sampling line of one border pixel from the SVM stage of CastBorderRaySVM
+// (diff_render/MultiRendererDR.cpp:1651-1816): count border samples (0: none)
+// at p0 + u r + v radius n (force: anywhere in the pixel), each weighted by pdf.
+struct SvmLine {
+  uint32_t count, force, pad0, pad1;
+  float p0x, p0y, rx, ry, nx, ny, radius, pdf;
+};
+constexpr uint32_t kMaxSvm = 256;   // SVM-stage rays per border pixel (border_spp <= 1024)
 
 struct DevView {
   uint32_t width, height;
@@ -52,12 +63,18 @@ struct DevView {
   uint32_t *border_list;
   uint32_t *border_count;
   double *loss;              // sum of pixel losses
+  uint8_t *cast_mask;        // ray-casting mask (masks[image]), null when off
+  SvmLine *svm;              // per border-list entry (SVM border sampling)
+  float up[3];               // row 1 of the world-view matrix
 };
 
 void launch_pixels(const DevScene &s, const DevPreset &p, const DevView &v, cudaStream_t st);
 void launch_border_detect(const DevPreset &p, const DevView &v, cudaStream_t st);
 void launch_border(const DevScene &s, const DevPreset &p, const DevView &v, uint32_t max_pixels, int n_sm,
                    cudaStream_t st);
+// the SVM stage of CastBorderRaySVM for every border pixel, into v.svm
+void launch_svm_lines(const DevScene &s, const DevPreset &p, const DevView &v, uint32_t max_pixels, int n_sm,
+                      cudaStream_t st);
 // Regularization (diff_render/MultiRendererDR.cpp:1933-2055) into s.grad
 void launch_regularize(const DevScene &s, uint32_t n_nodes, float lambda, float power, cudaStream_t st);
 // Redistance (:2122-2330) of the dense n^3 grid at the start of dist, in place

@@ -17,7 +17,7 @@ from . import lrt
 RENDER_DIFFUSE, RENDER_LAMBERT, RENDER_MASK, RENDER_LINEAR_DEPTH, RENDER_NORMAL = 0, 1, 2, 3, 4
 RECON_COLOR, RECON_GEOMETRY = 1, 2
 LIGHT_DIRECT, LIGHT_AMBIENT = 0, 2
-GET_PARAMS, GET_GRAD, GET_IMAGE, GET_DEPTH, GET_BORDER, GET_ADAM = 0, 1, 2, 3, 4, 5
+GET_PARAMS, GET_GRAD, GET_IMAGE, GET_DEPTH, GET_BORDER, GET_ADAM, GET_CAST_MASK = 0, 1, 2, 3, 4, 5, 6
 
 
 class Light(C.Structure):
@@ -31,7 +31,8 @@ class DrPreset(C.Structure):
                 ("lights", Light * 4), ("opt_lr", C.c_float), ("opt_beta_1", C.c_float), ("opt_beta_2", C.c_float),
                 ("opt_eps", C.c_float), ("accumulate_batch", C.c_uint32), ("warp_aggregate", C.c_uint32),
                 ("reg_function", C.c_uint32), ("reg_lambda", C.c_float), ("reg_power", C.c_float),
-                ("redistancing_enable", C.c_uint32), ("redistancing_interval", C.c_uint32)]
+                ("redistancing_enable", C.c_uint32), ("redistancing_interval", C.c_uint32),
+                ("border_sampling", C.c_uint32), ("raycasting_mask", C.c_uint32)]
 
 
 _bound = False
@@ -207,7 +208,7 @@ class MultiRendererDR:
         else:
             w, h = self.views[view][0], self.views[view][1]
             out = {GET_IMAGE: np.zeros((h * w, 4), np.float32), GET_DEPTH: np.zeros(h * w, np.float32),
-                   GET_BORDER: np.zeros(h * w, np.uint8)}[what]
+                   GET_BORDER: np.zeros(h * w, np.uint8), GET_CAST_MASK: np.zeros(h * w, np.uint8)}[what]
         self._chk(_lib().lrt_dr_get(self._ctx, what, view, lrt._ptr(out), out.nbytes))
         return out
 

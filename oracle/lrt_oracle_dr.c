@@ -249,6 +249,8 @@ typedef struct {
 static float cast_ray_grad(const rctx *r, uint32_t x, uint32_t y, float *g) {
   const orc_dr_preset *p = r->p;
   const uint32_t W = r->v->width, spp = p->spp;
+  uint8_t *mask = p->raycasting_mask ? r->v->cast_mask : NULL;
+  if (mask && !mask[(size_t)y * W + x]) return 0.0f;   /* masked pixel: not cast (:1097-1100) */
   ctx_f cx = {r->s, r->P};
   const uint32_t flags = pixel_flags(p);
   f3v res = mk_f(0, 0, 0);
@@ -290,6 +292,7 @@ static float cast_ray_grad(const rctx *r, uint32_t x, uint32_t y, float *g) {
     hit_count++;
   }
   const size_t px = (size_t)y * W + x;
+  if (mask) mask[px] = hit_count > 0 ? 1 : 0;           /* process_mask, copied to masks[image] (:443-448, :1164-1167) */
   float cm[4] = {res.x, res.y, res.z, (float)hit_count / (float)spp};
   memcpy(r->img + 4 * px, cm, 16);
   r->depth[px] = hit_count == 0 ? 0.0f : t_threshold(samples, hit_count, 1e9f, spp - hit_count);
@@ -368,6 +371,195 @@ static void cast_border_ray(const rctx *r, uint32_t x, uint32_t y, float *g) {
   free(pl);
 }
 
+/* ---- SVM border sampling, CastBorderRaySVM (:1651-1931) ---- */
+void orc_dr_svm_fit(float *X, uint32_t N, float W[4]) {   /* SVM_fit (:1518-1546) */
+  const float etha = 0.01f, alpha = 0.1f;
+  const int epochs = 200;
+  for (uint32_t i = 0; i < 3 * N; i++) X[i] = X[i] * etha;
+  uint32_t errors = N;
+  float w0 = -1.0f, w1 = 1.0f, w2 = 0.0f;
+  const float mult = 1.0f - etha * alpha / (float)epochs;
+  for (int e = 0; e < epochs && errors > 0; e++) {
+    errors = 0;
+    for (uint32_t j = 0; j < N; j++) {
+      const float margin = w0 * X[3 * j] + w1 * X[3 * j + 1] + w2 * X[3 * j + 2];
+      w0 = w0 * mult; w1 = w1 * mult; w2 = w2 * mult;
+      if (margin < 0) {
+        w0 = w0 + X[3 * j]; w1 = w1 + X[3 * j + 1]; w2 = w2 + X[3 * j + 2];
+        errors++;
+      }
+    }
+  }
+  W[0] = w0; W[1] = w1; W[2] = w2; W[3] = (float)errors / (float)N;
+}
+
+static uint32_t out_code(float x, float y) {   /* ComputeOutCode (:1552-1578), window [0,1]^2 */
+  uint32_t c = 0;
+  if (x < 0.0f) c |= 1u; else if (x > 1.0f) c |= 2u;
+  if (y < 0.0f) c |= 4u; else if (y > 1.0f) c |= 8u;
+  return c;
+}
+
+/* CohenSutherlandLineClip (:1580-1649).  Each pass moves one end onto a window
+ * edge; four passes settle a segment, and the loop is bounded at eight (a
+ * segment still unsettled then is rejected; the GPU kernel uses the same bound). */
+int orc_dr_line_clip(float *x0, float *y0, float *x1, float *y1) {
+  uint32_t c0 = out_code(*x0, *y0), c1 = out_code(*x1, *y1);
+  for (int it = 0; it < 8; it++) {
+    if (!(c0 | c1)) return 1;
+    if (c0 & c1) return 0;
+    float x = -1, y = -1;
+    const uint32_t co = c1 > c0 ? c1 : c0;
+    if (co & 8u) { x = *x0 + (*x1 - *x0) * (1.0f - *y0) / (*y1 - *y0); y = 1.0f; }
+    else if (co & 4u) { x = *x0 + (*x1 - *x0) * (0.0f - *y0) / (*y1 - *y0); y = 0.0f; }
+    else if (co & 2u) { y = *y0 + (*y1 - *y0) * (1.0f - *x0) / (*x1 - *x0); x = 1.0f; }
+    else if (co & 1u) { y = *y0 + (*y1 - *y0) * (0.0f - *x0) / (*x1 - *x0); x = 0.0f; }
+    if (co == c0) { *x0 = x; *y0 = y; c0 = out_code(*x0, *y0); }
+    else { *x1 = x; *y1 = y; c1 = out_code(*x1, *y1); }
+  }
+  return 0;
+}
+
+/* The SVM stage of CastBorderRaySVM for one border pixel: the sampling line, or
+ * count 0 when the pixel has no border to integrate.  The reference draws the
+ * stripe positions from the process-wide rand() (urand, :36-39), whose sequence
+ * depends on OpenMP scheduling; here both uniforms come from rand2 of the sample
+ * index, so every implementation draws the same stripe points. */
+void orc_dr_svm_line(const orc_dr_scene *s, const float *params, const orc_dr_preset *p, const orc_dr_view *v,
+                     uint32_t x, uint32_t y, orc_dr_svm_line_t *L) {
+  const float min_sample_radius = 0.15f, sample_radius_mult = 2.0f, max_error_rate = 0.05f;
+  const float min_stripe_area = 0.005f, svm_samples_budget = 0.25f;
+  const float relax_eps = p->border_relax_eps;
+  memset(L, 0, sizeof(*L));
+  unsigned svm_spp = (unsigned)(svm_samples_budget * (float)p->border_spp);
+  if (svm_spp < 1u) svm_spp = 1u;
+  const uint32_t sq = (uint32_t)sqrt((double)svm_spp);
+  const float isq = 1.0f / (float)sq;
+  svm_spp = sq * sq;
+  L->svm_spp = svm_spp;
+  ctx_f cx = {s, params};
+  payload_f *pl = (payload_f *)malloc(sizeof(payload_f));
+  float *X = (float *)malloc(sizeof(float) * 3 * svm_spp), *ts = (float *)malloc(sizeof(float) * svm_spp);
+  f3v closest = mk_f(1e6f, 1e6f, 1e6f);
+  float closest_t = 1e6f;
+  for (uint32_t k = 0; k < svm_spp; k++) {
+    float rx, ry, pos[4], dir[4];
+    rand2(x, y, k, p->seed, &rx, &ry);
+    const float dx = isq * ((float)(k / sq) + rx), dy = isq * ((float)(k % sq) + ry);
+    orc_eye_ray(x, y, v->width, v->height, dx, dy, v->proj_inv, v->wv_inv, pos, dir);
+    hitdr_f h = query_f(&cx, 0u, pos, dir, pl);
+    X[3 * k] = dx; X[3 * k + 1] = dy; X[3 * k + 2] = 1.0f;
+    ts[k] = h.t;
+    if (h.t < closest_t) {
+      closest_t = h.t;
+      closest = add_f(mk_f(pos[0], pos[1], pos[2]), scl_f(h.t, mk_f(dir[0], dir[1], dir[2])));
+    }
+  }
+  const float thr = t_threshold(ts, svm_spp, 0.0f, 0u);
+  unsigned type0 = 0;
+  for (uint32_t k = 0; k < svm_spp; k++) {
+    const float lab = ts[k] <= thr ? -1.0f : 1.0f;
+    type0 += ts[k] <= thr ? 1u : 0u;
+    X[3 * k] *= lab; X[3 * k + 1] *= lab; X[3 * k + 2] *= lab;
+  }
+  if (type0 == svm_spp || type0 == 0) goto done;
+  {
+    float W[4];
+    orc_dr_svm_fit(X, svm_spp, W);
+    const float err = W[3];
+    const float f0 = (float)type0 / (float)svm_spp;
+    const float rare = mn_f(f0, 1.0f - f0);
+    float p0x = 0, p0y = 0, p1x = 0, p1y = 0, rx = 0, ry = 0, nx = 0, ny = 0, radius = 0, area = 0;
+    int force = 0;
+    if (err > max_error_rate || 2 * err > rare) {
+      force = 1;
+      area = 1.0f;
+    } else {
+      if (fabsf(W[1]) > 1e-6f && fabsf(W[0]) > 1e-6f) {
+        p0x = 0.0f; p0y = -W[2] / W[1];
+        p1x = 1.0f; p1y = (-W[2] - W[0]) / W[1];
+        const float rY = p1y - p0y;
+        if (p0y < -1e-6f || p0y > 1 + 1e-6f) {
+          const float k1 = -p0y / rY, k2 = (1 - p0y) / rY, k = (fabsf(k1) < fabsf(k2)) ? k1 : k2;
+          p0x = p0x + k * 1.0f; p0y = p0y + k * rY;
+        }
+        if (p1y < -1e-6f || p1y > 1 + 1e-6f) {
+          const float k1 = -p1y / rY, k2 = (1 - p1y) / rY, k = (fabsf(k1) < fabsf(k2)) ? k1 : k2;
+          p1x = p1x + k * 1.0f; p1y = p1y + k * rY;
+        }
+      } else if (fabsf(W[0]) > 1e-6f) {
+        p0x = -W[2] / W[0]; p0y = 0.0f;
+        p1x = -W[2] / W[0]; p1y = 1.0f;
+      } else {
+        force = 1;
+      }
+      if (!orc_dr_line_clip(&p0x, &p0y, &p1x, &p1y)) goto done;
+      float thick;
+      {
+        const f3v up = mk_f(v->world_view[4], v->world_view[5], v->world_view[6]);
+        float ax, ay, bx, by;
+        float pv[16];
+        mat4_mul(v->proj, v->world_view, pv);
+        w2s(pv, closest, &ax, &ay);
+        w2s(pv, add_f(closest, scl_f(relax_eps, up)), &bx, &by);
+        const float ddx = bx - ax, ddy = by - ay;
+        thick = sqrtf(ddx * ddx + ddy * ddy) * (float)(v->width > v->height ? v->width : v->height);
+      }
+      radius = mx_f(min_sample_radius, thick) + sample_radius_mult * err;
+      rx = p1x - p0x; ry = p1y - p0y;
+      float l = sqrtf(rx * rx + ry * ry);
+      const float ux = rx / l, uy = ry / l;
+      p0x = p0x - radius * ux; p0y = p0y - radius * uy;
+      p1x = p1x + radius * ux; p1y = p1y + radius * uy;
+      rx = p1x - p0x; ry = p1y - p0y;
+      l = sqrtf(ry * ry + rx * rx);
+      nx = -ry / l; ny = rx / l;
+      area = 2 * radius * sqrtf(rx * rx + ry * ry);
+      if (!force && area < min_stripe_area) goto done;
+    }
+    const float area_mult = mn_f(1.0f, 0.05f + 2.0f * area);
+    unsigned cnt = (unsigned)(area_mult * (float)(p->border_spp - svm_spp));
+    if (cnt < 1u) cnt = 1u;
+    L->count = cnt;
+    L->force = (uint32_t)force;
+    L->p0[0] = p0x; L->p0[1] = p0y; L->r[0] = rx; L->r[1] = ry; L->n[0] = nx; L->n[1] = ny;
+    L->radius = radius;
+    L->pdf = force ? 1.0f / (float)cnt : area / (float)cnt;
+  }
+done:
+  free(pl); free(X); free(ts);
+}
+
+/* The sub-pixel position of border sample j (sample index svm_spp + j) of a line. */
+void orc_dr_svm_sample(const orc_dr_svm_line_t *L, uint32_t x, uint32_t y, uint32_t seed, uint32_t j, float d[2]) {
+  float u, w;
+  rand2(x, y, L->svm_spp + j, seed, &u, &w);
+  if (L->force) { d[0] = u; d[1] = w; return; }
+  const float a = u, b = w * 2.0f - 1.0f;         /* urand(0, 1), urand(-1, 1) */
+  const float br = b * L->radius;
+  d[0] = (L->p0[0] + a * L->r[0]) + br * L->n[0];
+  d[1] = (L->p0[1] + a * L->r[1]) + br * L->n[1];
+}
+
+/* CastBorderRaySVM (:1651-1931) */
+static void cast_border_ray_svm(const rctx *r, uint32_t x, uint32_t y, float *g) {
+  const orc_dr_preset *p = r->p;
+  orc_dr_svm_line_t L;
+  orc_dr_svm_line(r->s, r->P, p, r->v, x, y, &L);
+  if (L.count == 0) return;
+  ctx_f cx = {r->s, r->P};
+  payload_f *pl = (payload_f *)malloc(sizeof(payload_f));
+  for (uint32_t j = 0; j < L.count; j++) {
+    float d[2], pos[4], dir[4];
+    orc_dr_svm_sample(&L, x, y, p->seed, j, d);
+    if (!(d[0] > 0 && d[0] < 1 && d[1] > 0 && d[1] < 1)) continue;
+    orc_eye_ray(x, y, r->v->width, r->v->height, d[0], d[1], r->v->proj_inv, r->v->wv_inv, pos, dir);
+    hitdr_f h = query_f(&cx, ORC_DR_RAY_FLAG_BORDER, pos, dir, pl);
+    if (pl->missed_hit.sdf < p->border_relax_eps) border_ray_derivs(r, L.pdf, pl, &h, pos, dir, g);
+  }
+  free(pl);
+}
+
 static int nthreads(int threads) {
 #ifdef _OPENMP
   return threads > 0 ? threads : omp_get_max_threads();
@@ -417,7 +609,10 @@ double orc_dr_render(const orc_dr_scene *s, const float *params, const orc_dr_pr
 #pragma omp parallel for num_threads(T) schedule(static, 1)
     for (int t = 0; t < T; t++) {
       uint32_t b = t * bsteps, e = (t + 1) * bsteps < nb ? (t + 1) * bsteps : nb;
-      for (uint32_t i = b; i < e; i++) cast_border_ray(&r, border[i] % W, border[i] / W, slices + (size_t)np * t);
+      for (uint32_t i = b; i < e; i++) {
+        if (p->border_sampling == 1) cast_border_ray_svm(&r, border[i] % W, border[i] / W, slices + (size_t)np * t);
+        else cast_border_ray(&r, border[i] % W, border[i] / W, slices + (size_t)np * t);
+      }
     }
   }
   /* IV: getBaseGradientMult (:140-145), applied to every slice; slices summed in order */

@@ -59,12 +59,16 @@ typedef struct {
   uint32_t reg_function;                /* DR_REG_FUNCTION_NONE = 0, else Regularization runs */
   float reg_lambda, reg_power;
   uint32_t redistancing_enable, redistancing_interval;
+  uint32_t border_sampling;             /* DR_BORDER_SAMPLING_RANDOM 0 / _SVM 1 (DR_common.h:123-124) */
+  uint32_t raycasting_mask;             /* DR_RAYCASTING_MASK_OFF 0 / _ON 1 (DR_common.h:86-87) */
 } orc_dr_preset;
 
 typedef struct {
   uint32_t width, height;
   float proj_inv[16], wv_inv[16];
   float proj[16], world_view[16];
+  uint8_t *cast_mask;                   /* W x H ray-casting mask of the view (masks[image]), read and
+                                           rewritten by a render when raycasting_mask is on; may be NULL */
 } orc_dr_view;
 
 /* One RayQuery_NearestHitWithGrad per ray; 576-word records (oracle/ref_driver.cpp layout). */
@@ -92,6 +96,24 @@ double orc_dr_loss_f64(const orc_dr_scene *s, const double *params, const orc_dr
 void orc_dr_step(const orc_dr_scene *s, float *params, const orc_dr_preset *p, const orc_dr_view *views,
                  const float *images, uint32_t n_images, uint32_t iter, float *adam_state, float *grad_out,
                  double *losses, float *images_out, int threads);
+
+/* SVM_fit (diff_render/MultiRendererDR.cpp:1518-1546) on n rows (x, y, 1) * label
+ * (3 floats per row, scaled in place by etha as the reference does): W = (a, b, c,
+ * error rate) of the line a x + b y + c = 0. */
+void orc_dr_svm_fit(float *rows, uint32_t n, float W[4]);
+/* CohenSutherlandLineClip (:1580-1649) against [0,1]^2; returns 1 when accepted. */
+int orc_dr_line_clip(float *x0, float *y0, float *x1, float *y1);
+/* The SVM stage of CastBorderRaySVM (:1651-1816) for pixel (x, y) of a view:
+ * count border samples (0: the pixel is skipped) on the stripe p0 + u r + v radius n
+ * (force: uniformly over the pixel), each weighted by pdf; svm_spp rays were spent. */
+typedef struct {
+  uint32_t count, force, svm_spp, pad;
+  float p0[2], r[2], n[2], radius, pdf;
+} orc_dr_svm_line_t;
+void orc_dr_svm_line(const orc_dr_scene *s, const float *params, const orc_dr_preset *p, const orc_dr_view *v,
+                     uint32_t x, uint32_t y, orc_dr_svm_line_t *L);
+/* Sub-pixel position of border sample j of a line (sample index svm_spp + j). */
+void orc_dr_svm_sample(const orc_dr_svm_line_t *L, uint32_t x, uint32_t y, uint32_t seed, uint32_t j, float d[2]);
 
 /* Regularization (diff_render/MultiRendererDR.cpp:1933-2055): for every brick
  * value and each of its 6 neighbours inside the brick (brick_size + 1 values per

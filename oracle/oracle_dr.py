@@ -45,12 +45,20 @@ class DrPreset(C.Structure):
                 ("lights", Light * 4), ("lr", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float),
                 ("eps", C.c_float), ("accumulate_batch", C.c_uint32), ("reg_function", C.c_uint32),
                 ("reg_lambda", C.c_float), ("reg_power", C.c_float), ("redistancing_enable", C.c_uint32),
-                ("redistancing_interval", C.c_uint32)]
+                ("redistancing_interval", C.c_uint32), ("border_sampling", C.c_uint32),
+                ("raycasting_mask", C.c_uint32)]
 
 
 class DrView(C.Structure):
     _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("proj_inv", C.c_float * 16),
-                ("wv_inv", C.c_float * 16), ("proj", C.c_float * 16), ("world_view", C.c_float * 16)]
+                ("wv_inv", C.c_float * 16), ("proj", C.c_float * 16), ("world_view", C.c_float * 16),
+                ("cast_mask", VP)]
+
+
+class SvmLine(C.Structure):
+    _fields_ = [("count", C.c_uint32), ("force", C.c_uint32), ("svm_spp", C.c_uint32), ("pad", C.c_uint32),
+                ("p0", C.c_float * 2), ("r", C.c_float * 2), ("n", C.c_float * 2), ("radius", C.c_float),
+                ("pdf", C.c_float)]
 
 
 _bound = False
@@ -71,6 +79,12 @@ def _lib():
         L.orc_dr_adam.argtypes = [C.c_uint32, VP, VP, VP, C.c_uint32, C.c_float, C.c_float, C.c_float, C.c_float]
         L.orc_dr_regularize.argtypes = [C.POINTER(DrScene_), VP, C.POINTER(DrPreset), VP]
         L.orc_dr_redistance.argtypes = [VP, C.c_uint32, C.c_float, C.c_uint32]
+        L.orc_dr_svm_fit.argtypes = [VP, C.c_uint32, VP]
+        L.orc_dr_line_clip.restype = C.c_int
+        L.orc_dr_line_clip.argtypes = [C.POINTER(C.c_float)] * 4
+        L.orc_dr_svm_line.argtypes = [C.POINTER(DrScene_), VP, C.POINTER(DrPreset), C.POINTER(DrView), C.c_uint32,
+                                      C.c_uint32, C.POINTER(SvmLine)]
+        L.orc_dr_svm_sample.argtypes = [C.POINTER(SvmLine), C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, VP]
         L.orc_dr_grid_sbs.restype = C.c_uint32
         L.orc_dr_grid_sbs.argtypes = [C.c_uint32, C.c_uint32, C.c_void_p, VP, C.POINTER(SbsHeader), C.POINTER(VP),
                                       C.POINTER(VP), C.POINTER(C.c_uint32), C.POINTER(VP), C.POINTER(C.c_uint32)]
@@ -90,7 +104,7 @@ def default_lights():
 def make_preset(render_mode=RENDER_LAMBERT, reconstruction=RECON_COLOR | RECON_GEOMETRY, input_type=0, loss=0,
                 spp=1, border_spp=256, border_relax_eps=1e-3, seed=1, lights=None, lr=3e-3, beta1=0.9, beta2=0.999,
                 eps=1e-8, accumulate_batch=0, reg_function=0, reg_lambda=0.25, reg_power=2.0,
-                redistancing_enable=0, redistancing_interval=1):
+                redistancing_enable=0, redistancing_interval=1, border_sampling=0, raycasting_mask=0):
     p = DrPreset()
     p.render_mode, p.reconstruction_flags, p.input_type, p.loss_function = render_mode, reconstruction, input_type, loss
     p.spp, p.border_spp, p.border_relax_eps, p.seed = spp, border_spp, border_relax_eps, seed
@@ -103,7 +117,23 @@ def make_preset(render_mode=RENDER_LAMBERT, reconstruction=RECON_COLOR | RECON_G
     p.lr, p.beta1, p.beta2, p.eps, p.accumulate_batch = lr, beta1, beta2, eps, accumulate_batch
     p.reg_function, p.reg_lambda, p.reg_power = reg_function, reg_lambda, reg_power
     p.redistancing_enable, p.redistancing_interval = redistancing_enable, redistancing_interval
+    p.border_sampling, p.raycasting_mask = border_sampling, raycasting_mask
     return p
+
+
+def svm_fit(rows):
+    """SVM_fit on rows (n, 3) = (x, y, 1) * label; returns (a, b, c, error rate)."""
+    X = np.ascontiguousarray(rows, np.float32).copy()
+    W = np.zeros(4, np.float32)
+    _lib().orc_dr_svm_fit(_p(X), X.shape[0], _p(W))
+    return W
+
+
+def line_clip(x0, y0, x1, y1):
+    """CohenSutherlandLineClip against [0,1]^2: (accepted, x0, y0, x1, y1)."""
+    v = [C.c_float(x0), C.c_float(y0), C.c_float(x1), C.c_float(y1)]
+    ok = _lib().orc_dr_line_clip(*[C.byref(a) for a in v])
+    return bool(ok), v[0].value, v[1].value, v[2].value, v[3].value
 
 
 def make_view(width, height, world_view, proj, inverse4x4):
@@ -166,7 +196,10 @@ class DrScene:
         _lib().orc_dr_query(C.byref(self.s), _p(P), flags, _p(pos), _p(dr), pos.shape[0], _p(out))
         return out
 
-    def render(self, params, preset, view, image_ref, threads=0):
+    def render(self, params, preset, view, image_ref, threads=0, mask=None):
+        """mask: the view's W*H uint8 ray-casting mask, read and rewritten in place
+        (preset.raycasting_mask on)."""
+        view.cast_mask = None if mask is None else _p(mask)
         P = np.ascontiguousarray(params, np.float32)
         n = view.width * view.height
         ref = np.ascontiguousarray(image_ref, np.float32).reshape(n, 4)
@@ -193,11 +226,14 @@ class DrScene:
         _lib().orc_dr_regularize(C.byref(self.s), _p(params), C.byref(preset), _p(g))
         return g
 
-    def step(self, params, preset, views, images, it, adam_state, threads=0):
-        """One OptimizeFixedStructure iteration; params and adam_state are updated in place."""
+    def step(self, params, preset, views, images, it, adam_state, threads=0, masks=None):
+        """One OptimizeFixedStructure iteration; params and adam_state are updated in
+        place, and so are the views' uint8 ray-casting masks when given."""
         assert params.dtype == np.float32 and params.flags.c_contiguous
         assert adam_state.dtype == np.float32 and adam_state.size == 2 * params.size
         nv = len(views)
+        for k, v in enumerate(views):
+            v.cast_mask = None if masks is None else _p(masks[k])
         va = (DrView * nv)(*views)
         imgs = np.ascontiguousarray(np.concatenate([np.asarray(i, np.float32).reshape(-1, 4) for i in images]))
         grad = np.zeros(params.size, np.float32)
@@ -206,6 +242,13 @@ class DrScene:
         _lib().orc_dr_step(C.byref(self.s), _p(params), C.byref(preset), C.cast(va, VP), _p(imgs), nv, it,
                            _p(adam_state), _p(grad), _p(losses), _p(out_imgs), threads)
         return dict(grad=grad, losses=losses, images=out_imgs)
+
+    def svm_line(self, params, preset, view, x, y):
+        """The SVM stage of CastBorderRaySVM for pixel (x, y): an SvmLine."""
+        P = np.ascontiguousarray(params, np.float32)
+        L = SvmLine()
+        _lib().orc_dr_svm_line(C.byref(self.s), _p(P), C.byref(preset), C.byref(view), x, y, C.byref(L))
+        return L
 
 
 def adam(it, g, x, state, lr, b1=0.9, b2=0.999, eps=1e-8):
