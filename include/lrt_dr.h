@@ -141,6 +141,29 @@ lrt_status lrt_dr_grid_sbs(uint32_t brick_count, uint32_t brick_size, const lrt_
                            lrt_sbs_header *hdr, lrt_sbs_node **nodes, uint32_t *n_nodes, uint32_t **values,
                            uint64_t *n_values, float **params, uint32_t *n_params);
 
+/* create_grid_sbs as MultiRendererDR::OptimizeGrid calls it (diff_render/
+ * MultiRendererDR.cpp:228-276): brick_count^3 bricks of brick_size, colours
+ * gradient_color (diff_render/DR_common.cpp:25-35); distances circle_sdf((0,-0.15,0),
+ * 0.7) when old_params is NULL (the starting grid), else grid_sampler (:242-262):
+ * trilinear in the dense distances of old_params, a grid of the same brick count
+ * with bricks of old_brick_size.  Layout ID32F_IRGB32F_IN; host only; arrays
+ * malloc'd, free with lrt_free. */
+lrt_status lrt_dr_grid_resample(uint32_t brick_count, uint32_t brick_size, const float *old_params,
+                                uint32_t old_brick_size, lrt_sbs_header *hdr, lrt_sbs_node **nodes, uint32_t *n_nodes,
+                                uint32_t **values, uint64_t *n_values, float **params, uint32_t *n_params);
+/* MultiRendererDR::OptimizeGrid (:228-276) on the context's reference images:
+ * from the starting grid (start_grid_size bricks of size 1) each stage i sets the
+ * grid as the scene (BVH from the builder lrt_set_tuning "bvh_builder" selects),
+ * applies presets[i] and runs iterations[i] optimisation steps, then resamples the
+ * optimised distances into bricks twice as large (the same size after the last
+ * stage when no_last_step_resize).  Stages render at the reference images' size
+ * (the reference's per-stage render_width/height resampling of its images is left
+ * to the caller).  Returns the final grid (malloc'd, free with lrt_free) and the
+ * last step's per-view losses (n_views, may be NULL). */
+lrt_status lrt_dr_optimize_grid(lrt_ctx *ctx, uint32_t start_grid_size, uint32_t no_last_step_resize,
+                                const lrt_dr_preset *presets, const uint32_t *iterations, uint32_t n_stages,
+                                lrt_sbs_header *hdr, lrt_sbs_node **nodes, uint32_t *n_nodes, uint32_t **values,
+                                uint64_t *n_values, float **params, uint32_t *n_params, double *last_losses);
 #ifdef __cplusplus
 }
 #endif

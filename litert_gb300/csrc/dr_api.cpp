@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <new>
 #include <vector>
 
@@ -546,6 +547,79 @@ extern "C" lrt_status lrt_dr_optimize(lrt_ctx *ctx, uint32_t first_iter, uint32_
   return read_status(ctx);
 }
 
+namespace {
+// malloc'd arrays of one grid (lrt_dr_grid_resample's outputs)
+struct GridArrays {
+  lrt_sbs_header hdr{};
+  lrt_sbs_node *nodes = nullptr;
+  uint32_t n_nodes = 0, n_params = 0;
+  uint32_t *values = nullptr;
+  uint64_t n_values = 0;
+  float *params = nullptr;
+  void clear() {
+    std::free(nodes); std::free(values); std::free(params);
+    nodes = nullptr; values = nullptr; params = nullptr;
+  }
+  ~GridArrays() { clear(); }
+};
+}  // namespace
+
+extern "C" lrt_status lrt_dr_optimize_grid(lrt_ctx *ctx, uint32_t start_grid_size, uint32_t no_last_step_resize,
+                                           const lrt_dr_preset *presets, const uint32_t *iterations,
+                                           uint32_t n_stages, lrt_sbs_header *hdr, lrt_sbs_node **nodes,
+                                           uint32_t *n_nodes, uint32_t **values, uint64_t *n_values, float **params,
+                                           uint32_t *n_params, double *last_losses) {
+  if (!ctx) return LRT_ERR_INVALID;
+  if (!presets || !iterations || n_stages == 0 || start_grid_size == 0 || !hdr || !nodes || !n_nodes || !values ||
+      !n_values || !params || !n_params)
+    return fail(ctx, LRT_ERR_INVALID, "lrt_dr_optimize_grid: bad arguments");
+  for (uint32_t i = 0; i < n_stages; i++)
+    if (iterations[i] == 0) return fail(ctx, LRT_ERR_INVALID, "lrt_dr_optimize_grid: every stage needs iterations");
+  lrt_status s = ensure_state(ctx);
+  if (s != LRT_OK) return s;
+  if (!ctx->dr->has_ref) return fail(ctx, LRT_ERR_STATE, "lrt_dr_set_reference first");
+  GridArrays g;
+  uint32_t bs = 1;
+  s = lrt_dr_grid_resample(start_grid_size, bs, nullptr, 0, &g.hdr, &g.nodes, &g.n_nodes, &g.values, &g.n_values,
+                           &g.params, &g.n_params);
+  if (s != LRT_OK) return fail(ctx, s, "lrt_dr_optimize_grid: starting grid");
+  for (uint32_t i = 0; i < n_stages; i++) {
+    // OptimizeFixedStructure (:278-576): scene, preset, iterations; the optimised
+    // parameters become the grid's values_f (:574)
+    if ((s = lrt_dr_set_preset(ctx, &presets[i])) != LRT_OK) return s;
+    if ((s = lrt_dr_set_scene(ctx, &g.hdr, g.nodes, g.n_nodes, g.values, g.n_values, g.params, g.n_params, nullptr,
+                              0)) != LRT_OK)
+      return s;
+    if ((s = lrt_dr_optimize(ctx, 0, iterations[i], last_losses)) != LRT_OK) return s;
+    LRT_CUDA(ctx, cudaMemcpy(g.params, ctx->dr->d_params.p, sizeof(float) * g.n_params, cudaMemcpyDeviceToHost));
+    // the grid resampled into bricks twice as large, or as large after the last stage
+    // with no_last_step_resize (:264-273)
+    const uint32_t nbs = (i + 1 == n_stages && no_last_step_resize) ? bs : 2 * bs;
+    GridArrays n;
+    s = lrt_dr_grid_resample(start_grid_size, nbs, g.params, bs, &n.hdr, &n.nodes, &n.n_nodes, &n.values, &n.n_values,
+                             &n.params, &n.n_params);
+    if (s != LRT_OK) return fail(ctx, s, "lrt_dr_optimize_grid: resampled grid");
+    g.clear();
+    std::swap(g.hdr, n.hdr);
+    std::swap(g.nodes, n.nodes);
+    std::swap(g.n_nodes, n.n_nodes);
+    std::swap(g.values, n.values);
+    std::swap(g.n_values, n.n_values);
+    std::swap(g.params, n.params);
+    std::swap(g.n_params, n.n_params);
+    bs = nbs;
+  }
+  *hdr = g.hdr;
+  *nodes = g.nodes;
+  *n_nodes = g.n_nodes;
+  *values = g.values;
+  *n_values = g.n_values;
+  *params = g.params;
+  *n_params = g.n_params;
+  g.nodes = nullptr; g.values = nullptr; g.params = nullptr;
+  return LRT_OK;
+}
+
 extern "C" lrt_status lrt_dr_get(lrt_ctx *ctx, uint32_t what, uint32_t view, void *out, uint64_t bytes) {
   if (!ctx || !ctx->dr || !ctx->dr->has_scene || !out) return fail(ctx, LRT_ERR_STATE, "lrt_dr_set_scene first");
   DrState &st = *ctx->dr;
@@ -602,12 +676,15 @@ extern "C" uint32_t lrt_dr_last_launch_count(const lrt_ctx *ctx) {
   return (ctx && ctx->dr) ? ctx->dr->last_launches : 0;
 }
 
-extern "C" lrt_status lrt_dr_grid_sbs(uint32_t bc, uint32_t bs, const lrt_sdf_desc *sdf, const float *color3,
-                                      lrt_sbs_header *hdr, lrt_sbs_node **nodes_out, uint32_t *n_nodes,
-                                      uint32_t **values_out, uint64_t *n_values, float **params_out,
-                                      uint32_t *n_params) {
-  if (!sdf || !hdr || !nodes_out || !n_nodes || !values_out || !n_values || !params_out || !n_params || bc == 0 ||
-      bs == 0 || bc > 1024 || bs > 64 || (sdf->n_spheres + sdf->n_boxes) == 0)
+using DistFn = std::function<float(float, float, float)>;
+using ColorFn = std::function<void(float, float, float, float *)>;
+
+// create_grid_sbs (diff_render/DR_common.cpp:47-146) + SBS_ind_to_SBS_ind_with_neighbors
+static lrt_status make_grid(uint32_t bc, uint32_t bs, const DistFn &dist, const ColorFn &color, lrt_sbs_header *hdr,
+                            lrt_sbs_node **nodes_out, uint32_t *n_nodes, uint32_t **values_out, uint64_t *n_values,
+                            float **params_out, uint32_t *n_params) {
+  if (!hdr || !nodes_out || !n_nodes || !values_out || !n_values || !params_out || !n_params || bc == 0 || bs == 0 ||
+      bc > 1024 || bs > 64)
     return LRT_ERR_INVALID;
   const uint64_t v = bs + 1, dist_per_node = v * v * v, pc = uint64_t(bc) * bs + 1, cc = uint64_t(bc) + 1;
   const uint64_t c_off = pc * pc * pc, nn = uint64_t(bc) * bc * bc;
@@ -631,8 +708,8 @@ extern "C" lrt_status lrt_dr_grid_sbs(uint32_t bc, uint32_t bs, const lrt_sdf_de
   for (int64_t x = 0; x < int64_t(pc); x++)
     for (uint64_t y = 0; y < pc; y++)
       for (uint64_t z = 0; z < pc; z++)
-        P[uint64_t(x) * pc * pc + y * pc + z] = sdf_eval(*sdf, 2.0f * (float(x) / gdiv) - 1.0f,
-                                                         2.0f * (float(y) / gdiv) - 1.0f, 2.0f * (float(z) / gdiv) - 1.0f);
+        P[uint64_t(x) * pc * pc + y * pc + z] = dist(2.0f * (float(x) / gdiv) - 1.0f, 2.0f * (float(y) / gdiv) - 1.0f,
+                                                     2.0f * (float(z) / gdiv) - 1.0f);
   // colours at the brick corners (:87-102)
   const float cdiv = float(bc);
   for (uint64_t x = 0; x < cc; x++)
@@ -640,13 +717,7 @@ extern "C" lrt_status lrt_dr_grid_sbs(uint32_t bc, uint32_t bs, const lrt_sdf_de
       for (uint64_t z = 0; z < cc; z++) {
         const uint64_t idx = x * cc * cc + y * cc + z;
         float c[3];
-        if (color3) {
-          c[0] = color3[0]; c[1] = color3[1]; c[2] = color3[2];
-        } else {
-          const float q[3] = {2.0f * (float(x) / cdiv) - 1.0f, 2.0f * (float(y) / cdiv) - 1.0f,
-                              2.0f * (float(z) / cdiv) - 1.0f};
-          for (int k = 0; k < 3; k++) c[k] = 0.5f + 0.5f * q[k];
-        }
+        color(2.0f * (float(x) / cdiv) - 1.0f, 2.0f * (float(y) / cdiv) - 1.0f, 2.0f * (float(z) / cdiv) - 1.0f, c);
         for (int k = 0; k < 3; k++) P[c_off + 3 * idx + k] = c[k];
       }
   // nodes and indices (:104-143)
@@ -702,4 +773,77 @@ extern "C" lrt_status lrt_dr_grid_sbs(uint32_t bc, uint32_t bs, const lrt_sdf_de
   *params_out = P;
   *n_params = uint32_t(np);
   return LRT_OK;
+}
+
+extern "C" lrt_status lrt_dr_grid_sbs(uint32_t bc, uint32_t bs, const lrt_sdf_desc *sdf, const float *color3,
+                                      lrt_sbs_header *hdr, lrt_sbs_node **nodes_out, uint32_t *n_nodes,
+                                      uint32_t **values_out, uint64_t *n_values, float **params_out,
+                                      uint32_t *n_params) {
+  if (!sdf || (sdf->n_spheres + sdf->n_boxes) == 0) return LRT_ERR_INVALID;
+  const lrt_sdf_desc f = *sdf;
+  const DistFn dist = [f](float x, float y, float z) { return sdf_eval(f, x, y, z); };
+  const ColorFn color = [color3](float x, float y, float z, float *c) {
+    if (color3) {
+      c[0] = color3[0]; c[1] = color3[1]; c[2] = color3[2];
+    } else {
+      const float q[3] = {x, y, z};
+      for (int k = 0; k < 3; k++) c[k] = 0.5f + 0.5f * q[k];
+    }
+  };
+  return make_grid(bc, bs, dist, color, hdr, nodes_out, n_nodes, values_out, n_values, params_out, n_params);
+}
+
+// gradient_color (diff_render/DR_common.cpp:25-35): eight weighted corner colours
+// summed as float3 values, zero components included
+static void gradient_color(float px, float py, float pz, float *c) {
+  const float w[8] = {(1 - px) * (1 - py) * (1 - pz), (1 - px) * (1 - py) * (pz), (1 - px) * (py) * (1 - pz),
+                      (1 - px) * (py) * (pz),         (px) * (1 - py) * (1 - pz), (px) * (1 - py) * (pz),
+                      (px) * (py) * (1 - pz),         (px) * (py) * (pz)};
+  static const float col[8][3] = {{1, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 1, 0}, {1, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 1, 0}};
+  for (int k = 0; k < 3; k++) {
+    float a = w[0] * col[0][k];
+    for (int i = 1; i < 8; i++) a = a + w[i] * col[i][k];
+    c[k] = a;
+  }
+}
+
+// OptimizeGrid's grid_sampler (diff_render/MultiRendererDR.cpp:242-262): trilinear
+// in the dense distance grid of gs bricks of bs voxels, clamped to the cube
+static float grid_sample(const float *d, uint32_t gs, uint32_t bs, float px, float py, float pz) {
+  const uint32_t pc = gs * bs + 1u;
+  const float p[3] = {px, py, pz};
+  float f[3], dp[3];
+  uint32_t i[3];
+  for (int k = 0; k < 3; k++) {
+    float c = 0.5f * (p[k] + 1.0f);
+    c = std::min(std::max(c, 0.0f), 1.0f + 1e-6f);
+    f[k] = (c * float(gs)) * float(bs);
+    i[k] = uint32_t(f[k] + 1e-6f);
+    dp[k] = f[k] - float(i[k]);
+  }
+  auto at = [&](uint32_t x, uint32_t y, uint32_t z) { return d[x * pc * pc + y * pc + z]; };
+  if (i[0] < pc - 1 && i[1] < pc - 1 && i[2] < pc - 1) {
+    const float x = dp[0], y = dp[1], z = dp[2];
+    return (1 - x) * (1 - y) * (1 - z) * at(i[0], i[1], i[2]) + (1 - x) * (1 - y) * z * at(i[0], i[1], i[2] + 1) +
+           (1 - x) * y * (1 - z) * at(i[0], i[1] + 1, i[2]) + (1 - x) * y * z * at(i[0], i[1] + 1, i[2] + 1) +
+           x * (1 - y) * (1 - z) * at(i[0] + 1, i[1], i[2]) + x * (1 - y) * z * at(i[0] + 1, i[1], i[2] + 1) +
+           x * y * (1 - z) * at(i[0] + 1, i[1] + 1, i[2]) + x * y * z * at(i[0] + 1, i[1] + 1, i[2] + 1);
+  }
+  return at(i[0], i[1], i[2]);
+}
+
+extern "C" lrt_status lrt_dr_grid_resample(uint32_t bc, uint32_t bs, const float *old_params, uint32_t old_bs,
+                                           lrt_sbs_header *hdr, lrt_sbs_node **nodes, uint32_t *n_nodes,
+                                           uint32_t **values, uint64_t *n_values, float **params, uint32_t *n_params) {
+  if (old_params && (old_bs == 0 || old_bs > 64)) return LRT_ERR_INVALID;
+  DistFn dist;
+  if (old_params) {
+    dist = [=](float x, float y, float z) { return grid_sample(old_params, bc, old_bs, x, y, z); };
+  } else {   // circle_sdf(float3(0, -0.15, 0), 0.7, p) (:232-235; DR_common.cpp:16-19)
+    dist = [](float x, float y, float z) {
+      const float dx = x - 0.0f, dy = y - (-0.15f), dz = z - 0.0f;
+      return std::sqrt(dx * dx + dy * dy + dz * dz) - 0.7f;
+    };
+  }
+  return make_grid(bc, bs, dist, gradient_color, hdr, nodes, n_nodes, values, n_values, params, n_params);
 }

@@ -59,6 +59,11 @@ def _lib():
             "lrt_dr_grid_sbs": (I, [U32, U32, C.POINTER(lrt.SdfDesc), VP, C.POINTER(lrt.SbsHeader), C.POINTER(VP),
                                     C.POINTER(U32), C.POINTER(VP), C.POINTER(C.c_uint64), C.POINTER(VP),
                                     C.POINTER(U32)]),
+            "lrt_dr_grid_resample": (I, [U32, U32, VP, U32, C.POINTER(lrt.SbsHeader), C.POINTER(VP), C.POINTER(U32),
+                                         C.POINTER(VP), C.POINTER(C.c_uint64), C.POINTER(VP), C.POINTER(U32)]),
+            "lrt_dr_optimize_grid": (I, [P, U32, U32, VP, VP, U32, C.POINTER(lrt.SbsHeader), C.POINTER(VP),
+                                         C.POINTER(U32), C.POINTER(VP), C.POINTER(C.c_uint64), C.POINTER(VP),
+                                         C.POINTER(U32), VP]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -85,6 +90,31 @@ def default_preset(**kw):
             p.lights[i].dir[:] = [float(x) for x in np.asarray(d, np.float32)]
             p.lights[i].color[:] = [float(x) for x in np.asarray(c, np.float32)]
     return p
+
+
+def _take_grid(L, hdr, pn, nn, pv, nv, pp, npar):
+    try:
+        nodes = np.ctypeslib.as_array(C.cast(pn, C.POINTER(C.c_uint32)), (nn.value * 4,)).copy().reshape(-1, 4)
+        values = np.ctypeslib.as_array(C.cast(pv, C.POINTER(C.c_uint32)), (nv.value,)).copy()
+        params = np.ctypeslib.as_array(C.cast(pp, C.POINTER(C.c_float)), (npar.value,)).copy()
+    finally:
+        for q in (pn, pv, pp):
+            L.lrt_free(q)
+    return hdr, nodes, values, params
+
+
+def grid_resample(brick_count, brick_size, old_params=None, old_brick_size=0):
+    """create_grid_sbs as OptimizeGrid calls it: the starting grid (old_params None)
+    or old_params's distances resampled into bricks of brick_size; gradient colours."""
+    L = _lib()
+    hdr = lrt.SbsHeader()
+    pn, pv, pp = C.c_void_p(), C.c_void_p(), C.c_void_p()
+    nn, npar, nv = C.c_uint32(), C.c_uint32(), C.c_uint64()
+    op = None if old_params is None else np.ascontiguousarray(old_params, np.float32)
+    lrt._check(L.lrt_dr_grid_resample(brick_count, brick_size, lrt._ptr(op), old_brick_size, C.byref(hdr),
+                                      C.byref(pn), C.byref(nn), C.byref(pv), C.byref(nv), C.byref(pp),
+                                      C.byref(npar)), what="lrt_dr_grid_resample")
+    return _take_grid(L, hdr, pn, nn, pv, nv, pp, npar)
 
 
 def grid_sbs(brick_count, brick_size, sdf, color=None):
@@ -199,6 +229,24 @@ class MultiRendererDR:
         self._chk(_lib().lrt_dr_optimize(self._ctx, first_iter, iterations, lrt._ptr(last)))
         sbs[3][:] = self.get(GET_PARAMS)
         return last
+
+    def OptimizeGrid(self, start_grid_size, no_last_step_resize, presets, iterations):
+        """MultiRendererDR::OptimizeGrid on the reference set by SetReference: returns
+        (final grid [hdr, nodes, values, params], last step's per-view losses)."""
+        L = _lib()
+        pa = (DrPreset * len(presets))(*presets)
+        it = np.ascontiguousarray(iterations, np.uint32)
+        hdr = lrt.SbsHeader()
+        pn, pv, pp = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        nn, npar, nv = C.c_uint32(), C.c_uint32(), C.c_uint64()
+        last = np.zeros(len(self.views), np.float64)
+        self._chk(L.lrt_dr_optimize_grid(self._ctx, start_grid_size, int(bool(no_last_step_resize)),
+                                         C.cast(pa, C.c_void_p), lrt._ptr(it), len(presets), C.byref(hdr),
+                                         C.byref(pn), C.byref(nn), C.byref(pv), C.byref(nv), C.byref(pp),
+                                         C.byref(npar), lrt._ptr(last)))
+        grid = list(_take_grid(L, hdr, pn, nn, pv, nv, pp, npar))
+        self.n_params = grid[3].size
+        return grid, last
 
     def get(self, what, view=0):
         if what in (GET_PARAMS, GET_GRAD):

@@ -919,3 +919,65 @@ void orc_dr_redistance(float *dist, uint32_t n, float h, uint32_t n_iters) {
   memcpy(dist, b[1 - cur], 4 * N);
   free(b[0]); free(b[1]); free(frozen);
 }
+
+/* ---- OptimizeGrid's grids (diff_render/MultiRendererDR.cpp:228-276) ---- */
+static void gradient_color_f(float px, float py, float pz, float *c) {   /* DR_common.cpp:25-35 */
+  const float w[8] = {(1 - px) * (1 - py) * (1 - pz), (1 - px) * (1 - py) * (pz), (1 - px) * (py) * (1 - pz),
+                      (1 - px) * (py) * (pz),         (px) * (1 - py) * (1 - pz), (px) * (1 - py) * (pz),
+                      (px) * (py) * (1 - pz),         (px) * (py) * (pz)};
+  static const float col[8][3] = {{1, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 1, 0}, {1, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 1, 0}};
+  for (int k = 0; k < 3; k++) {
+    float a = w[0] * col[0][k];
+    for (int i = 1; i < 8; i++) a = a + w[i] * col[i][k];
+    c[k] = a;
+  }
+}
+
+static float grid_sampler_f(const float *d, uint32_t gs, uint32_t bs, const float p[3]) {   /* :242-262 */
+  const uint32_t pc = gs * bs + 1u;
+  float f[3], dp[3];
+  uint32_t i[3];
+  for (int k = 0; k < 3; k++) {
+    float c = 0.5f * (p[k] + 1.0f);
+    c = mn_f(mx_f(c, 0.0f), 1.0f + 1e-6f);
+    f[k] = (c * (float)gs) * (float)bs;
+    i[k] = (uint32_t)(f[k] + 1e-6f);
+    dp[k] = f[k] - (float)i[k];
+  }
+#define AT(a, b, c) d[(a) * pc * pc + (b) * pc + (c)]
+  if (i[0] < pc - 1 && i[1] < pc - 1 && i[2] < pc - 1) {
+    const float x = dp[0], y = dp[1], z = dp[2];
+    return (1 - x) * (1 - y) * (1 - z) * AT(i[0], i[1], i[2]) + (1 - x) * (1 - y) * z * AT(i[0], i[1], i[2] + 1) +
+           (1 - x) * y * (1 - z) * AT(i[0], i[1] + 1, i[2]) + (1 - x) * y * z * AT(i[0], i[1] + 1, i[2] + 1) +
+           x * (1 - y) * (1 - z) * AT(i[0] + 1, i[1], i[2]) + x * (1 - y) * z * AT(i[0] + 1, i[1], i[2] + 1) +
+           x * y * (1 - z) * AT(i[0] + 1, i[1] + 1, i[2]) + x * y * z * AT(i[0] + 1, i[1] + 1, i[2] + 1);
+  }
+  return AT(i[0], i[1], i[2]);
+#undef AT
+}
+
+void orc_dr_grid_resample(uint32_t gs, uint32_t bs, const float *old_params, uint32_t old_bs, float *out) {
+  const uint32_t pc = gs * bs + 1u, cc = gs + 1u, c_off = pc * pc * pc;
+  const float gdiv = (float)(gs * bs), cdiv = (float)gs;
+  for (uint32_t x = 0; x < pc; x++)
+    for (uint32_t y = 0; y < pc; y++)
+      for (uint32_t z = 0; z < pc; z++) {
+        const float p[3] = {2.0f * ((float)x / gdiv) - 1.0f, 2.0f * ((float)y / gdiv) - 1.0f,
+                            2.0f * ((float)z / gdiv) - 1.0f};
+        float v;
+        if (old_params) {
+          v = grid_sampler_f(old_params, gs, old_bs, p);
+        } else {   /* circle_sdf(float3(0, -0.15, 0), 0.7, p), DR_common.cpp:16-19 */
+          const float dx = p[0] - 0.0f, dy = p[1] - (-0.15f), dz = p[2] - 0.0f;
+          v = sqrtf(dx * dx + dy * dy + dz * dz) - 0.7f;
+        }
+        out[x * pc * pc + y * pc + z] = v;
+      }
+  for (uint32_t x = 0; x < cc; x++)
+    for (uint32_t y = 0; y < cc; y++)
+      for (uint32_t z = 0; z < cc; z++) {
+        const uint32_t idx = x * cc * cc + y * cc + z;
+        gradient_color_f(2.0f * ((float)x / cdiv) - 1.0f, 2.0f * ((float)y / cdiv) - 1.0f,
+                         2.0f * ((float)z / cdiv) - 1.0f, out + c_off + 3 * idx);
+      }
+}

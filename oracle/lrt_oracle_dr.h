@@ -138,6 +138,12 @@ uint32_t orc_dr_grid_sbs(uint32_t brick_count, uint32_t brick_size, const orc_sd
                          orc_sbs_header *hdr, orc_sbs_node **nodes, uint32_t **values, uint32_t *n_values,
                          float **params, uint32_t *n_params);
 
+/* The parameters (values_f) of create_grid_sbs(gs, bs, ...) as OptimizeGrid builds
+ * them (diff_render/MultiRendererDR.cpp:228-276): gradient_color colours; distances
+ * circle_sdf((0,-0.15,0), 0.7) for old_params NULL, else grid_sampler over the dense
+ * distances of old_params (gs bricks of old_bs).  out: (gs bs + 1)^3 + 3 (gs + 1)^3 floats. */
+void orc_dr_grid_resample(uint32_t gs, uint32_t bs, const float *old_params, uint32_t old_bs, float *out);
+
 #ifdef __cplusplus
 }
 #endif

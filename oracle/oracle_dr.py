@@ -79,6 +79,7 @@ def _lib():
         L.orc_dr_adam.argtypes = [C.c_uint32, VP, VP, VP, C.c_uint32, C.c_float, C.c_float, C.c_float, C.c_float]
         L.orc_dr_regularize.argtypes = [C.POINTER(DrScene_), VP, C.POINTER(DrPreset), VP]
         L.orc_dr_redistance.argtypes = [VP, C.c_uint32, C.c_float, C.c_uint32]
+        L.orc_dr_grid_resample.argtypes = [C.c_uint32, C.c_uint32, VP, C.c_uint32, VP]
         L.orc_dr_svm_fit.argtypes = [VP, C.c_uint32, VP]
         L.orc_dr_line_clip.restype = C.c_int
         L.orc_dr_line_clip.argtypes = [C.POINTER(C.c_float)] * 4
@@ -261,3 +262,14 @@ def redistance(dist, n, h, iters):
     d = np.ascontiguousarray(dist, np.float32).copy()
     _lib().orc_dr_redistance(_p(d), n, h, iters)
     return d
+
+
+def grid_resample(gs, bs, old_params=None, old_bs=0):
+    """OptimizeGrid's grid parameters: the starting grid (old_params None) or the
+    distances of old_params resampled into bricks of bs."""
+    n = (gs * bs + 1) ** 3 + 3 * (gs + 1) ** 3
+    out = np.zeros(n, np.float32)
+    op = None if old_params is None else np.ascontiguousarray(old_params, np.float32)
+    _lib().orc_dr_grid_resample(gs, bs, _p(op), old_bs, _p(out))
+    return out
+
