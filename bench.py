@@ -151,14 +151,15 @@ def gpu_build(args, host):
 
 
 def run_device_bvh(args, h, nodes, values, views, tuned, hits, flush, stream, torch):
-    """Scene commit wall time with the host binned-SAH BVH and with the device
-    linear BVH (second commit of each, after a warm-up commit), and the headline
-    render through the device-built tree with the same launch shape, timed like
-    the headline (CUDA events, L2 flush between steps)."""
+    """Scene commit wall time with the host binned-SAH BVH, the device SAH build
+    (the same tree) and the device linear BVH (second commit of each, after a
+    warm-up commit), and the headline render through each device-built tree with
+    the same launch shape, timed like the headline (CUDA events, L2 flush between
+    steps)."""
     from litert_gb300 import lrt
     out = {}
     n_rays = sum(w * hh for w, hh, _, _ in views)
-    for builder in (0, 1):
+    for builder, name in ((0, "host_sah"), (1, "device_sah"), (2, "device_lbvh")):
         s = lrt.Scene(0)
         s.set_tuning("bvh_builder", builder)
         gid = s.add_sbs(h, nodes, values)
@@ -166,7 +167,7 @@ def run_device_bvh(args, h, nodes, values, views, tuned, hits, flush, stream, to
         s.commit_scene()
         t0 = time.perf_counter()
         s.commit_scene()
-        out["commit_s_host_bvh" if builder == 0 else "commit_s_device_bvh"] = round(time.perf_counter() - t0, 3)
+        out["commit_s_" + name] = round(time.perf_counter() - t0, 3)
         if builder == 0:
             s.close()
             continue
@@ -191,8 +192,7 @@ def run_device_bvh(args, h, nodes, values, views, tuned, hits, flush, stream, to
         lrt.Scene.graph_destroy(g)
         s.close()
         ms = sum(ts) / len(ts)
-        out["render_ms"] = ms
-        out["render_value"] = n_rays / (ms * 1e-3) / 1e6
+        out["render_value_" + name] = n_rays / (ms * 1e-3) / 1e6
     return out
 
 

@@ -242,11 +242,6 @@ __device__ __forceinline__ Box node_box(const float *nb, uint32_t c) {   // writ
 __device__ __forceinline__ Box child_box(const float *b6, const uint32_t *sid, const float *nb, uint32_t c) {
   return (c & kLeafBit) ? prim_box(b6, sid[c & ~kLeafBit]) : node_box(nb, c);
 }
-__device__ __forceinline__ float area(const Box &b) {   // the host builder's Aabb::area
-  const float dx = fmaxf(0.0f, b.hi[0] - b.lo[0]), dy = fmaxf(0.0f, b.hi[1] - b.lo[1]),
-              dz = fmaxf(0.0f, b.hi[2] - b.lo[2]);
-  return 2.0f * (dx * dy + dy * dz + dz * dx);
-}
 
 // One thread per leaf climbs towards the root; the first thread to reach a node
 // stops there, the second (which sees both children finished) writes its box.
@@ -274,9 +269,260 @@ __global__ void node_boxes(const float *b6, const uint32_t *sid, uint32_t n, con
   }
 }
 
-// ---- collapse into 4-wide nodes, one wide level per pass ----
-__global__ void collapse_pick(const uint32_t *front, uint32_t nf, const uint32_t *child, const float *b6,
-                              const uint32_t *sid, const float *nb, uint32_t *pick, uint32_t *n_internal) {
+// ---- leaves of the radix tree in the common BVH2 form ----
+// Leaf i (sorted position i) holds primitive sid[i]: its box, and the payload a
+// wide node stores for it (box id, or a one-triangle range of the sorted order).
+__global__ void lbvh_leaves(const float *b6, const uint32_t *sid, uint32_t n, bool boxes, float *lbox,
+                            uint32_t *lpay) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t p = sid[i];
+#pragma unroll
+  for (int k = 0; k < 6; k++) lbox[6 * size_t(i) + k] = b6[6 * size_t(p) + k];
+  lpay[i] = boxes ? (kLeafBit | p) : (kLeafBit | (1u << 24) | i);
+}
+
+// ---- exact binned SAH, one tree level per pass (the host builder restated) ----
+// Segment k of a level is the primitive range [seg_b, seg_e) of `order` under
+// one BVH2 node.  A block per segment: box and centroid bounds, the 32 bins of
+// every axis with a non-zero centroid extent (the host's expressions), the cost
+// sweep on one thread in the host's order, and a stable partition (or the object
+// median by (centroid, id) when no split is found or below depth 40).  The tree's
+// shape depends only on these sets, so it is the host builder's tree.
+constexpr int kNB = 32;
+constexpr uint32_t kSahThreads = 128;
+constexpr uint32_t kMedianMax = 4096;   // larger median-fallback segments go back to the host builder
+
+__device__ __forceinline__ float fmn(float a, float b) { return (b < a) ? b : a; }   // std::min
+__device__ __forceinline__ float fmx(float a, float b) { return (a < b) ? b : a; }   // std::max
+__device__ __forceinline__ float area6(const float lo[3], const float hi[3]) {
+  const float dx = fmx(0.0f, hi[0] - lo[0]), dy = fmx(0.0f, hi[1] - lo[1]), dz = fmx(0.0f, hi[2] - lo[2]);
+  return 2.0f * (dx * dy + dy * dz + dz * dx);
+}
+
+__global__ void centroids(const float *b6, uint32_t n, float *cent, uint32_t *order) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+#pragma unroll
+  for (int k = 0; k < 3; k++) cent[3 * size_t(i) + k] = 0.5f * (b6[6 * size_t(i) + k] + b6[6 * size_t(i) + 3 + k]);
+  order[i] = i;
+}
+
+// block-wide min of v[0..5] and max of v[6..11] (12 values), result in out[12]
+__device__ void block_minmax12(float v[12], float *sh /* [kSahThreads/32][12] */, float out[12]) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 12; k++)
+    for (int o = 16; o > 0; o >>= 1) {
+      const float u = __shfl_xor_sync(0xffffffffu, v[k], o);
+      v[k] = k < 6 ? fminf(v[k], u) : fmaxf(v[k], u);
+    }
+  if (lane == 0)
+    for (int k = 0; k < 12; k++) sh[w * 12 + k] = v[k];
+  __syncthreads();
+  for (int k = 0; k < 12; k++) {
+    float r = sh[k];
+    for (uint32_t x = 1; x < kSahThreads / 32; x++) r = k < 6 ? fminf(r, sh[x * 12 + k]) : fmaxf(r, sh[x * 12 + k]);
+    out[k] = r;
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kSahThreads) sah_level(const float *b6, const float *cent, uint32_t *order,
+                                                         uint32_t *tmp, uint32_t *rank, const uint32_t *seg_b,
+                                                         const uint32_t *seg_e,
+                                                         uint32_t depth, uint32_t max_leaf, float *seg_box,
+                                                         uint32_t *seg_split, uint32_t *seg_flag, uint32_t *err) {
+  __shared__ float red[kSahThreads / 32 * 12];
+  __shared__ uint32_t bl[3][kNB][3], bh[3][kNB][3], bc[3][kNB];
+  __shared__ int s_axis, s_bin, s_median;
+  __shared__ uint32_t s_nleft, s_run, s_wsum[kSahThreads / 32];
+  const uint32_t k = blockIdx.x, b = seg_b[k], e = seg_e[k], m = e - b, tid = threadIdx.x;
+  // 1. node box and centroid bounds
+  float v[12];
+  for (int q = 0; q < 6; q++) { v[q] = 3.4e38f; v[6 + q] = -3.4e38f; }
+  for (uint32_t i = b + tid; i < e; i += kSahThreads) {
+    const uint32_t p = order[i];
+    for (int a = 0; a < 3; a++) {
+      v[a] = fminf(v[a], b6[6 * size_t(p) + a]);
+      v[6 + a] = fmaxf(v[6 + a], b6[6 * size_t(p) + 3 + a]);
+      v[3 + a] = fminf(v[3 + a], cent[3 * size_t(p) + a]);
+      v[9 + a] = fmaxf(v[9 + a], cent[3 * size_t(p) + a]);
+    }
+  }
+  float r[12];
+  block_minmax12(v, red, r);   // r: box lo 0-2, cb lo 3-5, box hi 6-8, cb hi 9-11
+  if (tid == 0) {
+    for (int a = 0; a < 3; a++) { seg_box[6 * size_t(k) + a] = r[a]; seg_box[6 * size_t(k) + 3 + a] = r[6 + a]; }
+    seg_flag[k] = m > max_leaf ? 1u : 0u;
+  }
+  if (m <= max_leaf) return;
+  const float cl[3] = {r[3], r[4], r[5]}, ch[3] = {r[9], r[10], r[11]};
+  float sc[3];
+  bool use[3];
+  for (int a = 0; a < 3; a++) {
+    const float ext = ch[a] - cl[a];
+    use[a] = depth < 40 && ext > 0;
+    sc[a] = use[a] ? kNB / ext : 0.0f;
+  }
+  // 2. bins: counts and boxes (ordered-integer atomics; empty bins stay the reset box)
+  for (uint32_t q = tid; q < 3 * kNB; q += kSahThreads) {
+    const uint32_t a = q / kNB, i = q % kNB;
+    bc[a][i] = 0;
+    for (int c = 0; c < 3; c++) { bl[a][i][c] = ord(3.4e38f); bh[a][i][c] = ord(-3.4e38f); }
+  }
+  __syncthreads();
+  for (uint32_t i = b + tid; i < e; i += kSahThreads) {
+    const uint32_t p = order[i];
+    for (int a = 0; a < 3; a++) {
+      if (!use[a]) continue;
+      int bi = int((cent[3 * size_t(p) + a] - cl[a]) * sc[a]);
+      bi = min(max(bi, 0), kNB - 1);
+      atomicAdd(&bc[a][bi], 1u);
+      for (int c = 0; c < 3; c++) {
+        atomicMin(&bl[a][bi][c], ord(b6[6 * size_t(p) + c]));
+        atomicMax(&bh[a][bi][c], ord(b6[6 * size_t(p) + 3 + c]));
+      }
+    }
+  }
+  __syncthreads();
+  // 3. cost sweep (Builder::split), one thread
+  if (tid == 0) {
+    float best_cost = 3.4e38f;
+    int best_axis = -1, best_bin = -1;
+    for (int a = 0; a < 3; a++) {
+      if (!use[a]) continue;
+      float rA[kNB];
+      uint32_t rN[kNB];
+      float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+      uint32_t cnt = 0;
+      for (int i = kNB - 1; i > 0; i--) {
+        for (int c = 0; c < 3; c++) { lo[c] = fmn(lo[c], unord(bl[a][i][c])); hi[c] = fmx(hi[c], unord(bh[a][i][c])); }
+        cnt += bc[a][i];
+        rA[i] = area6(lo, hi);
+        rN[i] = cnt;
+      }
+      for (int c = 0; c < 3; c++) { lo[c] = 3.4e38f; hi[c] = -3.4e38f; }
+      cnt = 0;
+      for (int i = 0; i < kNB - 1; i++) {
+        for (int c = 0; c < 3; c++) { lo[c] = fmn(lo[c], unord(bl[a][i][c])); hi[c] = fmx(hi[c], unord(bh[a][i][c])); }
+        cnt += bc[a][i];
+        if (cnt == 0 || rN[i + 1] == 0) continue;
+        const float cost = area6(lo, hi) * float(cnt) + rA[i + 1] * float(rN[i + 1]);
+        if (cost < best_cost) { best_cost = cost; best_axis = a; best_bin = i; }
+      }
+    }
+    s_median = best_axis < 0;
+    if (best_axis < 0) {   // object median on the widest centroid axis
+      int ax = 0;
+      for (int c = 1; c < 3; c++) if (ch[c] - cl[c] > ch[ax] - cl[ax]) ax = c;
+      best_axis = ax;
+      s_nleft = m / 2;
+    } else {
+      uint32_t nl = 0;
+      for (int i = 0; i <= best_bin; i++) nl += bc[best_axis][i];
+      s_nleft = nl;
+    }
+    s_axis = best_axis;
+    s_bin = best_bin;
+    s_run = 0;
+  }
+  __syncthreads();
+  const int ax = s_axis, bin = s_bin;
+  const bool median = s_median;
+  const uint32_t nleft = s_nleft;
+  if (median && m > kMedianMax) {   // too large for the quadratic rank below: the caller builds on the host
+    if (tid == 0) {
+      atomicOr(err, 1u);
+      seg_flag[k] = 0;   // closed as a leaf so the level stays well formed
+    }
+    return;
+  }
+  // median: rank of every element by (centroid, id) among the segment
+  if (median) {
+    for (uint32_t i = b + tid; i < e; i += kSahThreads) {
+      const uint32_t p = order[i];
+      const float cp = cent[3 * size_t(p) + ax];
+      uint32_t r = 0;
+      for (uint32_t j = b; j < e; j++) {
+        const uint32_t q = order[j];
+        const float cq = cent[3 * size_t(q) + ax];
+        r += (cq < cp || (cq == cp && q < p)) ? 1u : 0u;
+      }
+      rank[i] = r;
+    }
+    __syncthreads();
+  }
+  // 4. stable partition into tmp, chunk by chunk, then back into order
+  const uint32_t lane = tid & 31, w = tid >> 5;
+  for (uint32_t base = b; base < e; base += kSahThreads) {
+    const uint32_t i = base + tid;
+    bool in = i < e, left = false;
+    uint32_t p = 0;
+    if (in) {
+      p = order[i];
+      if (median) {
+        left = rank[i] < nleft;
+      } else {
+        int bi = int((cent[3 * size_t(p) + ax] - cl[ax]) * sc[ax]);
+        bi = min(max(bi, 0), kNB - 1);
+        left = bi <= bin;
+      }
+    }
+    const uint32_t bal = __ballot_sync(0xffffffffu, in && left);
+    if (lane == 0) s_wsum[w] = __popc(bal);
+    __syncthreads();
+    uint32_t before = s_run, chunk_left = 0;
+    for (uint32_t x = 0; x < kSahThreads / 32; x++) {
+      if (x < w) before += s_wsum[x];
+      chunk_left += s_wsum[x];
+    }
+    before += __popc(bal & ((1u << lane) - 1u));
+    __syncthreads();
+    if (in) {   // left: slot b + (lefts before it); right: slot b + nleft + (rights before it)
+      const uint32_t pos = left ? b + before : b + nleft + ((i - b) - before);
+      tmp[pos] = p;
+    }
+    if (tid == 0) s_run += chunk_left;
+    __syncthreads();
+  }
+  for (uint32_t i = b + tid; i < e; i += kSahThreads) order[i] = tmp[i];
+  if (tid == 0) seg_split[k] = b + nleft;
+}
+
+// After a level's scan of seg_flag: internal nodes and leaves get their ids (level
+// order, the host builder's breadth-first pair order), parents learn their
+// children, split segments emit their two halves for the next level.
+__global__ void sah_link(uint32_t nseg, const uint32_t *seg_b, const uint32_t *seg_e, const uint32_t *seg_parent,
+                         const float *seg_box, const uint32_t *seg_split, const uint32_t *seg_flag,
+                         const uint32_t *excl, uint32_t int_base, uint32_t leaf_base, const uint32_t *order,
+                         bool boxes, uint32_t *child, float *ibox, float *lbox, uint32_t *lpay, uint32_t *nb_,
+                         uint32_t *ne_, uint32_t *np_) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nseg) return;
+  const uint32_t b = seg_b[k], e = seg_e[k];
+  uint32_t ref;
+  if (seg_flag[k]) {
+    const uint32_t q = int_base + excl[k];
+    ref = q;
+    for (int c = 0; c < 6; c++) ibox[6 * size_t(q) + c] = seg_box[6 * size_t(k) + c];
+    const uint32_t j = 2 * excl[k], m = seg_split[k];
+    nb_[j] = b; ne_[j] = m; np_[j] = 2 * q;
+    nb_[j + 1] = m; ne_[j + 1] = e; np_[j + 1] = 2 * q + 1;
+  } else {
+    const uint32_t l = leaf_base + (k - excl[k]);
+    ref = kLeafBit | l;
+    for (int c = 0; c < 6; c++) lbox[6 * size_t(l) + c] = seg_box[6 * size_t(k) + c];
+    lpay[l] = boxes ? (kLeafBit | order[b]) : (kLeafBit | (((e - b) & 0x7Fu) << 24) | (b & 0x00FFFFFFu));
+  }
+  if (seg_parent[k] != kNone) child[seg_parent[k]] = ref;
+}
+
+// ---- collapse into 4-wide nodes, one wide level per pass (the host builder's) ----
+// child: 2 per internal node, internal id or kLeafBit | leaf id; ibox / lbox:
+// 6 floats per internal node / leaf; lpay: the leaf's wide-node payload.
+__global__ void collapse_pick(const uint32_t *front, uint32_t nf, const uint32_t *child, const float *ibox,
+                              uint32_t *pick, uint32_t *n_internal) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nf) return;
   const uint32_t r = front[k];
@@ -292,7 +538,9 @@ __global__ void collapse_pick(const uint32_t *front, uint32_t nf, const uint32_t
       float best_a = -1.0f;
       for (int i = 0; i < nc; i++)
         if (!(ch[i] & kLeafBit)) {
-          const float a = area(child_box(b6, sid, nb, ch[i]));
+          float lo[3], hi[3];
+          for (int c = 0; c < 3; c++) { lo[c] = ibox[6 * size_t(ch[i]) + c]; hi[c] = ibox[6 * size_t(ch[i]) + 3 + c]; }
+          const float a = area6(lo, hi);
           if (a > best_a) {
             best_a = a;
             best = i;
@@ -314,7 +562,7 @@ __global__ void collapse_pick(const uint32_t *front, uint32_t nf, const uint32_t
 }
 
 __global__ void collapse_write(const uint32_t *pick, uint32_t nf, const uint32_t *off, uint32_t level_base,
-                               uint32_t next_base, const float *b6, const uint32_t *sid, const float *nb, bool boxes,
+                               uint32_t next_base, const float *ibox, const float *lbox, const uint32_t *lpay,
                                WNode4 *wn, uint32_t *next_front) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nf) return;
@@ -330,12 +578,13 @@ __global__ void collapse_write(const uint32_t *pick, uint32_t nf, const uint32_t
       w.child[i] = kEmptyChild;
       continue;
     }
-    const Box b = child_box(b6, sid, nb, c);
-    w.lo_x[i] = b.lo[0]; w.lo_y[i] = b.lo[1]; w.lo_z[i] = b.lo[2];
-    w.hi_x[i] = b.hi[0]; w.hi_y[i] = b.hi[1]; w.hi_z[i] = b.hi[2];
-    if (c & kLeafBit) {
-      const uint32_t pos = c & ~kLeafBit;
-      w.child[i] = boxes ? (kLeafBit | sid[pos]) : (kLeafBit | (1u << 24) | pos);
+    const bool leaf = (c & kLeafBit) != 0;
+    const uint32_t id = c & ~kLeafBit;
+    const float *bx = leaf ? lbox + 6 * size_t(id) : ibox + 6 * size_t(id);
+    w.lo_x[i] = bx[0]; w.lo_y[i] = bx[1]; w.lo_z[i] = bx[2];
+    w.hi_x[i] = bx[3]; w.hi_y[i] = bx[4]; w.hi_z[i] = bx[5];
+    if (leaf) {
+      w.child[i] = lpay[id];
     } else {
       w.child[i] = next_base + off[k] + j;
       next_front[off[k] + j] = c;
@@ -346,41 +595,44 @@ __global__ void collapse_write(const uint32_t *pick, uint32_t nf, const uint32_t
 }
 
 // ---- reference fat-pair layout: pair i holds the two children of internal node i ----
-__device__ __forceinline__ void pair_side(lrt_bvh_node &s, uint32_t c, const float *b6, const uint32_t *sid,
-                                          const float *nb, bool boxes, uint32_t *lsc) {
-  const Box b = child_box(b6, sid, nb, c);
+// (breadth-first over internal nodes, leaves numbered in the same order, as
+// BVH/cbvh_fat.cpp:100-142 numbers them)
+__device__ __forceinline__ void pair_side(lrt_bvh_node &s, uint32_t c, const float *ibox, const float *lbox,
+                                          const uint32_t *lpay, bool boxes, uint32_t *lsc) {
+  const bool leaf = (c & kLeafBit) != 0;
+  const uint32_t id = c & ~kLeafBit;
+  const float *bx = leaf ? lbox + 6 * size_t(id) : ibox + 6 * size_t(id);
 #pragma unroll
   for (int k = 0; k < 3; k++) {
-    s.boxMin[k] = b.lo[k];
-    s.boxMax[k] = b.hi[k];
+    s.boxMin[k] = bx[k];
+    s.boxMax[k] = bx[3 + k];
   }
   s.escapeIndex = 0;
-  if (c & kLeafBit) {
-    const uint32_t pos = c & ~kLeafBit;
+  if (leaf) {
     if (boxes) {
-      s.leftOffset = kLeafBit | (1u << 24) | (sid[pos] & 0x00FFFFFFu);
+      s.leftOffset = kLeafBit | (1u << 24) | ((lpay[id] & ~kLeafBit) & 0x00FFFFFFu);
     } else {
-      s.leftOffset = kLeafBit | (1u << 24) | (pos & 0x00FFFFFFu);
-      if (lsc) lsc[pos] = kLeafBit | (1u << 24) | (pos & 0x00FFFFFFu);
+      s.leftOffset = kLeafBit | (1u << 24) | (id & 0x00FFFFFFu);
+      if (lsc) lsc[id] = lpay[id];
     }
   } else {
     s.leftOffset = c;
   }
 }
 
-__global__ void fat_pairs(uint32_t n, const uint32_t *child, const float *b6, const uint32_t *sid, const float *nb,
-                          bool boxes, lrt_bvh_pair *pairs, uint32_t *lsc) {
+__global__ void fat_pairs(uint32_t n_int, uint32_t root, const uint32_t *child, const float *ibox, const float *lbox,
+                          const uint32_t *lpay, bool boxes, lrt_bvh_pair *pairs, uint32_t *lsc) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (n == 1) {   // a single leaf: both sides are the root leaf
+  if (root & kLeafBit) {   // a single leaf: both sides are the root leaf
     if (i == 0) {
-      pair_side(pairs[0].left, kLeafBit, b6, sid, nb, boxes, lsc);
+      pair_side(pairs[0].left, root, ibox, lbox, lpay, boxes, lsc);
       pairs[0].right = pairs[0].left;
     }
     return;
   }
-  if (i >= n - 1) return;
-  pair_side(pairs[i].left, child[2 * i], b6, sid, nb, boxes, lsc);
-  pair_side(pairs[i].right, child[2 * i + 1], b6, sid, nb, boxes, lsc);
+  if (i >= n_int) return;
+  pair_side(pairs[i].left, child[2 * i], ibox, lbox, lpay, boxes, lsc);
+  pair_side(pairs[i].right, child[2 * i + 1], ibox, lbox, lpay, boxes, lsc);
 }
 
 // ---- refit of a wide tree, one level (deepest first) ----
@@ -470,79 +722,129 @@ struct Tmp {
     if (e_ != cudaSuccess) return e_;       \
   } while (0)
 
-cudaError_t build_bvh_gpu(const float *d_boxes6, uint32_t n, bool boxes, WNode4 *d_wnodes, uint32_t *d_order,
-                          lrt_bvh_pair *d_pairs, uint32_t *d_leaf_start_count, GpuBvhInfo &info, cudaStream_t st) {
+cudaError_t build_bvh_gpu(const float *d_boxes6, uint32_t n, bool boxes, bool sah, WNode4 *d_wnodes,
+                          uint32_t *d_order, lrt_bvh_pair *d_pairs, uint32_t *d_leaf_start_count, GpuBvhInfo &info,
+                          cudaStream_t st) {
   info = GpuBvhInfo{};
   if (n == 0) return cudaErrorInvalidValue;
-  const uint32_t n_int = n > 1 ? n - 1 : 1;
-  Tmp<uint32_t> ob, code, id, code2, id2, hist, hoff, child, par_i, par_l, visits, err, front, front2, pick, cnt, off;
-  Tmp<float> nb;
-  for (auto *t : {&ob, &code, &id, &code2, &id2, &hist, &hoff, &child, &par_i, &par_l, &visits, &err, &front, &front2,
-                  &pick, &cnt, &off})
-    t->st = st;
-  nb.st = st;
-  const uint32_t nblk = blocks(n, kSortTile);
-  LRT_TRY(ob.alloc(6, st));
-  LRT_TRY(code.alloc(n, st));
-  LRT_TRY(id.alloc(n, st));
-  LRT_TRY(code2.alloc(n, st));
-  LRT_TRY(id2.alloc(n, st));
-  LRT_TRY(hist.alloc(16 * size_t(nblk), st));
-  LRT_TRY(hoff.alloc(16 * size_t(nblk), st));
-  LRT_TRY(child.alloc(2 * size_t(n_int), st));
-  LRT_TRY(par_i.alloc(n_int, st));
-  LRT_TRY(par_l.alloc(n, st));
-  LRT_TRY(visits.alloc(n_int, st));
+  const uint32_t n_cap = n > 1 ? n - 1 : 1;   // internal nodes at most
+  // the BVH2 in common form
+  Tmp<uint32_t> child, lpay, sidb, err;
+  Tmp<float> ibox, lbox;
+  for (auto *t : {&child, &lpay, &sidb, &err}) t->st = st;
+  ibox.st = lbox.st = st;
+  LRT_TRY(child.alloc(2 * size_t(n_cap), st));
+  LRT_TRY(ibox.alloc(6 * size_t(n_cap), st));
+  LRT_TRY(lbox.alloc(6 * size_t(n), st));
+  LRT_TRY(lpay.alloc(n, st));
+  LRT_TRY(sidb.alloc(n, st));
   LRT_TRY(err.alloc(1, st));
-  LRT_TRY(nb.alloc(6 * size_t(n_int), st));
-  LRT_TRY(front.alloc(n, st));
-  LRT_TRY(front2.alloc(n, st));
-  LRT_TRY(pick.alloc(4 * size_t(n), st));
-  LRT_TRY(cnt.alloc(n, st));
-  LRT_TRY(off.alloc(n, st));
-
-  // 1-2. centroid bounds, Morton codes
-  bounds_init<<<1, 32, 0, st>>>(ob.p);
-  centroid_bounds<<<std::min<uint32_t>(blocks(n, 256), 2048), 256, 0, st>>>(d_boxes6, n, ob.p);
-  morton_codes<<<blocks(n, 256), 256, 0, st>>>(d_boxes6, n, ob.p, code.p, id.p);
-  LRT_TRY(cudaGetLastError());
-  // 3. radix sort, 8 passes of 4 bits (an even count: the result ends in code/id)
-  uint32_t *ki = code.p, *vi = id.p, *ko = code2.p, *vo = id2.p;
-  for (uint32_t shift = 0; shift < 32; shift += 4) {
-    radix_count<<<nblk, kSortThreads, 0, st>>>(ki, n, shift, nblk, hist.p);
+  LRT_TRY(cudaMemsetAsync(err.p, 0, 4, st));
+  uint32_t root = 0, n_int = 0, n_leaf = 0;
+  if (sah) {
+    // exact binned SAH, level by level
+    const uint32_t max_leaf = boxes ? 1u : 2u;
+    Tmp<float> cent, sbox;
+    Tmp<uint32_t> tmp, rank, sb, se, sp, nb_, ne_, np_, split, flag, excl;
+    cent.st = sbox.st = st;
+    for (auto *t : {&tmp, &rank, &sb, &se, &sp, &nb_, &ne_, &np_, &split, &flag, &excl}) t->st = st;
+    LRT_TRY(cent.alloc(3 * size_t(n), st));
+    LRT_TRY(sbox.alloc(6 * size_t(n), st));
+    for (auto *t : {&tmp, &rank, &sb, &se, &sp, &nb_, &ne_, &np_, &split, &flag, &excl}) LRT_TRY(t->alloc(n, st));
+    centroids<<<blocks(n, 256), 256, 0, st>>>(d_boxes6, n, cent.p, sidb.p);
+    const uint32_t seg0[3] = {0u, n, kNone};
+    LRT_TRY(cudaMemcpyAsync(sb.p, &seg0[0], 4, cudaMemcpyHostToDevice, st));
+    LRT_TRY(cudaMemcpyAsync(se.p, &seg0[1], 4, cudaMemcpyHostToDevice, st));
+    LRT_TRY(cudaMemcpyAsync(sp.p, &seg0[2], 4, cudaMemcpyHostToDevice, st));
+    uint32_t nseg = 1, depth = 0;
+    uint32_t *cb = sb.p, *ce = se.p, *cp = sp.p, *xb = nb_.p, *xe = ne_.p, *xp = np_.p;
+    while (nseg > 0) {
+      sah_level<<<nseg, kSahThreads, 0, st>>>(d_boxes6, cent.p, sidb.p, tmp.p, rank.p, cb, ce, depth, max_leaf, sbox.p,
+                                              split.p, flag.p, err.p);
+      LRT_TRY(cudaGetLastError());
+      uint64_t n_split = 0;
+      LRT_TRY(gpu_exclusive_scan(flag.p, excl.p, nseg, &n_split, st));
+      sah_link<<<blocks(nseg, 128), 128, 0, st>>>(nseg, cb, ce, cp, sbox.p, split.p, flag.p, excl.p, n_int, n_leaf,
+                                                  sidb.p, boxes, child.p, ibox.p, lbox.p, lpay.p, xb, xe, xp);
+      LRT_TRY(cudaGetLastError());
+      n_int += uint32_t(n_split);
+      n_leaf += nseg - uint32_t(n_split);
+      nseg = 2 * uint32_t(n_split);
+      std::swap(cb, xb);
+      std::swap(ce, xe);
+      std::swap(cp, xp);
+      depth++;
+    }
+    uint32_t herr = 0;
+    LRT_TRY(cudaMemcpyAsync(&herr, err.p, 4, cudaMemcpyDeviceToHost, st));
+    LRT_TRY(cudaStreamSynchronize(st));
+    if (herr) return cudaErrorNotSupported;   // a median split too large for the device path
+    root = n > max_leaf ? 0u : kLeafBit;
+  } else {
+    // linear BVH: Morton codes, radix sort, radix tree, node boxes
+    Tmp<uint32_t> ob, code, code2, id2, hist, hoff, par_i, par_l, visits;
+    for (auto *t : {&ob, &code, &code2, &id2, &hist, &hoff, &par_i, &par_l, &visits}) t->st = st;
+    const uint32_t nblk = blocks(n, kSortTile);
+    LRT_TRY(ob.alloc(6, st));
+    LRT_TRY(code.alloc(n, st));
+    LRT_TRY(code2.alloc(n, st));
+    LRT_TRY(id2.alloc(n, st));
+    LRT_TRY(hist.alloc(16 * size_t(nblk), st));
+    LRT_TRY(hoff.alloc(16 * size_t(nblk), st));
+    LRT_TRY(par_i.alloc(n_cap, st));
+    LRT_TRY(par_l.alloc(n, st));
+    LRT_TRY(visits.alloc(n_cap, st));
+    bounds_init<<<1, 32, 0, st>>>(ob.p);
+    centroid_bounds<<<std::min<uint32_t>(blocks(n, 256), 2048), 256, 0, st>>>(d_boxes6, n, ob.p);
+    morton_codes<<<blocks(n, 256), 256, 0, st>>>(d_boxes6, n, ob.p, code.p, sidb.p);
     LRT_TRY(cudaGetLastError());
-    LRT_TRY(gpu_exclusive_scan(hist.p, hoff.p, 16 * nblk, nullptr, st));
-    radix_scatter<<<nblk, kSortThreads, 0, st>>>(ki, vi, ko, vo, n, shift, nblk, hoff.p);
-    LRT_TRY(cudaGetLastError());
-    std::swap(ki, ko);
-    std::swap(vi, vo);
-  }
-  const uint32_t *sid = vi;
-  // 4-5. radix tree and node boxes
-  if (n > 1) {
-    radix_tree<<<blocks(n - 1, 256), 256, 0, st>>>(ki, n, child.p, par_i.p, par_l.p);
-    LRT_TRY(cudaMemsetAsync(visits.p, 0, size_t(n_int) * 4, st));
-    LRT_TRY(cudaMemsetAsync(err.p, 0, 4, st));
-    node_boxes<<<blocks(n, 256), 256, 0, st>>>(d_boxes6, sid, n, child.p, par_i.p, par_l.p, nb.p, visits.p, err.p);
+    // radix sort, 8 passes of 4 bits (an even count: the result ends in code / sidb)
+    uint32_t *ki = code.p, *vi = sidb.p, *ko = code2.p, *vo = id2.p;
+    for (uint32_t shift = 0; shift < 32; shift += 4) {
+      radix_count<<<nblk, kSortThreads, 0, st>>>(ki, n, shift, nblk, hist.p);
+      LRT_TRY(cudaGetLastError());
+      LRT_TRY(gpu_exclusive_scan(hist.p, hoff.p, 16 * nblk, nullptr, st));
+      radix_scatter<<<nblk, kSortThreads, 0, st>>>(ki, vi, ko, vo, n, shift, nblk, hoff.p);
+      LRT_TRY(cudaGetLastError());
+      std::swap(ki, ko);
+      std::swap(vi, vo);
+    }
+    if (n > 1) {
+      radix_tree<<<blocks(n - 1, 256), 256, 0, st>>>(ki, n, child.p, par_i.p, par_l.p);
+      LRT_TRY(cudaMemsetAsync(visits.p, 0, size_t(n_cap) * 4, st));
+      node_boxes<<<blocks(n, 256), 256, 0, st>>>(d_boxes6, sidb.p, n, child.p, par_i.p, par_l.p, ibox.p, visits.p,
+                                                 err.p);
+      LRT_TRY(cudaGetLastError());
+    }
+    lbvh_leaves<<<blocks(n, 256), 256, 0, st>>>(d_boxes6, sidb.p, n, boxes, lbox.p, lpay.p);
     LRT_TRY(cudaGetLastError());
     uint32_t herr = 0;
     LRT_TRY(cudaMemcpyAsync(&herr, err.p, 4, cudaMemcpyDeviceToHost, st));
     LRT_TRY(cudaStreamSynchronize(st));
     if (herr) return cudaErrorUnknown;
+    root = n > 1 ? 0u : kLeafBit;
+    n_int = n > 1 ? n - 1 : 0;
+    n_leaf = n;
   }
-  // 6. collapse, level by level
-  const uint32_t root = n > 1 ? 0u : kLeafBit;
+  // collapse, level by level
+  Tmp<uint32_t> front, front2, pick, cnt, off;
+  for (auto *t : {&front, &front2, &pick, &cnt, &off}) t->st = st;
+  LRT_TRY(front.alloc(n, st));
+  LRT_TRY(front2.alloc(n, st));
+  LRT_TRY(pick.alloc(4 * size_t(n), st));
+  LRT_TRY(cnt.alloc(n, st));
+  LRT_TRY(off.alloc(n, st));
   LRT_TRY(cudaMemcpyAsync(front.p, &root, 4, cudaMemcpyHostToDevice, st));
   uint32_t nf = 1, level_base = 0;
   uint32_t *fr = front.p, *fr2 = front2.p;
   while (nf > 0) {
     info.level_start.push_back(level_base);
-    collapse_pick<<<blocks(nf, 128), 128, 0, st>>>(fr, nf, child.p, d_boxes6, sid, nb.p, pick.p, cnt.p);
+    collapse_pick<<<blocks(nf, 128), 128, 0, st>>>(fr, nf, child.p, ibox.p, pick.p, cnt.p);
     LRT_TRY(cudaGetLastError());
     uint64_t total = 0;
     LRT_TRY(gpu_exclusive_scan(cnt.p, off.p, nf, &total, st));
-    collapse_write<<<blocks(nf, 128), 128, 0, st>>>(pick.p, nf, off.p, level_base, level_base + nf, d_boxes6, sid,
-                                                    nb.p, boxes, d_wnodes, fr2);
+    collapse_write<<<blocks(nf, 128), 128, 0, st>>>(pick.p, nf, off.p, level_base, level_base + nf, ibox.p, lbox.p,
+                                                    lpay.p, d_wnodes, fr2);
     LRT_TRY(cudaGetLastError());
     level_base += nf;
     nf = uint32_t(total);
@@ -550,11 +852,12 @@ cudaError_t build_bvh_gpu(const float *d_boxes6, uint32_t n, bool boxes, WNode4 
   }
   info.n_wnodes = level_base;
   info.max_depth = uint32_t(info.level_start.size()) - 1;
-  // 7. outputs
-  if (d_order) LRT_TRY(cudaMemcpyAsync(d_order, sid, size_t(n) * 4, cudaMemcpyDeviceToDevice, st));
+  info.n_pairs = std::max<uint32_t>(1, n_int);
+  info.n_leaves = n_leaf;
+  if (d_order) LRT_TRY(cudaMemcpyAsync(d_order, sidb.p, size_t(n) * 4, cudaMemcpyDeviceToDevice, st));
   if (d_pairs) {
-    fat_pairs<<<blocks(n_int, 256), 256, 0, st>>>(n, child.p, d_boxes6, sid, nb.p, boxes, d_pairs,
-                                                  boxes ? nullptr : d_leaf_start_count);
+    fat_pairs<<<blocks(info.n_pairs, 256), 256, 0, st>>>(n_int, root, child.p, ibox.p, lbox.p, lpay.p, boxes, d_pairs,
+                                                         boxes ? nullptr : d_leaf_start_count);
     LRT_TRY(cudaGetLastError());
   }
   return cudaStreamSynchronize(st);

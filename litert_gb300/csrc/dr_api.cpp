@@ -328,7 +328,8 @@ extern "C" lrt_status lrt_dr_set_scene(lrt_ctx *ctx, const lrt_sbs_header *hdr, 
         boxes[6 * i + 3 + k] = lo[k] + 2.0f * 1 / sz;
       }
     }
-    if (ctx->bvh_builder == 1) {   // device linear BVH (lrt_set_tuning "bvh_builder"), pairs fetched back
+    bool built = false;
+    if (ctx->bvh_builder != 0) {   // device build (lrt_set_tuning "bvh_builder"), pairs fetched back
       const uint32_t n_int = n_nodes > 1 ? n_nodes - 1 : 1;
       DevBuf<float> d_boxes;
       DevBuf<WNode4> d_wide;
@@ -337,15 +338,22 @@ extern "C" lrt_status lrt_dr_set_scene(lrt_ctx *ctx, const lrt_sbs_header *hdr, 
       if (e == cudaSuccess) e = d_wide.ensure(n_int);
       if (e == cudaSuccess) e = d_pairs.ensure(n_int);
       GpuBvhInfo info;
-      if (e == cudaSuccess) e = build_bvh_gpu(d_boxes.p, n_nodes, true, d_wide.p, nullptr, d_pairs.p, nullptr, info, 0);
-      st.pairs.resize(n_int);
       if (e == cudaSuccess)
-        e = cudaMemcpy(st.pairs.data(), d_pairs.p, size_t(n_int) * sizeof(lrt_bvh_pair), cudaMemcpyDeviceToHost);
+        e = build_bvh_gpu(d_boxes.p, n_nodes, true, ctx->bvh_builder == 1, d_wide.p, nullptr, d_pairs.p, nullptr,
+                          info, 0);
+      if (e == cudaSuccess) {
+        st.pairs.resize(info.n_pairs);
+        e = cudaMemcpy(st.pairs.data(), d_pairs.p, size_t(info.n_pairs) * sizeof(lrt_bvh_pair),
+                       cudaMemcpyDeviceToHost);
+        built = e == cudaSuccess;
+      }
       d_boxes.release();
       d_wide.release();
       d_pairs.release();
-      if (e != cudaSuccess) return cuda_fail(ctx, e, "lrt_dr_set_scene: device BVH build");
-    } else {
+      if (e == cudaErrorNotSupported) (void)cudaGetLastError();   // the host builder makes the same tree
+      else if (e != cudaSuccess) return cuda_fail(ctx, e, "lrt_dr_set_scene: device BVH build");
+    }
+    if (!built) {
       BvhData b;
       s = build_bvh(boxes.data(), n_nodes, true, b);
       if (s != LRT_OK) return fail(ctx, s, "BVH build failed");

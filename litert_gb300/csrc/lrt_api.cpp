@@ -332,15 +332,20 @@ static lrt_status device_bvh(lrt_ctx *ctx, const std::vector<float> &boxes, bool
     ctx->tri_indices_on_device = true;
   }
   GpuBvhInfo info;
-  e = build_bvh_gpu(ctx->d_boxes6.p, n, !tri, ctx->d_nodes.p, tri ? ctx->d_prim_indices.p : nullptr, ctx->d_pairs.p,
-                    tri ? ctx->d_leaf_start_count.p : nullptr, info, 0);
+  e = build_bvh_gpu(ctx->d_boxes6.p, n, !tri, ctx->bvh_builder == 1, ctx->d_nodes.p,
+                    tri ? ctx->d_prim_indices.p : nullptr, ctx->d_pairs.p, tri ? ctx->d_leaf_start_count.p : nullptr,
+                    info, 0);
+  if (e == cudaErrorNotSupported) {   // a split the device path does not take: the host builder, same tree
+    (void)cudaGetLastError();
+    return LRT_ERR_UNSUPPORTED;
+  }
   if (e != cudaSuccess) return cuda_fail(ctx, e, "lrt_commit_scene: device BVH build");
   ctx->bvh = BvhData{};
   ctx->bvh.max_depth = info.max_depth;
   ctx->bvh.level_start = info.level_start;
   ctx->n_wnodes = info.n_wnodes;
-  ctx->n_pairs = n_int;
-  ctx->n_leaf_start_count = tri ? n : 0;
+  ctx->n_pairs = info.n_pairs;
+  ctx->n_leaf_start_count = tri ? info.n_leaves : 0;
   ctx->bvh_on_device = true;
   return LRT_OK;
 }
@@ -392,8 +397,9 @@ extern "C" lrt_status lrt_commit_scene(lrt_ctx *ctx) {
   const bool tri = g.type == LRT_TYPE_MESH_TRIANGLE;
   const uint32_t n_prims = uint32_t(boxes.size() / 6);
   cudaError_t e;
-  if (ctx->bvh_builder == 1) {
-    if ((st = device_bvh(ctx, boxes, tri)) != LRT_OK) return st;
+  if (ctx->bvh_builder != 0) st = device_bvh(ctx, boxes, tri);
+  if (ctx->bvh_builder != 0 && st != LRT_ERR_UNSUPPORTED) {
+    if (st != LRT_OK) return st;
   } else {
     st = build_bvh(boxes.data(), n_prims, !tri, ctx->bvh);
     if (st != LRT_OK) return fail(ctx, st, "lrt_commit_scene: BVH build failed");
@@ -533,7 +539,7 @@ extern "C" lrt_status lrt_set_tuning(lrt_ctx *ctx, const char *key, int value) {
     if (value < 0 || value > 1) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: fma is 0 or 1");
     ctx->tuning.fma = value;
   } else if (k == "bvh_builder") {
-    if (value < 0 || value > 1) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: bvh_builder is 0 or 1");
+    if (value < 0 || value > 2) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: bvh_builder is 0, 1 or 2");
     ctx->bvh_builder = value;
   } else if (k == "proposal") {
     if (value < 0 || value > 1) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: proposal is 0 or 1");

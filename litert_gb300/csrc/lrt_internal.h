@@ -57,18 +57,23 @@ void build_occupancy(const SbsData &sbs, const std::vector<float> &values_f, uin
 // id; boxes=false: triangles, up to two per leaf, payload = range in `order`.
 lrt_status build_bvh(const float *boxes6, uint32_t n, bool boxes, BvhData &out);
 
-// The same wide BVH layout built on the device (bvh_gpu.cu): a linear BVH over
-// Morton codes, collapsed like build_bvh, one primitive per leaf.  All pointers
-// are device memory: d_boxes6 n x 6 floats; d_wnodes room for max(1, n-1)
-// nodes; optional outputs d_order (n: primitive of each sorted position),
-// d_pairs (max(1, n-1): the reference fat-pair layout) and, for triangles,
-// d_leaf_start_count (n).  Synchronises the stream.
+// The same wide BVH layout built on the device (bvh_gpu.cu).  sah: build_bvh's
+// binned SAH restated level by level (the same tree, nodes, order and fat pairs;
+// cudaErrorNotSupported when an object-median split too large for the device
+// path occurs, and the caller builds on the host); otherwise a linear BVH over
+// Morton codes with one primitive per leaf.  Both collapse like build_bvh.  All
+// pointers are device memory: d_boxes6 n x 6 floats; d_wnodes room for
+// max(1, n-1) nodes; optional outputs d_order (n: primitive of each leaf-order
+// position), d_pairs (max(1, n-1): the reference fat-pair layout) and, for
+// triangles, d_leaf_start_count (n).  Synchronises the stream.
 struct GpuBvhInfo {
   uint32_t n_wnodes = 0, max_depth = 0;
+  uint32_t n_pairs = 0, n_leaves = 0;  // fat pairs written, leaves (leaf_start_count entries)
   std::vector<uint32_t> level_start;   // first wide node of each depth
 };
-cudaError_t build_bvh_gpu(const float *d_boxes6, uint32_t n, bool boxes, WNode4 *d_wnodes, uint32_t *d_order,
-                          lrt_bvh_pair *d_pairs, uint32_t *d_leaf_start_count, GpuBvhInfo &info, cudaStream_t st);
+cudaError_t build_bvh_gpu(const float *d_boxes6, uint32_t n, bool boxes, bool sah, WNode4 *d_wnodes,
+                          uint32_t *d_order, lrt_bvh_pair *d_pairs, uint32_t *d_leaf_start_count, GpuBvhInfo &info,
+                          cudaStream_t st);
 // New slot boxes for an existing wide tree (host- or device-built) from new
 // primitive boxes; triangle leaf ranges index d_order (null: identity).
 cudaError_t refit_bvh_gpu(const float *d_boxes6, bool boxes, const uint32_t *d_order, WNode4 *d_wnodes,

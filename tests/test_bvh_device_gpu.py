@@ -1,11 +1,13 @@
-"""BVH built on the device (lrt_set_tuning "bvh_builder" = 1) and triangle refit.
+"""BVH built on the device (lrt_set_tuning "bvh_builder" 1: binned SAH, 2: linear
+BVH) and triangle refit.
 
-The device tree (linear BVH: Morton codes, radix sort, radix tree, 4-wide
-collapse) has a different topology from the host binned-SAH tree, so the
-closest hit is compared, not the tree: every leaf box is the primitive's box
-either way, so hit masks and t are bit-identical; the primitive may differ only
-where a ray meets two primitives at exactly the same t (a shared edge or brick
-face), and there the records must agree in t.  Refit keeps the topology and
+The device SAH builder restates the host builder level by level, so its tree is
+the host's: the fat pairs are byte-identical and renders bit-identical.  The
+linear BVH (Morton codes, radix sort, radix tree, 4-wide collapse) has another
+topology, so the closest hit is compared, not the tree: every leaf box is the
+primitive's box either way, so hit masks and t are bit-identical; the primitive
+may differ only where a ray meets two primitives at exactly the same t (a shared
+edge or brick face), and there the records must agree in t.  Refit keeps the topology and
 recomputes the boxes: a refit with unchanged vertices reproduces the committed
 boxes bit for bit, and a refit to moved vertices renders what a fresh build of
 the moved mesh renders.
@@ -45,12 +47,13 @@ def _same_closest_hits(a, b, tie_frac=1e-4):
     return int(ma.sum())
 
 
+@pytest.mark.parametrize("builder", [1, 2])
 @pytest.mark.parametrize("mode", [lrt.INTERSECT_ST, lrt.INTERSECT_NEWTON])
-def test_device_bvh_sbs_matches_host(mode):
+def test_device_bvh_sbs_matches_host(mode, builder):
     h, nodes, values = lrt.sbs_from_sdf(scenes.union_sdf(), 6, 4)
     views = scenes.union_views(n_views=3, lo=96, hi=200)
     outs = []
-    for builder in (0, 1):
+    for builder in (0, builder):
         s = _sbs_scene(builder, h, nodes, values, mode)
         outs.append(_render(s, views, hits=True, rgba=True))
         s.close()
@@ -60,9 +63,10 @@ def test_device_bvh_sbs_matches_host(mode):
     assert np.array_equal(canon_bits(outs[0]["rgba"][same]), canon_bits(outs[1]["rgba"][same]))
 
 
-def test_device_bvh_sbs_matches_oracle():
+@pytest.mark.parametrize("builder", [1, 2])
+def test_device_bvh_sbs_matches_oracle(builder):
     h, nodes, values = lrt.sbs_from_sdf(scenes.sphere_sdf(), 5, 4)
-    s = _sbs_scene(1, h, nodes, values)
+    s = _sbs_scene(builder, h, nodes, values)
     view = scenes.sphere_view(160, 128)
     out = _render(s, [view], hits=True)
     s.close()
@@ -73,11 +77,12 @@ def test_device_bvh_sbs_matches_oracle():
     assert r["hits"] > 1000 and r["mask"] == 0 and r["t"] == 0, r
 
 
-def test_device_bvh_svs_matches_host():
+@pytest.mark.parametrize("builder", [1, 2])
+def test_device_bvh_svs_matches_host(builder):
     n = lrt.svs_from_sdf(scenes.union_sdf(), 6)
     view = scenes.union_views(n_views=1, lo=160, hi=161)
     outs = []
-    for builder in (0, 1):
+    for builder in (0, builder):
         s = lrt.Scene(0)
         s.set_tuning("bvh_builder", builder)
         g = s.add_svs(n)
@@ -89,26 +94,53 @@ def test_device_bvh_svs_matches_host():
     assert _same_closest_hits(outs[0], outs[1]) > 2000
 
 
+@pytest.mark.parametrize("builder", [1, 2])
 @pytest.mark.parametrize("n_bricks", [1, 2, 3, 5])
-def test_device_bvh_tiny_scenes(n_bricks):
+def test_device_bvh_tiny_scenes(n_bricks, builder):
     h, nodes, values = lrt.sbs_from_sdf(scenes.sphere_sdf(), 3, 4)
     nodes = nodes[:n_bricks].copy()
     view = scenes.sphere_view(128, 128)
     outs = []
-    for builder in (0, 1):
+    for builder in (0, builder):
         s = _sbs_scene(builder, h, nodes, values)
         outs.append(_render(s, [view], hits=True)["hits"])
         s.close()
     _same_closest_hits(outs[0], outs[1])
 
 
-def test_device_bvh_fat_pairs_cover_every_brick():
+def _pairs_of(builder, h, nodes, values):
+    s = _sbs_scene(builder, h, nodes, values)
+    p = s.bvh2()
+    s.close()
+    return p
+
+
+@pytest.mark.parametrize("depth,brick", [(5, 4), (7, 8), (4, 2)])
+def test_device_sah_is_the_host_tree(depth, brick):
+    h, nodes, values = lrt.sbs_from_sdf(scenes.union_sdf(), depth, brick)
+    host = _pairs_of(0, h, nodes, values)
+    dev = _pairs_of(1, h, nodes, values)
+    assert host.shape == dev.shape and host.tobytes() == dev.tobytes()
+
+
+def test_device_sah_mesh_is_the_host_tree():
+    verts, faces = scenes.displaced_icosphere(subdiv=4)
+    view = scenes.mesh_view(width=240, height=160)
+    a = _mesh_render(verts, faces, 0, view, pairs=True)
+    b = _mesh_render(verts, faces, 1, view, pairs=True)
+    assert a["pairs"].tobytes() == b["pairs"].tobytes()
+    assert records_equal(a["hits"], b["hits"])
+    assert np.array_equal(canon_bits(a["rgba"]), canon_bits(b["rgba"]))
+
+
+@pytest.mark.parametrize("builder", [1, 2])
+def test_device_bvh_fat_pairs_cover_every_brick(builder):
     h, nodes, values = lrt.sbs_from_sdf(scenes.union_sdf(), 5, 4)
-    s = _sbs_scene(1, h, nodes, values)
+    s = _sbs_scene(builder, h, nodes, values)
     p = s.bvh2()
     s.close()
     nb = nodes.shape[0]
-    assert p.shape[0] == max(1, nb - 1)
+    assert p.shape[0] == max(1, nb - 1)   # one brick per leaf either way
     seen = np.zeros(nb, np.int64)
     # walk from the root pair: every pair reached once, child boxes inside the parent box
     stack = [(0, None)]
@@ -137,21 +169,24 @@ def _moved(verts, seed):
     return v
 
 
-def _mesh_render(verts, faces, builder, view, refit_to=None):
+def _mesh_render(verts, faces, builder, view, refit_to=None, pairs=False):
     s = lrt.Scene(0)
     s.set_tuning("bvh_builder", builder)
     g = s.add_triangles(verts, faces)
     s.add_instance(g)
     s.commit_scene()
     s.set_preset(render_mode=lrt.RENDER_MODE_NORMAL)
+    pr = s.bvh2() if pairs else None
     if refit_to is not None:
         s.refit_triangles(refit_to)
     out = _render(s, [view], hits=True, rgba=True)
     s.close()
+    if pairs:
+        out["pairs"] = pr
     return out
 
 
-@pytest.mark.parametrize("builder", [0, 1])
+@pytest.mark.parametrize("builder", [0, 1, 2])
 def test_device_bvh_mesh_matches_oracle(builder):
     verts, faces = scenes.displaced_icosphere(subdiv=4)
     view = scenes.mesh_view(width=240, height=160)
@@ -165,7 +200,7 @@ def test_device_bvh_mesh_matches_oracle(builder):
     assert (g["primId"] != hits["primId"]).sum() <= 1e-3 * mo.sum()
 
 
-@pytest.mark.parametrize("builder", [0, 1])
+@pytest.mark.parametrize("builder", [0, 1, 2])
 def test_refit_unchanged_is_identity(builder):
     verts, faces = scenes.displaced_icosphere(subdiv=4)
     view = scenes.mesh_view(width=240, height=160)
@@ -175,7 +210,7 @@ def test_refit_unchanged_is_identity(builder):
     assert np.array_equal(canon_bits(a["rgba"]), canon_bits(b["rgba"]))
 
 
-@pytest.mark.parametrize("builder", [0, 1])
+@pytest.mark.parametrize("builder", [0, 1, 2])
 def test_refit_moved_matches_fresh_build(builder):
     verts, faces = scenes.displaced_icosphere(subdiv=4)
     moved = _moved(verts, 7)

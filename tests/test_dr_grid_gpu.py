@@ -5,7 +5,7 @@ the final grid is the starting grid resampled stage after stage and must equal
 the oracle's chain of resamples bit for bit (growing after every stage, or not
 after the last).  With a learning rate the loss of the final stage falls below
 the loss of the same schedule cut to one iteration per stage, with the host and
-the device BVH builders alike."""
+both device BVH builders alike."""
 import numpy as np
 import pytest
 
@@ -48,7 +48,7 @@ def test_optimize_grid_zero_lr_is_the_resample_chain(no_last_step_resize):
     assert np.array_equal(grid[3].view(np.uint32), p.view(np.uint32))
 
 
-@pytest.mark.parametrize("bvh_builder", [0, 1])
+@pytest.mark.parametrize("bvh_builder", [0, 1, 2])
 def test_optimize_grid_reduces_the_loss(bvh_builder):
     presets = [dr.default_preset(opt_lr=0.02, border_spp=16, seed=3, accumulate_batch=1),
                dr.default_preset(opt_lr=0.01, border_spp=16, seed=4, accumulate_batch=1)]
