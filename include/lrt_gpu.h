@@ -71,12 +71,15 @@ lrt_status lrt_set_preset(lrt_ctx *ctx, const lrt_preset *preset);
  * x86-64 build, within the forward parity tolerance: same hit mask, depth within
  * 1e-4 of the scene extent, normals within 1e-3, apart from grazing and crease
  * pixels).  "proposal": see lrt_proposal.h.
- * "bvh_builder" (read by lrt_commit_scene: 0 = host binned-SAH build, default,
- * the reference's Embree build restated (BVH/cbvh.cpp:591-657); 1 = the BVH is
- * built on the device: Morton codes of the primitive centroids, a radix sort,
- * a binary radix tree and the same 4-wide collapse, one primitive per leaf.
- * Hits are the same apart from exact ties between primitives; traversal cost
- * depends on the tree). */
+ * "bvh_builder" (read by lrt_commit_scene and lrt_dr_set_scene: 0 = host
+ * binned-SAH build, default, standing in for the reference's Embree build
+ * (BVH/cbvh.cpp:591-657); 1 = the same binned SAH on the device, level by level:
+ * the same tree, fat pairs and hits (a rare object-median split of more than
+ * 4096 primitives sends the build back to the host, with the same result);
+ * 2 = a linear BVH on the device: Morton codes of the primitive centroids, a
+ * radix sort, a binary radix tree and the same 4-wide collapse, one primitive
+ * per leaf; hits are the same apart from exact ties between primitives, and
+ * traversal is a few percent slower). */
 lrt_status lrt_set_tuning(lrt_ctx *ctx, const char *key, int value);
 
 /* New vertex positions for the committed triangle mesh (same vertex count and
