@@ -653,7 +653,9 @@ void orc_dr_step(const orc_dr_scene *s, float *params, const orc_dr_preset *p, c
   for (uint32_t k = 0; k < n_images; k++) {
     const orc_dr_view *v = &views[k];
     const size_t n = (size_t)v->width * v->height;
-    float *img = (float *)malloc(16 * n), *dep = (float *)malloc(4 * n);
+    /* zeroed: a pixel outside the ray-casting mask is not rendered and keeps what the
+     * reference's image held there, the miss (0, 0, 0, 0) of its last cast */
+    float *img = (float *)calloc(4 * n, sizeof(float)), *dep = (float *)calloc(n, sizeof(float));
     double l = orc_dr_render(s, params, p, v, images + 4 * off, img, dep, g, NULL, threads);
     if (losses) losses[k] = l;
     if (images_out) memcpy(images_out + 4 * off, img, 16 * n);
