@@ -503,6 +503,34 @@ def run_dr(args, dev, torch):
                       "adam_lr": 3e-3, "batch": "8 views summed", "warp_aggregate": args.dr_aggregate,
                       "l2": "256 MiB write between timed iterations", "setup_s": round(t_setup, 2)},
            "clocks": clk}
+    # the iteration with random and with SVM border sampling, and with the ray-casting
+    # mask, each from the same parameters (Adam restarted), iterations numbered on
+    # from the timed run; device time, median of 10 after 3 warm-up iterations
+    variants = {}
+    saved = R.get(0)
+    it0 = warm + n_timed
+    for name, kw in (("random_border_sampling", {}), ("svm_border_sampling", dict(border_sampling=1)),
+                     ("raycasting_mask", dict(raycasting_mask=1))):
+        p2 = dr_preset(args.dr_aggregate)
+        for k, v in kw.items():
+            setattr(p2, k, v)
+        R.set_params(saved)
+        R.SetPreset(p2)
+        for i in range(3):
+            R.step(it0 + i, want_losses=False)
+        ts = []
+        for k in range(10):
+            flush.fill_(float(k))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            R.step(it0 + 3 + k, want_losses=False)
+            b.record(stream)
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+        variants[name + "_ms"] = statistics.median(ts)
+    out["variants"] = variants
+    R.set_params(saved)
+    R.SetPreset(preset)
     if not args.no_cpu_baseline:
         cpu = run_dr_cpu(R, [init[0], init[1], init[2], R.get(0)], views, imgs, preset)
         out["cpu_baseline"] = {"value": cpu["ms_per_iter"], "unit": "ms/iter", "cores": cpu["cores"], "kind": "port",
