@@ -292,6 +292,8 @@ __global__ void lbvh_leaves(const float *b6, const uint32_t *sid, uint32_t n, bo
 constexpr int kNB = 32;
 constexpr uint32_t kSahThreads = 128;
 constexpr uint32_t kMedianMax = 4096;   // larger median-fallback segments go back to the host builder
+constexpr uint32_t kBigMin = 16384;     // node ranges at least this large are split by many blocks
+constexpr uint32_t kBigMaxSegs = 64;    // ... looked for on levels of at most this many ranges
 
 __device__ __forceinline__ float fmn(float a, float b) { return (b < a) ? b : a; }   // std::min
 __device__ __forceinline__ float fmx(float a, float b) { return (a < b) ? b : a; }   // std::max
@@ -328,16 +330,70 @@ __device__ void block_minmax12(float v[12], float *sh /* [kSahThreads/32][12] */
   __syncthreads();
 }
 
+// The cost sweep of Builder::split over the bins of one node range (bl / bh:
+// [3][kNB][3] ordered box bounds, bc: [3][kNB] counts, shared or global memory),
+// in the host's order; no split (or below depth 40: use all false) selects the
+// object median on the widest centroid axis.
+__device__ void sah_sweep(const uint32_t *bl, const uint32_t *bh, const uint32_t *bc, const bool use[3],
+                          const float cl[3], const float ch[3], uint32_t m, int &axis, int &bin, int &median,
+                          uint32_t &nleft) {
+  float best_cost = 3.4e38f;
+  int best_axis = -1, best_bin = -1;
+  for (int a = 0; a < 3; a++) {
+    if (!use[a]) continue;
+    float rA[kNB];
+    uint32_t rN[kNB];
+    float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+    uint32_t cnt = 0;
+    for (int i = kNB - 1; i > 0; i--) {
+      for (int c = 0; c < 3; c++) {
+        lo[c] = fmn(lo[c], unord(bl[(a * kNB + i) * 3 + c]));
+        hi[c] = fmx(hi[c], unord(bh[(a * kNB + i) * 3 + c]));
+      }
+      cnt += bc[a * kNB + i];
+      rA[i] = area6(lo, hi);
+      rN[i] = cnt;
+    }
+    for (int c = 0; c < 3; c++) { lo[c] = 3.4e38f; hi[c] = -3.4e38f; }
+    cnt = 0;
+    for (int i = 0; i < kNB - 1; i++) {
+      for (int c = 0; c < 3; c++) {
+        lo[c] = fmn(lo[c], unord(bl[(a * kNB + i) * 3 + c]));
+        hi[c] = fmx(hi[c], unord(bh[(a * kNB + i) * 3 + c]));
+      }
+      cnt += bc[a * kNB + i];
+      if (cnt == 0 || rN[i + 1] == 0) continue;
+      const float cost = area6(lo, hi) * float(cnt) + rA[i + 1] * float(rN[i + 1]);
+      if (cost < best_cost) { best_cost = cost; best_axis = a; best_bin = i; }
+    }
+  }
+  median = best_axis < 0;
+  if (best_axis < 0) {
+    int ax = 0;
+    for (int c = 1; c < 3; c++) if (ch[c] - cl[c] > ch[ax] - cl[ax]) ax = c;
+    best_axis = ax;
+    nleft = m / 2;
+  } else {
+    uint32_t nl = 0;
+    for (int i = 0; i <= best_bin; i++) nl += bc[best_axis * kNB + i];
+    nleft = nl;
+  }
+  axis = best_axis;
+  bin = best_bin;
+}
+
 __global__ void __launch_bounds__(kSahThreads) sah_level(const float *b6, const float *cent, uint32_t *order,
                                                          uint32_t *tmp, uint32_t *rank, const uint32_t *seg_b,
                                                          const uint32_t *seg_e,
                                                          uint32_t depth, uint32_t max_leaf, float *seg_box,
-                                                         uint32_t *seg_split, uint32_t *seg_flag, uint32_t *err) {
+                                                         uint32_t *seg_split, uint32_t *seg_flag, uint32_t *err,
+                                                         uint32_t big_min) {
   __shared__ float red[kSahThreads / 32 * 12];
   __shared__ uint32_t bl[3][kNB][3], bh[3][kNB][3], bc[3][kNB];
   __shared__ int s_axis, s_bin, s_median;
   __shared__ uint32_t s_nleft, s_run, s_wsum[kSahThreads / 32];
   const uint32_t k = blockIdx.x, b = seg_b[k], e = seg_e[k], m = e - b, tid = threadIdx.x;
+  if (m >= big_min) return;   // done by the multi-block path (sah_big_*)
   // 1. node box and centroid bounds
   float v[12];
   for (int q = 0; q < 6; q++) { v[q] = 3.4e38f; v[6 + q] = -3.4e38f; }
@@ -388,41 +444,11 @@ __global__ void __launch_bounds__(kSahThreads) sah_level(const float *b6, const 
   __syncthreads();
   // 3. cost sweep (Builder::split), one thread
   if (tid == 0) {
-    float best_cost = 3.4e38f;
-    int best_axis = -1, best_bin = -1;
-    for (int a = 0; a < 3; a++) {
-      if (!use[a]) continue;
-      float rA[kNB];
-      uint32_t rN[kNB];
-      float lo[3] = {3.4e38f, 3.4e38f, 3.4e38f}, hi[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
-      uint32_t cnt = 0;
-      for (int i = kNB - 1; i > 0; i--) {
-        for (int c = 0; c < 3; c++) { lo[c] = fmn(lo[c], unord(bl[a][i][c])); hi[c] = fmx(hi[c], unord(bh[a][i][c])); }
-        cnt += bc[a][i];
-        rA[i] = area6(lo, hi);
-        rN[i] = cnt;
-      }
-      for (int c = 0; c < 3; c++) { lo[c] = 3.4e38f; hi[c] = -3.4e38f; }
-      cnt = 0;
-      for (int i = 0; i < kNB - 1; i++) {
-        for (int c = 0; c < 3; c++) { lo[c] = fmn(lo[c], unord(bl[a][i][c])); hi[c] = fmx(hi[c], unord(bh[a][i][c])); }
-        cnt += bc[a][i];
-        if (cnt == 0 || rN[i + 1] == 0) continue;
-        const float cost = area6(lo, hi) * float(cnt) + rA[i + 1] * float(rN[i + 1]);
-        if (cost < best_cost) { best_cost = cost; best_axis = a; best_bin = i; }
-      }
-    }
-    s_median = best_axis < 0;
-    if (best_axis < 0) {   // object median on the widest centroid axis
-      int ax = 0;
-      for (int c = 1; c < 3; c++) if (ch[c] - cl[c] > ch[ax] - cl[ax]) ax = c;
-      best_axis = ax;
-      s_nleft = m / 2;
-    } else {
-      uint32_t nl = 0;
-      for (int i = 0; i <= best_bin; i++) nl += bc[best_axis][i];
-      s_nleft = nl;
-    }
+    int best_axis, best_bin, med;
+    uint32_t nl;
+    sah_sweep(&bl[0][0][0], &bh[0][0][0], &bc[0][0], use, cl, ch, m, best_axis, best_bin, med, nl);
+    s_median = med;
+    s_nleft = nl;
     s_axis = best_axis;
     s_bin = best_bin;
     s_run = 0;
@@ -488,6 +514,149 @@ __global__ void __launch_bounds__(kSahThreads) sah_level(const float *b6, const 
   }
   for (uint32_t i = b + tid; i < e; i += kSahThreads) order[i] = tmp[i];
   if (tid == 0) seg_split[k] = b + nleft;
+}
+
+// ---- the same split for one large node range, spread over many blocks ----
+// Scratch layout (words): [0, 12) ordered bounds (box lo, centroid lo: min; box hi,
+// centroid hi: max), then bin lows [3][kNB][3], bin highs [3][kNB][3], bin counts
+// [3][kNB], then the sweep's axis, bin, median flag and left count.
+constexpr uint32_t kBigBL = 12, kBigBH = kBigBL + 3 * kNB * 3, kBigBC = kBigBH + 3 * kNB * 3,
+                   kBigRes = kBigBC + 3 * kNB, kBigWords = kBigRes + 4;
+
+__global__ void sah_big_init(uint32_t *sc) {
+  for (uint32_t i = threadIdx.x; i < kBigWords; i += blockDim.x) {
+    uint32_t v = 0;
+    if (i < 6) v = 0xFFFFFFFFu;
+    else if (i < 12) v = 0u;
+    else if (i < kBigBH) v = ord(3.4e38f);
+    else if (i < kBigBC) v = ord(-3.4e38f);
+    sc[i] = v;
+  }
+}
+
+__global__ void sah_big_bounds(const float *b6, const float *cent, const uint32_t *order, uint32_t b, uint32_t e,
+                               uint32_t *sc) {
+  float v[12];
+  for (int q = 0; q < 6; q++) { v[q] = 3.4e38f; v[6 + q] = -3.4e38f; }
+  for (uint32_t i = b + blockIdx.x * blockDim.x + threadIdx.x; i < e; i += gridDim.x * blockDim.x) {
+    const uint32_t p = order[i];
+    for (int a = 0; a < 3; a++) {
+      v[a] = fminf(v[a], b6[6 * size_t(p) + a]);
+      v[6 + a] = fmaxf(v[6 + a], b6[6 * size_t(p) + 3 + a]);
+      v[3 + a] = fminf(v[3 + a], cent[3 * size_t(p) + a]);
+      v[9 + a] = fmaxf(v[9 + a], cent[3 * size_t(p) + a]);
+    }
+  }
+  for (int q = 0; q < 12; q++)
+    for (int o = 16; o > 0; o >>= 1) {
+      const float u = __shfl_xor_sync(0xffffffffu, v[q], o);
+      v[q] = q < 6 ? fminf(v[q], u) : fmaxf(v[q], u);
+    }
+  if ((threadIdx.x & 31) == 0 && v[0] <= v[6])
+    for (int q = 0; q < 12; q++) {
+      if (q < 6) atomicMin(&sc[q], ord(v[q]));
+      else atomicMax(&sc[q], ord(v[q]));
+    }
+}
+
+__device__ __forceinline__ void big_axes(const uint32_t *sc, uint32_t depth, float cl[3], float ch[3], bool use[3],
+                                         float scl[3]) {
+  for (int a = 0; a < 3; a++) {
+    cl[a] = unord(sc[3 + a]);
+    ch[a] = unord(sc[9 + a]);
+    const float ext = ch[a] - cl[a];
+    use[a] = depth < 40 && ext > 0;
+    scl[a] = use[a] ? kNB / ext : 0.0f;
+  }
+}
+
+__global__ void __launch_bounds__(256) sah_big_bins(const float *b6, const float *cent, const uint32_t *order,
+                                                    uint32_t b, uint32_t e, uint32_t depth, uint32_t *sc) {
+  __shared__ uint32_t bl[3 * kNB * 3], bh[3 * kNB * 3], bc[3 * kNB];
+  float cl[3], ch[3], scl[3];
+  bool use[3];
+  big_axes(sc, depth, cl, ch, use, scl);
+  for (uint32_t q = threadIdx.x; q < 3 * kNB * 3; q += blockDim.x) { bl[q] = ord(3.4e38f); bh[q] = ord(-3.4e38f); }
+  for (uint32_t q = threadIdx.x; q < 3 * kNB; q += blockDim.x) bc[q] = 0;
+  __syncthreads();
+  for (uint32_t i = b + blockIdx.x * blockDim.x + threadIdx.x; i < e; i += gridDim.x * blockDim.x) {
+    const uint32_t p = order[i];
+    for (int a = 0; a < 3; a++) {
+      if (!use[a]) continue;
+      int bi = int((cent[3 * size_t(p) + a] - cl[a]) * scl[a]);
+      bi = min(max(bi, 0), kNB - 1);
+      atomicAdd(&bc[a * kNB + bi], 1u);
+      for (int c = 0; c < 3; c++) {
+        atomicMin(&bl[(a * kNB + bi) * 3 + c], ord(b6[6 * size_t(p) + c]));
+        atomicMax(&bh[(a * kNB + bi) * 3 + c], ord(b6[6 * size_t(p) + 3 + c]));
+      }
+    }
+  }
+  __syncthreads();
+  for (uint32_t q = threadIdx.x; q < 3 * kNB; q += blockDim.x) {
+    if (bc[q] == 0) continue;
+    atomicAdd(&sc[kBigBC + q], bc[q]);
+    for (int c = 0; c < 3; c++) {
+      atomicMin(&sc[kBigBL + q * 3 + c], bl[q * 3 + c]);
+      atomicMax(&sc[kBigBH + q * 3 + c], bh[q * 3 + c]);
+    }
+  }
+}
+
+__global__ void sah_big_sweep(uint32_t k, uint32_t b, uint32_t e, uint32_t depth, uint32_t *sc, float *seg_box,
+                              uint32_t *seg_split, uint32_t *seg_flag, uint32_t *err) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  float cl[3], ch[3], scl[3];
+  bool use[3];
+  big_axes(sc, depth, cl, ch, use, scl);
+  int axis, bin, median;
+  uint32_t nleft;
+  sah_sweep(sc + kBigBL, sc + kBigBH, sc + kBigBC, use, cl, ch, e - b, axis, bin, median, nleft);
+  for (int a = 0; a < 3; a++) {
+    seg_box[6 * size_t(k) + a] = unord(sc[a]);
+    seg_box[6 * size_t(k) + 3 + a] = unord(sc[6 + a]);
+  }
+  sc[kBigRes + 0] = uint32_t(axis);
+  sc[kBigRes + 1] = uint32_t(bin);
+  sc[kBigRes + 2] = uint32_t(median);
+  sc[kBigRes + 3] = nleft;
+  if (median) {   // an object median this large: the caller builds on the host
+    atomicOr(err, 1u);
+    seg_flag[k] = 0;
+    return;
+  }
+  seg_flag[k] = 1;
+  seg_split[k] = b + nleft;
+}
+
+__global__ void sah_big_flags(const float *cent, const uint32_t *order, uint32_t b, uint32_t e, uint32_t depth,
+                              const uint32_t *sc, uint32_t *flag) {
+  if (sc[kBigRes + 2]) return;
+  float cl[3], ch[3], scl[3];
+  bool use[3];
+  big_axes(sc, depth, cl, ch, use, scl);
+  const int ax = int(sc[kBigRes + 0]), bin = int(sc[kBigRes + 1]);
+  for (uint32_t i = b + blockIdx.x * blockDim.x + threadIdx.x; i < e; i += gridDim.x * blockDim.x) {
+    const uint32_t p = order[i];
+    int bi = int((cent[3 * size_t(p) + ax] - cl[ax]) * scl[ax]);
+    bi = min(max(bi, 0), kNB - 1);
+    flag[i - b] = bi <= bin ? 1u : 0u;
+  }
+}
+
+__global__ void sah_big_scatter(const uint32_t *order, uint32_t b, uint32_t e, const uint32_t *sc,
+                                const uint32_t *flag, const uint32_t *excl, uint32_t *tmp) {
+  if (sc[kBigRes + 2]) return;
+  const uint32_t nleft = sc[kBigRes + 3];
+  for (uint32_t i = b + blockIdx.x * blockDim.x + threadIdx.x; i < e; i += gridDim.x * blockDim.x) {
+    const uint32_t o = i - b, before = excl[o];
+    tmp[flag[o] ? b + before : b + nleft + (o - before)] = order[i];
+  }
+}
+
+__global__ void sah_big_copy(uint32_t *order, const uint32_t *tmp, uint32_t b, uint32_t e, const uint32_t *sc) {
+  if (sc[kBigRes + 2]) return;
+  for (uint32_t i = b + blockIdx.x * blockDim.x + threadIdx.x; i < e; i += gridDim.x * blockDim.x) order[i] = tmp[i];
 }
 
 // After a level's scan of seg_flag: internal nodes and leaves get their ids (level
@@ -745,12 +914,15 @@ cudaError_t build_bvh_gpu(const float *d_boxes6, uint32_t n, bool boxes, bool sa
     // exact binned SAH, level by level
     const uint32_t max_leaf = boxes ? 1u : 2u;
     Tmp<float> cent, sbox;
-    Tmp<uint32_t> tmp, rank, sb, se, sp, nb_, ne_, np_, split, flag, excl;
+    Tmp<uint32_t> tmp, rank, sb, se, sp, nb_, ne_, np_, split, flag, excl, bflag, bscan, big;
     cent.st = sbox.st = st;
-    for (auto *t : {&tmp, &rank, &sb, &se, &sp, &nb_, &ne_, &np_, &split, &flag, &excl}) t->st = st;
+    for (auto *t : {&tmp, &rank, &sb, &se, &sp, &nb_, &ne_, &np_, &split, &flag, &excl, &bflag, &bscan, &big})
+      t->st = st;
     LRT_TRY(cent.alloc(3 * size_t(n), st));
     LRT_TRY(sbox.alloc(6 * size_t(n), st));
-    for (auto *t : {&tmp, &rank, &sb, &se, &sp, &nb_, &ne_, &np_, &split, &flag, &excl}) LRT_TRY(t->alloc(n, st));
+    for (auto *t : {&tmp, &rank, &sb, &se, &sp, &nb_, &ne_, &np_, &split, &flag, &excl, &bflag, &bscan})
+      LRT_TRY(t->alloc(n, st));
+    LRT_TRY(big.alloc(kBigWords, st));
     centroids<<<blocks(n, 256), 256, 0, st>>>(d_boxes6, n, cent.p, sidb.p);
     const uint32_t seg0[3] = {0u, n, kNone};
     LRT_TRY(cudaMemcpyAsync(sb.p, &seg0[0], 4, cudaMemcpyHostToDevice, st));
@@ -759,8 +931,31 @@ cudaError_t build_bvh_gpu(const float *d_boxes6, uint32_t n, bool boxes, bool sa
     uint32_t nseg = 1, depth = 0;
     uint32_t *cb = sb.p, *ce = se.p, *cp = sp.p, *xb = nb_.p, *xe = ne_.p, *xp = np_.p;
     while (nseg > 0) {
+      // node ranges of kBigMin primitives or more (the top levels) are split by many
+      // blocks each; the level kernel skips them
+      if (nseg <= kBigMaxSegs) {
+        uint32_t hb[kBigMaxSegs], he[kBigMaxSegs];
+        LRT_TRY(cudaMemcpyAsync(hb, cb, nseg * 4, cudaMemcpyDeviceToHost, st));
+        LRT_TRY(cudaMemcpyAsync(he, ce, nseg * 4, cudaMemcpyDeviceToHost, st));
+        LRT_TRY(cudaStreamSynchronize(st));
+        for (uint32_t k = 0; k < nseg; k++) {
+          const uint32_t b = hb[k], e = he[k], m = e - b;
+          if (m < kBigMin) continue;
+          const unsigned g = std::min<unsigned>(blocks(m, 1024), 1024);
+          sah_big_init<<<1, 256, 0, st>>>(big.p);
+          sah_big_bounds<<<g, 256, 0, st>>>(d_boxes6, cent.p, sidb.p, b, e, big.p);
+          sah_big_bins<<<g, 256, 0, st>>>(d_boxes6, cent.p, sidb.p, b, e, depth, big.p);
+          sah_big_sweep<<<1, 32, 0, st>>>(k, b, e, depth, big.p, sbox.p, split.p, flag.p, err.p);
+          sah_big_flags<<<g, 256, 0, st>>>(cent.p, sidb.p, b, e, depth, big.p, bflag.p);
+          LRT_TRY(cudaGetLastError());
+          LRT_TRY(gpu_exclusive_scan(bflag.p, bscan.p, m, nullptr, st));
+          sah_big_scatter<<<g, 256, 0, st>>>(sidb.p, b, e, big.p, bflag.p, bscan.p, tmp.p);
+          sah_big_copy<<<g, 256, 0, st>>>(sidb.p, tmp.p, b, e, big.p);
+          LRT_TRY(cudaGetLastError());
+        }
+      }
       sah_level<<<nseg, kSahThreads, 0, st>>>(d_boxes6, cent.p, sidb.p, tmp.p, rank.p, cb, ce, depth, max_leaf, sbox.p,
-                                              split.p, flag.p, err.p);
+                                              split.p, flag.p, err.p, nseg <= kBigMaxSegs ? kBigMin : 0xFFFFFFFFu);
       LRT_TRY(cudaGetLastError());
       uint64_t n_split = 0;
       LRT_TRY(gpu_exclusive_scan(flag.p, excl.p, nseg, &n_split, st));

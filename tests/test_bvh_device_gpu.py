@@ -123,8 +123,9 @@ def test_device_sah_is_the_host_tree(depth, brick):
     assert host.shape == dev.shape and host.tobytes() == dev.tobytes()
 
 
-def test_device_sah_mesh_is_the_host_tree():
-    verts, faces = scenes.displaced_icosphere(subdiv=4)
+@pytest.mark.parametrize("subdiv", [4, 6])   # 6: 81,920 triangles, the top levels split by many blocks
+def test_device_sah_mesh_is_the_host_tree(subdiv):
+    verts, faces = scenes.displaced_icosphere(subdiv=subdiv)
     view = scenes.mesh_view(width=240, height=160)
     a = _mesh_render(verts, faces, 0, view, pairs=True)
     b = _mesh_render(verts, faces, 1, view, pairs=True)
