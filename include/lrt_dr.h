@@ -151,19 +151,29 @@ lrt_status lrt_dr_grid_sbs(uint32_t brick_count, uint32_t brick_size, const lrt_
 lrt_status lrt_dr_grid_resample(uint32_t brick_count, uint32_t brick_size, const float *old_params,
                                 uint32_t old_brick_size, lrt_sbs_header *hdr, lrt_sbs_node **nodes, uint32_t *n_nodes,
                                 uint32_t **values, uint64_t *n_values, float **params, uint32_t *n_params);
-/* MultiRendererDR::OptimizeGrid (:228-276) on the context's reference images:
- * from the starting grid (start_grid_size bricks of size 1) each stage i sets the
- * grid as the scene (BVH from the builder lrt_set_tuning "bvh_builder" selects),
- * applies presets[i] and runs iterations[i] optimisation steps, then resamples the
- * optimised distances into bricks twice as large (the same size after the last
- * stage when no_last_step_resize).  Stages render at the reference images' size
- * (the reference's per-stage render_width/height resampling of its images is left
- * to the caller).  Returns the final grid (malloc'd, free with lrt_free) and the
- * last step's per-view losses (n_views, may be NULL). */
+/* PreprocessRefImages (diff_render/MultiRendererDR.cpp:169-226) on the host: each
+ * view's image resampled to width x height, ceil(W/width) x ceil(H/height)
+ * bilinear samples a pixel, alpha from the mask "colour differs from black"
+ * (CreateRefImageMasks).  Bilinear: texel centres at (i + 0.5)/size, clamped at
+ * the edges (the reference's image-library sampler is not in its tree).
+ * out_views: the views with the new size; out_images: n_views x width x height float4. */
+lrt_status lrt_dr_preprocess_reference(uint32_t n_views, const lrt_view *views, const float *images, uint32_t width,
+                                       uint32_t height, lrt_view *out_views, float *out_images);
+/* MultiRendererDR::OptimizeGrid (:228-276) on the reference images given to
+ * lrt_dr_set_reference: from the starting grid (start_grid_size bricks of size 1)
+ * each stage i renders the reference resampled to render_sizes[2i] x
+ * render_sizes[2i+1] (0 x 0 or render_sizes NULL: as given; the preset's
+ * render_width/height), sets the grid as the scene (BVH from the builder
+ * lrt_set_tuning "bvh_builder" selects), applies presets[i] and runs iterations[i]
+ * optimisation steps (the preset's opt_iterations), then resamples the optimised
+ * distances into bricks twice as large (the same size after the last stage when
+ * no_last_step_resize).  Returns the final grid (malloc'd, free with lrt_free) and
+ * the last step's per-view losses (n_views, may be NULL). */
 lrt_status lrt_dr_optimize_grid(lrt_ctx *ctx, uint32_t start_grid_size, uint32_t no_last_step_resize,
-                                const lrt_dr_preset *presets, const uint32_t *iterations, uint32_t n_stages,
-                                lrt_sbs_header *hdr, lrt_sbs_node **nodes, uint32_t *n_nodes, uint32_t **values,
-                                uint64_t *n_values, float **params, uint32_t *n_params, double *last_losses);
+                                const lrt_dr_preset *presets, const uint32_t *iterations,
+                                const uint32_t *render_sizes, uint32_t n_stages, lrt_sbs_header *hdr,
+                                lrt_sbs_node **nodes, uint32_t *n_nodes, uint32_t **values, uint64_t *n_values,
+                                float **params, uint32_t *n_params, double *last_losses);
 #ifdef __cplusplus
 }
 #endif

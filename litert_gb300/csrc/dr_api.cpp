@@ -31,6 +31,8 @@ struct DrState {
   DevBuf<float> d_bvals;       // per-brick gathered distance values
   // views
   std::vector<lrt_view> views;
+  std::vector<lrt_view> orig_views;   // the reference as lrt_dr_set_reference received it
+  std::vector<float> orig_images;
   std::vector<size_t> off;     // pixel offset of each view
   size_t n_pix = 0, max_view_pix = 0;
   DevBuf<float4> d_ref, d_img;
@@ -398,10 +400,8 @@ extern "C" lrt_status lrt_dr_get_bvh2(lrt_ctx *ctx, const lrt_bvh_pair **pairs, 
   return LRT_OK;
 }
 
-extern "C" lrt_status lrt_dr_set_reference(lrt_ctx *ctx, uint32_t n_views, const lrt_view *views, const float *images) {
-  lrt_status s = ensure_state(ctx);
-  if (s != LRT_OK) return s;
-  if (n_views == 0 || !views || !images) return fail(ctx, LRT_ERR_INVALID, "lrt_dr_set_reference: no views");
+// the device side of SetReference: views, target images and per-view buffers
+static lrt_status upload_reference(lrt_ctx *ctx, uint32_t n_views, const lrt_view *views, const float *images) {
   DrState &st = *ctx->dr;
   st.views.assign(views, views + n_views);
   st.off.assign(n_views, 0);
@@ -432,6 +432,83 @@ extern "C" lrt_status lrt_dr_set_reference(lrt_ctx *ctx, uint32_t n_views, const
   if (st.d_adam.p) LRT_CUDA(ctx, cudaMemset(st.d_adam.p, 0, sizeof(float) * 2 * size_t(st.n_params)));
   st.has_ref = true;
   return prepare_extras(ctx);
+}
+
+extern "C" lrt_status lrt_dr_set_reference(lrt_ctx *ctx, uint32_t n_views, const lrt_view *views, const float *images) {
+  lrt_status s = ensure_state(ctx);
+  if (s != LRT_OK) return s;
+  if (n_views == 0 || !views || !images) return fail(ctx, LRT_ERR_INVALID, "lrt_dr_set_reference: no views");
+  if ((s = upload_reference(ctx, n_views, views, images)) != LRT_OK) return s;
+  DrState &st = *ctx->dr;
+  st.orig_views.assign(views, views + n_views);
+  st.orig_images.assign(images, images + 4 * st.n_pix);
+  return LRT_OK;
+}
+
+// Bilinear lookup of a float RGBA image at uv in [0,1]^2: texel centres at
+// (i + 0.5) / size, clamped at the edges.  (The reference samples through its
+// image library's LINEAR sampler, which is not part of the reference tree; this
+// is the usual definition of that filter.)
+static void sample_bilinear(const float *img, uint32_t w, uint32_t h, float u, float v, float out[4]) {
+  const float fx = u * float(w) - 0.5f, fy = v * float(h) - 0.5f;
+  const float x0f = std::floor(fx), y0f = std::floor(fy);
+  const float tx = fx - x0f, ty = fy - y0f;
+  const int x0 = int(x0f), y0 = int(y0f);
+  auto cx = [w](int x) { return uint32_t(std::min(std::max(x, 0), int(w) - 1)); };
+  auto cy = [h](int y) { return uint32_t(std::min(std::max(y, 0), int(h) - 1)); };
+  const uint32_t xa = cx(x0), xb = cx(x0 + 1), ya = cy(y0), yb = cy(y0 + 1);
+  for (int c = 0; c < 4; c++) {
+    const float a = img[4 * (size_t(ya) * w + xa) + c], b = img[4 * (size_t(ya) * w + xb) + c];
+    const float d = img[4 * (size_t(yb) * w + xa) + c], e = img[4 * (size_t(yb) * w + xb) + c];
+    out[c] = (1 - ty) * ((1 - tx) * a + tx * b) + ty * ((1 - tx) * d + tx * e);
+  }
+}
+
+extern "C" lrt_status lrt_dr_preprocess_reference(uint32_t n_views, const lrt_view *views, const float *images,
+                                                  uint32_t width, uint32_t height, lrt_view *out_views,
+                                                  float *out_images) {
+  if (n_views == 0 || !views || !images || !out_views || !out_images || width == 0 || height == 0 || width > 16384 ||
+      height > 16384)
+    return LRT_ERR_INVALID;
+  size_t in_off = 0, out_off = 0;
+  for (uint32_t n = 0; n < n_views; n++) {
+    const uint32_t w0 = views[n].width, h0 = views[n].height;
+    if (w0 == 0 || h0 == 0) return LRT_ERR_INVALID;
+    const float *src = images + 4 * in_off;
+    // CreateRefImageMasks (:169-185): 1 where the colour differs from the black background
+    std::vector<float> mask(4 * size_t(w0) * h0);
+    for (size_t i = 0; i < size_t(w0) * h0; i++) {
+      const float r = src[4 * i], g = src[4 * i + 1], b = src[4 * i + 2];
+      const float m = std::sqrt(r * r + g * g + b * b) < 0.001f ? 0.0f : 1.0f;
+      for (int c = 0; c < 4; c++) mask[4 * i + c] = m;
+    }
+    // PreprocessRefImages (:187-226): spp_x x spp_y samples a pixel, colour from the
+    // image, alpha from the mask, averaged
+    const uint32_t spp_x = uint32_t(std::ceil(float(w0) / width)), spp_y = uint32_t(std::ceil(float(h0) / height));
+    float *dst = out_images + 4 * out_off;
+    for (uint32_t y = 0; y < height; y++)
+      for (uint32_t x = 0; x < width; x++) {
+        float acc[4] = {0, 0, 0, 0};
+        for (uint32_t dx = 0; dx < spp_x; dx++)
+          for (uint32_t dy = 0; dy < spp_y; dy++) {
+            const float u = (float(spp_x * x + dx) + 0.5f) / float(spp_x * width);
+            const float v = (float(spp_y * y + dy) + 0.5f) / float(spp_y * height);
+            float col[4], msk[4];
+            sample_bilinear(src, w0, h0, u, v, col);
+            sample_bilinear(mask.data(), w0, h0, u, v, msk);
+            col[3] = msk[3];
+            const float k = float(spp_x * spp_y);
+            for (int c = 0; c < 4; c++) acc[c] += col[c] / k;
+          }
+        for (int c = 0; c < 4; c++) dst[4 * (size_t(y) * width + x) + c] = acc[c];
+      }
+    out_views[n] = views[n];
+    out_views[n].width = width;
+    out_views[n].height = height;
+    in_off += size_t(w0) * h0;
+    out_off += size_t(width) * height;
+  }
+  return LRT_OK;
 }
 
 extern "C" lrt_status lrt_dr_set_preset(lrt_ctx *ctx, const lrt_dr_preset *preset) {
@@ -574,7 +651,8 @@ struct GridArrays {
 
 extern "C" lrt_status lrt_dr_optimize_grid(lrt_ctx *ctx, uint32_t start_grid_size, uint32_t no_last_step_resize,
                                            const lrt_dr_preset *presets, const uint32_t *iterations,
-                                           uint32_t n_stages, lrt_sbs_header *hdr, lrt_sbs_node **nodes,
+                                           const uint32_t *render_sizes, uint32_t n_stages, lrt_sbs_header *hdr,
+                                           lrt_sbs_node **nodes,
                                            uint32_t *n_nodes, uint32_t **values, uint64_t *n_values, float **params,
                                            uint32_t *n_params, double *last_losses) {
   if (!ctx) return LRT_ERR_INVALID;
@@ -591,9 +669,23 @@ extern "C" lrt_status lrt_dr_optimize_grid(lrt_ctx *ctx, uint32_t start_grid_siz
   s = lrt_dr_grid_resample(start_grid_size, bs, nullptr, 0, &g.hdr, &g.nodes, &g.n_nodes, &g.values, &g.n_values,
                            &g.params, &g.n_params);
   if (s != LRT_OK) return fail(ctx, s, "lrt_dr_optimize_grid: starting grid");
+  DrState &st = *ctx->dr;
   for (uint32_t i = 0; i < n_stages; i++) {
-    // OptimizeFixedStructure (:278-576): scene, preset, iterations; the optimised
-    // parameters become the grid's values_f (:574)
+    // OptimizeFixedStructure (:278-576): the reference images at the stage's render
+    // size (PreprocessRefImages, :322-339; 0 x 0 = as given), scene, preset,
+    // iterations; the optimised parameters become the grid's values_f (:574)
+    const uint32_t rw = render_sizes ? render_sizes[2 * i] : 0, rh = render_sizes ? render_sizes[2 * i + 1] : 0;
+    const uint32_t nv = uint32_t(st.orig_views.size());
+    if (rw && rh) {
+      std::vector<lrt_view> v2(nv);
+      std::vector<float> im2(4 * size_t(rw) * rh * nv);
+      if ((s = lrt_dr_preprocess_reference(nv, st.orig_views.data(), st.orig_images.data(), rw, rh, v2.data(),
+                                           im2.data())) != LRT_OK)
+        return fail(ctx, s, "lrt_dr_optimize_grid: render size");
+      if ((s = upload_reference(ctx, nv, v2.data(), im2.data())) != LRT_OK) return s;
+    } else if ((s = upload_reference(ctx, nv, st.orig_views.data(), st.orig_images.data())) != LRT_OK) {
+      return s;
+    }
     if ((s = lrt_dr_set_preset(ctx, &presets[i])) != LRT_OK) return s;
     if ((s = lrt_dr_set_scene(ctx, &g.hdr, g.nodes, g.n_nodes, g.values, g.n_values, g.params, g.n_params, nullptr,
                               0)) != LRT_OK)

@@ -61,9 +61,10 @@ def _lib():
                                     C.POINTER(U32)]),
             "lrt_dr_grid_resample": (I, [U32, U32, VP, U32, C.POINTER(lrt.SbsHeader), C.POINTER(VP), C.POINTER(U32),
                                          C.POINTER(VP), C.POINTER(C.c_uint64), C.POINTER(VP), C.POINTER(U32)]),
-            "lrt_dr_optimize_grid": (I, [P, U32, U32, VP, VP, U32, C.POINTER(lrt.SbsHeader), C.POINTER(VP),
+            "lrt_dr_optimize_grid": (I, [P, U32, U32, VP, VP, VP, U32, C.POINTER(lrt.SbsHeader), C.POINTER(VP),
                                          C.POINTER(U32), C.POINTER(VP), C.POINTER(C.c_uint64), C.POINTER(VP),
                                          C.POINTER(U32), VP]),
+            "lrt_dr_preprocess_reference": (I, [U32, VP, VP, U32, U32, VP, VP]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -101,6 +102,21 @@ def _take_grid(L, hdr, pn, nn, pv, nv, pp, npar):
         for q in (pn, pv, pp):
             L.lrt_free(q)
     return hdr, nodes, values, params
+
+
+def preprocess_reference(views, images, width, height):
+    """PreprocessRefImages: the reference images (list of HxWx4 float) resampled to
+    width x height; returns (views with the new size, list of images)."""
+    from .lrt import make_views
+    va = make_views(views)
+    imgs = np.ascontiguousarray(np.concatenate([np.asarray(i, np.float32).reshape(-1, 4) for i in images]))
+    out_v = (lrt.View * len(views))()
+    out = np.zeros((len(views) * width * height, 4), np.float32)
+    lrt._check(_lib().lrt_dr_preprocess_reference(len(views), C.cast(va, C.c_void_p), lrt._ptr(imgs), width, height,
+                                                  C.cast(out_v, C.c_void_p), lrt._ptr(out)),
+               what="lrt_dr_preprocess_reference")
+    return out_v, [out[k * width * height:(k + 1) * width * height].reshape(height, width, 4)
+                   for k in range(len(views))]
 
 
 def grid_resample(brick_count, brick_size, old_params=None, old_brick_size=0):
@@ -230,18 +246,20 @@ class MultiRendererDR:
         sbs[3][:] = self.get(GET_PARAMS)
         return last
 
-    def OptimizeGrid(self, start_grid_size, no_last_step_resize, presets, iterations):
-        """MultiRendererDR::OptimizeGrid on the reference set by SetReference: returns
-        (final grid [hdr, nodes, values, params], last step's per-view losses)."""
+    def OptimizeGrid(self, start_grid_size, no_last_step_resize, presets, iterations, render_sizes=None):
+        """MultiRendererDR::OptimizeGrid on the reference set by SetReference (each
+        stage at render_sizes[i] = (width, height), or as given): returns (final grid
+        [hdr, nodes, values, params], last step's per-view losses)."""
         L = _lib()
         pa = (DrPreset * len(presets))(*presets)
         it = np.ascontiguousarray(iterations, np.uint32)
+        rs = None if render_sizes is None else np.ascontiguousarray(render_sizes, np.uint32).reshape(-1)
         hdr = lrt.SbsHeader()
         pn, pv, pp = C.c_void_p(), C.c_void_p(), C.c_void_p()
         nn, npar, nv = C.c_uint32(), C.c_uint32(), C.c_uint64()
         last = np.zeros(len(self.views), np.float64)
         self._chk(L.lrt_dr_optimize_grid(self._ctx, start_grid_size, int(bool(no_last_step_resize)),
-                                         C.cast(pa, C.c_void_p), lrt._ptr(it), len(presets), C.byref(hdr),
+                                         C.cast(pa, C.c_void_p), lrt._ptr(it), lrt._ptr(rs), len(presets), C.byref(hdr),
                                          C.byref(pn), C.byref(nn), C.byref(pv), C.byref(nv), C.byref(pp),
                                          C.byref(npar), lrt._ptr(last)))
         grid = list(_take_grid(L, hdr, pn, nn, pv, nv, pp, npar))

@@ -61,3 +61,53 @@ def test_layout_matches_sdf_grid():
     h2, n2, v2, _ = dr.grid_sbs(3, 2, lrt.Sdf(spheres=np.array([[0, 0, 0, 0.5]], np.float32)), None)
     assert (h1.brick_size, h1.aux_data) == (h2.brick_size, h2.aux_data)
     assert np.array_equal(n1, n2) and np.array_equal(v1, v2)
+
+
+def _preprocess_np(img, width, height):
+    """PreprocessRefImages restated with numpy float32 scalars (bilinear, texel centres,
+    clamped edges; alpha from the 'colour differs from black' mask)."""
+    f = np.float32
+    h0, w0 = img.shape[:2]
+    rgb = img[..., :3].astype(np.float32)
+    m = (np.sqrt(rgb[..., 0] * rgb[..., 0] + rgb[..., 1] * rgb[..., 1] + rgb[..., 2] * rgb[..., 2]) <
+         f(0.001)).astype(np.float32)
+    mask = np.repeat((f(1) - m)[..., None], 4, axis=2).astype(np.float32)
+    sx, sy = int(np.ceil(f(w0) / f(width))), int(np.ceil(f(h0) / f(height)))
+
+    def sample(im, u, v):
+        fx, fy = u * f(w0) - f(0.5), v * f(h0) - f(0.5)
+        x0f, y0f = np.floor(fx), np.floor(fy)
+        tx, ty = fx - x0f, fy - y0f
+        xa, xb = min(max(int(x0f), 0), w0 - 1), min(max(int(x0f) + 1, 0), w0 - 1)
+        ya, yb = min(max(int(y0f), 0), h0 - 1), min(max(int(y0f) + 1, 0), h0 - 1)
+        a, b, d, e = im[ya, xa], im[ya, xb], im[yb, xa], im[yb, xb]
+        return (f(1) - ty) * ((f(1) - tx) * a + tx * b) + ty * ((f(1) - tx) * d + tx * e)
+
+    out = np.zeros((height, width, 4), np.float32)
+    k = f(sx * sy)
+    for y in range(height):
+        for x in range(width):
+            acc = np.zeros(4, np.float32)
+            for dx in range(sx):
+                for dy in range(sy):
+                    u = (f(sx * x + dx) + f(0.5)) / f(sx * width)
+                    v = (f(sy * y + dy) + f(0.5)) / f(sy * height)
+                    col = sample(img.astype(np.float32), u, v).astype(np.float32)
+                    col[3] = sample(mask, u, v)[3]
+                    acc = (acc + col / k).astype(np.float32)
+            out[y, x] = acc
+    return out
+
+
+@pytest.mark.parametrize("size", [(7, 5), (16, 16), (30, 11)])
+def test_preprocess_reference_matches_restatement(size):
+    rng = np.random.default_rng(size[0])
+    imgs = [rng.uniform(0, 1, (16, 20, 4)).astype(np.float32) for _ in range(2)]
+    imgs[0][3:9, 4:12, :3] = 0.0            # background patches: mask 0 there
+    pj = lrt.perspective(45.0, 1.0, 0.01, 100.0)
+    views = [(20, 16, lrt.look_at([0, 0, 3], [0, 0, 0], [0, 1, 0]), pj)] * 2
+    out_v, out = dr.preprocess_reference(views, imgs, *size)
+    assert out_v[0].width == size[0] and out_v[0].height == size[1]
+    for k in range(2):
+        want = _preprocess_np(imgs[k], *size)
+        assert np.array_equal(out[k].view(np.uint32), want.view(np.uint32))

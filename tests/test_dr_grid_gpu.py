@@ -60,3 +60,23 @@ def test_optimize_grid_reduces_the_loss(bvh_builder):
     R.close()
     assert grid[0].brick_size == 2
     assert np.all(np.isfinite(long)) and long.mean() < 0.8 * short.mean()
+
+
+def test_optimize_grid_per_stage_render_size():
+    """Each stage renders the reference resampled to its own size (the reference's
+    preset render_width/height): the context ends at the last stage's size and the
+    loss still falls."""
+    presets = [dr.default_preset(opt_lr=0.02, border_spp=16, seed=3, accumulate_batch=1),
+               dr.default_preset(opt_lr=0.01, border_spp=16, seed=4, accumulate_batch=1)]
+    sizes = [(24, 24), (32, 32)]
+    R = _renderer()
+    _, short = R.OptimizeGrid(4, True, presets, [1, 1], render_sizes=sizes)
+    R.close()
+    R = _renderer()
+    grid, long = R.OptimizeGrid(4, True, presets, [30, 30], render_sizes=sizes)
+    img = np.zeros((32 * 32, 4), np.float32)
+    R._chk(dr._lib().lrt_dr_get(R._ctx, dr.GET_IMAGE, 0, lrt._ptr(img), img.nbytes))
+    R.close()
+    assert img[:, 3].max() > 0
+    assert np.all(np.isfinite(long)) and long.mean() < 0.8 * short.mean()
+
