@@ -50,7 +50,7 @@ def _orc_preset(p):
     return od.make_preset(render_mode=p.render_mode, reconstruction=p.reconstruction_flags, input_type=p.input_type,
                           loss=p.loss_function, spp=p.spp, border_spp=p.border_spp, border_relax_eps=p.border_relax_eps,
                           seed=p.seed, lights=lights, lr=p.opt_lr, beta1=p.opt_beta_1, beta2=p.opt_beta_2,
-                          eps=p.opt_eps, accumulate_batch=p.accumulate_batch)
+                          eps=p.opt_eps, accumulate_batch=p.accumulate_batch, border_sampling=p.border_sampling)
 
 
 def _targets(R, views, target_params, preset):
@@ -99,6 +99,12 @@ def _oview(v):
     dict(loss_function=1),
     dict(layout_in=False),
     dict(render_mode=dr.RENDER_LINEAR_DEPTH, input_type=1, reconstruction_flags=dr.RECON_GEOMETRY),
+    # SVM border sampling (CastBorderRaySVM) across the render modes of the reference's test 4
+    dict(border_sampling=1),
+    dict(border_sampling=1, render_mode=dr.RENDER_DIFFUSE),
+    dict(border_sampling=1, render_mode=dr.RENDER_MASK, reconstruction_flags=dr.RECON_GEOMETRY),
+    dict(border_sampling=1, render_mode=dr.RENDER_LINEAR_DEPTH, input_type=1, reconstruction_flags=dr.RECON_GEOMETRY),
+    dict(border_sampling=1, border_relax_eps=2e-4),
 ])
 def test_render_grad_matches_oracle(cfg):
     cfg = dict(cfg)
@@ -118,10 +124,13 @@ def test_render_grad_matches_oracle(cfg):
     R.close()
 
 
-def test_border_integral_alone_matches_oracle():
+@pytest.mark.parametrize("sampling", [0, 1])
+def test_border_integral_alone_matches_oracle(sampling):
     """The border term by itself (colour reconstruction off, interior geometry
-    PDs cancelled by rendering with DNORM/DDIFFUSE only through the border)."""
-    preset = dr.default_preset(border_spp=128, seed=3, reconstruction_flags=dr.RECON_GEOMETRY, render_mode=dr.RENDER_MASK)
+    PDs cancelled by rendering with DNORM/DDIFFUSE only through the border), with
+    random and with SVM border sampling."""
+    preset = dr.default_preset(border_spp=128, seed=3, reconstruction_flags=dr.RECON_GEOMETRY, render_mode=dr.RENDER_MASK,
+                               border_sampling=sampling)
     R, osc, init, views, imgs = _setup(preset)
     _, g = R.render_grad(0)
     o = osc.render(init, _orc_preset(preset), _oview(views[0]), imgs[0], threads=1)
