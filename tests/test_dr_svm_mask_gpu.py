@@ -77,8 +77,10 @@ def test_svm_rejects_too_many_border_samples():
     R.close()
 
 
-def test_raycasting_mask_matches_oracle_over_steps():
-    R, osc, init, op, oviews, imgs = _setup(border_spp=16, raycasting_mask=1, opt_lr=0.02)
+@pytest.mark.parametrize("spp,sampling", [(1, 0), (4, 0), (1, 1)])
+def test_raycasting_mask_matches_oracle_over_steps(spp, sampling):
+    R, osc, init, op, oviews, imgs = _setup(border_spp=16, raycasting_mask=1, opt_lr=0.02, spp=spp,
+                                            border_sampling=sampling)
     masks = [np.ones(S * S, np.uint8) for _ in oviews]
     params = init.copy()
     state = np.zeros(2 * params.size, np.float32)
