@@ -99,3 +99,43 @@ def test_raycasting_mask_matches_oracle_over_steps(spp, sampling):
         R.set_params(params)
     assert shrank
     R.close()
+
+
+@pytest.mark.parametrize("case", ["away", "one_pixel", "ragged"])
+def test_dr_edge_views_match_oracle(case):
+    """RenderDR on a view that sees nothing (loss from the reference image alone, no
+    gradient), a one-pixel view and a ragged 13 x 7 view: image, loss and gradient
+    against the oracle."""
+    up = scenes.union_params()
+    hdr, nodes, values, target = dr.grid_sbs(6, 4, lrt.Sdf(up["spheres"], up["boxes"], up["k"]), None)
+    _, _, _, init = dr.grid_sbs(6, 4, lrt.Sdf(spheres=np.array([[0, 0, 0, 0.55]], np.float32)), [0.8, 0.3, 0.2])
+    if case == "away":
+        w, h, eye, at = 24, 16, [0, 0, 2.6], [0, 0, 6]
+    elif case == "one_pixel":
+        w, h, eye, at = 1, 1, [0.05, 0.02, 2.6], [0, 0, 0]
+    else:
+        w, h, eye, at = 13, 7, [1.5, 1.0, 2.2], [0, 0, 0]
+    wv, pj = lrt.look_at(eye, at, [0, 1, 0]), lrt.perspective(45.0, float(w) / h, 0.01, 100.0)
+    ref = np.random.default_rng(5).uniform(0, 1, (h, w, 4)).astype(np.float32)
+    R = dr.MultiRendererDR()
+    R.SetScene(hdr, nodes, values, init)
+    R.SetReference([ref], [wv], [pj])
+    preset = dr.default_preset(seed=3, border_spp=32)
+    R.SetPreset(preset)
+    loss, g = R.render_grad(0)
+    img = R.getLastImage(0).reshape(-1, 4)
+    osc = od.DrScene(orc.SbsHeader(hdr.brick_size, hdr.brick_pad, hdr.bytes_per_value, hdr.aux_data), nodes, values,
+                     init.size, pairs=R.bvh2())
+    lights = [(preset.lights[i].type, np.array(preset.lights[i].dir[:], np.float32),
+               np.array(preset.lights[i].color[:], np.float32)) for i in range(preset.n_lights)]
+    op = od.make_preset(render_mode=preset.render_mode, reconstruction=preset.reconstruction_flags, border_spp=32,
+                        seed=3, lights=lights, lr=preset.opt_lr)
+    o = osc.render(init, op, od.make_view(w, h, wv, pj, lrt.inverse4x4), ref.reshape(-1, 4), threads=1)
+    R.close()
+    assert np.array_equal(img.view(np.uint32), o["image"].view(np.uint32))
+    assert abs(loss - o["loss"]) <= 1e-9 * max(1.0, abs(o["loss"]))
+    if case == "away":
+        assert not np.any(img[:, 3]) and not np.any(g) and not np.any(o["grad"])
+    else:
+        nrm = np.linalg.norm(o["grad"])
+        assert np.linalg.norm(g - o["grad"]) <= 1e-3 * max(nrm, 1e-30)
