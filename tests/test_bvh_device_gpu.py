@@ -123,6 +123,21 @@ def test_device_sah_is_the_host_tree(depth, brick):
     assert host.shape == dev.shape and host.tobytes() == dev.tobytes()
 
 
+@pytest.mark.parametrize("depth", [5, 7])
+def test_device_sah_svs_is_the_host_tree(depth):
+    n = lrt.svs_from_sdf(scenes.union_sdf(), depth)
+    pairs = []
+    for builder in (0, 1):
+        s = lrt.Scene(0)
+        s.set_tuning("bvh_builder", builder)
+        g = s.add_svs(n)
+        s.add_instance(g)
+        s.commit_scene()
+        pairs.append(s.bvh2())
+        s.close()
+    assert pairs[0].tobytes() == pairs[1].tobytes()
+
+
 @pytest.mark.parametrize("subdiv", [4, 6])   # 6: 81,920 triangles, the top levels split by many blocks
 def test_device_sah_mesh_is_the_host_tree(subdiv):
     verts, faces = scenes.displaced_icosphere(subdiv=subdiv)
