@@ -55,7 +55,9 @@ lrt_status lrt_add_instance(lrt_ctx *ctx, uint32_t geom_id, const float matrix[1
 /* BVHRT::CommitScene, BVH/BVH2Common_host.cpp:1416-1448: builds the BVH and
  * uploads the scene to the device.  One instance per scene. */
 lrt_status lrt_commit_scene(lrt_ctx *ctx);
-/* BVHRT::SetPreset / MultiRenderer::SetPreset, Renderer/eye_ray_host.cpp:549-556 */
+/* BVHRT::SetPreset / MultiRenderer::SetPreset, Renderer/eye_ray_host.cpp:549-556.
+ * ray_gen_mode 0 (regular sub-pixel grid) or 1 (RAY_GEN_MODE_RANDOM, see
+ * lrt_set_seed); interpolation_mode 0 (trilinear) only. */
 lrt_status lrt_set_preset(lrt_ctx *ctx, const lrt_preset *preset);
 
 /* Launch-shape and kernel choices; no reference counterpart (the reference's
@@ -79,8 +81,51 @@ lrt_status lrt_set_preset(lrt_ctx *ctx, const lrt_preset *preset);
  * 2 = a linear BVH on the device: Morton codes of the primitive centroids, a
  * radix sort, a binary radix tree and the same 4-wide collapse, one primitive
  * per leaf; hits are the same apart from exact ties between primitives, and
- * traversal is a few percent slower). */
+ * traversal is a few percent slower).
+ * "first_hit" (0 = default: the closest hit, independent of the BVH's shape;
+ * 1 = SBS and SVS renders, queries and graphs walk the BVH2 fat pairs in
+ * BVH2TraverseF32's order and stop at the first SDF leaf that reports a hit,
+ * BVH/BVH2Common.cpp:3402-3405, 3407-3488 -- the reference's own result, which
+ * depends on the tree: the committed BVH's pairs, or the caller's through
+ * lrt_set_bvh2.  Triangle meshes have no early-out in the reference and keep
+ * the closest hit.  Not used by lrt_render_noalloc, lrt_render_counters or the
+ * autotuner). */
 lrt_status lrt_set_tuning(lrt_ctx *ctx, const char *key, int value);
+
+/* MultiRenderer::setSeed (Renderer/eye_ray.h:173): the seed of the sub-pixel
+ * offsets of RAY_GEN_MODE_RANDOM (preset ray_gen_mode 1), drawn as the
+ * reference does with rand2(x, y, i + seed % 2) (Renderer/eye_ray.cpp:53-80,
+ * 100-107).  Default 0 (the reference seeds from rand()). */
+lrt_status lrt_set_seed(lrt_ctx *ctx, uint32_t seed);
+
+/* The BVH2 of the first-hit walk ("first_hit" tuning) for the committed SBS or
+ * SVS scene, in the reference's fat-pair layout (root pair at 0, leaf payload
+ * PackOffsetAndSize(brick, 1)) -- e.g. the tree the reference's own builder made
+ * for the same bricks (BVHRT::m_allNodePairs), so that renders reproduce the
+ * reference's first hits exactly.  Copied; checked first (a tree rooted at pair
+ * 0, every index in range, at most 80 inner pairs on a path: LRT_ERR_INVALID
+ * otherwise).  Valid until the next commit.  No reference counterpart. */
+lrt_status lrt_set_bvh2(lrt_ctx *ctx, const lrt_bvh_pair *pairs, uint32_t n_pairs);
+
+/* BVHRT::UpdateInstance, BVH/BVH2Common_host.cpp:1489-1520: a new matrix for an
+ * instance; the committed scene follows at once (no rebuild: the instance box
+ * and inverse matrices are recomputed). */
+lrt_status lrt_update_instance(lrt_ctx *ctx, uint32_t inst_id, const float matrix[16]);
+
+/* BVHRT::UpdateGeom_Triangles3f, BVH/BVH2Common_host.cpp:258-261 (which the
+ * reference leaves unimplemented): new vertex positions for the committed mesh,
+ * refit on the device as lrt_refit_triangles does.  `indices` may be NULL or
+ * must equal the committed ones (new connectivity: LRT_ERR_UNSUPPORTED; add the
+ * mesh again and commit). */
+lrt_status lrt_update_geom_triangles(lrt_ctx *ctx, uint32_t geom_id, const float *vpos, size_t n_vert,
+                                     const uint32_t *indices, size_t n_indices, size_t v_byte_stride);
+
+/* BVHRT::AddGeom_AABB, BVH/BVH2Common_host.cpp:264-280: always
+ * LRT_ERR_UNSUPPORTED.  The reference builds a BVH over the boxes but registers
+ * no geometry object for them, so its traversal has no intersector to call for
+ * such a leaf; this path has none either (custom primitives are outside the
+ * SBS / SVS / triangle leaves it accelerates). */
+lrt_status lrt_add_aabb(lrt_ctx *ctx, uint32_t type_id, const float *boxes8, size_t n_boxes, uint32_t *geom_id);
 
 /* New vertex positions for the committed triangle mesh (same vertex count and
  * indices; n_vert positions, v_byte_stride bytes apart): the BVH keeps its
@@ -140,18 +185,25 @@ lrt_status lrt_render_host(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views
  * (a cudaMalloc from the library would fail or fragment that pool), and a
  * real-time frame loop where cudaMalloc's implicit device synchronisation and
  * latency are not acceptable.  Same results as lrt_render for the committed
- * scene (the inputs were allocated once, by lrt_commit_scene).  The per-call
- * scratch -- the persistent kernel's work-queue head and the per-view table --
- * lives in one file-scope device array of 256 + LRT_NOALLOC_MAX_VIEWS * 160
- * bytes that every GPU loading the library keeps until exit.  At most
- * LRT_NOALLOC_MAX_VIEWS views per call; more returns LRT_ERR_INVALID.  The
- * first call on a device looks up the array's device address: make that first
- * call before any stream capture.  All calls share the array, which keeps the
- * last call's contents (the queue head is cleared on every call): calls whose
- * GPU work overlaps -- on different streams, or from several host threads --
- * race on it; serialise them on one stream.  Outputs are device memory, as in
- * lrt_render; asynchronous on `stream`.  Errors are reported through the
- * status only (lrt_last_error is not updated, which could allocate). */
+ * scene (the inputs were allocated once, by lrt_commit_scene), rendered with
+ * the plain finder: the "proposal" tuning key is ignored here (the proposal
+ * kernels need the network's buffers, which this call does not touch).  The
+ * per-call scratch -- the persistent kernel's work-queue head and the per-view
+ * table -- lives in one file-scope device array of 256 +
+ * LRT_NOALLOC_MAX_VIEWS * 160 bytes that every GPU loading the library keeps
+ * until exit.  At most LRT_NOALLOC_MAX_VIEWS views per call; more returns
+ * LRT_ERR_INVALID.  The view table is passed to a small set-up kernel by
+ * value (two launches per call: set-up, render), so the `views` array may be
+ * reused as soon as the call returns.  The first call on a device looks up
+ * the array's device address and keeps it for the life of the process: make
+ * that first call before any stream capture, and do not use the library on a
+ * device after cudaDeviceReset (which also invalidates every context's device
+ * buffers).  All calls share the array, which keeps the last call's contents
+ * (the queue head is cleared on every call): calls whose GPU work overlaps --
+ * on different streams, or from several host threads -- race on it; serialise
+ * them on one stream.  Outputs are device memory, as in lrt_render;
+ * asynchronous on `stream`.  Errors are reported through the status only
+ * (lrt_last_error is not updated, which could allocate). */
 #define LRT_NOALLOC_MAX_VIEWS 64
 lrt_status lrt_render_noalloc(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, lrt_hit16 *hits16,
                               float *rgba, uint32_t *rgba8, void *stream);

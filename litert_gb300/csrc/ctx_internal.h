@@ -110,6 +110,11 @@ struct lrt_ctx {
   lrt::DrState *dr = nullptr;  // differentiable-render state (dr_api.cpp)
   lrt::ProposalState *prop = nullptr;   // learned proposal (proposal_api.cpp)
   int use_proposal = 0;        // render SBS leaves with the proposal kernel
+  uint32_t seed = 0;           // MultiRenderer::setSeed
+  // the BVH2 of the first-hit walk ("first_hit" tuning): checked and uploaded on
+  // first use, or given by the caller (lrt_set_bvh2); reset by a commit
+  DevBuf<lrt_bvh_pair> d_ref_pairs;
+  bool ref_pairs_ready = false;
 };
 
 static inline lrt_status fail(lrt_ctx *ctx, lrt_status s, const std::string &msg) {

@@ -609,19 +609,6 @@ __device__ float3 color_grad(const DevPreset &p, float t, float3 hcolor, float3 
   return c;
 }
 
-// rand3 / rand2, Renderer/eye_ray.cpp:53-80
-__device__ __forceinline__ float2 rand2(uint32_t x, uint32_t y, uint32_t iter, uint32_t seed) {
-  x = x + 1233u * (iter + seed) % 171u;
-  y = y + 453u * (iter + seed) % 765u;
-  uint32_t v0 = x, v1 = y, v2 = x ^ y;
-  v0 = v0 * 1664525u + 1013904223u; v1 = v1 * 1664525u + 1013904223u; v2 = v2 * 1664525u + 1013904223u;
-  v0 += v1 * v2; v1 += v2 * v0; v2 += v0 * v1;
-  v0 ^= v0 >> 16u; v1 ^= v1 >> 16u; v2 ^= v2 >> 16u;
-  v0 += v1 * v2; v1 += v2 * v0; v2 += v0 * v1;
-  const float k = 1.0f / float(0xffffffffu);
-  return make_float2(__uint2float_rn(v0) * k, __uint2float_rn(v1) * k);
-}
-
 // Gradient scatter.  With warp aggregation every lane of the warp must call it
 // (converged); lanes adding to the same index are summed through shared memory
 // and one lane issues the global atomic.

@@ -133,7 +133,11 @@ static void release_scene(lrt_ctx *ctx) {
   ctx->d_leaf_start_count.release();
   ctx->d_vpos.release();
   ctx->d_tri_indices.release();
+  ctx->d_ref_pairs.release();
   ctx->bvh_on_device = ctx->bvh_refit = ctx->tri_indices_on_device = false;
+  ctx->ref_pairs_ready = false;
+  ctx->dev.pairs = nullptr;
+  ctx->dev.n_pairs = 0;
   ctx->committed = false;
 }
 
@@ -485,6 +489,7 @@ extern "C" lrt_status lrt_commit_scene(lrt_ctx *ctx) {
   std::memcpy(s.inst_inv, in.inv, sizeof(s.inst_inv));
   std::memcpy(s.inst_inv_t, in.inv_t, sizeof(s.inst_inv_t));
   s.preset = ctx->preset;
+  s.seed = ctx->seed;
   ctx->dev = s;
   ctx->committed = true;
   return LRT_OK;
@@ -495,7 +500,7 @@ extern "C" lrt_status lrt_set_preset(lrt_ctx *ctx, const lrt_preset *preset) {
   if (preset->sdf_node_intersect > LRT_INTERSECT_IT) return fail(ctx, LRT_ERR_INVALID, "lrt_set_preset: bad intersect mode");
   if (preset->interpolation_mode != 0)
     return fail(ctx, LRT_ERR_UNSUPPORTED, "lrt_set_preset: only trilinear interpolation is supported");
-  if (preset->ray_gen_mode != 0) return fail(ctx, LRT_ERR_UNSUPPORTED, "lrt_set_preset: only regular ray generation");
+  if (preset->ray_gen_mode > 1) return fail(ctx, LRT_ERR_INVALID, "lrt_set_preset: ray_gen_mode is 0 or 1");
   if (preset->spp == 0 || preset->spp > 1024) return fail(ctx, LRT_ERR_INVALID, "lrt_set_preset: bad spp");
   switch (preset->render_mode) {   // kernel_RayTrace's modes for the geometry types of this path
     case LRT_RENDER_MODE_MASK: case LRT_RENDER_MODE_LAMBERT_NO_TEX: case LRT_RENDER_MODE_DEPTH:
@@ -541,6 +546,9 @@ extern "C" lrt_status lrt_set_tuning(lrt_ctx *ctx, const char *key, int value) {
   } else if (k == "bvh_builder") {
     if (value < 0 || value > 2) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: bvh_builder is 0, 1 or 2");
     ctx->bvh_builder = value;
+  } else if (k == "first_hit") {
+    if (value < 0 || value > 1) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: first_hit is 0 or 1");
+    ctx->tuning.first_hit = value;
   } else if (k == "proposal") {
     if (value < 0 || value > 1) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: proposal is 0 or 1");
     ctx->use_proposal = value;
@@ -611,6 +619,116 @@ extern "C" lrt_status lrt_get_bvh2(lrt_ctx *ctx, const lrt_bvh_pair **pairs, uin
   return LRT_OK;
 }
 
+// A BVH2 the first-hit walk can follow: pair 0 is the root, every inner child
+// names a pair that no other node names (a tree: the walk ends), every leaf names
+// a primitive of the committed geometry (or is the empty marker 0xFFFFFFFF), and
+// no path holds more inner pairs than the walk's 80-entry stack.
+static bool check_bvh2(const lrt_bvh_pair *pairs, uint32_t n_pairs, uint32_t n_prims, std::string &why) {
+  if (n_pairs == 0) { why = "no pairs"; return false; }
+  std::vector<uint8_t> seen(n_pairs, 0);
+  std::vector<std::pair<uint32_t, uint32_t>> todo{{0u, 1u}};   // (pair, inner pairs on the path)
+  seen[0] = 1;
+  while (!todo.empty()) {
+    const auto [p, depth] = todo.back();
+    todo.pop_back();
+    if (depth > 80) { why = "a path needs more than 80 stack entries"; return false; }
+    for (const lrt_bvh_node *c : {&pairs[p].left, &pairs[p].right}) {
+      const uint32_t off = c->leftOffset;
+      if (off & 0x80000000u) {
+        if (off != 0xFFFFFFFFu && (off & 0x00FFFFFFu) >= n_prims) { why = "leaf names no primitive"; return false; }
+      } else {
+        if (off >= n_pairs || seen[off]) { why = "child index out of range or shared"; return false; }
+        seen[off] = 1;
+        todo.push_back({off, depth + 1});
+      }
+    }
+  }
+  return true;
+}
+
+static uint32_t committed_prims(const lrt_ctx *ctx) {
+  const Geom &g = ctx->geoms[ctx->insts[0].geom];
+  return g.type == LRT_TYPE_SDF_SVS ? uint32_t(g.svs.size()) : uint32_t(g.sbs.nodes.size());
+}
+
+static lrt_status upload_ref_pairs(lrt_ctx *ctx, const lrt_bvh_pair *pairs, uint32_t n_pairs) {
+  std::string why;
+  if (!check_bvh2(pairs, n_pairs, committed_prims(ctx), why)) return fail(ctx, LRT_ERR_INVALID, "BVH2: " + why);
+  cudaError_t e = upload(ctx->d_ref_pairs, pairs, n_pairs);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "upload BVH2");
+  ctx->dev.pairs = reinterpret_cast<const float4 *>(ctx->d_ref_pairs.p);
+  ctx->dev.n_pairs = n_pairs;
+  ctx->ref_pairs_ready = true;
+  return LRT_OK;
+}
+
+// The first-hit walk's tree, on its first use after a commit: the committed BVH's
+// own fat pairs (the tree the closest-hit kernels collapse into 4-wide nodes).
+static lrt_status ensure_walk(lrt_ctx *ctx) {
+  if (!ctx->tuning.first_hit || !sdf_scene(ctx->dev) || ctx->ref_pairs_ready) return LRT_OK;
+  const lrt_bvh_pair *p = nullptr;
+  uint32_t n = 0;
+  lrt_status s = lrt_get_bvh2(ctx, &p, &n);
+  if (s != LRT_OK) return s;
+  return upload_ref_pairs(ctx, p, n);
+}
+
+extern "C" lrt_status lrt_set_bvh2(lrt_ctx *ctx, const lrt_bvh_pair *pairs, uint32_t n_pairs) {
+  if (!ctx || !pairs) return LRT_ERR_INVALID;
+  if (!ctx->committed) return fail(ctx, LRT_ERR_STATE, "lrt_set_bvh2: commit the scene first");
+  if (!sdf_scene(ctx->dev))
+    return fail(ctx, LRT_ERR_UNSUPPORTED, "lrt_set_bvh2: triangle meshes have no first-hit walk");
+  LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+  return upload_ref_pairs(ctx, pairs, n_pairs);
+}
+
+extern "C" lrt_status lrt_set_seed(lrt_ctx *ctx, uint32_t seed) {
+  if (!ctx) return LRT_ERR_INVALID;
+  ctx->seed = seed;
+  ctx->dev.seed = seed;
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_update_instance(lrt_ctx *ctx, uint32_t inst_id, const float matrix[16]) {
+  if (!ctx || !matrix) return LRT_ERR_INVALID;
+  if (inst_id >= ctx->insts.size()) return fail(ctx, LRT_ERR_INVALID, "lrt_update_instance: bad instance id");
+  Inst &in = ctx->insts[inst_id];
+  std::memcpy(in.m, matrix, sizeof(in.m));
+  lrt_inverse4x4(matrix, in.inv);
+  for (int i = 0; i < 4; i++)
+    for (int j = 0; j < 4; j++) in.inv_t[i * 4 + j] = in.inv[j * 4 + i];
+  instance_bounds(ctx->geoms[in.geom], in);
+  if (ctx->committed && inst_id == 0) {   // the committed single instance: no rebuild needed
+    for (int k = 0; k < 3; k++) { ctx->dev.inst_bmin[k] = in.bmin[k]; ctx->dev.inst_bmax[k] = in.bmax[k]; }
+    std::memcpy(ctx->dev.inst_inv, in.inv, sizeof(in.inv));
+    std::memcpy(ctx->dev.inst_inv_t, in.inv_t, sizeof(in.inv_t));
+  }
+  return LRT_OK;
+}
+
+extern "C" lrt_status lrt_update_geom_triangles(lrt_ctx *ctx, uint32_t geom_id, const float *vpos, size_t n_vert,
+                                                const uint32_t *indices, size_t n_indices, size_t v_byte_stride) {
+  if (!ctx) return LRT_ERR_INVALID;
+  if (geom_id >= ctx->geoms.size() || ctx->geoms[geom_id].type != LRT_TYPE_MESH_TRIANGLE)
+    return fail(ctx, LRT_ERR_INVALID, "lrt_update_geom_triangles: not a triangle geometry");
+  const Geom &g = ctx->geoms[geom_id];
+  if (indices && (n_indices != g.indices.size() || !std::equal(g.indices.begin(), g.indices.end(), indices)))
+    return fail(ctx, LRT_ERR_UNSUPPORTED,
+                "lrt_update_geom_triangles: new connectivity needs lrt_add_triangles and a commit");
+  if (!ctx->committed || ctx->insts[0].geom != geom_id)
+    return fail(ctx, LRT_ERR_STATE, "lrt_update_geom_triangles: the geometry is not the committed one");
+  return lrt_refit_triangles(ctx, vpos, n_vert, v_byte_stride);
+}
+
+extern "C" lrt_status lrt_add_aabb(lrt_ctx *ctx, uint32_t type_id, const float *boxes8, size_t n_boxes,
+                                   uint32_t *geom_id) {
+  (void)type_id; (void)boxes8; (void)n_boxes;
+  if (geom_id) *geom_id = 0xFFFFFFFFu;
+  return fail(ctx, LRT_ERR_UNSUPPORTED,
+              "lrt_add_aabb: custom-box geometry has no intersector on this path (the reference's AddGeom_AABB "
+              "registers boxes but no geometry object to intersect them)");
+}
+
 // ---------------------------------------------------------------- rendering
 static lrt_status prepare_views(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, cudaStream_t st,
                                 uint32_t *total_tiles, uint64_t *total_pix) {
@@ -663,6 +781,7 @@ static lrt_status render_impl(lrt_ctx *ctx, const lrt_view *views, uint32_t n_vi
   uint64_t pix = 0;
   lrt_status s = prepare_views(ctx, views, n_views, st, &tiles, &pix);
   if (s != LRT_OK) return s;
+  if ((s = ensure_walk(ctx)) != LRT_OK) return s;
   RenderLaunch L;
   L.views = ctx->d_views.p;
   L.n_views = n_views;
@@ -727,8 +846,8 @@ extern "C" lrt_status lrt_render_host(lrt_ctx *ctx, const lrt_view *views, uint3
 }
 
 // No allocation anywhere on this path: the view table is built in a stack array
-// and copied into the file-scope scratch array of trace.cu; errors are returned
-// as codes only.
+// and handed by value to a set-up kernel that writes it into the file-scope
+// scratch array of trace.cu; errors are returned as codes only.
 extern "C" lrt_status lrt_render_noalloc(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, lrt_hit16 *hits16,
                                          float *rgba, uint32_t *rgba8, void *stream) {
   if (!ctx || !views || n_views == 0 || n_views > LRT_NOALLOC_MAX_VIEWS) return LRT_ERR_INVALID;
@@ -759,7 +878,7 @@ extern "C" lrt_status lrt_render_noalloc(lrt_ctx *ctx, const lrt_view *views, ui
                                               reinterpret_cast<float4 *>(rgba), rgba8, ctx->device, ctx->num_sms,
                                               static_cast<cudaStream_t>(stream), ctx->tuning);
   if (e != cudaSuccess) return e == cudaErrorInvalidValue ? LRT_ERR_INVALID : LRT_ERR_CUDA;
-  ctx->last_launches = 1;
+  ctx->last_launches = 2;   // set-up kernel + render kernel
   return LRT_OK;
 }
 
@@ -783,9 +902,14 @@ extern "C" lrt_status lrt_query_rays(lrt_ctx *ctx, const float *pos_near, const 
   if (!pos_near || !dir_far || !out) return fail(ctx, LRT_ERR_INVALID, "lrt_query_rays: null array");
   LRT_CUDA(ctx, cudaSetDevice(ctx->device));
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  lrt_status ws = ensure_walk(ctx);
+  if (ws != LRT_OK) return ws;
+  const bool ref = ctx->tuning.first_hit && sdf_scene(ctx->dev);
+  auto launch_q = [&](const float4 *p, const float4 *d, lrt_hit *o) {
+    return ref ? launch_query_ref(ctx->dev, p, d, n, o, st) : launch_query(ctx->dev, p, d, n, o, st);
+  };
   if (device_ptrs) {
-    LRT_CUDA(ctx, launch_query(ctx->dev, reinterpret_cast<const float4 *>(pos_near),
-                               reinterpret_cast<const float4 *>(dir_far), n, out, st));
+    LRT_CUDA(ctx, launch_q(reinterpret_cast<const float4 *>(pos_near), reinterpret_cast<const float4 *>(dir_far), out));
     ctx->last_launches = 1;
     return LRT_OK;
   }
@@ -794,7 +918,7 @@ extern "C" lrt_status lrt_query_rays(lrt_ctx *ctx, const float *pos_near, const 
   LRT_CUDA(ctx, ctx->d_q_out.ensure(n));
   LRT_CUDA(ctx, cudaMemcpyAsync(ctx->d_q_pos.p, pos_near, size_t(n) * 16, cudaMemcpyHostToDevice, st));
   LRT_CUDA(ctx, cudaMemcpyAsync(ctx->d_q_dir.p, dir_far, size_t(n) * 16, cudaMemcpyHostToDevice, st));
-  LRT_CUDA(ctx, launch_query(ctx->dev, ctx->d_q_pos.p, ctx->d_q_dir.p, n, ctx->d_q_out.p, st));
+  LRT_CUDA(ctx, launch_q(ctx->d_q_pos.p, ctx->d_q_dir.p, ctx->d_q_out.p));
   LRT_CUDA(ctx, cudaMemcpyAsync(out, ctx->d_q_out.p, size_t(n) * sizeof(lrt_hit), cudaMemcpyDeviceToHost, st));
   LRT_CUDA(ctx, cudaStreamSynchronize(st));
   ctx->last_launches = 1;
@@ -981,6 +1105,7 @@ extern "C" lrt_status lrt_render_graph_create(lrt_ctx *ctx, const lrt_view *view
   uint32_t tiles = 0;
   lrt_status s = fill_views(ctx, views, n_views, hv, &tiles);
   if (s != LRT_OK) return s;
+  if ((s = ensure_walk(ctx)) != LRT_OK) return s;
   lrt_graph *g = new (std::nothrow) lrt_graph();
   if (!g) return fail(ctx, LRT_ERR_OOM, "graph allocation failed");
   g->device = ctx->device;

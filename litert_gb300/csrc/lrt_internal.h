@@ -108,6 +108,11 @@ struct DevScene {
   float inst_bmin[3], inst_bmax[3];
   float inst_inv[16], inst_inv_t[16];
   lrt_preset preset;
+  uint32_t seed;                 // MultiRenderer::m_seed (setSeed), for RAY_GEN_MODE_RANDOM
+  // the BVH2 in the reference's fat-pair layout (4 float4 per pair), for the
+  // first-hit walk of the "first_hit" tuning (null until that walk is used)
+  const float4 *pairs;
+  uint32_t n_pairs;
 };
 
 // A view prepared for the kernel: inverse matrices and its place in the
@@ -144,6 +149,8 @@ struct Tuning {
   int stack = 64;           // per-ray traversal stack entries (32 or 64; 32 only for shallow trees)
   int refill = 8;           // variant 2: idle lanes of a warp that trigger fetching new rays
   int fma = 0;              // 1: variant 0 without counters runs the kernels compiled with FP contraction
+  int first_hit = 0;        // 1: SBS / SVS renders and queries walk the BVH2 in the reference's order and
+                            // stop at the first SDF leaf that hits (BVH2TraverseF32's result)
 };
 
 cudaError_t launch_render(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st, bool count,
@@ -179,6 +186,12 @@ cudaError_t launch_render_noalloc(const DevScene &s, const DevView *host_views, 
                                   int device, int num_sms, cudaStream_t st, const Tuning &tu);
 cudaError_t launch_query(const DevScene &s, const float4 *pos_near, const float4 *dir_far, uint32_t n,
                          lrt_hit *out, cudaStream_t st);
+// The same two launches with the reference's first-hit BVH2 walk (trace_ref.cu);
+// SBS and SVS scenes whose s.pairs is set.
+cudaError_t launch_render_ref(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st);
+cudaError_t launch_query_ref(const DevScene &s, const float4 *pos_near, const float4 *dir_far, uint32_t n,
+                             lrt_hit *out, cudaStream_t st);
+inline bool sdf_scene(const DevScene &s) { return s.type != LRT_TYPE_MESH_TRIANGLE; }
 
 }  // namespace lrt
 

@@ -116,14 +116,18 @@ __device__ __forceinline__ float forward_warp(const Weights &W, const __nv_bfloa
   for (int mt = 0; mt < 2; mt++) {
     uint32_t a[4];
     ld_a(a, x, kIn, mt * 16, 0, lane);
+    // Each layer sums its products in the tensor core from zero and adds the bias
+    // afterwards in FP32, as the tcgen05 engine's epilogue does, so both engines
+    // round at the same points.
     float c1[4][4];
 #pragma unroll
     for (int nt = 0; nt < 4; nt++) {
       const int col = nt * 8 + 2 * t;
-      c1[nt][0] = W.b1[col]; c1[nt][1] = W.b1[col + 1]; c1[nt][2] = W.b1[col]; c1[nt][3] = W.b1[col + 1];
+      c1[nt][0] = c1[nt][1] = c1[nt][2] = c1[nt][3] = 0.0f;
       uint32_t b0, b1;
       ld_b_nk(b0, b1, W.w + kBfW1, kIn, nt * 8, 0, lane);
       mma16816(c1[nt], a, b0, b1);
+      c1[nt][0] += W.b1[col]; c1[nt][1] += W.b1[col + 1]; c1[nt][2] += W.b1[col]; c1[nt][3] += W.b1[col + 1];
 #pragma unroll
       for (int e = 0; e < 4; e++) c1[nt][e] = fmaxf(c1[nt][e], 0.0f);
     }
@@ -133,27 +137,28 @@ __device__ __forceinline__ float forward_warp(const Weights &W, const __nv_bfloa
 #pragma unroll
     for (int nt = 0; nt < 4; nt++) {
       const int col = nt * 8 + 2 * t;
-      c2[nt][0] = W.b2[col]; c2[nt][1] = W.b2[col + 1]; c2[nt][2] = W.b2[col]; c2[nt][3] = W.b2[col + 1];
+      c2[nt][0] = c2[nt][1] = c2[nt][2] = c2[nt][3] = 0.0f;
 #pragma unroll
       for (int kb = 0; kb < 2; kb++) {
         uint32_t b0, b1;
         ld_b_nk(b0, b1, W.w + kBfW2, kHid, nt * 8, kb * 16, lane);
         mma16816(c2[nt], a2[kb], b0, b1);
       }
+      c2[nt][0] += W.b2[col]; c2[nt][1] += W.b2[col + 1]; c2[nt][2] += W.b2[col]; c2[nt][3] += W.b2[col + 1];
 #pragma unroll
       for (int e = 0; e < 4; e++) c2[nt][e] = fmaxf(c2[nt][e], 0.0f);
     }
     uint32_t a3[2][4];
     c_to_a(c2, a3);
-    float c3[4] = {t == 0 ? W.b3 : 0.0f, 0.0f, t == 0 ? W.b3 : 0.0f, 0.0f};
+    float c3[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
     for (int kb = 0; kb < 2; kb++) {
       uint32_t b0, b1;
       ld_b_nk(b0, b1, W.w + kBfW3, kHid, 0, kb * 16, lane);
       mma16816(c3, a3[kb], b0, b1);
     }
-    out_lo[mt] = c3[0];
-    out_hi[mt] = c3[2];
+    out_lo[mt] = c3[0] + W.b3;
+    out_hi[mt] = c3[2] + W.b3;
     if (KEEP) {
 #pragma unroll
       for (int nt = 0; nt < 4; nt++)

@@ -86,10 +86,12 @@ lrt_status ensure(lrt_ctx *ctx) {
 }
 }  // namespace
 
-// the plain kernels, or the proposal kernel for DX-layout SBS scenes with the
-// NEWTON finder when it is switched on and the network has weights
+// the reference's first-hit walk when "first_hit" is set (SDF scenes), else the
+// plain kernels, or the proposal kernel for DX-layout SBS scenes with the NEWTON
+// finder when it is switched on and the network has weights
 cudaError_t dispatch_render(lrt_ctx *ctx, const RenderLaunch &L, cudaStream_t st, bool count) {
   const DevScene &s = ctx->dev;
+  if (ctx->tuning.first_hit && sdf_scene(s) && s.pairs) return launch_render_ref(s, L, ctx->num_sms, st);
   const uint32_t layout = s.sbs_hdr.aux_data & 0xFF000000u;
   const bool dx = s.type == LRT_TYPE_SDF_SBS && layout != LRT_SBS_LAYOUT_ID32F_IRGB32F &&
                   layout != LRT_SBS_LAYOUT_ID32F_IRGB32F_IN;

@@ -81,8 +81,17 @@ __global__ void __launch_bounds__(128, 5) render_kernel(DevScene s, RenderLaunch
     float4 acc = make_float4(0, 0, 0, 0);
     Hit first;
     for (uint32_t si = 0; si < spp; si++) {
-      const float dx = i_spp_sqrt * float(double(si / spp_sqrt) + 0.5);
-      const float dy = i_spp_sqrt * float(double(si % spp_sqrt) + 0.5);
+      // sub-pixel offset, CastRaySingle (Renderer/eye_ray.cpp:100-107): the regular
+      // grid, or rand2(x, y, i + m_seed % 2) for RAY_GEN_MODE_RANDOM
+      float dx, dy;
+      if (s.preset.ray_gen_mode == 1) {
+        const float2 r = rand2(x, y, si + s.seed % 2u, s.seed);
+        dx = r.x;
+        dy = r.y;
+      } else {
+        dx = i_spp_sqrt * float(double(si / spp_sqrt) + 0.5);
+        dy = i_spp_sqrt * float(double(si % spp_sqrt) + 0.5);
+      }
       float3 pos, dir;
       eye_ray(x, y, V.width, V.height, dx, dy, V.proj_inv, V.wv_inv, pos, dir);
       Hit hit;
@@ -115,6 +124,29 @@ __global__ void __launch_bounds__(128, 5) render_kernel(DevScene s, RenderLaunch
     atomicAdd(&L.counters[2], (unsigned long long)cnt.voxels);
     atomicAdd(&L.counters[3], (unsigned long long)cnt.finder);
   }
+}
+
+// Batched RayQuery_NearestHit: one thread per ray, full CRT_Hit output.
+template <int TYPE, int FEAT = 0>
+__global__ void __launch_bounds__(128) query_kernel(DevScene s, const float4 *pos_near, const float4 *dir_far,
+                                                   uint32_t n, lrt_hit *out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 p = pos_near[i], d = dir_far[i];
+  Counters cnt = {0, 0, 0, 0};
+  Hit hit;
+  trace<TYPE, false, -1, kStackSize, FEAT>(s, f3(p.x, p.y, p.z), p.w, f3(d.x, d.y, d.z), d.w, hit, cnt);
+  if (TYPE == LRT_TYPE_SDF_SBS && !(FEAT & 2)) hit_colour(s, f3(p.x, p.y, p.z), f3(d.x, d.y, d.z), hit);
+  lrt_hit o;
+  o.t = hit.t;
+  o.primId = (hit.prim != kMiss && (hit.geom >> 24) == LRT_TYPE_MESH_TRIANGLE) ? s.prim_indices[hit.prim] : hit.prim;
+  o.instId = hit.prim == kMiss ? kMiss : 0u;
+  o.geomId = hit.geom;
+  o.coords[0] = hit.c0;
+  o.coords[1] = hit.c1;
+  o.coords[2] = hit.c2;
+  o.coords[3] = hit.c3;
+  out[i] = o;
 }
 
 }  // namespace dev

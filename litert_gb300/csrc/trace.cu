@@ -116,29 +116,6 @@ __global__ void __launch_bounds__(128, 5) render_refill_kernel(DevScene s, Rende
   }
 }
 
-// Batched RayQuery_NearestHit: one thread per ray, full CRT_Hit output.
-template <int TYPE, int FEAT = 0>
-__global__ void __launch_bounds__(128) query_kernel(DevScene s, const float4 *pos_near, const float4 *dir_far,
-                                                   uint32_t n, lrt_hit *out) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float4 p = pos_near[i], d = dir_far[i];
-  Counters cnt = {0, 0, 0, 0};
-  Hit hit;
-  trace<TYPE, false, -1, kStackSize, FEAT>(s, f3(p.x, p.y, p.z), p.w, f3(d.x, d.y, d.z), d.w, hit, cnt);
-  if (TYPE == LRT_TYPE_SDF_SBS && !(FEAT & 2)) hit_colour(s, f3(p.x, p.y, p.z), f3(d.x, d.y, d.z), hit);
-  lrt_hit o;
-  o.t = hit.t;
-  o.primId = (hit.prim != kMiss && (hit.geom >> 24) == LRT_TYPE_MESH_TRIANGLE) ? s.prim_indices[hit.prim] : hit.prim;
-  o.instId = hit.prim == kMiss ? kMiss : 0u;
-  o.geomId = hit.geom;
-  o.coords[0] = hit.c0;
-  o.coords[1] = hit.c1;
-  o.coords[2] = hit.c2;
-  o.coords[3] = hit.c3;
-  out[i] = o;
-}
-
 }  // namespace dev
 
 template <int TYPE, bool COUNT, int MODE, int STACK>
@@ -300,6 +277,7 @@ cudaError_t launch_query(const DevScene &s, const float4 *pos_near, const float4
 // itself to a kernel (on the host it is only a stand-in); the device address
 // is looked up once per device with cudaGetSymbolAddress, with that device
 // current, on the first call on that device.
+#include <cstring>
 #include <mutex>
 
 namespace lrt {
@@ -324,6 +302,23 @@ cudaError_t noalloc_scratch(int device, unsigned char **out) {
   *out = static_cast<unsigned char *>(g_noalloc_addr[device]);
   return cudaSuccess;
 }
+
+// The view table travels as a kernel argument (10 KB, inside the 32 KB argument
+// limit) and this kernel writes it into the scratch array and clears the queue
+// head: no host buffer has to outlive the call, pageable or not.
+struct NoAllocViews {
+  DevView v[LRT_NOALLOC_MAX_VIEWS];
+};
+static_assert(sizeof(NoAllocViews) <= 30000, "view table must fit the kernel argument space");
+
+__global__ void __launch_bounds__(256) noalloc_setup_kernel(const __grid_constant__ NoAllocViews tab, uint32_t n_views,
+                                                            DevView *views, uint32_t *head) {
+  const uint32_t words = n_views * uint32_t(sizeof(DevView) / sizeof(uint32_t));
+  const uint32_t *src = reinterpret_cast<const uint32_t *>(tab.v);
+  uint32_t *dst = reinterpret_cast<uint32_t *>(views);
+  for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
+  if (threadIdx.x == 0) *head = 0u;
+}
 }  // namespace
 
 cudaError_t launch_render_noalloc(const DevScene &s, const DevView *host_views, uint32_t n_views,
@@ -336,10 +331,11 @@ cudaError_t launch_render_noalloc(const DevScene &s, const DevView *host_views, 
   uint32_t *head = reinterpret_cast<uint32_t *>(scratch);
   DevView *views = reinterpret_cast<DevView *>(scratch + kNoAllocViewOffset);
   // The array keeps the previous call's contents: the view table is rewritten and
-  // the queue head cleared on every call.
-  e = cudaMemcpyAsync(views, host_views, n_views * sizeof(DevView), cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) return e;
-  e = cudaMemsetAsync(head, 0, sizeof(uint32_t), st);
+  // the queue head cleared on every call, by a kernel on the caller's stream.
+  NoAllocViews tab;
+  std::memcpy(tab.v, host_views, n_views * sizeof(DevView));
+  noalloc_setup_kernel<<<1, 256, 0, st>>>(tab, n_views, views, head);
+  e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   RenderLaunch L;
   L.views = views;

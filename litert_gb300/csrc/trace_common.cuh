@@ -58,6 +58,20 @@ __device__ __forceinline__ float3 safe_inverse(float3 d) {
 __device__ __forceinline__ float fmn(float a, float b) { return fminf(a, b); }
 __device__ __forceinline__ float fmx(float a, float b) { return fmaxf(a, b); }
 
+// rand3 / rand2, Renderer/eye_ray.cpp:53-80 (the pcg3d hash of JCGT 2020 on the pixel
+// and sample index; `seed` is MultiRenderer::m_seed)
+__device__ __forceinline__ float2 rand2(uint32_t x, uint32_t y, uint32_t iter, uint32_t seed) {
+  x = x + 1233u * (iter + seed) % 171u;
+  y = y + 453u * (iter + seed) % 765u;
+  uint32_t v0 = x, v1 = y, v2 = x ^ y;
+  v0 = v0 * 1664525u + 1013904223u; v1 = v1 * 1664525u + 1013904223u; v2 = v2 * 1664525u + 1013904223u;
+  v0 += v1 * v2; v1 += v2 * v0; v2 += v0 * v1;
+  v0 ^= v0 >> 16u; v1 ^= v1 >> 16u; v2 ^= v2 >> 16u;
+  v0 += v1 * v2; v1 += v2 * v0; v2 += v0 * v1;
+  const float k = 1.0f / float(0xffffffffu);
+  return make_float2(__uint2float_rn(v0) * k, __uint2float_rn(v1) * k);
+}
+
 // RayBoxIntersection2, raytrace_common.h:69-82
 __device__ __forceinline__ float2 ray_box(float3 o, float3 inv, float lox, float loy, float loz, float hix,
                                           float hiy, float hiz) {

@@ -10,10 +10,66 @@ template <bool COUNT, int STACK>
 __device__ __forceinline__ void visit_node(const DevScene &s, uint32_t ref, float3 rp, float3 inv, float tNear,
                                            float hit_t, uint2 *st, int &sp, Counters &cnt);
 
+constexpr int kRefStack = 80;   // BVH2TraverseF32's stack, BVH/BVH2Common.cpp:3412
+
+// BVH2TraverseF32 (BVH/BVH2Common.cpp:3407-3488) on the reference's fat-pair
+// layout: both children of a pair are slab-tested, the nearer entered child is
+// walked first and the other pushed, and the walk stops after the first SDF leaf
+// that reports a hit (:3402-3405, :3478) -- the reference's result, which depends
+// on the tree's topology.  SBS / SVS leaves only (their payload is the brick or
+// voxel index).  The host checks that the tree is acyclic, that every index lies
+// inside the pair and brick arrays and that no path needs more than kRefStack
+// entries before it uploads the pairs, so neither bound below ever binds.
+template <int TYPE, bool COUNT, int MODE, int FEAT>
+__device__ void walk_bvh2(const DevScene &s, float3 rp, float3 rd, float3 inv, float tNear, float tNearSdf,
+                          Hit &hit, Counters &cnt) {
+  uint32_t stack[kRefStack];
+  int top = 0;
+  uint32_t left = 0;
+  bool found = false;
+  uint32_t visits = 0;
+  while (top >= 0 && !found) {
+    while (top >= 0 && (left & kLeafBit) == 0) {
+      if (++visits > s.n_pairs) return;
+      if (COUNT) cnt.nodes++;
+      const float4 a0 = __ldg(&s.pairs[4 * left + 0]), a1 = __ldg(&s.pairs[4 * left + 1]);
+      const float4 b0 = __ldg(&s.pairs[4 * left + 2]), b1 = __ldg(&s.pairs[4 * left + 3]);
+      const uint32_t n0 = __float_as_uint(a0.w), n1 = __float_as_uint(b0.w);
+      const float2 tm0 = ray_box(rp, inv, a0.x, a0.y, a0.z, a1.x, a1.y, a1.z);
+      const float2 tm1 = ray_box(rp, inv, b0.x, b0.y, b0.z, b1.x, b1.y, b1.z);
+      const bool h0 = (tm0.x <= tm0.y) && (tm0.y >= tNear) && (tm0.x <= hit.t);
+      const bool h1 = (tm1.x <= tm1.y) && (tm1.y >= tNear) && (tm1.x <= hit.t);
+      left = h0 ? n0 : n1;
+      if (h0 && h1) {
+        left = (tm0.x <= tm1.x) ? n0 : n1;
+        if (top >= kRefStack) return;
+        stack[top] = (tm0.x <= tm1.x) ? n1 : n0;
+        top++;
+      }
+      if (!h0 && !h1) {
+        top--;
+        left = stack[top > 0 ? top : 0];
+      }
+    }
+    if (top >= 0 && left != 0xFFFFFFFFu) {
+      const float t_before = hit.t;
+      const uint32_t prim = left & 0x00FFFFFFu;   // EXTRACT_START
+      if (TYPE == LRT_TYPE_SDF_SVS)
+        svs_intersect<COUNT, MODE>(s, rp, rd, tNearSdf, prim, hit, cnt);
+      else
+        brick_intersect<COUNT, false, MODE, FEAT>(s, rp, rd, inv, tNearSdf, prim, hit, cnt);
+      found = hit.t < t_before;
+    }
+    top--;
+    left = stack[top > 0 ? top : 0];
+  }
+}
+
 // RayQuery_NearestHit (BVH/BVH2Common.cpp:3490-3559) over the 4-wide BVH.
 // stopOnFirstHit (tFar <= 0) returns the first hit found (RayQuery_AnyHit).
 // SBS brick colours are added by the caller (hit_colour) unless FEAT bit 1 has
-// them computed in the leaf loop.
+// them computed in the leaf loop.  FEAT bit 2: the reference's BVH2 walk with
+// its first-hit early-out (walk_bvh2) instead of the closest-hit 4-wide walk.
 template <int TYPE, bool COUNT, int MODE = -1, int STACK = kStackSize, int FEAT = 0>
 __device__ void trace(const DevScene &s, float3 pos, float tNear, float3 dir, float tFar, Hit &hit, Counters &cnt) {
   const bool stop_first = (tFar <= 0.0f);
@@ -33,6 +89,10 @@ __device__ void trace(const DevScene &s, float3 pos, float tNear, float3 dir, fl
   const float3 rd = matmul3x3(s.inst_inv, dir);
   const float3 inv = safe_inverse(rd);
   const float tNearSdf = mx(tNear, 0.1f);   // SDF bias passed to every leaf type (:3472-3476)
+  if (FEAT & 4) {   // the reference's first-hit walk over its BVH2 layout
+    walk_bvh2<TYPE, COUNT, MODE, FEAT & 3>(s, rp, rd, inv, tNear, tNearSdf, hit, cnt);
+    return;
+  }
 
   // per-ray stack of (node ref, entry distance as float bits), one 8-byte entry each
   uint2 st[STACK];

@@ -131,6 +131,11 @@ def lib():
             "lrt_render_graph_launch": (I, [P, P, VP]),
             "lrt_render_graph_set_views": (I, [P, P, VP, U32]),
             "lrt_render_graph_destroy": (None, [P]),
+            "lrt_set_seed": (I, [P, U32]),
+            "lrt_set_bvh2": (I, [P, VP, U32]),
+            "lrt_update_instance": (I, [P, U32, VP]),
+            "lrt_update_geom_triangles": (I, [P, U32, VP, C.c_size_t, VP, C.c_size_t, C.c_size_t]),
+            "lrt_add_aabb": (I, [P, U32, VP, C.c_size_t, C.POINTER(U32)]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -380,9 +385,41 @@ class Scene:
     def commit_scene(self):
         self._chk(lib().lrt_commit_scene(self._ctx))
 
+    def update_instance(self, inst_id, matrix):
+        """BVHRT::UpdateInstance: a new matrix for a committed instance."""
+        m = np.ascontiguousarray(matrix, np.float32).reshape(16)
+        self._chk(lib().lrt_update_instance(self._ctx, inst_id, _ptr(m)))
+
+    def update_geom_triangles(self, geom_id, vpos, indices=None):
+        """BVHRT::UpdateGeom_Triangles3f: new positions for the committed mesh (same connectivity)."""
+        vpos = np.ascontiguousarray(vpos, np.float32)
+        idx = None if indices is None else np.ascontiguousarray(indices, np.uint32).reshape(-1)
+        self._chk(lib().lrt_update_geom_triangles(self._ctx, geom_id, _ptr(vpos), vpos.shape[0], _ptr(idx),
+                                                  0 if idx is None else idx.size, vpos.shape[1] * 4))
+
+    def add_aabb(self, boxes8, type_id=0):
+        """BVHRT::AddGeom_AABB: refused (no intersector for custom boxes on this path)."""
+        b = np.ascontiguousarray(boxes8, np.float32).reshape(-1, 8)
+        gid = C.c_uint32()
+        self._chk(lib().lrt_add_aabb(self._ctx, type_id, _ptr(b), b.shape[0], C.byref(gid)))
+        return gid.value
+
+    def set_seed(self, seed):
+        """MultiRenderer::setSeed: seed of RAY_GEN_MODE_RANDOM's sub-pixel offsets."""
+        self._chk(lib().lrt_set_seed(self._ctx, int(seed) & 0xFFFFFFFF))
+
+    def set_bvh2(self, pairs):
+        """The BVH2 (reference fat-pair layout, BVH_PAIR_DTYPE or 64-byte records) of the
+        first-hit walk ("first_hit" tuning)."""
+        p = np.ascontiguousarray(pairs)
+        assert p.nbytes % 64 == 0
+        self._chk(lib().lrt_set_bvh2(self._ctx, _ptr(p), p.nbytes // 64))
+
     def set_preset(self, render_mode=None, sdf_node_intersect=None, spp=None, representation_mode=None,
-                   normal_mode=None):
+                   normal_mode=None, ray_gen_mode=None):
         p = self.preset
+        if ray_gen_mode is not None:
+            p.ray_gen_mode = ray_gen_mode
         if render_mode is not None:
             p.render_mode = render_mode
         if normal_mode is not None:

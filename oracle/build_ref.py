@@ -15,6 +15,8 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+# The reference tree: LRT_REFERENCE_TREE, else the checkout this recipe was written
+# against.  This recipe is the only file that locates it; tests ask it.
 REF = os.environ.get("LRT_REFERENCE_TREE", "/root/reference")
 OUT = os.path.join(HERE, "_ref")
 LIB = os.path.join(OUT, "libref_bvh.so")

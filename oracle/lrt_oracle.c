@@ -717,6 +717,20 @@ void orc_shade(const orc_scene *s, const orc_hit *hit, const float pos_near[4], 
   }
 }
 
+/* rand3 / rand2, Renderer/eye_ray.cpp:53-80 */
+void orc_rand2(uint32_t x, uint32_t y, uint32_t iter, uint32_t seed, float *rx, float *ry) {
+  x = x + 1233u * (iter + seed) % 171u;
+  y = y + 453u * (iter + seed) % 765u;
+  uint32_t v0 = x, v1 = y, v2 = x ^ y;
+  v0 = v0 * 1664525u + 1013904223u; v1 = v1 * 1664525u + 1013904223u; v2 = v2 * 1664525u + 1013904223u;
+  v0 += v1 * v2; v1 += v2 * v0; v2 += v0 * v1;
+  v0 ^= v0 >> 16u; v1 ^= v1 >> 16u; v2 ^= v2 >> 16u;
+  v0 += v1 * v2; v1 += v2 * v0; v2 += v0 * v1;
+  const float k = 1.0f / (float)0xffffffffu;
+  *rx = (float)v0 * k;
+  *ry = (float)v1 * k;
+}
+
 static orc_counters render_impl(const orc_scene *s, uint32_t w, uint32_t h, const float proj_inv[16],
                                 const float wv_inv[16], const uint32_t *pix, uint32_t n_pix,
                                 orc_hit *hits, float *rgba, int threads) {
@@ -739,7 +753,9 @@ static orc_counters render_impl(const orc_scene *s, uint32_t w, uint32_t h, cons
     float acc[4] = {0, 0, 0, 0};
     orc_hit first;
     for (uint32_t sidx = 0; sidx < spp; sidx++) {
+      /* CastRaySingle's sub-pixel offset, Renderer/eye_ray.cpp:100-107 */
       float dx = i_spp_sqrt * (float)(sidx / spp_sqrt + 0.5), dy = i_spp_sqrt * (float)(sidx % spp_sqrt + 0.5);
+      if (s->preset.ray_gen_mode == 1) orc_rand2(x, y, sidx + s->seed % 2u, s->seed, &dx, &dy);
       float pn[4], df[4], col[4];
       orc_eye_ray(x, y, w, h, dx, dy, proj_inv, wv_inv, pn, df);
       orc_hit hh = orc_ray_query_nearest(s, pn, df, &c);

@@ -65,7 +65,11 @@ typedef struct {
   float inst_inv[16], inst_inv_t[16];
   orc_preset preset;
   int closest_hit;                  /* 0: reference first-hit early-out; 1: true closest hit */
+  uint32_t seed;                    /* MultiRenderer::m_seed (RAY_GEN_MODE_RANDOM) */
 } orc_scene;
+
+/* rand3 / rand2 of MultiRenderer, Renderer/eye_ray.cpp:53-80 */
+void orc_rand2(uint32_t x, uint32_t y, uint32_t iter, uint32_t seed, float *rx, float *ry);
 
 typedef struct { uint64_t n_fat, n_leaf, n_vox, n_vox_loaded, n_finder, n_tri; } orc_counters;
 

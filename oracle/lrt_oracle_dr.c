@@ -84,18 +84,9 @@ void orc_dr_query(const orc_dr_scene *s, const float *params, uint32_t flags, co
 
 /* ---------------- pixel glue, diff_render/MultiRendererDR.cpp ---------------- */
 
-/* rand3 / rand2, Renderer/eye_ray.cpp:53-80 */
+/* rand3 / rand2, Renderer/eye_ray.cpp:53-80 (lrt_oracle.c) */
 static void rand2(uint32_t x, uint32_t y, uint32_t iter, uint32_t seed, float *rx, float *ry) {
-  x = x + 1233u * (iter + seed) % 171u;
-  y = y + 453u * (iter + seed) % 765u;
-  uint32_t v0 = x, v1 = y, v2 = x ^ y;
-  v0 = v0 * 1664525u + 1013904223u; v1 = v1 * 1664525u + 1013904223u; v2 = v2 * 1664525u + 1013904223u;
-  v0 += v1 * v2; v1 += v2 * v0; v2 += v0 * v1;
-  v0 ^= v0 >> 16u; v1 ^= v1 >> 16u; v2 ^= v2 >> 16u;
-  v0 += v1 * v2; v1 += v2 * v0; v2 += v0 * v1;
-  const float k = 1.0f / (float)0xffffffffu;
-  *rx = (float)v0 * k;
-  *ry = (float)v1 * k;
+  orc_rand2(x, y, iter, seed, rx, ry);
 }
 
 static const float Z_NEAR = 0.1f, Z_FAR = 10.0f;   /* diff_render/MultiRendererDR.cpp:25-26 */

@@ -36,7 +36,7 @@ class OrcScene(C.Structure):
                 ("pairs", VP), ("n_pairs", C.c_uint32), ("tri_indices_orig", VP),
                 ("inst_bmin", C.c_float * 3), ("inst_bmax", C.c_float * 3),
                 ("inst_inv", C.c_float * 16), ("inst_inv_t", C.c_float * 16), ("preset", Preset),
-                ("closest_hit", C.c_int)]
+                ("closest_hit", C.c_int), ("seed", C.c_uint32)]
 
 
 class Counters(C.Structure):
@@ -156,7 +156,7 @@ class Scene:
     """One geometry + identity-or-given instance, as the oracle sees it."""
 
     def __init__(self, kind, *, sbs=None, svs=None, mesh=None, pairs=None, matrix=None, closest_hit=True,
-                 render_mode=1, intersect=2, representation_mode=1, spp=1, normal_mode=0):
+                 render_mode=1, intersect=2, representation_mode=1, spp=1, normal_mode=0, ray_gen_mode=0, seed=0):
         self.keep = []
         s = OrcScene()
         m = np.eye(4, dtype=np.float32) if matrix is None else np.asarray(matrix, np.float32)
@@ -221,8 +221,9 @@ class Scene:
         tc = corners @ m.T
         s.inst_bmin[:] = tc[:, :3].min(0).tolist()
         s.inst_bmax[:] = tc[:, :3].max(0).tolist()
-        s.preset = Preset(render_mode, intersect, normal_mode, 0, 0, representation_mode, spp)
+        s.preset = Preset(render_mode, intersect, normal_mode, ray_gen_mode, 0, representation_mode, spp)
         s.closest_hit = 1 if closest_hit else 0
+        s.seed = seed & 0xFFFFFFFF
         self.s = s
 
     def render(self, w, h, proj_inv, wv_inv, hits=True, rgba=False, threads=0):

@@ -16,7 +16,7 @@ import pytest
 from litert_gb300 import lrt, scenes
 from oracle import oracle as orc
 
-REF_TREE = os.environ.get("LRT_REFERENCE_TREE", "/root/reference")
+from oracle.build_ref import REF as REF_TREE   # the one place that locates the reference tree
 
 
 def _sbs():
