@@ -522,7 +522,7 @@ extern "C" lrt_status lrt_set_tuning(lrt_ctx *ctx, const char *key, int value) {
   if (!ctx || !key) return LRT_ERR_INVALID;
   const std::string k(key);
   if (k == "variant") {
-    if (value < 0 || value > 2) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: variant is 0, 1 or 2");
+    if (value < 0 || value > 3) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: variant is 0, 1, 2 or 3");
     ctx->tuning.variant = value;
   } else if (k == "block_warps") {
     if (value < 1 || value > 8) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: block_warps in 1..8");

@@ -177,6 +177,11 @@ inline int render_features(const DevScene &s) {
 // The variant-0 render kernel compiled with FP contraction (trace_fused.cu).
 cudaError_t launch_render_fused(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st,
                                 const Tuning &tu);
+// Variant 3: the block-regrouped SBS kernel (render_lq.cuh), uncontracted (trace.cu)
+// and contracted (trace_fused.cu).
+cudaError_t launch_render_lq(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st, const Tuning &tu);
+cudaError_t launch_render_lq_fused(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st,
+                                   const Tuning &tu);
 // Warp-packet SBS render kernel (trace_pkt.cu).
 cudaError_t launch_render_packet(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st, bool count,
                                  const Tuning &tu);

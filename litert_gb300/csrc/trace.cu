@@ -10,6 +10,7 @@
 // and the reference's slab arithmetic exactly, internal boxes enclose their leaf
 // boxes, so culling never removes a leaf the reference would have entered.
 #include "render_kernel.cuh"
+#include "render_lq.cuh"
 
 namespace lrt {
 namespace dev {
@@ -215,6 +216,33 @@ static cudaError_t launch_phong_t(const DevScene &s, const RenderLaunch &L, int 
   return launch_feature_t<TYPE, true, 0>(s, L, num_sms, st);
 }
 
+template <int MODE, int STACK>
+static cudaError_t launch_lq_m0(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st) {
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::render_lq_kernel<MODE, STACK, 0>,
+                                                                dev::kLqThreads, 0);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  uint32_t blocks = uint32_t(num_sms) * uint32_t(per_sm);
+  const uint32_t max_blocks = (L.total_tiles + 3) / 4;
+  if (blocks > max_blocks) blocks = max_blocks;
+  if (blocks == 0) blocks = 1;
+  dev::render_lq_kernel<MODE, STACK, 0><<<blocks, dev::kLqThreads, 0, st>>>(s, L);
+  return cudaGetLastError();
+}
+
+// variant 3: traversal and leaf phases regrouped across the block (render_lq.cuh)
+cudaError_t launch_render_lq(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st,
+                              const Tuning &tu) {
+  switch (s.preset.sdf_node_intersect) {
+    case LRT_INTERSECT_NEWTON:
+      if (tu.stack == 32) return launch_lq_m0<LRT_INTERSECT_NEWTON, 32>(s, L, num_sms, st);
+      return launch_lq_m0<LRT_INTERSECT_NEWTON, kStackSize>(s, L, num_sms, st);
+    case LRT_INTERSECT_ST: return launch_lq_m0<LRT_INTERSECT_ST, kStackSize>(s, L, num_sms, st);
+    default: return launch_lq_m0<-1, kStackSize>(s, L, num_sms, st);
+  }
+}
+
 cudaError_t launch_render(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st, bool count,
                           const Tuning &tu) {
   const uint32_t rm = s.preset.render_mode;
@@ -239,6 +267,8 @@ cudaError_t launch_render(const DevScene &s, const RenderLaunch &L, int num_sms,
                           (s.type == LRT_TYPE_SDF_SBS && s.preset.sdf_node_intersect == LRT_INTERSECT_NEWTON)) &&
                          s.preset.spp <= 1 && !count && uint64_t(L.total_tiles) * 32u < (1ull << 31);
   if (tu.variant == 2 && refill_ok) return launch_refill(s, L, num_sms, st, tu);
+  if (tu.variant == 3 && sbs && render_features(s) == 0 && s.preset.spp <= 1 && !count)
+    return tu.fma ? launch_render_lq_fused(s, L, num_sms, st, tu) : launch_render_lq(s, L, num_sms, st, tu);
   // contraction only for the SDF leaves: in the triangle test it would open cracks along shared edges
   if (tu.fma && !count && tu.variant != 1 && s.type != LRT_TYPE_MESH_TRIANGLE)
     return launch_render_fused(s, L, num_sms, st, tu);

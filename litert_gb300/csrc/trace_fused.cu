@@ -9,6 +9,7 @@
 // a ray through the crack between two triangles); spp loop, outputs and work
 // distribution are those of trace.cu's instantiations.
 #include "render_kernel.cuh"
+#include "render_lq.cuh"
 
 namespace lrt {
 
@@ -37,6 +38,33 @@ static cudaError_t launch_fused_t(const DevScene &s, const RenderLaunch &L, int 
       return launch_fused_m<TYPE, LRT_INTERSECT_NEWTON, kStackSize>(s, L, num_sms, st);
     case LRT_INTERSECT_ST: return launch_fused_m<TYPE, LRT_INTERSECT_ST, kStackSize>(s, L, num_sms, st);
     default: return launch_fused_m<TYPE, -1, kStackSize>(s, L, num_sms, st);
+  }
+}
+
+template <int MODE, int STACK>
+static cudaError_t launch_lq_m1(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st) {
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::render_lq_kernel<MODE, STACK, 1>,
+                                                                dev::kLqThreads, 0);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  uint32_t blocks = uint32_t(num_sms) * uint32_t(per_sm);
+  const uint32_t max_blocks = (L.total_tiles + 3) / 4;
+  if (blocks > max_blocks) blocks = max_blocks;
+  if (blocks == 0) blocks = 1;
+  dev::render_lq_kernel<MODE, STACK, 1><<<blocks, dev::kLqThreads, 0, st>>>(s, L);
+  return cudaGetLastError();
+}
+
+// variant 3: traversal and leaf phases regrouped across the block (render_lq.cuh)
+cudaError_t launch_render_lq_fused(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st,
+                              const Tuning &tu) {
+  switch (s.preset.sdf_node_intersect) {
+    case LRT_INTERSECT_NEWTON:
+      if (tu.stack == 32) return launch_lq_m1<LRT_INTERSECT_NEWTON, 32>(s, L, num_sms, st);
+      return launch_lq_m1<LRT_INTERSECT_NEWTON, kStackSize>(s, L, num_sms, st);
+    case LRT_INTERSECT_ST: return launch_lq_m1<LRT_INTERSECT_ST, kStackSize>(s, L, num_sms, st);
+    default: return launch_lq_m1<-1, kStackSize>(s, L, num_sms, st);
   }
 }
 

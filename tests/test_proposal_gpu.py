@@ -163,3 +163,22 @@ def test_trained_network_skips_voxel_steps(union_scene):
         assert np.array_equal(got, plain)
     assert res[True]["steps_skipped"] > 1.2 * res[False]["steps_skipped"] + 1000, res
     assert res[True]["steps_skipped"] >= res[True]["jumps"]
+
+
+def test_tcgen05_matches_mma_on_collected_triples(union_scene):
+    """Both tensor-core engines round at the same points (products summed from zero
+    in the tensor core, bias added after in FP32, ReLU, BF16): on triples collected
+    from plain renders and a trained network their outputs agree to 1e-3 of the
+    output range."""
+    pp.set_weights(union_scene, pp.init_weights(7))
+    pp.clear(union_scene)
+    n = pp.collect(union_scene, scenes.union_views(n_views=6, lo=192, hi=320, cam_seed=6), capacity=2_000_000)
+    assert n > 50000
+    pp.train(union_scene, 600, batch=4096, lr=1e-3, seed=7)
+    y_mma = pp.infer(union_scene, 0, n, engine=pp.ENGINE_MMA)
+    y_tc = pp.infer(union_scene, 0, n, engine=pp.ENGINE_TCGEN05)
+    rng = float(y_mma.max() - y_mma.min())
+    d = np.abs(y_tc - y_mma)
+    print(f"{n} triples: max |tcgen05 - mma.sync| = {d.max():.3e} ({d.max() / rng:.3e} of the range), "
+          f"{int((d > 0).sum())} outputs differ")
+    assert d.max() <= 1e-3 * rng

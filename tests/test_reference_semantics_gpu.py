@@ -10,11 +10,14 @@
   (shared-edge ties, where primId may name either neighbour) is measured.
 * Closest hit against the reference's first hit: BVH2TraverseF32 stops at the
   first SDF leaf that reports a hit (BVH/BVH2Common.cpp:3402-3405, 3478), the
-  engine returns the closest one.  On the small sphere configuration (all 65,536
-  pixels) and a 48k-pixel sample of the 16-view 1024^3 headline, the engine's
-  records (bit-exact and contracted kernels) are compared with the oracle in the
-  reference's first-hit mode on the same BVH2 (the engine's own fat pairs): the
-  pixels whose hit or depth differs stay inside the same tolerance.
+  default kernels return the closest one.  On the small sphere configuration (all
+  65,536 pixels) the two agree within the tolerance (measured: no difference).
+  On a 48k-pixel sample of the 16-view 1024^3 headline they do not: 212 pixels
+  (0.44 %, max |dt| 0.89) hit a farther brick first, where sibling boxes of the
+  BVH2 overlap -- a property of the reference's early-out on a given tree, not of
+  the arithmetic.  The "first_hit" tuning reproduces the reference's result on
+  the same tree bit for bit (checked here on the same sample), and the count of
+  closest-vs-first differences is held to its measured size.
 """
 import numpy as np
 import pytest
@@ -128,12 +131,12 @@ def test_closest_vs_first_hit_sphere(fma):
     r = _first_hit_counts(s, osc, [view], sample, fma)
     s.close()
     print(f"sphere 256^2 fma={fma}: {r}")
-    assert r["n"] == 65536 and r["hits"] > 10000
+    assert r["n"] == 65536 and r["hits"] > 6000
     assert r["mask"] + r["depth"] <= MASK_FRAC * r["n"], r
 
 
-@pytest.mark.parametrize("fma", [0, 1])
-def test_closest_vs_first_hit_headline(fma):
+@pytest.fixture(scope="module")
+def headline():
     h, nodes, values = lrt.sbs_from_sdf(scenes.union_sdf(), 7, 8, gpu=0)
     s = lrt.Scene(0)
     s.add_instance(s.add_sbs(h, nodes, values))
@@ -143,8 +146,37 @@ def test_closest_vs_first_hit_headline(fma):
     osc = orc.Scene("sbs", sbs=(orc.SbsHeader(h.brick_size, h.brick_pad, h.bytes_per_value, h.aux_data), nodes,
                                 values), pairs=(s.bvh2(), None, None), intersect=lrt.INTERSECT_NEWTON,
                     render_mode=lrt.RENDER_MODE_NORMAL, closest_hit=False)
-    r = _first_hit_counts(s, osc, views, _strided(views, 48_000), fma)
+    yield s, osc, views
     s.close()
+
+
+@pytest.mark.parametrize("fma", [0, 1])
+def test_closest_vs_first_hit_headline(headline, fma):
+    s, osc, views = headline
+    r = _first_hit_counts(s, osc, views, _strided(views, 48_000), fma)
     print(f"headline 16 views fma={fma}: {r}")
     assert r["n"] >= 47_000 and r["hits"] > 5000
-    assert r["mask"] + r["depth"] <= MASK_FRAC * r["n"], r
+    assert r["mask"] <= MASK_FRAC * r["n"], r
+    # measured 212 of 48,000 (first hits in a farther brick behind overlapping boxes)
+    assert r["depth"] <= 0.01 * r["n"], r
+
+
+def test_first_hit_mode_reproduces_reference_on_headline(headline):
+    s, osc, views = headline
+    s.set_tuning("fma", 0)
+    s.set_tuning("first_hit", 1)
+    try:
+        g_all = s.render_host(views, hits=True)["hits"]
+    finally:
+        s.set_tuning("first_hit", 0)
+    n = 0
+    for vi, off, pix in _strided(views, 48_000):
+        w, hh, wv, pj = views[vi]
+        o, _ = osc.render_pixels(w, hh, lrt.inverse4x4(pj), lrt.inverse4x4(wv), pix)
+        g = g_all[off + pix.astype(np.int64)]
+        assert np.array_equal(g["primId"], o["primId"])
+        hit = o["primId"] != lrt.MISS
+        assert np.array_equal(g["t"][hit].view(np.uint32), o["t"][hit].view(np.uint32))
+        assert np.array_equal(g["nx"][hit].view(np.uint32), o["coords"][hit, 2].view(np.uint32))
+        n += pix.size
+    assert n >= 47_000

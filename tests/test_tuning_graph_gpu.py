@@ -33,7 +33,8 @@ def _render(s, views):
 
 
 @pytest.mark.parametrize("tile_w,stack,variant", [(4, 64, 0), (16, 64, 0), (32, 64, 0), (8, 32, 0), (8, 64, 1),
-                                                  (16, 32, 0), (8, 64, 2), (4, 32, 2), (16, 64, 2)])
+                                                  (16, 32, 0), (8, 64, 2), (4, 32, 2), (16, 64, 2), (8, 64, 3),
+                                                  (4, 64, 3), (8, 32, 3), (32, 64, 3)])
 def test_launch_shapes_bit_identical(scene, tile_w, stack, variant):
     views = _views()
     ref = _render(scene, views)
@@ -136,3 +137,20 @@ def test_render_into_page_locked_host_memory(scene, fma):
         assert np.array_equal(rgba8.numpy().view(np.uint32), ref["rgba8"])
     finally:
         scene.set_tuning("fma", 0)
+
+
+@pytest.mark.parametrize("mode", [lrt.RENDER_MODE_LAMBERT_NO_TEX, lrt.RENDER_MODE_DEPTH])
+def test_regrouped_variant_colours_and_rgba8(scene, mode):
+    """Variant 3 (traversal and leaf phases regrouped across the block) gives the
+    per-lane kernel's records, float colours and packed RGBA8 bit for bit."""
+    views = _views()
+    scene.set_preset(render_mode=mode)
+    try:
+        ref = scene.render_host(views, hits=True, rgba=True, rgba8=True)
+        scene.set_tuning("variant", 3)
+        got = scene.render_host(views, hits=True, rgba=True, rgba8=True)
+    finally:
+        scene.set_tuning("variant", 0)
+        scene.set_preset(render_mode=lrt.RENDER_MODE_NORMAL)
+    for k in ("hits", "rgba", "rgba8"):
+        assert np.array_equal(np.ascontiguousarray(got[k]).view(np.uint32), np.ascontiguousarray(ref[k]).view(np.uint32)), k
