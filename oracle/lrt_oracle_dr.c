@@ -560,6 +560,32 @@ static int nthreads(int threads) {
 #endif
 }
 
+/* The reference's pixel order: SuperBlockIndex2DOpt / kernel_PackXY
+ * (Renderer/eye_ray.cpp:524-570) over the size padded to PACK_XY_BLOCK_SIZE (8):
+ * 4x4 blocks inside 2x2 super-blocks.  RenderDR walks tidX = 0, 1, ... through
+ * this table; out[] receives the row-major indices of the in-image entries in
+ * that order (all W*H pixels; the reference's loop bound W*H leaves some out
+ * when W or H is not a multiple of 8, which is rendered fully here). */
+static uint32_t packed_order(uint32_t W, uint32_t H, uint32_t *out) {
+  const uint32_t W8 = 8 * ((W + 7) / 8), H8 = 8 * ((H + 7) / 8);
+  uint32_t *tab = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)W8 * H8);
+  for (uint32_t y = 0; y < H8; y++)
+    for (uint32_t x = 0; x < W8; x++) {
+      const uint32_t inBlockIdX = x & 3u, inBlockIdY = y & 3u, localIndex = inBlockIdY * 4 + inBlockIdX;
+      const uint32_t wBlocks = W8 >> 2, blockX = x >> 2, blockY = y >> 2;
+      const uint32_t inHBlockIdX = blockX & 1u, inHBlockIdY = blockY & 1u, localIndexH = inHBlockIdY * 2 + inHBlockIdX;
+      const uint32_t wBlocksH = wBlocks >> 1, blockHX = blockX >> 1, blockHY = blockY >> 1;
+      tab[(blockHX + blockHY * wBlocksH) * 64 + localIndexH * 16 + localIndex] = (y << 16) | x;
+    }
+  uint32_t n = 0;
+  for (uint32_t i = 0; i < W8 * H8; i++) {
+    const uint32_t x = tab[i] & 0xFFFFu, y = tab[i] >> 16;
+    if (x < W && y < H) out[n++] = y * W + x;
+  }
+  free(tab);
+  return n;
+}
+
 double orc_dr_render(const orc_dr_scene *s, const float *params, const orc_dr_preset *p, const orc_dr_view *v,
                      const float *image_ref, float *out_image, float *out_depth, float *grad,
                      uint8_t *border_mask, int threads) {
@@ -571,16 +597,22 @@ double orc_dr_render(const orc_dr_scene *s, const float *params, const orc_dr_pr
   float *slices = (float *)calloc((size_t)np * T, sizeof(float));
   double *lv = (double *)calloc(T, sizeof(double));
   const uint32_t steps = (N + T - 1) / T;
-  /* I: pixels, split into T contiguous ranges (:596-607) */
+  uint32_t *order = (uint32_t *)malloc(sizeof(uint32_t) * N);
+  packed_order(W, H, order);
+  /* I: pixels in the packed order, split into T contiguous ranges (:596-607) */
 #pragma omp parallel for num_threads(T) schedule(static, 1)
   for (int t = 0; t < T; t++) {
     uint32_t b = t * steps, e = (t + 1) * steps < N ? (t + 1) * steps : N;
-    for (uint32_t i = b; i < e; i++) lv[t] += cast_ray_grad(&r, i % W, i / W, slices + (size_t)np * t);
+    for (uint32_t k = b; k < e; k++) {
+      const uint32_t i = order[k];
+      lv[t] += cast_ray_grad(&r, i % W, i / W, slices + (size_t)np * t);
+    }
   }
-  /* II: border pixels (:609-685) */
+  /* II: border pixels, listed in the packed order (:609-685) */
   uint32_t *border = (uint32_t *)malloc(sizeof(uint32_t) * N);
   uint32_t nb = 0;
-  for (uint32_t i = 0; i < N; i++) {
+  for (uint32_t k = 0; k < N; k++) {
+    const uint32_t i = order[k];
     uint32_t x = i % W, y = i / W;
     float d0 = out_image[4 * (size_t)i + 3], max_diff = 0, max_thr = 0;
     if (x >= 1 && x < W - 1 && y >= 1 && y < H - 1)
@@ -616,7 +648,7 @@ double orc_dr_render(const orc_dr_scene *s, const float *params, const orc_dr_pr
   }
   double loss = 0;
   for (int t = 0; t < T; t++) loss += lv[t];
-  free(slices); free(lv); free(border);
+  free(slices); free(lv); free(border); free(order);
   return loss / (double)N;
 }
 

@@ -148,6 +148,7 @@ static inline float2 floor(float2 a) { return float2(std::floor(a.x), std::floor
 static inline float3 floor(float3 a) { return float3(std::floor(a.x), std::floor(a.y), std::floor(a.z)); }
 static inline float4 floor(float4 a) { return float4(std::floor(a.x), std::floor(a.y), std::floor(a.z), std::floor(a.w)); }
 static inline float3 sign(float3 a) { return float3(sign(a.x), sign(a.y), sign(a.z)); }
+static inline float4 sign(float4 a) { return float4(sign(a.x), sign(a.y), sign(a.z), sign(a.w)); }
 static inline float3 lerp(float3 a, float3 b, float t) { return a + t * (b - a); }
 static inline float4 lerp(float4 a, float4 b, float t) { return a + t * (b - a); }
 static inline float3 mix(float3 a, float3 b, float t) { return a + t * (b - a); }
@@ -178,9 +179,6 @@ static inline float3x3 make_float3x3_by_columns(float3 c0, float3 c1, float3 c2)
   float3x3 m;
   m.row[0] = float3(c0.x, c1.x, c2.x); m.row[1] = float3(c0.y, c1.y, c2.y); m.row[2] = float3(c0.z, c1.z, c2.z);
   return m;
-}
-static inline float3x3 &operator+=(float3x3 &a, const float3x3 &b) {
-  a.row[0] += b.row[0]; a.row[1] += b.row[1]; a.row[2] += b.row[2]; return a;
 }
 
 struct float4x4 {
@@ -223,6 +221,36 @@ static inline float4x4 inverse4x4(const float4x4 &a) {
   }
   float4x4 r;
   for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) r(i, j) = float(t[i][j + 4]);
+  return r;
+}
+// perspectiveMatrix / lookAt with the conventions the engine's camera helpers use
+// (row-major, right-handed view looking down -z, OpenGL depth range)
+static inline float4x4 perspectiveMatrix(float fovy, float aspect, float zNear, float zFar) {
+  float4x4 r;
+  std::memset(r.m, 0, sizeof(r.m));
+  const float ymax = zNear * std::tan(fovy * 3.14159265358979323846f / 180.0f * 0.5f);
+  const float xmax = ymax * aspect;
+  const float left = -xmax, right = xmax, bottom = -ymax, top = ymax;
+  r(0, 0) = 2.0f * zNear / (right - left);
+  r(0, 2) = (right + left) / (right - left);
+  r(1, 1) = 2.0f * zNear / (top - bottom);
+  r(1, 2) = (top + bottom) / (top - bottom);
+  r(2, 2) = (-zFar - zNear) / (zFar - zNear);
+  r(2, 3) = (-2.0f * zNear * zFar) / (zFar - zNear);
+  r(3, 2) = -1.0f;
+  return r;
+}
+static inline float4x4 lookAt(float3 eye, float3 center, float3 up) {
+  float3 z = eye - center;
+  z = z / std::sqrt(dot(z, z));
+  float3 x = cross(up, z);
+  x = x / std::sqrt(dot(x, x));
+  const float3 y = cross(z, x);
+  float4x4 r;
+  r(0, 0) = x.x; r(0, 1) = x.y; r(0, 2) = x.z; r(0, 3) = -(x.x * eye.x + x.y * eye.y + x.z * eye.z);
+  r(1, 0) = y.x; r(1, 1) = y.y; r(1, 2) = y.z; r(1, 3) = -(y.x * eye.x + y.y * eye.y + y.z * eye.z);
+  r(2, 0) = z.x; r(2, 1) = z.y; r(2, 2) = z.z; r(2, 3) = -(z.x * eye.x + z.y * eye.y + z.z * eye.z);
+  r(3, 0) = 0; r(3, 1) = 0; r(3, 2) = 0; r(3, 3) = 1;
   return r;
 }
 static inline float4x4 translate4x4(float3 t) { float4x4 r; r(0, 3) = t.x; r(1, 3) = t.y; r(2, 3) = t.z; return r; }
