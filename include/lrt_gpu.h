@@ -89,7 +89,13 @@ lrt_status lrt_set_preset(lrt_ctx *ctx, const lrt_preset *preset);
  * depends on the tree: the committed BVH's pairs, or the caller's through
  * lrt_set_bvh2.  Triangle meshes have no early-out in the reference and keep
  * the closest hit.  Not used by lrt_render_noalloc, lrt_render_counters or the
- * autotuner). */
+ * autotuner).
+ * "tc_wait" (default 4194304): how many times the tcgen05 network engine polls
+ * a layer's completion barrier before it gives up; a timeout makes
+ * lrt_proposal_infer_ex return LRT_ERR_TIMEOUT after the block has drained its
+ * issued tensor-core work and freed its tensor memory (the next call runs
+ * normally).  0 makes every block give up at its first wait: the failure path,
+ * for tests. */
 lrt_status lrt_set_tuning(lrt_ctx *ctx, const char *key, int value);
 
 /* MultiRenderer::setSeed (Renderer/eye_ray.h:173): the seed of the sub-pixel

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
+#include <cstring>
 #include <string>
 #include <vector>
 
@@ -20,6 +22,17 @@ cudaError_t dispatch_render(struct ::lrt_ctx *ctx, const RenderLaunch &L, cudaSt
 }  // namespace lrt
 
 namespace lrt {
+
+// Host-side fault injection for the failure-path tests: while the environment
+// variable LRT_INJECT_FAULT names a site ("alloc": device buffer allocation,
+// "upload": host-to-device scene upload, "graph": CUDA-graph instantiation), every
+// call through that site fails as the CUDA runtime would (cudaErrorMemoryAllocation
+// / cudaErrorInvalidValue), before any device work.  Read on each call (cold
+// paths only); unset, it costs one getenv.
+inline bool inject_fault(const char *site) {
+  const char *v = std::getenv("LRT_INJECT_FAULT");
+  return v && std::strcmp(v, site) == 0;
+}
 
 struct Geom {
   uint32_t type = 0;
@@ -43,6 +56,7 @@ struct DevBuf {
   size_t cap = 0;  // elements
   cudaError_t ensure(size_t n) {
     if (n <= cap) return cudaSuccess;
+    if (inject_fault("alloc")) return cudaErrorMemoryAllocation;
     if (p) cudaFree(p);
     p = nullptr;
     cap = 0;

@@ -308,6 +308,7 @@ extern "C" lrt_status lrt_add_instance(lrt_ctx *ctx, uint32_t geom_id, const flo
 
 template <typename T>
 static cudaError_t upload(DevBuf<T> &b, const T *src, size_t n) {
+  if (inject_fault("upload")) return cudaErrorInvalidValue;
   cudaError_t e = b.ensure(n);
   if (e != cudaSuccess || n == 0) return e;
   return cudaMemcpy(b.p, src, n * sizeof(T), cudaMemcpyHostToDevice);
@@ -549,6 +550,9 @@ extern "C" lrt_status lrt_set_tuning(lrt_ctx *ctx, const char *key, int value) {
   } else if (k == "first_hit") {
     if (value < 0 || value > 1) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: first_hit is 0 or 1");
     ctx->tuning.first_hit = value;
+  } else if (k == "tc_wait") {
+    if (value < 0) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: tc_wait is a poll count >= 0");
+    ctx->tuning.tc_wait = value;
   } else if (k == "proposal") {
     if (value < 0 || value > 1) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: proposal is 0 or 1");
     ctx->use_proposal = value;
@@ -1133,7 +1137,7 @@ extern "C" lrt_status lrt_render_graph_create(lrt_ctx *ctx, const lrt_view *view
       e = cudaStreamEndCapture(cs, &g->graph);
       if (e == cudaSuccess) e = e2;
     }
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+    if (e == cudaSuccess) e = inject_fault("graph") ? cudaErrorInvalidValue : cudaGraphInstantiate(&g->exec, g->graph, 0);
   }
   if (cs) cudaStreamDestroy(cs);
   if (e != cudaSuccess) {

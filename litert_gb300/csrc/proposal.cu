@@ -395,10 +395,12 @@ __global__ void __launch_bounds__(128) mlp_infer_kernel(TripleView data, MlpStat
 // layer's A operand to shared memory.  A tile's features are staged while the
 // previous tile is still in layers 2-3, and loaded into registers one tile
 // earlier still.  Ten CTAs per SM keep ten chains in flight.  Waits are bounded:
-// a timeout sets status bit 1, the CTA leaves its loop at the next barrier, waits
-// once more (bounded) for its MMAs and frees its TMEM.
+// the per-layer waits poll the commit mbarrier at most `wait_limit` times; a
+// timeout sets status bit 1, the CTA leaves its loop at the next barrier, waits
+// once more (at most kTcWait polls, whatever wait_limit is) for the MMAs it has
+// issued and frees its TMEM.
 constexpr uint32_t kTcLbo = 128;         // adjacent core matrices along K
-constexpr uint32_t kTcWait = 1u << 22;   // mbarrier polls before giving up
+constexpr uint32_t kTcWait = 1u << 22;   // mbarrier polls of the final drain (and the default per-layer limit)
 constexpr int kTcBlocksPerSm = 10;
 
 __device__ __forceinline__ void stage_row16(uint8_t *tile, uint32_t row, uint32_t sbo, const uint4 &lo, const uint4 &hi) {
@@ -436,7 +438,7 @@ __device__ __forceinline__ void load_row16(const TripleView &data, uint64_t gid,
 }
 
 __global__ void __launch_bounds__(128, kTcBlocksPerSm) mlp_infer_tc_kernel(TripleView data, MlpState m, float *out,
-                                                                           unsigned int *status) {
+                                                                           unsigned int *status, uint32_t wait_limit) {
   __shared__ __align__(128) uint8_t sX[128 * kIn * 2];
   __shared__ __align__(128) uint8_t sH[128 * kHid * 2];
   __shared__ __align__(128) uint8_t sW1[kHid * kIn * 2];
@@ -493,7 +495,7 @@ __global__ void __launch_bounds__(128, kTcBlocksPerSm) mlp_infer_tc_kernel(Tripl
     if (tid == 0) {
       tc05::mma_bf16(tbase, tc05::smem_desc(aX, kTcLbo, 256), tc05::smem_desc(aW1, kTcLbo, 256), kId32, false);
       tc05::mma_commit(&mbar);
-      t_ok = tc05::mbar_wait(&mbar, phase, kTcWait);
+      t_ok = tc05::mbar_wait(&mbar, phase, wait_limit);
     }
     phase ^= 1u;
     tc05::fence_before_sync();
@@ -513,7 +515,7 @@ __global__ void __launch_bounds__(128, kTcBlocksPerSm) mlp_infer_tc_kernel(Tripl
       tc05::mma_bf16(tbase, tc05::smem_desc(aH + 2 * kTcLbo, kTcLbo, 512), tc05::smem_desc(aW2 + 2 * kTcLbo, kTcLbo, 512),
                      kId32, true);
       tc05::mma_commit(&mbar);
-      t_ok = tc05::mbar_wait(&mbar, phase, kTcWait);
+      t_ok = tc05::mbar_wait(&mbar, phase, wait_limit);
     }
     phase ^= 1u;
     tc05::fence_before_sync();
@@ -531,7 +533,7 @@ __global__ void __launch_bounds__(128, kTcBlocksPerSm) mlp_infer_tc_kernel(Tripl
       tc05::mma_bf16(tbase, tc05::smem_desc(aH + 2 * kTcLbo, kTcLbo, 512), tc05::smem_desc(aW3 + 2 * kTcLbo, kTcLbo, 512),
                      kId16, true);
       tc05::mma_commit(&mbar);
-      t_ok = tc05::mbar_wait(&mbar, phase, kTcWait);
+      t_ok = tc05::mbar_wait(&mbar, phase, wait_limit);
     }
     phase ^= 1u;
     tc05::fence_before_sync();
@@ -697,7 +699,7 @@ cudaError_t launch_mlp_infer(const TripleView &data, const MlpState &m, float *o
 }
 
 cudaError_t launch_mlp_infer_tc(const TripleView &data, const MlpState &m, float *out, unsigned int *status,
-                                cudaStream_t st) {
+                                cudaStream_t st, uint32_t wait_limit) {
   int device = 0, sms = 0;
   cudaError_t e = cudaGetDevice(&device);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
@@ -706,7 +708,7 @@ cudaError_t launch_mlp_infer_tc(const TripleView &data, const MlpState &m, float
   uint64_t blocks = uint64_t(sms) * dev::kTcBlocksPerSm;
   if (blocks > tiles) blocks = tiles;
   if (blocks == 0) return cudaSuccess;
-  dev::mlp_infer_tc_kernel<<<unsigned(blocks), 128, 0, st>>>(data, m, out, status);
+  dev::mlp_infer_tc_kernel<<<unsigned(blocks), 128, 0, st>>>(data, m, out, status, wait_limit);
   return cudaGetLastError();
 }
 

@@ -294,7 +294,8 @@ extern "C" lrt_status lrt_proposal_infer_ex(lrt_ctx *ctx, uint64_t first, uint64
     if (e == cudaSuccess) e = cudaEventRecord(ev[0], nullptr);
   }
   if (e == cudaSuccess)
-    e = engine == LRT_MLP_ENGINE_TCGEN05 ? lrt::launch_mlp_infer_tc(data, lrt::mlp_state(p, nullptr), d.p, status.p, nullptr)
+    e = engine == LRT_MLP_ENGINE_TCGEN05 ? lrt::launch_mlp_infer_tc(data, lrt::mlp_state(p, nullptr), d.p, status.p, nullptr,
+                                                                   uint32_t(ctx->tuning.tc_wait))
                                          : lrt::launch_mlp_infer(data, lrt::mlp_state(p, nullptr), d.p, nullptr);
   if (e == cudaSuccess && ms) e = cudaEventRecord(ev[1], nullptr);
   if (e == cudaSuccess) e = ms ? cudaEventSynchronize(ev[1]) : cudaStreamSynchronize(nullptr);

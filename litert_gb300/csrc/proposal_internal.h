@@ -38,7 +38,8 @@ cudaError_t launch_mlp_step(const TripleView &data, const MlpState &m, uint32_t 
                             bool random, bool update, float lr, float b1, float b2, float eps, cudaStream_t st);
 cudaError_t launch_mlp_infer(const TripleView &data, const MlpState &m, float *out, cudaStream_t st);
 cudaError_t launch_mlp_infer_tc(const TripleView &data, const MlpState &m, float *out, unsigned int *status,
-                                cudaStream_t st);
+                                cudaStream_t st,
+                                uint32_t wait_limit);
 cudaError_t launch_render_proposal(const DevScene &s, const RenderLaunch &L, const MlpState &m,
                                    unsigned long long *stats, int num_sms, cudaStream_t st);
 
