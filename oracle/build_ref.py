@@ -66,6 +66,30 @@ def build_dr():
     return DR_LIB
 
 
+ADAPTER = os.path.join(OUT, "adapter_check")
+
+
+def build_adapter_check(engine_lib):
+    """oracle/_ref/adapter_check: the reference-side binding
+    (litert_gb300/ref_side/lrt_bvhrt_gpu.h) compiled against the reference's own
+    headers and linked with the engine and the in-place renderer."""
+    if not available():
+        return None
+    build_dr()
+    root = os.path.dirname(HERE)
+    flags = ["-std=c++17", "-O1", "-w", "-fopenmp", "-I" + os.path.join(HERE, "ref_shim"), "-I" + REF,
+             "-I" + os.path.join(root, "include"), "-I" + os.path.join(root, "litert_gb300", "ref_side")] + \
+            ["-D" + d for d in DR_DEFINES]
+    objs = [os.path.join(OUT, o) for _, o in DR_SOURCES] + [os.path.join(OUT, "dr_driver.o")]
+    r = subprocess.run(["g++", *flags, os.path.join(HERE, "ref_adapter_check.cpp"), *objs, engine_lib,
+                        "-Wl,-rpath," + os.path.dirname(engine_lib), "-o", ADAPTER],
+                       stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        sys.stderr.write(r.stdout)
+        raise RuntimeError("reference-side binding does not build against the reference headers")
+    return ADAPTER
+
+
 def build():
     if not available():
         return None
