@@ -53,7 +53,12 @@ lrt_status lrt_clear_scene(lrt_ctx *ctx);
 /* BVHRT::AddInstance, BVH/BVH2Common_host.cpp:1450-1487 (matrix row-major) */
 lrt_status lrt_add_instance(lrt_ctx *ctx, uint32_t geom_id, const float matrix[16], uint32_t *inst_id);
 /* BVHRT::CommitScene, BVH/BVH2Common_host.cpp:1416-1448: builds the BVH and
- * uploads the scene to the device.  One instance per scene. */
+ * uploads the scene to the device.  Any number of instances, all of one
+ * geometry (instances of different geometries: LRT_ERR_UNSUPPORTED); with
+ * several, every ray tests each instance box in instance order and walks the
+ * instances it enters with the closest hit so far (the reference's TLAS walk,
+ * BVH/BVH2Common.cpp:3508-3547, gives the same closest hit), and query records
+ * carry the instance in instId. */
 lrt_status lrt_commit_scene(lrt_ctx *ctx);
 /* BVHRT::SetPreset / MultiRenderer::SetPreset, Renderer/eye_ray_host.cpp:549-556.
  * ray_gen_mode 0 (regular sub-pixel grid) or 1 (RAY_GEN_MODE_RANDOM, see

@@ -17,7 +17,7 @@ LIB = os.path.join(OUT, "liblrt_gb300.so")
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
-CU_SOURCES = ["trace.cu", "trace_fused.cu", "trace_ref.cu", "trace_pkt.cu", "dr.cu", "proposal.cu", "build_gpu.cu", "bvh_gpu.cu"]
+CU_SOURCES = ["trace.cu", "trace_fused.cu", "trace_ref.cu", "trace_inst.cu", "trace_pkt.cu", "dr.cu", "proposal.cu", "build_gpu.cu", "bvh_gpu.cu"]
 # translation units compiled with floating-point contraction (the opt-in "fma" kernels)
 CONTRACTED = {"trace_fused.cu"}
 CPP_SOURCES = ["lrt_api.cpp", "scene_build.cpp", "scene_io.cpp", "bvh_build.cpp", "dr_api.cpp", "proposal_api.cpp"]

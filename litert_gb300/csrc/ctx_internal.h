@@ -128,6 +128,7 @@ struct lrt_ctx {
   // the BVH2 of the first-hit walk ("first_hit" tuning): checked and uploaded on
   // first use, or given by the caller (lrt_set_bvh2); reset by a commit
   DevBuf<lrt_bvh_pair> d_ref_pairs;
+  DevBuf<DevInst> d_insts;     // all instances, when the scene has several
   bool ref_pairs_ready = false;
 };
 

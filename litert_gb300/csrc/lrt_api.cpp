@@ -134,6 +134,7 @@ static void release_scene(lrt_ctx *ctx) {
   ctx->d_vpos.release();
   ctx->d_tri_indices.release();
   ctx->d_ref_pairs.release();
+  ctx->d_insts.release();
   ctx->bvh_on_device = ctx->bvh_refit = ctx->tri_indices_on_device = false;
   ctx->ref_pairs_ready = false;
   ctx->dev.pairs = nullptr;
@@ -288,6 +289,13 @@ static void instance_bounds(const Geom &g, Inst &in) {
   }
 }
 
+static void dev_inst(const Inst &in, DevInst &o) {
+  std::memset(&o, 0, sizeof(o));
+  for (int k = 0; k < 3; k++) { o.bmin[k] = in.bmin[k]; o.bmax[k] = in.bmax[k]; }
+  std::memcpy(o.inv, in.inv, sizeof(o.inv));
+  std::memcpy(o.inv_t, in.inv_t, sizeof(o.inv_t));
+}
+
 extern "C" lrt_status lrt_add_instance(lrt_ctx *ctx, uint32_t geom_id, const float matrix[16], uint32_t *inst_id) {
   if (!ctx) return LRT_ERR_INVALID;
   geom_id &= 0x7fffffffu;   // CRT_GEOM_MASK_AABB_BIT, BVH/BVH2Common_host.cpp:1452-1453
@@ -357,9 +365,10 @@ static lrt_status device_bvh(lrt_ctx *ctx, const std::vector<float> &boxes, bool
 
 extern "C" lrt_status lrt_commit_scene(lrt_ctx *ctx) {
   if (!ctx) return LRT_ERR_INVALID;
-  if (ctx->insts.size() != 1)
-    return fail(ctx, ctx->insts.empty() ? LRT_ERR_STATE : LRT_ERR_UNSUPPORTED,
-                "lrt_commit_scene: exactly one instance per scene is supported");
+  if (ctx->insts.empty()) return fail(ctx, LRT_ERR_STATE, "lrt_commit_scene: no instance");
+  for (const Inst &i : ctx->insts)
+    if (i.geom != ctx->insts[0].geom)
+      return fail(ctx, LRT_ERR_UNSUPPORTED, "lrt_commit_scene: the instances of a scene must share one geometry");
   LRT_CUDA(ctx, cudaSetDevice(ctx->device));
   release_scene(ctx);
   const Inst &in = ctx->insts[0];
@@ -489,6 +498,14 @@ extern "C" lrt_status lrt_commit_scene(lrt_ctx *ctx) {
   for (int k = 0; k < 3; k++) { s.inst_bmin[k] = in.bmin[k]; s.inst_bmax[k] = in.bmax[k]; }
   std::memcpy(s.inst_inv, in.inv, sizeof(s.inst_inv));
   std::memcpy(s.inst_inv_t, in.inv_t, sizeof(s.inst_inv_t));
+  s.n_inst = uint32_t(ctx->insts.size());
+  s.insts = nullptr;
+  if (s.n_inst > 1) {
+    std::vector<DevInst> di(ctx->insts.size());
+    for (size_t i = 0; i < di.size(); i++) dev_inst(ctx->insts[i], di[i]);
+    if ((e = upload(ctx->d_insts, di.data(), di.size())) != cudaSuccess) return cuda_fail(ctx, e, "upload instances");
+    s.insts = ctx->d_insts.p;
+  }
   s.preset = ctx->preset;
   s.seed = ctx->seed;
   ctx->dev = s;
@@ -581,9 +598,14 @@ extern "C" lrt_status lrt_refit_triangles(lrt_ctx *ctx, const float *vpos, size_
       g.bmin[k] = std::min(g.bmin[k], v);
       g.bmax[k] = std::max(g.bmax[k], v);
     }
-  instance_bounds(g, in);
+  for (Inst &i : ctx->insts) instance_bounds(g, i);
   for (int k = 0; k < 3; k++) { ctx->dev.inst_bmin[k] = in.bmin[k]; ctx->dev.inst_bmax[k] = in.bmax[k]; }
   cudaError_t e;
+  if (ctx->dev.n_inst > 1) {
+    std::vector<DevInst> di(ctx->insts.size());
+    for (size_t i = 0; i < di.size(); i++) dev_inst(ctx->insts[i], di[i]);
+    if ((e = upload(ctx->d_insts, di.data(), di.size())) != cudaSuccess) return cuda_fail(ctx, e, "upload instances");
+  }
   if ((e = upload(ctx->d_vpos, reinterpret_cast<const float4 *>(g.vpos.data()), n_vert)) != cudaSuccess)
     return cuda_fail(ctx, e, "lrt_refit_triangles: upload vertices");
   if (!ctx->tri_indices_on_device) {
@@ -702,10 +724,18 @@ extern "C" lrt_status lrt_update_instance(lrt_ctx *ctx, uint32_t inst_id, const 
   for (int i = 0; i < 4; i++)
     for (int j = 0; j < 4; j++) in.inv_t[i * 4 + j] = in.inv[j * 4 + i];
   instance_bounds(ctx->geoms[in.geom], in);
-  if (ctx->committed && inst_id == 0) {   // the committed single instance: no rebuild needed
+  if (!ctx->committed) return LRT_OK;
+  // the committed scene follows at once: no rebuild (the BLAS is in object space)
+  if (inst_id == 0) {
     for (int k = 0; k < 3; k++) { ctx->dev.inst_bmin[k] = in.bmin[k]; ctx->dev.inst_bmax[k] = in.bmax[k]; }
     std::memcpy(ctx->dev.inst_inv, in.inv, sizeof(in.inv));
     std::memcpy(ctx->dev.inst_inv_t, in.inv_t, sizeof(in.inv_t));
+  }
+  if (ctx->dev.n_inst > 1) {
+    DevInst di;
+    dev_inst(in, di);
+    LRT_CUDA(ctx, cudaSetDevice(ctx->device));
+    LRT_CUDA(ctx, cudaMemcpy(ctx->d_insts.p + inst_id, &di, sizeof(di), cudaMemcpyHostToDevice));
   }
   return LRT_OK;
 }

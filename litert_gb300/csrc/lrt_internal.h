@@ -86,6 +86,14 @@ cudaError_t gather_triangles_gpu(const float4 *d_vpos, const uint32_t *d_indices
 cudaError_t gpu_exclusive_scan(const uint32_t *in, uint32_t *out, uint32_t n, uint64_t *total, cudaStream_t st);
 
 // ------------------------------------------------------------------ device side
+// One instance of the committed geometry: its box in world space and the
+// inverse matrix (and its transpose) of AddInstance (BVH/BVH2Common_host.cpp:1450-1487).
+struct DevInst {
+  float bmin[3], bmax[3];
+  float inv[16], inv_t[16];
+  float _pad[2];
+};
+
 // Scene as the kernels see it (all pointers device memory).
 struct DevScene {
   uint32_t type;                 // LRT_TYPE_*
@@ -104,9 +112,13 @@ struct DevScene {
   // triangles: vertex positions gathered per reordered triangle (A,B,C as float4)
   const float4 *tri_verts;
   const uint32_t *prim_indices;  // reordered -> original triangle id
-  // single instance
+  // instance 0 (the only one, or the one the shading functions read)
   float inst_bmin[3], inst_bmax[3];
   float inst_inv[16], inst_inv_t[16];
+  // all instances of the geometry, when there are several (kernels instantiated
+  // with FEAT bit 3 walk them; null otherwise)
+  const DevInst *insts;
+  uint32_t n_inst;
   lrt_preset preset;
   uint32_t seed;                 // MultiRenderer::m_seed (setSeed), for RAY_GEN_MODE_RANDOM
   // the BVH2 in the reference's fat-pair layout (4 float4 per pair), for the
@@ -198,6 +210,11 @@ cudaError_t launch_render_ref(const DevScene &s, const RenderLaunch &L, int num_
 cudaError_t launch_query_ref(const DevScene &s, const float4 *pos_near, const float4 *dir_far, uint32_t n,
                              lrt_hit *out, cudaStream_t st);
 inline bool sdf_scene(const DevScene &s) { return s.type != LRT_TYPE_MESH_TRIANGLE; }
+// The same launches for a scene with several instances of its geometry (trace_inst.cu);
+// first_hit: the reference's BVH2 walk per instance (SDF scenes whose s.pairs is set).
+cudaError_t launch_render_inst(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st, bool first_hit);
+cudaError_t launch_query_inst(const DevScene &s, const float4 *pos_near, const float4 *dir_far, uint32_t n,
+                              lrt_hit *out, cudaStream_t st, bool first_hit);
 
 }  // namespace lrt
 

@@ -95,7 +95,7 @@ cudaError_t dispatch_render(lrt_ctx *ctx, const RenderLaunch &L, cudaStream_t st
   const uint32_t layout = s.sbs_hdr.aux_data & 0xFF000000u;
   const bool dx = s.type == LRT_TYPE_SDF_SBS && layout != LRT_SBS_LAYOUT_ID32F_IRGB32F &&
                   layout != LRT_SBS_LAYOUT_ID32F_IRGB32F_IN;
-  if (ctx->use_proposal && !count && dx && s.preset.sdf_node_intersect == LRT_INTERSECT_NEWTON && ctx->prop &&
+  if (ctx->use_proposal && !count && dx && s.n_inst <= 1 && s.preset.sdf_node_intersect == LRT_INTERSECT_NEWTON && ctx->prop &&
       ctx->prop->has_weights && s.preset.spp <= 1)
     return launch_render_proposal(s, L, mlp_state(*ctx->prop, nullptr), ctx->prop->stats.p, ctx->num_sms, st);
   return launch_render(s, L, ctx->num_sms, st, count, ctx->tuning);

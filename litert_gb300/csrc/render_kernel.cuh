@@ -16,7 +16,8 @@ namespace dev {
 // shadow ray is a nearest-hit query from just before the hit point towards the
 // light with the eye ray's tNear and tFar; only hit / miss is used, so an any-hit
 // query (the first leaf that reports a hit) decides the same.
-template <int TYPE, int MODE, int STACK>
+// MI: the scene has several instances (the shadow ray tests them all).
+template <int TYPE, int MODE, int STACK, int MI = 0>
 __device__ __noinline__ float4 shade_phong(const DevScene &s, const Hit &hit, float3 pos, float3 dir) {
   if (hit.prim == kMiss) return make_float4(0, 0, 0, 1);
   const uint32_t type = hit.geom >> 24;
@@ -46,7 +47,7 @@ __device__ __noinline__ float4 shade_phong(const DevScene &s, const Hit &hit, fl
     fc = add(fc, scl(q, mul(lc, color)));
     Hit sh;
     Counters cnt = {0, 0, 0, 0};
-    trace<TYPE, false, MODE, STACK>(s, surf, 0.0f, ld, -1e9f, sh, cnt);   // tFar <= 0: any hit
+    trace<TYPE, false, MODE, STACK, MI>(s, surf, 0.0f, ld, -1e9f, sh, cnt);   // tFar <= 0: any hit
     const float shade = (sh.prim == kMiss) ? 1.0f : 0.0f;
     const float3 refl = add(scl(-1.0f, ld), scl(2.0f * dot(norm, ld), norm));
     const float inner = Kd * mx(0.0f, dot(norm, ld)) + Ks * powf(mx(0.0f, dot(norm, refl)), 32.0f);
@@ -96,12 +97,21 @@ __global__ void __launch_bounds__(128, 5) render_kernel(DevScene s, RenderLaunch
       eye_ray(x, y, V.width, V.height, dx, dy, V.proj_inv, V.wv_inv, pos, dir);
       Hit hit;
       trace<TYPE, COUNT, MODE, STACK, FEAT>(s, pos, 0.0f, dir, 1e9f, hit, cnt);
-      if (TYPE == LRT_TYPE_SDF_SBS && !(FEAT & 2)) hit_colour(s, pos, dir, hit);
-      if (si == 0) first = hit;
-      if (L.rgba || L.rgba8) {
-        const float4 c = PHONG ? shade_phong<TYPE, MODE, STACK>(s, hit, pos, dir) : shade(s, hit, pos, dir);
-        acc.x += c.x; acc.y += c.y; acc.z += c.z; acc.w += c.w;
+      if (FEAT & 8) {   // colours and shading in the frame of the instance hit
+        const DevScene sh = scene_of_instance(s, hit.prim != kMiss ? hit.inst : 0u);
+        if (TYPE == LRT_TYPE_SDF_SBS && !(FEAT & 2)) hit_colour(sh, pos, dir, hit);
+        if (L.rgba || L.rgba8) {
+          const float4 c = PHONG ? shade_phong<TYPE, MODE, STACK, 8>(sh, hit, pos, dir) : shade(sh, hit, pos, dir);
+          acc.x += c.x; acc.y += c.y; acc.z += c.z; acc.w += c.w;
+        }
+      } else {
+        if (TYPE == LRT_TYPE_SDF_SBS && !(FEAT & 2)) hit_colour(s, pos, dir, hit);
+        if (L.rgba || L.rgba8) {
+          const float4 c = PHONG ? shade_phong<TYPE, MODE, STACK>(s, hit, pos, dir) : shade(s, hit, pos, dir);
+          acc.x += c.x; acc.y += c.y; acc.z += c.z; acc.w += c.w;
+        }
       }
+      if (si == 0) first = hit;
     }
     const size_t pix = size_t(V.pix_offset) + size_t(y) * V.width + x;
     if (L.hits16) {
@@ -136,11 +146,16 @@ __global__ void __launch_bounds__(128) query_kernel(DevScene s, const float4 *po
   Counters cnt = {0, 0, 0, 0};
   Hit hit;
   trace<TYPE, false, -1, kStackSize, FEAT>(s, f3(p.x, p.y, p.z), p.w, f3(d.x, d.y, d.z), d.w, hit, cnt);
-  if (TYPE == LRT_TYPE_SDF_SBS && !(FEAT & 2)) hit_colour(s, f3(p.x, p.y, p.z), f3(d.x, d.y, d.z), hit);
+  if (TYPE == LRT_TYPE_SDF_SBS && !(FEAT & 2)) {
+    if (FEAT & 8)
+      hit_colour(scene_of_instance(s, hit.prim != kMiss ? hit.inst : 0u), f3(p.x, p.y, p.z), f3(d.x, d.y, d.z), hit);
+    else
+      hit_colour(s, f3(p.x, p.y, p.z), f3(d.x, d.y, d.z), hit);
+  }
   lrt_hit o;
   o.t = hit.t;
   o.primId = (hit.prim != kMiss && (hit.geom >> 24) == LRT_TYPE_MESH_TRIANGLE) ? s.prim_indices[hit.prim] : hit.prim;
-  o.instId = hit.prim == kMiss ? kMiss : 0u;
+  o.instId = hit.prim == kMiss ? kMiss : ((FEAT & 8) ? hit.inst : 0u);
   o.geomId = hit.geom;
   o.coords[0] = hit.c0;
   o.coords[1] = hit.c1;

@@ -245,6 +245,7 @@ cudaError_t launch_render_lq(const DevScene &s, const RenderLaunch &L, int num_s
 
 cudaError_t launch_render(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st, bool count,
                           const Tuning &tu) {
+  if (s.n_inst > 1) return launch_render_inst(s, L, num_sms, st, false);
   const uint32_t rm = s.preset.render_mode;
   const bool phong = (rm == LRT_RENDER_MODE_PHONG || rm == LRT_RENDER_MODE_PHONG_NO_TEX) && (L.rgba || L.rgba8);
   switch (render_features(s)) {   // SBS only; smoothed normals need a normal mode, so never with ST_ITERATIONS
@@ -281,6 +282,7 @@ cudaError_t launch_render(const DevScene &s, const RenderLaunch &L, int num_sms,
 
 cudaError_t launch_query(const DevScene &s, const float4 *pos_near, const float4 *dir_far, uint32_t n, lrt_hit *out,
                          cudaStream_t st) {
+  if (s.n_inst > 1) return launch_query_inst(s, pos_near, dir_far, n, out, st, false);
   if (n == 0) return cudaSuccess;
   const uint32_t blocks = (n + 127) / 128;
   switch (s.type) {

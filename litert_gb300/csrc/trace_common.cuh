@@ -143,7 +143,20 @@ struct Hit {
   uint32_t prim;      // brick / voxel / reordered triangle id (remapped at the end)
   uint32_t geom;      // geomId | type << 24
   float c0, c1, c2, c3;
+  uint32_t inst;      // instance of the hit (kernels walking several instances only)
 };
+
+// The scene as seen from instance `ii`: its box and matrices in the instance-0
+// fields the leaf and shading functions read (kernels walking several instances).
+__device__ __forceinline__ DevScene scene_of_instance(const DevScene &s, uint32_t ii) {
+  DevScene r = s;
+  const DevInst &I = s.insts[ii];
+#pragma unroll
+  for (int k = 0; k < 3; k++) { r.inst_bmin[k] = I.bmin[k]; r.inst_bmax[k] = I.bmax[k]; }
+#pragma unroll
+  for (int k = 0; k < 16; k++) { r.inst_inv[k] = I.inv[k]; r.inst_inv_t[k] = I.inv_t[k]; }
+  return r;
+}
 
 struct Counters { uint32_t nodes, leaves, voxels, finder; };
 

@@ -38,6 +38,7 @@ static cudaError_t launch_ref_t(const DevScene &s, const RenderLaunch &L, int nu
 
 cudaError_t launch_render_ref(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st) {
   if (!s.pairs || !sdf_scene(s)) return cudaErrorInvalidValue;
+  if (s.n_inst > 1) return launch_render_inst(s, L, num_sms, st, true);
   const uint32_t rm = s.preset.render_mode;
   const bool phong = (rm == LRT_RENDER_MODE_PHONG || rm == LRT_RENDER_MODE_PHONG_NO_TEX) && (L.rgba || L.rgba8);
   if (s.type == LRT_TYPE_SDF_SVS)
@@ -57,6 +58,7 @@ cudaError_t launch_render_ref(const DevScene &s, const RenderLaunch &L, int num_
 cudaError_t launch_query_ref(const DevScene &s, const float4 *pos_near, const float4 *dir_far, uint32_t n,
                              lrt_hit *out, cudaStream_t st) {
   if (!s.pairs || !sdf_scene(s)) return cudaErrorInvalidValue;
+  if (s.n_inst > 1) return launch_query_inst(s, pos_near, dir_far, n, out, st, true);
   if (n == 0) return cudaSuccess;
   const uint32_t blocks = (n + 127) / 128;
   if (s.type == LRT_TYPE_SDF_SVS) {

@@ -65,21 +65,14 @@ __device__ void walk_bvh2(const DevScene &s, float3 rp, float3 rd, float3 inv, f
   }
 }
 
-// RayQuery_NearestHit (BVH/BVH2Common.cpp:3490-3559) over the 4-wide BVH.
-// stopOnFirstHit (tFar <= 0) returns the first hit found (RayQuery_AnyHit).
-// SBS brick colours are added by the caller (hit_colour) unless FEAT bit 1 has
-// them computed in the leaf loop.  FEAT bit 2: the reference's BVH2 walk with
-// its first-hit early-out (walk_bvh2) instead of the closest-hit 4-wide walk.
-template <int TYPE, bool COUNT, int MODE = -1, int STACK = kStackSize, int FEAT = 0>
-__device__ void trace(const DevScene &s, float3 pos, float tNear, float3 dir, float tFar, Hit &hit, Counters &cnt) {
-  const bool stop_first = (tFar <= 0.0f);
-  if (stop_first) tFar *= -1.0f;
-  hit.t = tFar;
-  hit.prim = kMiss;
-  hit.geom = kMiss;
-  hit.c0 = 1.0f;
-  hit.c1 = hit.c2 = hit.c3 = 0.0f;
-  {  // TLAS: one leaf node holding the instance box (:3508-3529)
+// One instance of RayQuery_NearestHit (BVH/BVH2Common.cpp:3490-3559): the
+// instance box (the TLAS leaf), the ray in object space, the BLAS walk.  `s`
+// carries the instance in its instance-0 fields.  Returns after the first hit
+// when stop_first (RayQuery_AnyHit).
+template <int TYPE, bool COUNT, int MODE, int STACK, int FEAT>
+__device__ __forceinline__ void trace_instance(const DevScene &s, float3 pos, float tNear, float3 dir, bool stop_first,
+                                               Hit &hit, Counters &cnt) {
+  {  // TLAS leaf: the instance box (:3508-3529)
     const float3 invw = safe_inverse(dir);
     const float2 bh = ray_box(pos, invw, s.inst_bmin[0], s.inst_bmin[1], s.inst_bmin[2], s.inst_bmax[0],
                               s.inst_bmax[1], s.inst_bmax[2]);
@@ -125,9 +118,41 @@ __device__ void trace(const DevScene &s, float3 pos, float tNear, float3 dir, fl
     else if (TYPE == LRT_TYPE_SDF_SVS)
       svs_intersect<COUNT, MODE>(s, rp, rd, tNearSdf, leaf, hit, cnt);
     else
-      brick_intersect<COUNT, false, MODE, FEAT>(s, rp, rd, inv, tNearSdf, leaf, hit, cnt);
+      brick_intersect<COUNT, false, MODE, FEAT & 3>(s, rp, rd, inv, tNearSdf, leaf, hit, cnt);
     if (stop_first && hit.t < t_before) break;
   }
+}
+
+// RayQuery_NearestHit (BVH/BVH2Common.cpp:3490-3559) over the 4-wide BVH.
+// stopOnFirstHit (tFar <= 0) returns the first hit found (RayQuery_AnyHit).
+// SBS brick colours are added by the caller (hit_colour) unless FEAT bit 1 has
+// them computed in the leaf loop.  FEAT bit 2: the reference's BVH2 walk with
+// its first-hit early-out (walk_bvh2) instead of the closest-hit 4-wide walk.
+// FEAT bit 3: several instances of the geometry (s.insts), each tested and
+// walked in instance order with the closest hit so far -- the reference walks
+// its TLAS over the instance boxes (:3508-3547) with the same hit.t culling, so
+// the closest hit is the same; hit.inst names the instance hit.
+template <int TYPE, bool COUNT, int MODE = -1, int STACK = kStackSize, int FEAT = 0>
+__device__ void trace(const DevScene &s, float3 pos, float tNear, float3 dir, float tFar, Hit &hit, Counters &cnt) {
+  const bool stop_first = (tFar <= 0.0f);
+  if (stop_first) tFar *= -1.0f;
+  hit.t = tFar;
+  hit.prim = kMiss;
+  hit.geom = kMiss;
+  hit.c0 = 1.0f;
+  hit.c1 = hit.c2 = hit.c3 = 0.0f;
+  if (FEAT & 8) {
+    hit.inst = kMiss;
+    for (uint32_t ii = 0; ii < s.n_inst; ii++) {
+      const DevScene si = scene_of_instance(s, ii);
+      const float t_before = hit.t;
+      trace_instance<TYPE, COUNT, MODE, STACK, FEAT & 7>(si, pos, tNear, dir, stop_first, hit, cnt);
+      if (hit.t < t_before) hit.inst = ii;
+      if (stop_first && hit.prim != kMiss) break;
+    }
+    return;
+  }
+  trace_instance<TYPE, COUNT, MODE, STACK, FEAT>(s, pos, tNear, dir, stop_first, hit, cnt);
 }
 
 // One inner node of the per-ray traversal: test the four child boxes with the
