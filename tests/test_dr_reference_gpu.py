@@ -17,7 +17,7 @@ import numpy as np
 import pytest
 
 import _dr_glue_cases as cases
-from litert_gb300 import dr
+from litert_gb300 import dr, lrt
 
 pytestmark = pytest.mark.gpu
 
@@ -36,7 +36,8 @@ def test_engine_optimize_matches_reference_run(name):
         R.SetPreset(dr.default_preset(render_mode=case["render_mode"],
                                       reconstruction_flags=case["reconstruction_flags"],
                                       border_spp=case["border_spp"], seed=cases.DR_SEED, opt_lr=cases.DR_LR, spp=1))
-        R.SetScene(hdr, nodes, values, params.copy(), pairs=pairs)
+        R.SetScene(lrt.SbsHeader(hdr.brick_size, hdr.brick_pad, hdr.bytes_per_value, hdr.aux_data), nodes, values,
+                   params.copy(), pairs=pairs)
         assert np.array_equal(R.bvh2(), np.ascontiguousarray(pairs).view(np.uint8).reshape(-1))
         for it in range(case["iterations"]):
             R.step(it)
