@@ -1206,20 +1206,22 @@ __global__ void __launch_bounds__(128, 4) dr_border_kernel(DevScene s, DevPreset
   }
 }
 
-// OptimizeStepAdam (:828-853) after the batch division (:475-476)
-// The bias corrections 1 - beta^(iter+1) are formed in double on the host as the
-// reference does; the divisions by them run in float here (the reference
-// divides in double, a difference of at most one rounding).
+// OptimizeStepAdam (:828-853) after the batch division (:475-476), in the
+// reference's arithmetic: the bias corrections 1 - beta^(iter+1) are doubles
+// (pow of a float and an unsigned), V and S are divided by them in double and
+// rounded to float, the update lr * Vh / (sqrt(Sh) + eps) is float with a float
+// square root, and the result is clamped to +-1000 (LiteMath::clamp).  Given the
+// same gradient, the parameters and moments equal the reference's bit for bit.
 __global__ void dr_adam_kernel(float *x, float *V, float *S, const float *g, uint32_t n, float batch, float lr,
-                               float b1, float b2, float eps, float c1, float c2) {
+                               float b1, float b2, float eps, double c1, double c2) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float gi = g[i] / batch;
     const float Vi = b1 * V[i] + (1 - b1) * gi;
     V[i] = Vi;
-    const float Vh = Vi / c1;
+    const float Vh = float(double(Vi) / c1);
     const float Si = b2 * S[i] + (1 - b2) * gi * gi;
     S[i] = Si;
-    const float Sh = Si / c2;
+    const float Sh = float(double(Si) / c2);
     x[i] = clampf(x[i] - lr * Vh / (sqrtf(Sh) + eps), -1000.0f, 1000.0f);
   }
 }
@@ -1482,7 +1484,7 @@ cudaError_t launch_redistance(float *dist, uint32_t n, float h, uint32_t n_iters
 void launch_adam(float *x, float *V, float *S, const float *g, uint32_t n, float batch, float lr, float b1, float b2,
                  float eps, double c1, double c2, cudaStream_t st) {
   dr_adam_kernel<<<(n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096, 256, 0, st>>>(x, V, S, g, n, batch, lr, b1, b2,
-                                                                                  eps, float(c1), float(c2));
+                                                                                  eps, c1, c2);
 }
 
 void launch_scale(float *g, uint32_t n, float s, cudaStream_t st) {

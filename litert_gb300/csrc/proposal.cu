@@ -138,9 +138,10 @@ __global__ void __launch_bounds__(128) gen_triples_kernel(DevScene s, const DevV
   if (!(t1 > t0)) return;
   const unsigned long long k = atomicAdd(out.count, 1ull);
   if (k >= out.capacity) return;
-  uint4 *dst = reinterpret_cast<uint4 *>(out.feat + k * 16);
-  dst[0] = make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]), pack_bf16(f[4], f[5]), pack_bf16(f[6], f[7]));
-  dst[1] = make_uint4(pack_bf16(f[8], f[9]), pack_bf16(f[10], f[11]), pack_bf16(f[12], f[13]), pack_bf16(f[14], f[15]));
+  uint4 *dst = reinterpret_cast<uint4 *>(out.feat);
+  dst[feat_u4(k, 0)] = make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]), pack_bf16(f[4], f[5]), pack_bf16(f[6], f[7]));
+  dst[feat_u4(k, 1)] =
+      make_uint4(pack_bf16(f[8], f[9]), pack_bf16(f[10], f[11]), pack_bf16(f[12], f[13]), pack_bf16(f[14], f[15]));
   out.target[k] = (hit.t - t0) / (t1 - t0);
 }
 
@@ -193,9 +194,9 @@ __global__ void __launch_bounds__(128) mlp_train_kernel(TripleView data, MlpStat
   {
     uint4 a = make_uint4(0, 0, 0, 0), b = a;
     if (valid) {
-      const uint4 *src = reinterpret_cast<const uint4 *>(data.feat + idx * 16);
-      a = src[0];
-      b = src[1];
+      const uint4 *src = reinterpret_cast<const uint4 *>(data.feat);
+      a = src[feat_u4(data.first + idx, 0)];
+      b = src[feat_u4(data.first + idx, 1)];
     }
     uint4 *dst = reinterpret_cast<uint4 *>(&sx[w][lane * kIn]);
     dst[0] = a;
@@ -204,7 +205,7 @@ __global__ void __launch_bounds__(128) mlp_train_kernel(TripleView data, MlpStat
   __syncwarp();
   float h1[2][4][4], h2[2][4][4];
   const float y = forward_warp<true>(W, sx[w], sy[w], lane, h1, h2);
-  const float target = valid ? data.target[idx] : 0.0f;
+  const float target = valid ? data.target[data.first + idx] : 0.0f;
   const float err = valid ? (y - target) : 0.0f;
   float l = err * err;
 #pragma unroll
@@ -371,9 +372,9 @@ __global__ void __launch_bounds__(128) mlp_infer_kernel(TripleView data, MlpStat
   const uint64_t gid = uint64_t(blockIdx.x) * 128 + threadIdx.x;
   uint4 a = make_uint4(0, 0, 0, 0), b = a;
   if (gid < data.n) {
-    const uint4 *src = reinterpret_cast<const uint4 *>(data.feat + gid * 16);
-    a = src[0];
-    b = src[1];
+    const uint4 *src = reinterpret_cast<const uint4 *>(data.feat);
+    a = src[feat_u4(data.first + gid, 0)];
+    b = src[feat_u4(data.first + gid, 1)];
   }
   uint4 *dst = reinterpret_cast<uint4 *>(&sx[w][lane * kIn]);
   dst[0] = a;
@@ -384,29 +385,35 @@ __global__ void __launch_bounds__(128) mlp_infer_kernel(TripleView data, MlpStat
 }
 
 // ---------------------------------------------------------------- 128-sample tiles on tcgen05
-// The network on the fifth-generation tensor cores.  A persistent CTA of 4 warps
-// stages the BF16 weights once in shared memory (K-major canonical layout:
-// 8-row x 16-byte core matrices), allocates 32 TMEM columns once, and then walks
-// 128-sample tiles (one M = 128 MMA tile each).  Per layer one elected thread
-// issues tcgen05.mma (K = 16 per instruction) into the same 32 accumulator
-// columns, commits to an mbarrier and waits on it; after a CTA barrier each warp
-// reads its 32 TMEM lanes with tcgen05.ld, adds the bias and applies ReLU and
-// BF16 rounding (the rounding points of the mma.sync path), writing the next
-// layer's A operand to shared memory.  A tile's features are staged while the
-// previous tile is still in layers 2-3, and loaded into registers one tile
-// earlier still.  Ten CTAs per SM keep ten chains in flight.  Waits are bounded:
-// the per-layer waits poll the commit mbarrier at most `wait_limit` times; a
-// timeout sets status bit 1, the CTA leaves its loop at the next barrier, waits
-// once more (at most kTcWait polls, whatever wait_limit is) for the MMAs it has
-// issued and frees its TMEM.
-constexpr uint32_t kTcLbo = 128;         // adjacent core matrices along K
+// The network on the fifth-generation tensor cores, warp-specialised and
+// pipelined.  A persistent CTA of six warps walks the 128-sample tiles of the
+// store that hold the requested window:
+//   warp 0 (one thread)  loads each tile's 4 KB of features with one bulk copy
+//                        (cp.async.bulk) into a ring of four shared-memory
+//                        stages -- the store's tile layout is the MMA's
+//                        operand layout -- completing on the stage's mbarrier;
+//   warp 1 (one thread)  issues each layer's tcgen05.mma (M = 128, N = 32/32/16,
+//                        K = 16 per instruction) into one of two TMEM
+//                        accumulators (tiles alternate), committing each layer
+//                        to an mbarrier; layer 1 of tile j+1 is issued before
+//                        layers 2 and 3 of tile j, so the tensor core works on
+//                        one tile while the epilogue warps finish the other;
+//   warps 2-5            the epilogue: each reads its 32 TMEM lanes, adds the
+//                        bias, applies ReLU and BF16 rounding (one
+//                        cvt.rn.relu.bf16x2.f32 per pair) into the next layer's
+//                        A operand in shared memory, and after layer 3 writes
+//                        column 0 plus the output bias.
+// Every hand-off is an mbarrier (no CTA barrier inside the loop).  The weights
+// are staged once per CTA in the canonical K-major layout.  Waits are bounded by
+// `wait_limit` polls: a timeout sets status bit 1 and makes the role leave its
+// loop; the others run out the same way, then the MMA thread waits (at most
+// kTcWait polls) for everything it issued, the loader for every copy it
+// started, and the TMEM is freed.
+constexpr uint32_t kTcLbo = 128;         // adjacent core matrices along K (weights, hidden operands)
 constexpr uint32_t kTcWait = 1u << 22;   // mbarrier polls of the final drain (and the default per-layer limit)
-constexpr int kTcBlocksPerSm = 10;
-
-__device__ __forceinline__ void stage_row16(uint8_t *tile, uint32_t row, uint32_t sbo, const uint4 &lo, const uint4 &hi) {
-  *reinterpret_cast<uint4 *>(tile + tc05::kmajor_offset(row, 0, kTcLbo, sbo)) = lo;
-  *reinterpret_cast<uint4 *>(tile + tc05::kmajor_offset(row, 8, kTcLbo, sbo)) = hi;
-}
+constexpr int kTcStages = 4;
+constexpr int kTcThreads = 192;
+constexpr int kTcBlocksPerSm = 4;
 
 // bias + ReLU + BF16 of one 32-wide accumulator row (this lane's TMEM lane, read in
 // two 16-column halves to keep registers low) into the A operand of the next layer
@@ -427,136 +434,159 @@ __device__ __forceinline__ void hidden_to_smem(uint32_t trow, const float *bias,
   }
 }
 
-__device__ __forceinline__ void load_row16(const TripleView &data, uint64_t gid, uint4 &lo, uint4 &hi) {
-  lo = make_uint4(0, 0, 0, 0);
-  hi = lo;
-  if (gid < data.n) {
-    const uint4 *src = reinterpret_cast<const uint4 *>(data.feat + gid * 16);
-    lo = __ldg(src);
-    hi = __ldg(src + 1);
-  }
-}
-
-__global__ void __launch_bounds__(128, kTcBlocksPerSm) mlp_infer_tc_kernel(TripleView data, MlpState m, float *out,
-                                                                           unsigned int *status, uint32_t wait_limit) {
-  __shared__ __align__(128) uint8_t sX[128 * kIn * 2];
-  __shared__ __align__(128) uint8_t sH[128 * kHid * 2];
+__global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) mlp_infer_tc_kernel(TripleView data, MlpState m,
+                                                                                  float *out, unsigned int *status,
+                                                                                  uint32_t wait_limit) {
+  __shared__ __align__(128) uint8_t sX[kTcStages][4096];
+  __shared__ __align__(128) uint8_t sH[2][128 * kHid * 2];
   __shared__ __align__(128) uint8_t sW1[kHid * kIn * 2];
   __shared__ __align__(128) uint8_t sW2[kHid * kHid * 2];
   __shared__ __align__(128) uint8_t sW3[16 * kHid * 2];
   __shared__ __align__(16) float sb1[kHid];
   __shared__ __align__(16) float sb2[kHid];
   __shared__ float sb3;
-  __shared__ __align__(8) uint64_t mbar;
-  __shared__ uint32_t tmem_slot;
-  const uint32_t tid = threadIdx.x, warp = tid >> 5;
-  const uint64_t n_tiles = (data.n + 127) / 128;
-  uint64_t tile = blockIdx.x;
-  uint4 lo, hi;
-  load_row16(data, tile * 128 + tid, lo, hi);
+  __shared__ __align__(8) uint64_t full[kTcStages], empty[kTcStages];
+  __shared__ __align__(8) uint64_t l1[2], l2[2], l3[2], h1[2], h2[2], afree[2], fin;
+  __shared__ uint32_t tmem_slot, s_consumed;
+  const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+  const uint64_t t_first = data.first >> 7;
+  const uint64_t n_tiles = data.n ? ((data.first + data.n - 1) >> 7) - t_first + 1 : 0;
+  const uint32_t my_tiles = blockIdx.x < n_tiles ? uint32_t((n_tiles - 1 - blockIdx.x) / gridDim.x + 1) : 0u;
   // weights into the canonical layout (W stored [n][k] is the K-major B operand)
-  for (uint32_t i = tid; i < kHid * kIn; i += 128)
+  for (uint32_t i = tid; i < kHid * kIn; i += kTcThreads)
     *reinterpret_cast<__nv_bfloat16 *>(sW1 + tc05::kmajor_offset(i / kIn, i % kIn, kTcLbo, 256)) = m.wbf[kBfW1 + i];
-  for (uint32_t i = tid; i < kHid * kHid; i += 128)
+  for (uint32_t i = tid; i < kHid * kHid; i += kTcThreads)
     *reinterpret_cast<__nv_bfloat16 *>(sW2 + tc05::kmajor_offset(i / kHid, i % kHid, kTcLbo, 512)) = m.wbf[kBfW2 + i];
-  for (uint32_t i = tid; i < 16 * kHid; i += 128)
+  for (uint32_t i = tid; i < 16 * kHid; i += kTcThreads)
     *reinterpret_cast<__nv_bfloat16 *>(sW3 + tc05::kmajor_offset(i / kHid, i % kHid, kTcLbo, 512)) =
         i < kHid ? m.wbf[kBfW3 + i] : __float2bfloat16_rn(0.0f);
   if (tid < kHid) {
     sb1[tid] = m.master[kOffB1 + tid];
     sb2[tid] = m.master[kOffB2 + tid];
   }
-  if (tid == 0) sb3 = m.master[kOffB3];
-  if (warp == 0) tc05::tmem_alloc(&tmem_slot, 32);
-  if (tid == 0) tc05::mbar_init(&mbar, 1);
-  tc05::fence_before_sync();
-  __syncthreads();
-  tc05::fence_after_sync();
-  const uint32_t tbase = tmem_slot, trow = tbase + ((warp * 32u) << 16);
-  const uint32_t aX = tc05::smem_addr(sX), aH = tc05::smem_addr(sH);
-  const uint32_t aW1 = tc05::smem_addr(sW1), aW2 = tc05::smem_addr(sW2), aW3 = tc05::smem_addr(sW3);
-  constexpr uint32_t kId32 = tc05::idesc_bf16_f32(128, 32), kId16 = tc05::idesc_bf16_f32(128, 16);
-  uint32_t phase = 0;
-  bool ok = true;
-  // One thread issues each layer's MMAs and waits for their commit; the CTA barrier
-  // that follows carries the completion (and a timeout) to the other warps, which
-  // do not poll.  The first tile's features go to shared memory here, each later
-  // tile's as soon as the previous tile's layer 1 has consumed them.
-  stage_row16(sX, tid, 256, lo, hi);
-  load_row16(data, (tile + gridDim.x) * 128 + tid, lo, hi);
+  if (tid == 0) {
+    sb3 = m.master[kOffB3];
+    for (int i = 0; i < kTcStages; i++) {
+      tc05::mbar_init(&full[i], 1);
+      tc05::mbar_init(&empty[i], 1);
+    }
+    for (int a = 0; a < 2; a++) {
+      tc05::mbar_init(&l1[a], 1);
+      tc05::mbar_init(&l2[a], 1);
+      tc05::mbar_init(&l3[a], 1);
+      tc05::mbar_init(&h1[a], 4);
+      tc05::mbar_init(&h2[a], 4);
+      tc05::mbar_init(&afree[a], 4);
+    }
+    tc05::mbar_init(&fin, 1);
+    s_consumed = 0;
+    tc05::fence_mbar_init();
+  }
+  if (warp == 0) tc05::tmem_alloc(&tmem_slot, 64);
   tc05::fence_proxy_async();
   tc05::fence_before_sync();
   __syncthreads();
   tc05::fence_after_sync();
-  for (; tile < n_tiles; tile += gridDim.x) {
-    const uint64_t row = tile * 128 + tid;
-    // layer 1: D[128 x 32] = X W1^T
-    bool t_ok = true;
-    if (tid == 0) {
-      tc05::mma_bf16(tbase, tc05::smem_desc(aX, kTcLbo, 256), tc05::smem_desc(aW1, kTcLbo, 256), kId32, false);
-      tc05::mma_commit(&mbar);
-      t_ok = tc05::mbar_wait(&mbar, phase, wait_limit);
+  const uint32_t tbase = tmem_slot;
+  auto tile_of = [&](uint32_t j) { return t_first + blockIdx.x + uint64_t(j) * gridDim.x; };
+  uint32_t issued = 0;
+
+  if (warp == 0) {
+    // ---- loader
+    if (lane == 0) {
+      for (uint32_t j = 0; j < my_tiles; j++) {
+        const uint32_t st = j % kTcStages;
+        if (j >= uint32_t(kTcStages) && !tc05::mbar_wait(&empty[st], ((j / kTcStages) - 1) & 1u, wait_limit)) {
+          atomicOr(status, 2u);
+          break;
+        }
+        tc05::mbar_arrive_expect_tx(&full[st], 4096);
+        tc05::bulk_g2s(sX[st], data.feat + tile_of(j) * 2048, 4096, &full[st]);
+        issued = j + 1;
+      }
     }
-    phase ^= 1u;
-    tc05::fence_before_sync();
-    ok = __syncthreads_and(t_ok);
-    tc05::fence_after_sync();
-    if (!ok) break;
-    hidden_to_smem(trow, sb1, sH, tid);
-    stage_row16(sX, tid, 256, lo, hi);                              // next tile's features
-    load_row16(data, (tile + 2 * uint64_t(gridDim.x)) * 128 + tid, lo, hi);   // and the one after, in flight
-    tc05::fence_proxy_async();
-    tc05::fence_before_sync();
-    __syncthreads();
-    tc05::fence_after_sync();
-    // layer 2: D = H1 W2^T, two K = 16 steps (the next K block starts 2 core matrices on)
-    if (tid == 0) {
-      tc05::mma_bf16(tbase, tc05::smem_desc(aH, kTcLbo, 512), tc05::smem_desc(aW2, kTcLbo, 512), kId32, false);
-      tc05::mma_bf16(tbase, tc05::smem_desc(aH + 2 * kTcLbo, kTcLbo, 512), tc05::smem_desc(aW2 + 2 * kTcLbo, kTcLbo, 512),
-                     kId32, true);
-      tc05::mma_commit(&mbar);
-      t_ok = tc05::mbar_wait(&mbar, phase, wait_limit);
+  } else if (warp == 1) {
+    // ---- MMA issuer
+    if (lane == 0) {
+      constexpr uint32_t kId32 = tc05::idesc_bf16_f32(128, 32), kId16 = tc05::idesc_bf16_f32(128, 16);
+      const uint32_t aH[2] = {tc05::smem_addr(sH[0]), tc05::smem_addr(sH[1])};
+      const uint32_t aW1 = tc05::smem_addr(sW1), aW2 = tc05::smem_addr(sW2), aW3 = tc05::smem_addr(sW3);
+      uint32_t consumed = 0;
+      bool ok = true;
+      for (uint32_t j = 0; ok && j <= my_tiles; j++) {
+        if (j < my_tiles) {   // layer 1 of tile j
+          const uint32_t a = j & 1u, st = j % kTcStages;
+          if (j >= 2 && !tc05::mbar_wait(&afree[a], ((j >> 1) - 1) & 1u, wait_limit)) { ok = false; break; }
+          if (!tc05::mbar_wait(&full[st], (j / kTcStages) & 1u, wait_limit)) { ok = false; break; }
+          tc05::fence_after_sync();
+          tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(tc05::smem_addr(sX[st]), 2048, 128),
+                         tc05::smem_desc(aW1, kTcLbo, 256), kId32, false);
+          tc05::mma_commit(&l1[a]);
+          tc05::mma_commit(&empty[st]);   // the stage is free once layer 1 has read it
+          consumed = j + 1;
+        }
+        if (j >= 1) {         // layers 2 and 3 of tile j - 1
+          const uint32_t jj = j - 1, a = jj & 1u, ph = (jj >> 1) & 1u;
+          if (!tc05::mbar_wait(&h1[a], ph, wait_limit)) { ok = false; break; }
+          tc05::fence_after_sync();
+          tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(aH[a], kTcLbo, 512), tc05::smem_desc(aW2, kTcLbo, 512), kId32,
+                         false);
+          tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(aH[a] + 2 * kTcLbo, kTcLbo, 512),
+                         tc05::smem_desc(aW2 + 2 * kTcLbo, kTcLbo, 512), kId32, true);
+          tc05::mma_commit(&l2[a]);
+          if (!tc05::mbar_wait(&h2[a], ph, wait_limit)) { ok = false; break; }
+          tc05::fence_after_sync();
+          tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(aH[a], kTcLbo, 512), tc05::smem_desc(aW3, kTcLbo, 512), kId16,
+                         false);
+          tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(aH[a] + 2 * kTcLbo, kTcLbo, 512),
+                         tc05::smem_desc(aW3 + 2 * kTcLbo, kTcLbo, 512), kId16, true);
+          tc05::mma_commit(&l3[a]);
+        }
+      }
+      if (!ok) atomicOr(status, 2u);
+      // every MMA this thread issued has completed before the TMEM is freed
+      tc05::mma_commit(&fin);
+      if (!tc05::mbar_wait(&fin, 0, kTcWait)) atomicOr(status, 2u);
+      s_consumed = consumed;
     }
-    phase ^= 1u;
-    tc05::fence_before_sync();
-    ok = __syncthreads_and(t_ok);
-    tc05::fence_after_sync();
-    if (!ok) break;
-    hidden_to_smem(trow, sb2, sH, tid);
-    tc05::fence_proxy_async();
-    tc05::fence_before_sync();
-    __syncthreads();
-    tc05::fence_after_sync();
-    // layer 3: D[:, 0:16] = H2 W3pad^T (column 0 is the output)
-    if (tid == 0) {
-      tc05::mma_bf16(tbase, tc05::smem_desc(aH, kTcLbo, 512), tc05::smem_desc(aW3, kTcLbo, 512), kId16, false);
-      tc05::mma_bf16(tbase, tc05::smem_desc(aH + 2 * kTcLbo, kTcLbo, 512), tc05::smem_desc(aW3 + 2 * kTcLbo, kTcLbo, 512),
-                     kId16, true);
-      tc05::mma_commit(&mbar);
-      t_ok = tc05::mbar_wait(&mbar, phase, wait_limit);
+  } else {
+    // ---- epilogue: warp w reads TMEM lanes 32 * (w % 4) .. + 31 (rows of the tile)
+    const uint32_t q = warp & 3u, row = 32u * q + lane, trow = tbase + ((32u * q) << 16);
+    for (uint32_t j = 0; j < my_tiles; j++) {
+      const uint32_t a = j & 1u, ph = (j >> 1) & 1u;
+      if (!tc05::mbar_wait(&l1[a], ph, wait_limit)) { atomicOr(status, 2u); break; }
+      tc05::fence_after_sync();
+      hidden_to_smem(trow + a * 32u, sb1, sH[a], row);
+      tc05::fence_proxy_async();
+      tc05::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc05::mbar_arrive(&h1[a]);
+      if (!tc05::mbar_wait(&l2[a], ph, wait_limit)) { atomicOr(status, 2u); break; }
+      tc05::fence_after_sync();
+      hidden_to_smem(trow + a * 32u, sb2, sH[a], row);
+      tc05::fence_proxy_async();
+      tc05::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc05::mbar_arrive(&h2[a]);
+      if (!tc05::mbar_wait(&l3[a], ph, wait_limit)) { atomicOr(status, 2u); break; }
+      tc05::fence_after_sync();
+      const float y = tc05::tmem_ld1(trow + a * 32u);
+      const uint64_t g = tile_of(j) * 128 + row;
+      if (g >= data.first && g < data.first + data.n) out[g - data.first] = y + sb3;
+      tc05::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc05::mbar_arrive(&afree[a]);
     }
-    phase ^= 1u;
-    tc05::fence_before_sync();
-    ok = __syncthreads_and(t_ok);
-    tc05::fence_after_sync();
-    if (!ok) break;
-    {
-      float v[16];
-      tc05::tmem_ld16(trow, v);
-      if (row < data.n) out[row] = v[0] + sb3;
-    }
-    tc05::fence_before_sync();
-    __syncthreads();   // every lane has read D before the next tile's MMA overwrites it
-    tc05::fence_after_sync();
   }
-  if (!ok && tid == 0) {
-    tc05::mbar_wait(&mbar, phase ^ 1u, kTcWait);   // the MMAs of the step that timed out, if they finish
-    atomicOr(status, 2u);
-  }
+  __syncthreads();
+  // copies the MMA issuer never consumed (after a timeout) land before the CTA exits
+  if (warp == 0 && lane == 0)
+    for (uint32_t j = s_consumed; j < issued; j++)
+      if (!tc05::mbar_wait(&full[j % kTcStages], (j / kTcStages) & 1u, kTcWait)) atomicOr(status, 2u);
   tc05::fence_before_sync();
   __syncthreads();
   tc05::fence_after_sync();
-  if (warp == 0) tc05::tmem_dealloc(tbase, 32);
+  if (warp == 0) tc05::tmem_dealloc(tbase, 64);
 }
 
 // ---------------------------------------------------------------- render with the proposal
@@ -704,11 +734,11 @@ cudaError_t launch_mlp_infer_tc(const TripleView &data, const MlpState &m, float
   cudaError_t e = cudaGetDevice(&device);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   if (e != cudaSuccess) return e;
-  const uint64_t tiles = (data.n + 127) / 128;
+  if (data.n == 0) return cudaSuccess;
+  const uint64_t tiles = ((data.first + data.n - 1) >> 7) - (data.first >> 7) + 1;
   uint64_t blocks = uint64_t(sms) * dev::kTcBlocksPerSm;
   if (blocks > tiles) blocks = tiles;
-  if (blocks == 0) return cudaSuccess;
-  dev::mlp_infer_tc_kernel<<<unsigned(blocks), 128, 0, st>>>(data, m, out, status, wait_limit);
+  dev::mlp_infer_tc_kernel<<<unsigned(blocks), dev::kTcThreads, 0, st>>>(data, m, out, status, wait_limit);
   return cudaGetLastError();
 }
 

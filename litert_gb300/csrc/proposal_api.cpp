@@ -135,14 +135,15 @@ extern "C" lrt_status lrt_proposal_get_weights(lrt_ctx *ctx, float *params) {
 
 static lrt_status reserve(lrt_ctx *ctx, uint64_t capacity) {
   ProposalState &p = *ctx->prop;
-  if (p.feat.cap >= capacity * 16 && p.target.cap >= capacity) return LRT_OK;
-  // grow, keeping what is held
+  if (p.feat.cap >= lrt::feat_elems(capacity) && p.target.cap >= capacity) return LRT_OK;
+  // grow, keeping what is held (whole tiles; the tile layout does not depend on the capacity)
   lrt::DevBuf<__nv_bfloat16> nf;
   lrt::DevBuf<float> nt;
-  LRT_CUDA(ctx, nf.ensure(size_t(capacity) * 16));
+  LRT_CUDA(ctx, nf.ensure(size_t(lrt::feat_elems(capacity))));
   LRT_CUDA(ctx, nt.ensure(size_t(capacity)));
+  LRT_CUDA(ctx, cudaMemset(nf.p, 0, size_t(lrt::feat_elems(capacity)) * 2));   // padding rows of a tile stay zero
   if (p.n) {
-    LRT_CUDA(ctx, cudaMemcpy(nf.p, p.feat.p, size_t(p.n) * 32, cudaMemcpyDeviceToDevice));
+    LRT_CUDA(ctx, cudaMemcpy(nf.p, p.feat.p, size_t(lrt::feat_elems(p.n)) * 2, cudaMemcpyDeviceToDevice));
     LRT_CUDA(ctx, cudaMemcpy(nt.p, p.target.p, size_t(p.n) * 4, cudaMemcpyDeviceToDevice));
   }
   p.feat.release();
@@ -210,8 +211,9 @@ extern "C" lrt_status lrt_proposal_set_triples(lrt_ctx *ctx, const float *featur
   ProposalState &p = *ctx->prop;
   p.n = 0;
   if ((s = reserve(ctx, n)) != LRT_OK) return s;
-  std::vector<uint16_t> bf(size_t(n) * 16);
-  for (size_t i = 0; i < bf.size(); i++) bf[i] = lrt::f2bf(features[i]);
+  std::vector<uint16_t> bf(size_t(lrt::feat_elems(n)), 0);
+  for (uint64_t r = 0; r < n; r++)
+    for (uint32_t k = 0; k < 16; k++) bf[lrt::feat_u4(r, k >> 3) * 8 + (k & 7)] = lrt::f2bf(features[r * 16 + k]);
   LRT_CUDA(ctx, cudaSetDevice(ctx->device));
   LRT_CUDA(ctx, cudaMemcpy(p.feat.p, bf.data(), bf.size() * 2, cudaMemcpyHostToDevice));
   LRT_CUDA(ctx, cudaMemcpy(p.target.p, targets, size_t(n) * 4, cudaMemcpyHostToDevice));
@@ -224,10 +226,13 @@ extern "C" lrt_status lrt_proposal_get_triples(lrt_ctx *ctx, uint64_t first, uin
   if (!ctx || !ctx->prop || first + n > ctx->prop->n) return fail(ctx, LRT_ERR_INVALID, "triple range");
   ProposalState &p = *ctx->prop;
   LRT_CUDA(ctx, cudaSetDevice(ctx->device));
-  if (features) {
-    std::vector<uint16_t> bf(size_t(n) * 16);
-    LRT_CUDA(ctx, cudaMemcpy(bf.data(), p.feat.p + size_t(first) * 16, bf.size() * 2, cudaMemcpyDeviceToHost));
-    for (size_t i = 0; i < bf.size(); i++) features[i] = lrt::bf2f(bf[i]);
+  if (features && n) {
+    const uint64_t t0 = first >> 7, t1 = (first + n - 1) >> 7;   // the tiles holding the range
+    std::vector<uint16_t> bf(size_t(t1 - t0 + 1) * 2048);
+    LRT_CUDA(ctx, cudaMemcpy(bf.data(), p.feat.p + size_t(t0) * 2048, bf.size() * 2, cudaMemcpyDeviceToHost));
+    for (uint64_t i = 0; i < n; i++)
+      for (uint32_t k = 0; k < 16; k++)
+        features[i * 16 + k] = lrt::bf2f(bf[(lrt::feat_u4(first + i, k >> 3) - t0 * 256) * 8 + (k & 7)]);
   }
   if (targets) LRT_CUDA(ctx, cudaMemcpy(targets, p.target.p + first, size_t(n) * 4, cudaMemcpyDeviceToHost));
   return LRT_OK;
@@ -243,7 +248,7 @@ extern "C" lrt_status lrt_proposal_train(lrt_ctx *ctx, uint32_t first_step, uint
   LRT_CUDA(ctx, cudaSetDevice(ctx->device));
   LRT_CUDA(ctx, p.losses.ensure(steps));
   LRT_CUDA(ctx, cudaMemset(p.losses.p, 0, 4 * size_t(steps)));
-  const lrt::TripleView data{p.feat.p, p.target.p, p.n};
+  const lrt::TripleView data{p.feat.p, p.target.p, 0, p.n};
   for (uint32_t k = 0; k < steps; k++) {
     const lrt::MlpState m = lrt::mlp_state(p, p.losses.p + k);
     LRT_CUDA(ctx, lrt::launch_mlp_step(data, m, batch, first_step + k, seed, true, true, lr, 0.9f, 0.999f, 1e-8f,
@@ -263,7 +268,7 @@ extern "C" lrt_status lrt_proposal_gradient(lrt_ctx *ctx, uint32_t n, float *gra
   LRT_CUDA(ctx, p.losses.ensure(1));
   LRT_CUDA(ctx, cudaMemset(p.losses.p, 0, 4));
   LRT_CUDA(ctx, cudaMemset(p.grad.p, 0, 4 * LRT_MLP_PARAMS));
-  const lrt::TripleView data{p.feat.p, p.target.p, p.n};
+  const lrt::TripleView data{p.feat.p, p.target.p, 0, p.n};
   const lrt::MlpState m = lrt::mlp_state(p, p.losses.p);
   LRT_CUDA(ctx, lrt::launch_mlp_step(data, m, n, 0, 0, false, false, 0.0f, 0.9f, 0.999f, 1e-8f, nullptr));
   if (grad) LRT_CUDA(ctx, cudaMemcpy(grad, p.grad.p, 4 * LRT_MLP_PARAMS, cudaMemcpyDeviceToHost));
@@ -285,7 +290,7 @@ extern "C" lrt_status lrt_proposal_infer_ex(lrt_ctx *ctx, uint64_t first, uint64
   LRT_CUDA(ctx, d.ensure(size_t(n)));
   LRT_CUDA(ctx, status.ensure(1));
   LRT_CUDA(ctx, cudaMemset(status.p, 0, 4));
-  const lrt::TripleView data{p.feat.p + size_t(first) * 16, p.target.p + first, n};
+  const lrt::TripleView data{p.feat.p, p.target.p, first, n};
   cudaEvent_t ev[2] = {nullptr, nullptr};
   cudaError_t e = cudaSuccess;
   if (ms) {

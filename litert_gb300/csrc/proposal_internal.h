@@ -10,16 +10,29 @@
 namespace lrt {
 
 // Training triples: 16 bf16 features and the crossing fraction per sample.
+// Features are stored in tiles of 128 samples, 4 KB each: the 16-byte halves
+// holding features 0-7 of the tile's 128 samples, then the halves holding
+// features 8-15.  One 4 KB bulk copy of a tile is then the tcgen05 A operand
+// in the no-swizzle K-major layout (8-row x 16-byte core matrices, 16 bytes
+// between rows, 2 KB between the two K halves).  Index of a half in 16-byte
+// units:
+__host__ __device__ inline uint64_t feat_u4(uint64_t row, uint32_t half) {
+  return (row >> 7) * 256u + uint64_t(half) * 128u + (row & 127u);
+}
+// bf16 elements a store of n samples occupies (whole tiles)
+__host__ __device__ inline uint64_t feat_elems(uint64_t n) { return ((n + 127u) >> 7) * 2048u; }
+
 struct TripleBuf {
   __nv_bfloat16 *feat;
   float *target;
   unsigned long long *count;   // samples written (may exceed capacity: extra ones are dropped)
   unsigned long long capacity;
 };
+// Samples [first, first + n) of a store (feat and target point at the store's start).
 struct TripleView {
   const __nv_bfloat16 *feat;
   const float *target;
-  uint64_t n;
+  uint64_t first, n;
 };
 
 // Network parameters and optimiser state (device).

@@ -72,6 +72,23 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *mbar, uint32_t phase) {
       : "memory");
   return ok != 0;
 }
+__device__ __forceinline__ void mbar_arrive(uint64_t *mbar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(mbar)) : "memory");
+}
+// arrive and announce `bytes` of asynchronous copies that will complete on this barrier
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(mbar)), "r"(bytes) : "memory");
+}
+// barrier initialisation made visible to the asynchronous proxy (bulk copies, tcgen05)
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+// one-dimensional bulk copy global -> shared (both 16-byte aligned, size a multiple
+// of 16), completing `bytes` on the barrier
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *mbar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(mbar))
+               : "memory");
+}
 // bounded wait: false after `limit` polls (the caller records the timeout)
 __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t phase, uint32_t limit) {
   for (uint32_t i = 0; i < limit; i++)
@@ -99,6 +116,14 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float v[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
   for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// one column (this warp's 32 lanes)
+__device__ __forceinline__ float tmem_ld1(uint32_t taddr) {
+  uint32_t r;
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];" : "=r"(r) : "r"(taddr) : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+  return __uint_as_float(r);
 }
 
 // the same for 16 consecutive columns

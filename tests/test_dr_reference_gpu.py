@@ -41,7 +41,7 @@ def test_engine_optimize_matches_reference_run(name):
         assert np.array_equal(R.bvh2(), np.ascontiguousarray(pairs).view(np.uint8).reshape(-1))
         for it in range(case["iterations"]):
             R.step(it)
-        g = R.getLastdLoss_dS()
+        g = R.getLastdLoss_dS() / np.float32(len(views))   # LRT_DR_GRAD is taken before the batch division
         p = R.get(dr.GET_PARAMS)
         got = np.stack([R.getLastImage(k) for k in range(len(views))])
     finally:
