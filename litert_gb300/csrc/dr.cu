@@ -119,6 +119,19 @@ struct Relax {
   float3 color, normal;    // missed_hit.color, .normal
   uint32_t idx[8];         // missed_indices
   float dth[8];            // missed_dSDF_dtheta
+  // Early skipping (border integral only).  A border sample contributes only when
+  // its final sdf is below relax_eps, so a voxel whose corner values all exceed
+  // min(sdf, skip_t) + margin may be skipped before the walk has met a local
+  // minimum (skip_t = relax_eps; +inf restores the reference's walk exactly).
+  // The two walks agree from the first update below skip_t on, and no value below
+  // skip_t exists in one walk only, except through the events recorded in flags:
+  // bit 0, a voxel-entry update (check_vox_border) or the final candidate that
+  // could reach below skip_t while the walks may still differ; bit 1, the
+  // record's indices / dSDF/dtheta / colour / normal were written after sdf fell
+  // below skip_t.  The caller re-walks with skip_t = +inf unless bit 0 is clear
+  // and either sdf >= skip_t or bit 1 is set.
+  float skip_t;
+  uint32_t flags;
 };
 
 // BVHDR::Intersect, NEWTON branch (diff_render/BVH2DR.cpp:623-1073).  Returns t in
@@ -195,6 +208,7 @@ __device__ float intersect(const float values[8], float d, float qFar, float3 st
       t_min = -c / b;
     }
     const float sdf_min = (c0 + t_min * (c1 + t_min * (c2 + t_min * c3)));
+    if (c1 <= 0 && sdf0 < 0.f && -sdf0 * d < rl->skip_t && rl->sdf >= rl->skip_t) rl->flags |= 1u;
     if (rl->cvb == 1) {
       if (c1 <= 0) {
         if (sdf0 < 0.f && -sdf0 * d < rl->sdf) { rl->t = t0; rl->sdf = -sdf0 * d; }
@@ -315,7 +329,7 @@ __device__ bool brick_visit(const DevScene &s, uint32_t node, float3 pos, float3
   if (!(bnf.x < bnf.y)) return false;
   {
     const float2 bb = __ldg(&s.brick_bounds[node]);   // min v, max |v| over the brick
-    const float thr = (BORDER ? rl->sdf : 0.0f) + skip_margin(bb.y);
+    const float thr = (BORDER ? fminf(rl->sdf, rl->skip_t) : 0.0f) + skip_margin(bb.y);
     if (bb.x > thr) {
       if (!BORDER) return false;
       // border mode: the walk would call Intersect at least once if its first voxel does
@@ -344,7 +358,7 @@ __device__ bool brick_visit(const DevScene &s, uint32_t node, float3 pos, float3
     float vmin = values[0], vmax = fabsf(values[0]);
 #pragma unroll
     for (int i = 1; i < 8; i++) { vmin = fminf(vmin, values[i]); vmax = fmaxf(vmax, fabsf(values[i])); }
-    if (tNear < fnf.x && vmin > (BORDER ? rl->sdf : 0.0f) + skip_margin(vmax)) {
+    if (tNear < fnf.x && vmin > (BORDER ? fminf(rl->sdf, rl->skip_t) : 0.0f) + skip_margin(vmax)) {
       skipped_intersect<BORDER>(rl);
     } else if (tNear < fnf.x) {
       const float3 start_q = scr(sub(add(pos, scl(fnf.x, dir)), min_pos), B.scale);
@@ -375,6 +389,7 @@ __device__ bool brick_visit(const DevScene &s, uint32_t node, float3 pos, float3
             rl->color = tri3(cols, dp_ast);
             rl->normal = divs(g, gl);
             load_idx(s, B.data_offset, vox, rl->idx);
+            if (rl->sdf < rl->skip_t) rl->flags |= 2u;
           }
         }
       }
@@ -443,10 +458,12 @@ __device__ void traverse(const DevScene &s, float3 pos, float3 dir, float tNear,
 // RayQuery_NearestHitWithGrad (:12-102): TLAS leaf box of the single instance,
 // ray to object space, BLAS traversal, candidate merge of the relaxation point
 template <bool BORDER>
-__device__ void query(const DevScene &s, float3 P, float3 D, float tfar, HitRec &hr, Relax *rl) {
+__device__ void query(const DevScene &s, float3 P, float3 D, float tfar, HitRec &hr, Relax *rl,
+                      float skip_t = __builtin_huge_valf()) {
   hr.t = tfar;
   hr.prim = kNoIndex;
   if (BORDER) {
+    rl->skip_t = skip_t; rl->flags = 0;
     rl->t = tfar; rl->sdf = 1000.0f; rl->cvb = 1;
     rl->ct = tfar; rl->csdf = 1000.0f;
     rl->color = f3(0, 0, 0); rl->normal = f3(1, 0, 0);
@@ -462,8 +479,22 @@ __device__ void query(const DevScene &s, float3 P, float3 D, float tfar, HitRec 
     traverse<BORDER>(s, hr.pos, hr.dir, 0.0f, hr, rl);
   }
   if (BORDER && rl->csdf < rl->sdf) {   // missed_hit = missed_hit_candidate (whole struct)
+    if (rl->csdf < rl->skip_t && rl->sdf >= rl->skip_t) rl->flags |= 1u;
     rl->t = rl->ct; rl->sdf = rl->csdf; rl->cvb = 1;
     rl->color = f3(0, 0, 0); rl->normal = f3(1, 0, 0);
+  }
+}
+
+// A border sample's query: the walk with early skipping below relax_eps, and the
+// reference's own walk again where the skipping could have changed the record
+// (Relax::flags); the record is the reference walk's in either case.
+__device__ __forceinline__ void border_query(const DevScene &s, float3 P, float3 D, float eps, HitRec &hr, Relax &rl) {
+  float skip_t = eps;
+#pragma unroll 1
+  for (int pass = 0; pass < 2; pass++) {
+    query<true>(s, P, D, 1e9f, hr, &rl, skip_t);
+    if (!(rl.flags & 1u) && !(rl.sdf < eps && !(rl.flags & 2u))) break;
+    skip_t = __builtin_huge_valf();
   }
 }
 
@@ -1141,14 +1172,14 @@ __global__ void __launch_bounds__(128, 4) dr_border_kernel(DevScene s, DevPreset
           }
           if (d.x > 0 && d.x < 1 && d.y > 0 && d.y < 1) {
             eye_ray(x, y, W, H, d.x, d.y, v.proj_inv, v.wv_inv, P, D);
-            query<true>(s, P, D, 1e9f, hr, &rl);
+            border_query(s, P, D, p.relax_eps, hr, rl);
             br = rl.sdf < p.relax_eps;
           }
         }
       } else if (sid < p.border_spp) {
         const float2 d = rand2(x, y, sid, p.seed);
         eye_ray(x, y, W, H, d.x, d.y, v.proj_inv, v.wv_inv, P, D);
-        query<true>(s, P, D, 1e9f, hr, &rl);
+        border_query(s, P, D, p.relax_eps, hr, rl);
         br = rl.sdf < p.relax_eps;
       }
       float cd[4] = {0, 0, 0, 0};

@@ -421,38 +421,54 @@ __device__ void brick_intersect(const DevScene &s, float3 ray_pos, float3 ray_di
   const uint32_t max_steps = 8u * bsz + 16u;
   const GlobalLoader gl(s, nd.z, sz_inv);
   const SharedLoader sl{staged, v_size, h.brick_pad};
-  for (uint32_t step = 0; bnf.x < bnf.y && hit.t == old_t && step < max_steps; step++) {
-    const float3 hit_pos = add(ray_pos, scl(bnf.x, ray_dir));
-    const float3 local_pos = scr(sub(hit_pos, bmin), scale);
-    const float3 vp = f3(floorf(fmn(fmx(local_pos.x, 1e-6f), bs - 1e-6f)), floorf(fmn(fmx(local_pos.y, 1e-6f), bs - 1e-6f)),
-                         floorf(fmn(fmx(local_pos.z, 1e-6f), bs - 1e-6f)));
-    const float3 min_pos = add(bmin, scl(d, vp));
-    // exit distance: far plane per axis (max_pos = min_pos + d*1)
-    const float fx = inv.x * ((posx ? min_pos.x + d : min_pos.x) - ray_pos.x);
-    const float fy = inv.y * ((posy ? min_pos.y + d : min_pos.y) - ray_pos.y);
-    const float fz = inv.z * ((posz ? min_pos.z + d : min_pos.z) - ray_pos.z);
-    const float exit_t = fmn(fmn(fx, fy), fz);
-    const uint32_t vid = (uint32_t(vp.x) * bsz + uint32_t(vp.y)) * bsz + uint32_t(vp.z);
-    if (COUNT) cnt.voxels++;
-    if ((__ldg(&occ[vid >> 5]) >> (vid & 31u)) & 1u) {
-      const float nx = inv.x * ((posx ? min_pos.x : min_pos.x + d) - ray_pos.x);
-      const float ny = inv.y * ((posy ? min_pos.y : min_pos.y + d) - ray_pos.y);
-      const float nz = inv.z * ((posz ? min_pos.z : min_pos.z + d) - ray_pos.z);
-      const float2 fnf = make_float2(fmx(fmx(nx, ny), nz), exit_t);
-      if (tNear < fnf.x) {
-        float vmin;
-        if (STAGED) vmin = sl.load(vp, values);
-        else vmin = gl.load(vp, values);
-        if (vmin <= 0.0f) {
-          const float3 start_pos = add(ray_pos, scl(fnf.x, ray_dir));
-          const float3 start_q = scr(sub(start_pos, min_pos), scale);
-          const float qFar = (fnf.y - fnf.x) * scale;
-          local_surface<COUNT, MODE>(pr, s, type, ray_dir, values, brick, d, 0.0f, qFar, fnf, start_q, hit, cnt);
-          if ((FEAT & 1) && hit.t != old_t)
-            smooth_normal(s, brick, vp, start_q, fnf.x, d, ray_dir, v_size, hit);
+  // Two nested loops: the inner one steps through voxels until one needs the
+  // finder (occupied, entered after tNear, some corner value <= 0) or the brick
+  // ends; the finder runs after it.  A lane's sequence of voxels and finder calls
+  // is the single loop's, but the lanes of a warp that reach a candidate voxel
+  // after different numbers of steps run the finder together.
+  uint32_t step = 0;
+  while (hit.t == old_t) {
+    bool cand = false;
+    float3 vp, min_pos;
+    float2 fnf;
+    float exit_t;
+    while (bnf.x < bnf.y && step < max_steps) {
+      const float3 hit_pos = add(ray_pos, scl(bnf.x, ray_dir));
+      const float3 local_pos = scr(sub(hit_pos, bmin), scale);
+      vp = f3(floorf(fmn(fmx(local_pos.x, 1e-6f), bs - 1e-6f)), floorf(fmn(fmx(local_pos.y, 1e-6f), bs - 1e-6f)),
+              floorf(fmn(fmx(local_pos.z, 1e-6f), bs - 1e-6f)));
+      min_pos = add(bmin, scl(d, vp));
+      // exit distance: far plane per axis (max_pos = min_pos + d*1)
+      const float fx = inv.x * ((posx ? min_pos.x + d : min_pos.x) - ray_pos.x);
+      const float fy = inv.y * ((posy ? min_pos.y + d : min_pos.y) - ray_pos.y);
+      const float fz = inv.z * ((posz ? min_pos.z + d : min_pos.z) - ray_pos.z);
+      exit_t = fmn(fmn(fx, fy), fz);
+      const uint32_t vid = (uint32_t(vp.x) * bsz + uint32_t(vp.y)) * bsz + uint32_t(vp.z);
+      step++;
+      if (COUNT) cnt.voxels++;
+      if ((__ldg(&occ[vid >> 5]) >> (vid & 31u)) & 1u) {
+        const float nx = inv.x * ((posx ? min_pos.x : min_pos.x + d) - ray_pos.x);
+        const float ny = inv.y * ((posy ? min_pos.y : min_pos.y + d) - ray_pos.y);
+        const float nz = inv.z * ((posz ? min_pos.z : min_pos.z + d) - ray_pos.z);
+        fnf = make_float2(fmx(fmx(nx, ny), nz), exit_t);
+        if (tNear < fnf.x) {
+          float vmin;
+          if (STAGED) vmin = sl.load(vp, values);
+          else vmin = gl.load(vp, values);
+          if (vmin <= 0.0f) {
+            cand = true;
+            break;
+          }
         }
       }
+      bnf.x += fmx(0.0f, exit_t - bnf.x) + 1e-6f;
     }
+    if (!cand) break;
+    const float3 start_pos = add(ray_pos, scl(fnf.x, ray_dir));
+    const float3 start_q = scr(sub(start_pos, min_pos), scale);
+    const float qFar = (fnf.y - fnf.x) * scale;
+    local_surface<COUNT, MODE>(pr, s, type, ray_dir, values, brick, d, 0.0f, qFar, fnf, start_q, hit, cnt);
+    if ((FEAT & 1) && hit.t != old_t) smooth_normal(s, brick, vp, start_q, fnf.x, d, ray_dir, v_size, hit);
     bnf.x += fmx(0.0f, exit_t - bnf.x) + 1e-6f;
   }
   if ((FEAT & 2) && hit.t < old_t && (h.aux_data & 0xFF000000u) != LRT_SBS_LAYOUT_DX &&

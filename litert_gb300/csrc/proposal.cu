@@ -386,34 +386,40 @@ __global__ void __launch_bounds__(128) mlp_infer_kernel(TripleView data, MlpStat
 
 // ---------------------------------------------------------------- 128-sample tiles on tcgen05
 // The network on the fifth-generation tensor cores, warp-specialised and
-// pipelined.  A persistent CTA of six warps walks the 128-sample tiles of the
-// store that hold the requested window:
+// pipelined.  A persistent CTA of ten warps walks the 128-sample tiles of the
+// store that hold the requested window, up to four tiles in flight (one TMEM
+// accumulator of 32 columns each, tile j in accumulator j % 4):
 //   warp 0 (one thread)  loads each tile's 4 KB of features with one bulk copy
 //                        (cp.async.bulk) into a ring of four shared-memory
 //                        stages -- the store's tile layout is the MMA's
 //                        operand layout -- completing on the stage's mbarrier;
-//   warp 1 (one thread)  issues each layer's tcgen05.mma (M = 128, N = 32/32/16,
-//                        K = 16 per instruction) into one of two TMEM
-//                        accumulators (tiles alternate), committing each layer
-//                        to an mbarrier; layer 1 of tile j+1 is issued before
-//                        layers 2 and 3 of tile j, so the tensor core works on
-//                        one tile while the epilogue warps finish the other;
-//   warps 2-5            the epilogue: each reads its 32 TMEM lanes, adds the
-//                        bias, applies ReLU and BF16 rounding (one
-//                        cvt.rn.relu.bf16x2.f32 per pair) into the next layer's
-//                        A operand in shared memory, and after layer 3 writes
-//                        column 0 plus the output bias.
+//   warp 1 (one thread)  issues the tcgen05.mma of every layer (M = 128,
+//                        N = 32/32/16, K = 16 per instruction), committing each
+//                        to an mbarrier.  It polls its inputs without blocking
+//                        and issues whatever is ready -- layer 3 of the oldest
+//                        tile, layer 2 of the next, layer 1 of a newly loaded
+//                        one -- so that no tile waits behind another's epilogue;
+//   warps 2-9            the epilogue, two groups of four warps (even and odd
+//                        tiles) working on two tiles at once: each warp reads its
+//                        32 TMEM lanes, adds the bias, applies ReLU and BF16
+//                        rounding (one cvt.rn.relu.bf16x2.f32 per pair) into the
+//                        next layer's A operand in the tile's shared-memory
+//                        buffer, and after layer 3 writes column 0 plus the
+//                        output bias.
 // Every hand-off is an mbarrier (no CTA barrier inside the loop).  The weights
 // are staged once per CTA in the canonical K-major layout.  Waits are bounded by
-// `wait_limit` polls: a timeout sets status bit 1 and makes the role leave its
-// loop; the others run out the same way, then the MMA thread waits (at most
-// kTcWait polls) for everything it issued, the loader for every copy it
-// started, and the TMEM is freed.
+// `wait_limit` polls (the MMA thread counts polls without progress): a timeout
+// sets status bit 1 and makes the role leave its loop; the others run out the
+// same way, then the MMA thread waits (at most kTcWait polls) for everything it
+// issued, the loader for every copy it started, and the TMEM is freed.
 constexpr uint32_t kTcLbo = 128;         // adjacent core matrices along K (weights, hidden operands)
-constexpr uint32_t kTcWait = 1u << 22;   // mbarrier polls of the final drain (and the default per-layer limit)
-constexpr int kTcStages = 4;
-constexpr int kTcThreads = 192;
-constexpr int kTcBlocksPerSm = 4;
+constexpr uint32_t kTcWait = 1u << 22;   // mbarrier polls of the final drain (and the default limit)
+constexpr int kTcStages = 4;             // feature tiles in shared memory
+constexpr int kTcAcc = 4;                // tiles in flight (TMEM accumulators, hidden buffers)
+constexpr int kTcThreads = 320;
+constexpr int kTcBlocksPerSm = 4;        // 4 x 128 TMEM columns
+constexpr uint32_t kTcHidBytes = 128 * kHid * 2;
+constexpr uint32_t kTcDynSmem = kTcStages * 4096 + kTcAcc * kTcHidBytes;
 
 // bias + ReLU + BF16 of one 32-wide accumulator row (this lane's TMEM lane, read in
 // two 16-column halves to keep registers low) into the A operand of the next layer
@@ -437,8 +443,9 @@ __device__ __forceinline__ void hidden_to_smem(uint32_t trow, const float *bias,
 __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) mlp_infer_tc_kernel(TripleView data, MlpState m,
                                                                                   float *out, unsigned int *status,
                                                                                   uint32_t wait_limit) {
-  __shared__ __align__(128) uint8_t sX[kTcStages][4096];
-  __shared__ __align__(128) uint8_t sH[2][128 * kHid * 2];
+  extern __shared__ __align__(128) uint8_t tc_dyn[];
+  uint8_t *const sX = tc_dyn;                           // kTcStages x 4 KB feature tiles
+  uint8_t *const sH = tc_dyn + kTcStages * 4096;        // kTcAcc x hidden operand
   __shared__ __align__(128) uint8_t sW1[kHid * kIn * 2];
   __shared__ __align__(128) uint8_t sW2[kHid * kHid * 2];
   __shared__ __align__(128) uint8_t sW3[16 * kHid * 2];
@@ -446,7 +453,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) mlp_infer_tc_kerne
   __shared__ __align__(16) float sb2[kHid];
   __shared__ float sb3;
   __shared__ __align__(8) uint64_t full[kTcStages], empty[kTcStages];
-  __shared__ __align__(8) uint64_t l1[2], l2[2], l3[2], h1[2], h2[2], afree[2], fin;
+  __shared__ __align__(8) uint64_t l1[kTcAcc], l2[kTcAcc], l3[kTcAcc], h1[kTcAcc], h2[kTcAcc], afree[kTcAcc], fin;
   __shared__ uint32_t tmem_slot, s_consumed;
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
   const uint64_t t_first = data.first >> 7;
@@ -470,7 +477,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) mlp_infer_tc_kerne
       tc05::mbar_init(&full[i], 1);
       tc05::mbar_init(&empty[i], 1);
     }
-    for (int a = 0; a < 2; a++) {
+    for (int a = 0; a < kTcAcc; a++) {
       tc05::mbar_init(&l1[a], 1);
       tc05::mbar_init(&l2[a], 1);
       tc05::mbar_init(&l3[a], 1);
@@ -482,7 +489,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) mlp_infer_tc_kerne
     s_consumed = 0;
     tc05::fence_mbar_init();
   }
-  if (warp == 0) tc05::tmem_alloc(&tmem_slot, 64);
+  if (warp == 0) tc05::tmem_alloc(&tmem_slot, 32 * kTcAcc);
   tc05::fence_proxy_async();
   tc05::fence_before_sync();
   __syncthreads();
@@ -501,69 +508,87 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) mlp_infer_tc_kerne
           break;
         }
         tc05::mbar_arrive_expect_tx(&full[st], 4096);
-        tc05::bulk_g2s(sX[st], data.feat + tile_of(j) * 2048, 4096, &full[st]);
+        tc05::bulk_g2s(sX + st * 4096, data.feat + tile_of(j) * 2048, 4096, &full[st]);
         issued = j + 1;
       }
     }
   } else if (warp == 1) {
-    // ---- MMA issuer
+    // ---- MMA issuer: n1 / n2 / n3 tiles have had layer 1 / 2 / 3 issued
     if (lane == 0) {
       constexpr uint32_t kId32 = tc05::idesc_bf16_f32(128, 32), kId16 = tc05::idesc_bf16_f32(128, 16);
-      const uint32_t aH[2] = {tc05::smem_addr(sH[0]), tc05::smem_addr(sH[1])};
+      const uint32_t aX = tc05::smem_addr(sX), aH = tc05::smem_addr(sH);
       const uint32_t aW1 = tc05::smem_addr(sW1), aW2 = tc05::smem_addr(sW2), aW3 = tc05::smem_addr(sW3);
-      uint32_t consumed = 0;
+      uint32_t n1 = 0, n2 = 0, n3 = 0, idle = 0;
       bool ok = true;
-      for (uint32_t j = 0; ok && j <= my_tiles; j++) {
-        if (j < my_tiles) {   // layer 1 of tile j
-          const uint32_t a = j & 1u, st = j % kTcStages;
-          if (j >= 2 && !tc05::mbar_wait(&afree[a], ((j >> 1) - 1) & 1u, wait_limit)) { ok = false; break; }
-          if (!tc05::mbar_wait(&full[st], (j / kTcStages) & 1u, wait_limit)) { ok = false; break; }
-          tc05::fence_after_sync();
-          tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(tc05::smem_addr(sX[st]), 2048, 128),
-                         tc05::smem_desc(aW1, kTcLbo, 256), kId32, false);
-          tc05::mma_commit(&l1[a]);
-          tc05::mma_commit(&empty[st]);   // the stage is free once layer 1 has read it
-          consumed = j + 1;
+      while (n3 < my_tiles) {
+        bool prog = false;
+        if (n3 < n2) {   // layer 3 of the oldest tile, once its second hidden layer is in shared memory
+          const uint32_t a = n3 % kTcAcc;
+          if (tc05::mbar_test(&h2[a], (n3 / kTcAcc) & 1u)) {
+            tc05::fence_after_sync();
+            const uint32_t h = aH + a * kTcHidBytes;
+            tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(h, kTcLbo, 512), tc05::smem_desc(aW3, kTcLbo, 512), kId16,
+                           false);
+            tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(h + 2 * kTcLbo, kTcLbo, 512),
+                           tc05::smem_desc(aW3 + 2 * kTcLbo, kTcLbo, 512), kId16, true);
+            tc05::mma_commit(&l3[a]);
+            n3++;
+            prog = true;
+          }
         }
-        if (j >= 1) {         // layers 2 and 3 of tile j - 1
-          const uint32_t jj = j - 1, a = jj & 1u, ph = (jj >> 1) & 1u;
-          if (!tc05::mbar_wait(&h1[a], ph, wait_limit)) { ok = false; break; }
-          tc05::fence_after_sync();
-          tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(aH[a], kTcLbo, 512), tc05::smem_desc(aW2, kTcLbo, 512), kId32,
-                         false);
-          tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(aH[a] + 2 * kTcLbo, kTcLbo, 512),
-                         tc05::smem_desc(aW2 + 2 * kTcLbo, kTcLbo, 512), kId32, true);
-          tc05::mma_commit(&l2[a]);
-          if (!tc05::mbar_wait(&h2[a], ph, wait_limit)) { ok = false; break; }
-          tc05::fence_after_sync();
-          tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(aH[a], kTcLbo, 512), tc05::smem_desc(aW3, kTcLbo, 512), kId16,
-                         false);
-          tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(aH[a] + 2 * kTcLbo, kTcLbo, 512),
-                         tc05::smem_desc(aW3 + 2 * kTcLbo, kTcLbo, 512), kId16, true);
-          tc05::mma_commit(&l3[a]);
+        if (n2 < n1) {   // layer 2, once the first hidden layer is in shared memory
+          const uint32_t a = n2 % kTcAcc;
+          if (tc05::mbar_test(&h1[a], (n2 / kTcAcc) & 1u)) {
+            tc05::fence_after_sync();
+            const uint32_t h = aH + a * kTcHidBytes;
+            tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(h, kTcLbo, 512), tc05::smem_desc(aW2, kTcLbo, 512), kId32,
+                           false);
+            tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(h + 2 * kTcLbo, kTcLbo, 512),
+                           tc05::smem_desc(aW2 + 2 * kTcLbo, kTcLbo, 512), kId32, true);
+            tc05::mma_commit(&l2[a]);
+            n2++;
+            prog = true;
+          }
         }
+        if (n1 < my_tiles) {   // layer 1 of a loaded tile, once its accumulator is free
+          const uint32_t a = n1 % kTcAcc, st = n1 % kTcStages;
+          const bool acc_free = n1 < uint32_t(kTcAcc) || tc05::mbar_test(&afree[a], ((n1 / kTcAcc) - 1) & 1u);
+          if (acc_free && tc05::mbar_test(&full[st], (n1 / kTcStages) & 1u)) {
+            tc05::fence_after_sync();
+            tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(aX + st * 4096, 2048, 128),
+                           tc05::smem_desc(aW1, kTcLbo, 256), kId32, false);
+            tc05::mma_commit(&l1[a]);
+            tc05::mma_commit(&empty[st]);   // the stage is free once layer 1 has read it
+            n1++;
+            prog = true;
+          }
+        }
+        if (prog) idle = 0;
+        else if (++idle >= wait_limit) { ok = false; break; }
       }
       if (!ok) atomicOr(status, 2u);
       // every MMA this thread issued has completed before the TMEM is freed
       tc05::mma_commit(&fin);
       if (!tc05::mbar_wait(&fin, 0, kTcWait)) atomicOr(status, 2u);
-      s_consumed = consumed;
+      s_consumed = n1;
     }
   } else {
-    // ---- epilogue: warp w reads TMEM lanes 32 * (w % 4) .. + 31 (rows of the tile)
-    const uint32_t q = warp & 3u, row = 32u * q + lane, trow = tbase + ((32u * q) << 16);
-    for (uint32_t j = 0; j < my_tiles; j++) {
-      const uint32_t a = j & 1u, ph = (j >> 1) & 1u;
+    // ---- epilogue: group g takes tiles g, g + 2, ...; warp w reads TMEM lanes
+    // 32 * (w % 4) .. + 31 (rows of the tile)
+    const uint32_t g = (warp - 2) >> 2, q = warp & 3u, row = 32u * q + lane, trow = tbase + ((32u * q) << 16);
+    for (uint32_t j = g; j < my_tiles; j += 2) {
+      const uint32_t a = j % kTcAcc, ph = (j / kTcAcc) & 1u;
+      uint8_t *const hb = sH + a * kTcHidBytes;
       if (!tc05::mbar_wait(&l1[a], ph, wait_limit)) { atomicOr(status, 2u); break; }
       tc05::fence_after_sync();
-      hidden_to_smem(trow + a * 32u, sb1, sH[a], row);
+      hidden_to_smem(trow + a * 32u, sb1, hb, row);
       tc05::fence_proxy_async();
       tc05::fence_before_sync();
       __syncwarp();
       if (lane == 0) tc05::mbar_arrive(&h1[a]);
       if (!tc05::mbar_wait(&l2[a], ph, wait_limit)) { atomicOr(status, 2u); break; }
       tc05::fence_after_sync();
-      hidden_to_smem(trow + a * 32u, sb2, sH[a], row);
+      hidden_to_smem(trow + a * 32u, sb2, hb, row);
       tc05::fence_proxy_async();
       tc05::fence_before_sync();
       __syncwarp();
@@ -571,8 +596,8 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) mlp_infer_tc_kerne
       if (!tc05::mbar_wait(&l3[a], ph, wait_limit)) { atomicOr(status, 2u); break; }
       tc05::fence_after_sync();
       const float y = tc05::tmem_ld1(trow + a * 32u);
-      const uint64_t g = tile_of(j) * 128 + row;
-      if (g >= data.first && g < data.first + data.n) out[g - data.first] = y + sb3;
+      const uint64_t gi = tile_of(j) * 128 + row;
+      if (gi >= data.first && gi < data.first + data.n) out[gi - data.first] = y + sb3;
       tc05::fence_before_sync();
       __syncwarp();
       if (lane == 0) tc05::mbar_arrive(&afree[a]);
@@ -586,7 +611,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) mlp_infer_tc_kerne
   tc05::fence_before_sync();
   __syncthreads();
   tc05::fence_after_sync();
-  if (warp == 0) tc05::tmem_dealloc(tbase, 64);
+  if (warp == 0) tc05::tmem_dealloc(tbase, 32 * kTcAcc);
 }
 
 // ---------------------------------------------------------------- render with the proposal
@@ -738,7 +763,10 @@ cudaError_t launch_mlp_infer_tc(const TripleView &data, const MlpState &m, float
   const uint64_t tiles = ((data.first + data.n - 1) >> 7) - (data.first >> 7) + 1;
   uint64_t blocks = uint64_t(sms) * dev::kTcBlocksPerSm;
   if (blocks > tiles) blocks = tiles;
-  dev::mlp_infer_tc_kernel<<<unsigned(blocks), dev::kTcThreads, 0, st>>>(data, m, out, status, wait_limit);
+  e = cudaFuncSetAttribute(dev::mlp_infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(dev::kTcDynSmem));
+  if (e != cudaSuccess) return e;
+  dev::mlp_infer_tc_kernel<<<unsigned(blocks), dev::kTcThreads, dev::kTcDynSmem, st>>>(data, m, out, status,
+                                                                                        wait_limit);
   return cudaGetLastError();
 }
 
