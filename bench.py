@@ -382,6 +382,13 @@ def run_proposal(args, scene, dev, torch):
 
     def per_step(d):
         return {k: v // reps for k, v in d.items()}
+    # per-ray work of the plain walk (lrt_render_counters) and what the proposal removes from it
+    cnt = scene.render_counters(eval_views).astype(np.float64) / n
+    counters = {"plain_per_ray": {"nodes": cnt[0], "bricks": cnt[1], "voxel_steps": cnt[2], "finder_calls": cnt[3]},
+                "proposal_per_ray": {"bricks_proposed": st["proposals"] / reps / n, "jumps": st["jumps"] / reps / n,
+                                     "voxel_steps_skipped": st["steps_skipped"] / reps / n,
+                                     "voxel_steps": cnt[2] - st["steps_skipped"] / reps / n,
+                                     "finder_calls": cnt[3]}}
     a, b = recs["plain"], recs["proposal"]
     mask_same = np.array_equal(a[:, 1] != lrt.MISS, b[:, 1] != lrt.MISS)
     both = (a[:, 1] != lrt.MISS) & (b[:, 1] != lrt.MISS)
@@ -395,6 +402,7 @@ def run_proposal(args, scene, dev, torch):
             "proposals_per_step": st["proposals"] // max(1, len(ts)), "acceptance": st["jumps"] / max(1, st["proposals"]),
             "jump_hit_rate": st["jump_hits"] / max(1, st["jumps"]),
             "trained": per_step(stats["proposal"]), "untrained": per_step(stats["untrained"]),
+            "counters": counters,
             "untrained_mrays": out["untrained"]["mrays"],
             "untrained_records_identical": bool(np.array_equal(recs["plain"], recs["untrained"])),
             "triples": int(n_trip), "train_steps": args.prop_steps, "batch": 8192,

@@ -123,13 +123,27 @@ struct Relax {
   // its final sdf is below relax_eps, so a voxel whose corner values all exceed
   // min(sdf, skip_t) + margin may be skipped before the walk has met a local
   // minimum (skip_t = relax_eps; +inf restores the reference's walk exactly).
-  // The two walks agree from the first update below skip_t on, and no value below
-  // skip_t exists in one walk only, except through the events recorded in flags:
-  // bit 0, a voxel-entry update (check_vox_border) or the final candidate that
-  // could reach below skip_t while the walks may still differ; bit 1, the
-  // record's indices / dSDF/dtheta / colour / normal were written after sdf fell
-  // below skip_t.  The caller re-walks with skip_t = +inf unless bit 0 is clear
-  // and either sdf >= skip_t or bit 1 is set.
+  // The skipped voxels hold no value below skip_t, so until the first update
+  // below skip_t both walks' running minima are >= skip_t, an update below skip_t
+  // from a voxel's interior or exit happens in both walks alike, and from then on
+  // the walks are in the same state.  What can differ is a voxel-entry update
+  // (check_vox_border), which depends on the previous voxel's outcome.  flags:
+  //   bit 0  re-walk needed: an entry update below skip_t while the two walks'
+  //          check_vox_border may differ, or a final candidate below skip_t while
+  //          the running minimum is not;
+  //   bit 1  the record's indices / dSDF/dtheta / colour / normal were written
+  //          after sdf fell below skip_t (else they may be an older voxel's);
+  //   bit 2  no voxel of the current brick has been intersected or skipped yet;
+  //   bit 3  the walks have diverged (a voxel was skipped that only skip_t skips);
+  //   bit 4  check_vox_border may differ between the walks.  It cannot after a
+  //          voxel both walks intersected whose exit is inside the surface,
+  //          below skip_t, or with the distance still falling there; inside a
+  //          brick the next voxel's entry value is that face's value up to
+  //          rounding, so after a skipped voxel or an exit above skip_t it lies
+  //          above skip_t - margin: bit 0 is set only at a brick's first voxel or
+  //          for an entry value within the margin below skip_t.
+  // The caller re-walks with skip_t = +inf unless bit 0 is clear and either
+  // sdf >= skip_t or bit 1 is set.
   float skip_t;
   uint32_t flags;
 };
@@ -137,7 +151,8 @@ struct Relax {
 // BVHDR::Intersect, NEWTON branch (diff_render/BVH2DR.cpp:623-1073).  Returns t in
 // voxel units on a hit, else qFar + 1e-6.
 template <bool BORDER>
-__device__ float intersect(const float values[8], float d, float qFar, float3 start_q, float3 dir, Relax *rl) {
+__device__ float intersect(const float values[8], float d, float qFar, float3 start_q, float3 dir, Relax *rl,
+                          float band = 0.0f) {
   const float EPS = 1e-6f, SDF_EPS = 1e-7f;
   const float d_inv = 1.0f / d;
   float t = 0.0f;
@@ -208,7 +223,10 @@ __device__ float intersect(const float values[8], float d, float qFar, float3 st
       t_min = -c / b;
     }
     const float sdf_min = (c0 + t_min * (c1 + t_min * (c2 + t_min * c3)));
-    if (c1 <= 0 && sdf0 < 0.f && -sdf0 * d < rl->skip_t && rl->sdf >= rl->skip_t) rl->flags |= 1u;
+    if ((rl->flags & 16u) && c1 <= 0 && sdf0 < 0.f && rl->sdf >= rl->skip_t) {
+      const float v = -sdf0 * d;
+      if (v < rl->skip_t && ((rl->flags & 4u) || v >= rl->skip_t - band)) rl->flags |= 1u;
+    }
     if (rl->cvb == 1) {
       if (c1 <= 0) {
         if (sdf0 < 0.f && -sdf0 * d < rl->sdf) { rl->t = t0; rl->sdf = -sdf0 * d; }
@@ -219,11 +237,16 @@ __device__ float intersect(const float values[8], float d, float qFar, float3 st
       rl->t = t_min;
       rl->sdf = -sdf_min * d;
     }
-    if (sdf3 < 0.f && -sdf3 * d < rl->sdf && (c1 + qFar * (2 * c2 + qFar * 3 * c3)) >= 0.f) {
+    const float dexit = c1 + qFar * (2 * c2 + qFar * 3 * c3);
+    if (sdf3 < 0.f && -sdf3 * d < rl->sdf && dexit >= 0.f) {
       rl->cvb = 1;
       rl->ct = qFar;
       rl->csdf = -sdf3 * d;
     }
+    // bit 4 for the next voxel: known equal unless the walks have diverged and this
+    // exit is outside, not below skip_t and not falling
+    const bool known = !(rl->flags & 8u) || !(sdf3 < 0.f) || dexit < 0.f || -sdf3 * d < rl->skip_t;
+    rl->flags = (rl->flags & ~(4u | 16u)) | (known ? 0u : 16u);
   }
   return hit ? t : qFar + EPS;
 }
@@ -311,11 +334,16 @@ struct HitRec {
 // on [0, qFar] (qFar <= sqrt 3) with a wide safety factor.
 __device__ __forceinline__ float skip_margin(float maxabs) { return 2e-3f * maxabs + 1e-6f; }
 
+// by_t: only skip_t skips this voxel (the reference's walk intersects it)
 template <bool BORDER>
-__device__ __forceinline__ void skipped_intersect(Relax *rl) {
+__device__ __forceinline__ void skipped_intersect(Relax *rl, bool by_t) {
   if (BORDER) {
     rl->csdf = 1000.f;
     if (rl->cvb == 1) rl->cvb = 0;
+    uint32_t f = rl->flags & ~4u;
+    if (by_t) f |= 8u;
+    f = (f & ~16u) | ((f & 8u) ? 16u : 0u);
+    rl->flags = f;
   }
 }
 
@@ -327,6 +355,7 @@ __device__ bool brick_visit(const DevScene &s, uint32_t node, float3 pos, float3
   const float bs = float(s.brick_size);
   const uint32_t max_steps = 8u * s.brick_size + 16u;
   if (!(bnf.x < bnf.y)) return false;
+  if (BORDER) rl->flags |= 4u;
   {
     const float2 bb = __ldg(&s.brick_bounds[node]);   // min v, max |v| over the brick
     const float thr = (BORDER ? fminf(rl->sdf, rl->skip_t) : 0.0f) + skip_margin(bb.y);
@@ -340,7 +369,7 @@ __device__ bool brick_visit(const DevScene &s, uint32_t node, float3 pos, float3
       const float3 max_pos = add(min_pos, scl(B.d, f3(1, 1, 1)));
       const float2 fnf = ray_box(pos, inv, min_pos.x, min_pos.y, min_pos.z, max_pos.x, max_pos.y, max_pos.z);
       if (tNear < fnf.x) {
-        skipped_intersect<BORDER>(rl);
+        skipped_intersect<BORDER>(rl, !(bb.x > rl->sdf + skip_margin(bb.y)));
         return false;
       }
     }
@@ -359,12 +388,12 @@ __device__ bool brick_visit(const DevScene &s, uint32_t node, float3 pos, float3
 #pragma unroll
     for (int i = 1; i < 8; i++) { vmin = fminf(vmin, values[i]); vmax = fmaxf(vmax, fabsf(values[i])); }
     if (tNear < fnf.x && vmin > (BORDER ? fminf(rl->sdf, rl->skip_t) : 0.0f) + skip_margin(vmax)) {
-      skipped_intersect<BORDER>(rl);
+      skipped_intersect<BORDER>(rl, BORDER && !(vmin > rl->sdf + skip_margin(vmax)));
     } else if (tNear < fnf.x) {
       const float3 start_q = scr(sub(add(pos, scl(fnf.x, dir)), min_pos), B.scale);
       const float qFar = (fnf.y - fnf.x) * B.scale;
       const float prev = BORDER ? rl->sdf : 0.0f;
-      const float t = intersect<BORDER>(values, B.d, qFar, start_q, dir, rl);
+      const float t = intersect<BORDER>(values, B.d, qFar, start_q, dir, rl, skip_margin(vmax));
       const float tReal = fnf.x + B.d * t;
       if (BORDER) {
         if (rl->sdf < prev && rl->t < t) {

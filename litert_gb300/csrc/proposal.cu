@@ -392,13 +392,12 @@ __global__ void __launch_bounds__(128) mlp_infer_kernel(TripleView data, MlpStat
 //   warp 0 (one thread)  loads each tile's 4 KB of features with one bulk copy
 //                        (cp.async.bulk) into a ring of four shared-memory
 //                        stages -- the store's tile layout is the MMA's
-//                        operand layout -- completing on the stage's mbarrier;
-//   warp 1 (one thread)  issues the tcgen05.mma of every layer (M = 128,
-//                        N = 32/32/16, K = 16 per instruction), committing each
-//                        to an mbarrier.  It polls its inputs without blocking
-//                        and issues whatever is ready -- layer 3 of the oldest
-//                        tile, layer 2 of the next, layer 1 of a newly loaded
-//                        one -- so that no tile waits behind another's epilogue;
+//                        operand layout -- and issues layer 1 (M = 128, N = 32,
+//                        K = 16) of the tile loaded three copies earlier, once
+//                        its accumulator is free;
+//   warp 1 (one thread)  issues layer 2 of tile j (N = 32, K = 2 x 16), then
+//                        layer 3 of tile j - 1 (N = 16), each once the epilogue
+//                        has put the layer's input into shared memory;
 //   warps 2-9            the epilogue, two groups of four warps (even and odd
 //                        tiles) working on two tiles at once: each warp reads its
 //                        32 TMEM lanes, adds the bias, applies ReLU and BF16
@@ -406,12 +405,13 @@ __global__ void __launch_bounds__(128) mlp_infer_kernel(TripleView data, MlpStat
 //                        next layer's A operand in the tile's shared-memory
 //                        buffer, and after layer 3 writes column 0 plus the
 //                        output bias.
-// Every hand-off is an mbarrier (no CTA barrier inside the loop).  The weights
-// are staged once per CTA in the canonical K-major layout.  Waits are bounded by
-// `wait_limit` polls (the MMA thread counts polls without progress): a timeout
-// sets status bit 1 and makes the role leave its loop; the others run out the
-// same way, then the MMA thread waits (at most kTcWait polls) for everything it
-// issued, the loader for every copy it started, and the TMEM is freed.
+// Every hand-off is an mbarrier, waited on with the blocking try_wait (no CTA
+// barrier inside the loop, no spinning issuer).  The weights are staged once per
+// CTA in the canonical K-major layout.  Waits are bounded by `wait_limit` polls:
+// a timeout sets status bit 1 and makes the role leave its loop; the others run
+// out the same way, then each issuing thread waits (at most kTcWait polls) for
+// everything it issued, the loader for every copy it started, and the TMEM is
+// freed.
 constexpr uint32_t kTcLbo = 128;         // adjacent core matrices along K (weights, hidden operands)
 constexpr uint32_t kTcWait = 1u << 22;   // mbarrier polls of the final drain (and the default limit)
 constexpr int kTcStages = 4;             // feature tiles in shared memory
@@ -453,8 +453,8 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) mlp_infer_tc_kerne
   __shared__ __align__(16) float sb2[kHid];
   __shared__ float sb3;
   __shared__ __align__(8) uint64_t full[kTcStages], empty[kTcStages];
-  __shared__ __align__(8) uint64_t l1[kTcAcc], l2[kTcAcc], l3[kTcAcc], h1[kTcAcc], h2[kTcAcc], afree[kTcAcc], fin;
-  __shared__ uint32_t tmem_slot, s_consumed;
+  __shared__ __align__(8) uint64_t l1[kTcAcc], l2[kTcAcc], l3[kTcAcc], h1[kTcAcc], h2[kTcAcc], afree[kTcAcc], fin[2];
+  __shared__ uint32_t tmem_slot;
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
   const uint64_t t_first = data.first >> 7;
   const uint64_t n_tiles = data.n ? ((data.first + data.n - 1) >> 7) - t_first + 1 : 0;
@@ -485,8 +485,8 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) mlp_infer_tc_kerne
       tc05::mbar_init(&h2[a], 4);
       tc05::mbar_init(&afree[a], 4);
     }
-    tc05::mbar_init(&fin, 1);
-    s_consumed = 0;
+    tc05::mbar_init(&fin[0], 1);
+    tc05::mbar_init(&fin[1], 1);
     tc05::fence_mbar_init();
   }
   if (warp == 0) tc05::tmem_alloc(&tmem_slot, 32 * kTcAcc);
@@ -496,81 +496,78 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) mlp_infer_tc_kerne
   tc05::fence_after_sync();
   const uint32_t tbase = tmem_slot;
   auto tile_of = [&](uint32_t j) { return t_first + blockIdx.x + uint64_t(j) * gridDim.x; };
-  uint32_t issued = 0;
+  uint32_t issued = 0, consumed = 0;   // the loader's copies started / read by a layer 1
 
   if (warp == 0) {
-    // ---- loader
+    // ---- loader and layer 1: tile j's copy is started three tiles ahead of its layer 1
     if (lane == 0) {
-      for (uint32_t j = 0; j < my_tiles; j++) {
-        const uint32_t st = j % kTcStages;
-        if (j >= uint32_t(kTcStages) && !tc05::mbar_wait(&empty[st], ((j / kTcStages) - 1) & 1u, wait_limit)) {
-          atomicOr(status, 2u);
-          break;
+      constexpr uint32_t kId32 = tc05::idesc_bf16_f32(128, 32);
+      const uint32_t aX = tc05::smem_addr(sX), aW1 = tc05::smem_addr(sW1);
+      bool ok = true;
+      for (uint32_t j = 0; ok && j < my_tiles + kTcStages - 1; j++) {
+        if (j < my_tiles) {
+          const uint32_t st = j % kTcStages;
+          if (j >= uint32_t(kTcStages) && !tc05::mbar_wait(&empty[st], ((j / kTcStages) - 1) & 1u, wait_limit)) {
+            ok = false;
+            break;
+          }
+          tc05::mbar_arrive_expect_tx(&full[st], 4096);
+          tc05::bulk_g2s(sX + st * 4096, data.feat + tile_of(j) * 2048, 4096, &full[st]);
+          issued = j + 1;
         }
-        tc05::mbar_arrive_expect_tx(&full[st], 4096);
-        tc05::bulk_g2s(sX + st * 4096, data.feat + tile_of(j) * 2048, 4096, &full[st]);
-        issued = j + 1;
+        if (j + 1 >= uint32_t(kTcStages) && j + 1 - kTcStages < my_tiles) {
+          const uint32_t jj = j + 1 - kTcStages, a = jj % kTcAcc, st = jj % kTcStages;
+          if (jj >= uint32_t(kTcAcc) && !tc05::mbar_wait(&afree[a], ((jj / kTcAcc) - 1) & 1u, wait_limit)) {
+            ok = false;
+            break;
+          }
+          if (!tc05::mbar_wait(&full[st], (jj / kTcStages) & 1u, wait_limit)) { ok = false; break; }
+          tc05::fence_after_sync();
+          tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(aX + st * 4096, 2048, 128),
+                         tc05::smem_desc(aW1, kTcLbo, 256), kId32, false);
+          tc05::mma_commit(&l1[a]);
+          tc05::mma_commit(&empty[st]);   // the stage is free once layer 1 has read it
+          consumed = jj + 1;
+        }
       }
+      if (!ok) atomicOr(status, 2u);
+      tc05::mma_commit(&fin[0]);
+      if (!tc05::mbar_wait(&fin[0], 0, kTcWait)) atomicOr(status, 2u);
     }
   } else if (warp == 1) {
-    // ---- MMA issuer: n1 / n2 / n3 tiles have had layer 1 / 2 / 3 issued
+    // ---- layers 2 and 3, one tile apart: layer 2 of tile j, then layer 3 of tile j - 1
     if (lane == 0) {
       constexpr uint32_t kId32 = tc05::idesc_bf16_f32(128, 32), kId16 = tc05::idesc_bf16_f32(128, 16);
-      const uint32_t aX = tc05::smem_addr(sX), aH = tc05::smem_addr(sH);
-      const uint32_t aW1 = tc05::smem_addr(sW1), aW2 = tc05::smem_addr(sW2), aW3 = tc05::smem_addr(sW3);
-      uint32_t n1 = 0, n2 = 0, n3 = 0, idle = 0;
+      const uint32_t aH = tc05::smem_addr(sH), aW2 = tc05::smem_addr(sW2), aW3 = tc05::smem_addr(sW3);
       bool ok = true;
-      while (n3 < my_tiles) {
-        bool prog = false;
-        if (n3 < n2) {   // layer 3 of the oldest tile, once its second hidden layer is in shared memory
-          const uint32_t a = n3 % kTcAcc;
-          if (tc05::mbar_test(&h2[a], (n3 / kTcAcc) & 1u)) {
-            tc05::fence_after_sync();
-            const uint32_t h = aH + a * kTcHidBytes;
-            tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(h, kTcLbo, 512), tc05::smem_desc(aW3, kTcLbo, 512), kId16,
-                           false);
-            tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(h + 2 * kTcLbo, kTcLbo, 512),
-                           tc05::smem_desc(aW3 + 2 * kTcLbo, kTcLbo, 512), kId16, true);
-            tc05::mma_commit(&l3[a]);
-            n3++;
-            prog = true;
-          }
+      for (uint32_t j = 0; ok && j <= my_tiles; j++) {
+        if (j < my_tiles) {
+          const uint32_t a = j % kTcAcc;
+          if (!tc05::mbar_wait(&h1[a], (j / kTcAcc) & 1u, wait_limit)) { ok = false; break; }
+          tc05::fence_after_sync();
+          const uint32_t h = aH + a * kTcHidBytes;
+          tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(h, kTcLbo, 512), tc05::smem_desc(aW2, kTcLbo, 512), kId32,
+                         false);
+          tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(h + 2 * kTcLbo, kTcLbo, 512),
+                         tc05::smem_desc(aW2 + 2 * kTcLbo, kTcLbo, 512), kId32, true);
+          tc05::mma_commit(&l2[a]);
         }
-        if (n2 < n1) {   // layer 2, once the first hidden layer is in shared memory
-          const uint32_t a = n2 % kTcAcc;
-          if (tc05::mbar_test(&h1[a], (n2 / kTcAcc) & 1u)) {
-            tc05::fence_after_sync();
-            const uint32_t h = aH + a * kTcHidBytes;
-            tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(h, kTcLbo, 512), tc05::smem_desc(aW2, kTcLbo, 512), kId32,
-                           false);
-            tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(h + 2 * kTcLbo, kTcLbo, 512),
-                           tc05::smem_desc(aW2 + 2 * kTcLbo, kTcLbo, 512), kId32, true);
-            tc05::mma_commit(&l2[a]);
-            n2++;
-            prog = true;
-          }
+        if (j >= 1) {
+          const uint32_t jj = j - 1, a = jj % kTcAcc;
+          if (!tc05::mbar_wait(&h2[a], (jj / kTcAcc) & 1u, wait_limit)) { ok = false; break; }
+          tc05::fence_after_sync();
+          const uint32_t h = aH + a * kTcHidBytes;
+          tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(h, kTcLbo, 512), tc05::smem_desc(aW3, kTcLbo, 512), kId16,
+                         false);
+          tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(h + 2 * kTcLbo, kTcLbo, 512),
+                         tc05::smem_desc(aW3 + 2 * kTcLbo, kTcLbo, 512), kId16, true);
+          tc05::mma_commit(&l3[a]);
         }
-        if (n1 < my_tiles) {   // layer 1 of a loaded tile, once its accumulator is free
-          const uint32_t a = n1 % kTcAcc, st = n1 % kTcStages;
-          const bool acc_free = n1 < uint32_t(kTcAcc) || tc05::mbar_test(&afree[a], ((n1 / kTcAcc) - 1) & 1u);
-          if (acc_free && tc05::mbar_test(&full[st], (n1 / kTcStages) & 1u)) {
-            tc05::fence_after_sync();
-            tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(aX + st * 4096, 2048, 128),
-                           tc05::smem_desc(aW1, kTcLbo, 256), kId32, false);
-            tc05::mma_commit(&l1[a]);
-            tc05::mma_commit(&empty[st]);   // the stage is free once layer 1 has read it
-            n1++;
-            prog = true;
-          }
-        }
-        if (prog) idle = 0;
-        else if (++idle >= wait_limit) { ok = false; break; }
       }
       if (!ok) atomicOr(status, 2u);
       // every MMA this thread issued has completed before the TMEM is freed
-      tc05::mma_commit(&fin);
-      if (!tc05::mbar_wait(&fin, 0, kTcWait)) atomicOr(status, 2u);
-      s_consumed = n1;
+      tc05::mma_commit(&fin[1]);
+      if (!tc05::mbar_wait(&fin[1], 0, kTcWait)) atomicOr(status, 2u);
     }
   } else {
     // ---- epilogue: group g takes tiles g, g + 2, ...; warp w reads TMEM lanes
@@ -604,9 +601,9 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) mlp_infer_tc_kerne
     }
   }
   __syncthreads();
-  // copies the MMA issuer never consumed (after a timeout) land before the CTA exits
+  // copies no layer 1 consumed (after a timeout) land before the CTA exits
   if (warp == 0 && lane == 0)
-    for (uint32_t j = s_consumed; j < issued; j++)
+    for (uint32_t j = consumed; j < issued; j++)
       if (!tc05::mbar_wait(&full[j % kTcStages], (j / kTcStages) & 1u, kTcWait)) atomicOr(status, 2u);
   tc05::fence_before_sync();
   __syncthreads();

@@ -72,16 +72,6 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *mbar, uint32_t phase) {
       : "memory");
   return ok != 0;
 }
-// non-blocking test: has the phase of this parity completed?
-__device__ __forceinline__ bool mbar_test(uint64_t *mbar, uint32_t phase) {
-  uint32_t ok = 0;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_addr(mbar)), "r"(phase)
-      : "memory");
-  return ok != 0;
-}
 __device__ __forceinline__ void mbar_arrive(uint64_t *mbar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(mbar)) : "memory");
 }
