@@ -353,7 +353,7 @@ __device__ bool brick_visit(const DevScene &s, uint32_t node, float3 pos, float3
   const Brick B = brick_of(s, node);
   float2 bnf = ray_box(pos, inv, B.bmin.x, B.bmin.y, B.bmin.z, B.bmax.x, B.bmax.y, B.bmax.z);
   const float bs = float(s.brick_size);
-  const uint32_t max_steps = 8u * s.brick_size + 16u;
+  const uint32_t max_steps = walk_step_bound(s.brick_size, bnf.y - bnf.x);
   if (!(bnf.x < bnf.y)) return false;
   if (BORDER) rl->flags |= 4u;
   {

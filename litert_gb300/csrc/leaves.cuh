@@ -415,10 +415,7 @@ __device__ void brick_intersect(const DevScene &s, float3 ray_pos, float3 ray_di
   const bool posx = inv.x > 0.0f, posy = inv.y > 0.0f, posz = inv.z > 0.0f;
   float values[8];
   if (COUNT) cnt.leaves++;
-  // A ray crosses at most 3*brick_size voxels.  The reference's loop has no
-  // bound; its +1e-6 step stops advancing beyond t ~ 32, where a degenerate
-  // voxel would loop forever.  The bound below never binds otherwise.
-  const uint32_t max_steps = 8u * bsz + 16u;
+  const uint32_t max_steps = walk_step_bound(bsz, bnf.y - bnf.x);
   const GlobalLoader gl(s, nd.z, sz_inv);
   const SharedLoader sl{staged, v_size, h.brick_pad};
   // Two nested loops: the inner one steps through voxels until one needs the

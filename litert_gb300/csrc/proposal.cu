@@ -386,7 +386,7 @@ __global__ void __launch_bounds__(128) mlp_infer_kernel(TripleView data, MlpStat
 
 // ---------------------------------------------------------------- 128-sample tiles on tcgen05
 // The network on the fifth-generation tensor cores, warp-specialised and
-// pipelined.  A persistent CTA of ten warps walks the 128-sample tiles of the
+// pipelined.  A persistent CTA of nine warps walks the 128-sample tiles of the
 // store that hold the requested window, up to four tiles in flight (one TMEM
 // accumulator of 32 columns each, tile j in accumulator j % 4):
 //   warp 0 (one thread)  loads each tile's 4 KB of features with one bulk copy
@@ -395,20 +395,22 @@ __global__ void __launch_bounds__(128) mlp_infer_kernel(TripleView data, MlpStat
 //                        operand layout -- and issues layer 1 (M = 128, N = 32,
 //                        K = 16) of the tile loaded three copies earlier, once
 //                        its accumulator is free;
-//   warp 1 (one thread)  issues layer 2 of tile j (N = 32, K = 2 x 16), then
-//                        layer 3 of tile j - 1 (N = 16), each once the epilogue
-//                        has put the layer's input into shared memory;
-//   warps 2-9            the epilogue, two groups of four warps (even and odd
-//                        tiles) working on two tiles at once: each warp reads its
-//                        32 TMEM lanes, adds the bias, applies ReLU and BF16
+//   warps 1-8            two epilogue groups of four warps (even and odd tiles)
+//                        working on two tiles at once: each warp reads its 32
+//                        TMEM lanes, adds the bias, applies ReLU and BF16
 //                        rounding (one cvt.rn.relu.bf16x2.f32 per pair) into the
 //                        next layer's A operand in the tile's shared-memory
-//                        buffer, and after layer 3 writes column 0 plus the
-//                        output bias.
+//                        buffer; the group's first thread issues layer 2
+//                        (N = 32) and layer 3 (N = 16) as soon as its four warps
+//                        have written the layer's input, and after layer 3 each
+//                        warp writes column 0 plus the output bias.
 // Every hand-off is an mbarrier, waited on with the blocking try_wait (no CTA
-// barrier inside the loop, no spinning issuer).  The weights are staged once per
-// CTA in the canonical K-major layout.  Waits are bounded by `wait_limit` polls:
-// a timeout sets status bit 1 and makes the role leave its loop; the others run
+// barrier inside the loop).  Measured with clock64 stamps, the previous form --
+// one thread issuing layers 2 and 3 for both groups in tile order -- held each
+// layer 3 back until the other group's layer-2 input was ready (2,150 of the
+// 4,800 cycles a group spent per tile).  The weights are staged once per CTA in
+// the canonical K-major layout.  Waits are bounded by `wait_limit` polls: a
+// timeout sets status bit 1 and makes the role leave its loop; the others run
 // out the same way, then each issuing thread waits (at most kTcWait polls) for
 // everything it issued, the loader for every copy it started, and the TMEM is
 // freed.
@@ -416,7 +418,7 @@ constexpr uint32_t kTcLbo = 128;         // adjacent core matrices along K (weig
 constexpr uint32_t kTcWait = 1u << 22;   // mbarrier polls of the final drain (and the default limit)
 constexpr int kTcStages = 4;             // feature tiles in shared memory
 constexpr int kTcAcc = 4;                // tiles in flight (TMEM accumulators, hidden buffers)
-constexpr int kTcThreads = 320;
+constexpr int kTcThreads = 288;
 constexpr int kTcBlocksPerSm = 4;        // 4 x 128 TMEM columns
 constexpr uint32_t kTcHidBytes = 128 * kHid * 2;
 constexpr uint32_t kTcDynSmem = kTcStages * 4096 + kTcAcc * kTcHidBytes;
@@ -453,7 +455,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) mlp_infer_tc_kerne
   __shared__ __align__(16) float sb2[kHid];
   __shared__ float sb3;
   __shared__ __align__(8) uint64_t full[kTcStages], empty[kTcStages];
-  __shared__ __align__(8) uint64_t l1[kTcAcc], l2[kTcAcc], l3[kTcAcc], h1[kTcAcc], h2[kTcAcc], afree[kTcAcc], fin[2];
+  __shared__ __align__(8) uint64_t l1[kTcAcc], l2[kTcAcc], l3[kTcAcc], h1[kTcAcc], h2[kTcAcc], afree[kTcAcc], fin[3];
   __shared__ uint32_t tmem_slot;
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
   const uint64_t t_first = data.first >> 7;
@@ -485,8 +487,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) mlp_infer_tc_kerne
       tc05::mbar_init(&h2[a], 4);
       tc05::mbar_init(&afree[a], 4);
     }
-    tc05::mbar_init(&fin[0], 1);
-    tc05::mbar_init(&fin[1], 1);
+    for (int k = 0; k < 3; k++) tc05::mbar_init(&fin[k], 1);
     tc05::fence_mbar_init();
   }
   if (warp == 0) tc05::tmem_alloc(&tmem_slot, 32 * kTcAcc);
@@ -534,63 +535,66 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) mlp_infer_tc_kerne
       tc05::mma_commit(&fin[0]);
       if (!tc05::mbar_wait(&fin[0], 0, kTcWait)) atomicOr(status, 2u);
     }
-  } else if (warp == 1) {
-    // ---- layers 2 and 3, one tile apart: layer 2 of tile j, then layer 3 of tile j - 1
-    if (lane == 0) {
-      constexpr uint32_t kId32 = tc05::idesc_bf16_f32(128, 32), kId16 = tc05::idesc_bf16_f32(128, 16);
-      const uint32_t aH = tc05::smem_addr(sH), aW2 = tc05::smem_addr(sW2), aW3 = tc05::smem_addr(sW3);
-      bool ok = true;
-      for (uint32_t j = 0; ok && j <= my_tiles; j++) {
-        if (j < my_tiles) {
-          const uint32_t a = j % kTcAcc;
-          if (!tc05::mbar_wait(&h1[a], (j / kTcAcc) & 1u, wait_limit)) { ok = false; break; }
-          tc05::fence_after_sync();
-          const uint32_t h = aH + a * kTcHidBytes;
-          tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(h, kTcLbo, 512), tc05::smem_desc(aW2, kTcLbo, 512), kId32,
-                         false);
-          tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(h + 2 * kTcLbo, kTcLbo, 512),
-                         tc05::smem_desc(aW2 + 2 * kTcLbo, kTcLbo, 512), kId32, true);
-          tc05::mma_commit(&l2[a]);
-        }
-        if (j >= 1) {
-          const uint32_t jj = j - 1, a = jj % kTcAcc;
-          if (!tc05::mbar_wait(&h2[a], (jj / kTcAcc) & 1u, wait_limit)) { ok = false; break; }
-          tc05::fence_after_sync();
-          const uint32_t h = aH + a * kTcHidBytes;
-          tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(h, kTcLbo, 512), tc05::smem_desc(aW3, kTcLbo, 512), kId16,
-                         false);
-          tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(h + 2 * kTcLbo, kTcLbo, 512),
-                         tc05::smem_desc(aW3 + 2 * kTcLbo, kTcLbo, 512), kId16, true);
-          tc05::mma_commit(&l3[a]);
-        }
-      }
-      if (!ok) atomicOr(status, 2u);
-      // every MMA this thread issued has completed before the TMEM is freed
-      tc05::mma_commit(&fin[1]);
-      if (!tc05::mbar_wait(&fin[1], 0, kTcWait)) atomicOr(status, 2u);
-    }
   } else {
     // ---- epilogue: group g takes tiles g, g + 2, ...; warp w reads TMEM lanes
-    // 32 * (w % 4) .. + 31 (rows of the tile)
-    const uint32_t g = (warp - 2) >> 2, q = warp & 3u, row = 32u * q + lane, trow = tbase + ((32u * q) << 16);
+    // 32 * (w % 4) .. + 31 (rows of the tile).  The group's first warp issues the
+    // group's layers 2 and 3 once all four warps have written the layer's input.
+    constexpr uint32_t kId32 = tc05::idesc_bf16_f32(128, 32), kId16 = tc05::idesc_bf16_f32(128, 16);
+    const uint32_t g = (warp - 1) >> 2, q = warp & 3u, row = 32u * q + lane, trow = tbase + ((32u * q) << 16);
+    const bool leader = ((warp - 1) & 3u) == 0;   // the whole warp waits, its lane 0 issues
+    const uint32_t aW2 = tc05::smem_addr(sW2), aW3 = tc05::smem_addr(sW3);
+    bool ok = true;
     for (uint32_t j = g; j < my_tiles; j += 2) {
       const uint32_t a = j % kTcAcc, ph = (j / kTcAcc) & 1u;
       uint8_t *const hb = sH + a * kTcHidBytes;
-      if (!tc05::mbar_wait(&l1[a], ph, wait_limit)) { atomicOr(status, 2u); break; }
+      const uint32_t h = tc05::smem_addr(hb);
+      if (!tc05::mbar_wait(&l1[a], ph, wait_limit)) { ok = false; break; }
       tc05::fence_after_sync();
       hidden_to_smem(trow + a * 32u, sb1, hb, row);
       tc05::fence_proxy_async();
       tc05::fence_before_sync();
       __syncwarp();
       if (lane == 0) tc05::mbar_arrive(&h1[a]);
-      if (!tc05::mbar_wait(&l2[a], ph, wait_limit)) { atomicOr(status, 2u); break; }
+      if (leader) {   // layer 2 (N = 32, K = 2 x 16)
+        const bool ready = tc05::mbar_wait(&h1[a], ph, wait_limit);
+        if (lane == 0) {
+          if (ready) {
+            tc05::fence_after_sync();
+            tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(h, kTcLbo, 512), tc05::smem_desc(aW2, kTcLbo, 512), kId32,
+                           false);
+            tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(h + 2 * kTcLbo, kTcLbo, 512),
+                           tc05::smem_desc(aW2 + 2 * kTcLbo, kTcLbo, 512), kId32, true);
+            tc05::mma_commit(&l2[a]);
+          } else {
+            atomicOr(status, 2u);
+          }
+        }
+        __syncwarp();
+      }
+      if (!tc05::mbar_wait(&l2[a], ph, wait_limit)) { ok = false; break; }
       tc05::fence_after_sync();
       hidden_to_smem(trow + a * 32u, sb2, hb, row);
       tc05::fence_proxy_async();
       tc05::fence_before_sync();
       __syncwarp();
       if (lane == 0) tc05::mbar_arrive(&h2[a]);
-      if (!tc05::mbar_wait(&l3[a], ph, wait_limit)) { atomicOr(status, 2u); break; }
+      if (leader) {   // layer 3 (N = 16, K = 2 x 16)
+        const bool ready = tc05::mbar_wait(&h2[a], ph, wait_limit);
+        if (lane == 0) {
+          if (ready) {
+            tc05::fence_after_sync();
+            tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(h, kTcLbo, 512), tc05::smem_desc(aW3, kTcLbo, 512), kId16,
+                           false);
+            tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(h + 2 * kTcLbo, kTcLbo, 512),
+                           tc05::smem_desc(aW3 + 2 * kTcLbo, kTcLbo, 512), kId16, true);
+            tc05::mma_commit(&l3[a]);
+          } else {
+            atomicOr(status, 2u);
+          }
+        }
+        __syncwarp();
+      }
+      if (!tc05::mbar_wait(&l3[a], ph, wait_limit)) { ok = false; break; }
       tc05::fence_after_sync();
       const float y = tc05::tmem_ld1(trow + a * 32u);
       const uint64_t gi = tile_of(j) * 128 + row;
@@ -598,6 +602,11 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) mlp_infer_tc_kerne
       tc05::fence_before_sync();
       __syncwarp();
       if (lane == 0) tc05::mbar_arrive(&afree[a]);
+    }
+    if (!ok) atomicOr(status, 2u);
+    if (leader && lane == 0) {   // every MMA this thread issued has completed before the TMEM is freed
+      tc05::mma_commit(&fin[1 + g]);
+      if (!tc05::mbar_wait(&fin[1 + g], 0, kTcWait)) atomicOr(status, 2u);
     }
   }
   __syncthreads();

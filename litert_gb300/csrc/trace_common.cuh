@@ -58,6 +58,18 @@ __device__ __forceinline__ float3 safe_inverse(float3 d) {
 __device__ __forceinline__ float fmn(float a, float b) { return fminf(a, b); }
 __device__ __forceinline__ float fmx(float a, float b) { return fmaxf(a, b); }
 
+// Step bound of a voxel walk over a brick segment of t-length `extent`.  The
+// reference's loop (BVH/BVH2Common.cpp:764-984, diff_render/BVH2DR.cpp:1160-1240)
+// has none: a ray crosses at most 3 * brick_size voxels, but where the position
+// rounds back into a voxel the ray has left (grazing rays), a step advances t by
+// only +1e-6, which rounds to at least 7.6e-7 for t < 32 and to nothing beyond.
+// 8 * brick_size + 16 steps plus 1.5e6 per unit of extent therefore cover every
+// walk the reference finishes; beyond t ~ 32 its loop would not end.
+__host__ __device__ __forceinline__ uint32_t walk_step_bound(uint32_t brick_size, float extent) {
+  const float e = extent > 0.0f ? extent : 0.0f;   // NaN -> 0
+  return 8u * brick_size + 16u + uint32_t(e < 2.6f ? e * 1.5e6f : 3.9e6f);
+}
+
 // rand3 / rand2, Renderer/eye_ray.cpp:53-80 (the pcg3d hash of JCGT 2020 on the pixel
 // and sample index; `seed` is MultiRenderer::m_seed)
 __device__ __forceinline__ float2 rand2(uint32_t x, uint32_t y, uint32_t iter, uint32_t seed) {

@@ -314,10 +314,12 @@ static void brick_intersect(const orc_scene *s, uint32_t type, f3 ray_pos, f3 ra
   float old_t = hit->t;
   const float scale = 0.5f * sz * bs;
   if (cnt) cnt->n_leaf++;
-  /* the reference loop is unbounded; bounded here at 8*brick_size+16 steps (a ray
-   * crosses at most 3*brick_size voxels), which only binds where its +1e-6 step
-   * no longer advances (entry t beyond ~32) */
-  const uint32_t max_steps = 8u * h->brick_size + 16u;
+  /* the reference loop is unbounded: a ray crosses at most 3*brick_size voxels,
+   * but a grazing ray whose position rounds back into the voxel it left advances
+   * by only +1e-6 a step (at least 7.6e-7 once rounded, for t < 32; nothing
+   * beyond).  8*brick_size+16 steps plus 1.5e6 per unit of segment length cover
+   * every walk the reference finishes (orc_walk_step_bound, the engine's bound) */
+  const uint32_t max_steps = orc_walk_step_bound(h->brick_size, bnf.y - bnf.x);
   for (uint32_t step = 0; bnf.x < bnf.y && hit->t == old_t && step < max_steps; step++) {
     f3 hit_pos = add3(ray_pos, scl3(bnf.x, ray_dir));
     f3 local_pos = mul3s(sub3(hit_pos, brick_min), scale);

@@ -73,6 +73,14 @@ void orc_rand2(uint32_t x, uint32_t y, uint32_t iter, uint32_t seed, float *rx, 
 
 typedef struct { uint64_t n_fat, n_leaf, n_vox, n_vox_loaded, n_finder, n_tri; } orc_counters;
 
+/* Step bound of a voxel walk over a brick segment of t-length `extent` (the
+ * reference's loops have none; this covers every walk they finish).  The
+ * engine's walk_step_bound computes the same number. */
+static inline uint32_t orc_walk_step_bound(uint32_t brick_size, float extent) {
+  const float e = extent > 0.0f ? extent : 0.0f;
+  return 8u * brick_size + 16u + (uint32_t)(e < 2.6f ? e * 1.5e6f : 3.9e6f);
+}
+
 /* ---- BVH2 (oracle's own simple median-split builder, left/right fat pairs) ---- */
 /* boxes: n x 6 floats (min xyz, max xyz).  prims_in_leaf >= 1.  Returns number of
  * pairs written to *out_pairs (malloc'd; free with orc_free).  For prims_in_leaf>1

@@ -310,9 +310,9 @@ static void SFX(brick_grad)(const SFX(ctx) *cx, uint32_t type, uint32_t flags, V
   V2 bnf = SFX(box)(ray_pos, SFX(safe_inv)(ray_dir), bmin, bmax);
   R old_t = hit->t;
   const R scale = (R)0.5f * sz * bs;
-  /* bounded voxel walk: the reference's loop has no bound and stops advancing
-   * where its +1e-6 step vanishes against t (beyond t ~ 32) */
-  const uint32_t max_steps = 8u * h->brick_size + 16u;
+  /* bounded voxel walk: the reference's loop has no bound; orc_walk_step_bound
+   * covers every walk it finishes (see brick_intersect in lrt_oracle.c) */
+  const uint32_t max_steps = orc_walk_step_bound(h->brick_size, (float)(bnf.y - bnf.x));
   for (uint32_t step = 0; bnf.x < bnf.y && hit->t == old_t && step < max_steps; step++) {
     V3 hit_pos = SFX(add)(ray_pos, SFX(scl)(bnf.x, ray_dir));
     V3 local_pos = SFX(muls)(SFX(sub)(hit_pos, bmin), scale);
