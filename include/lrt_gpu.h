@@ -95,8 +95,9 @@ lrt_status lrt_set_preset(lrt_ctx *ctx, const lrt_preset *preset);
  * lrt_set_bvh2.  Triangle meshes have no early-out in the reference and keep
  * the closest hit.  Not used by lrt_render_noalloc, lrt_render_counters or the
  * autotuner).
- * "tc_wait" (default 4194304): how many times the tcgen05 network engine polls
- * a layer's completion barrier before it gives up; a timeout makes
+ * "tc_wait" (default 1048576): how many times the tcgen05 network engine polls
+ * a completion barrier before it gives up (a poll sleeps up to about 1 us, so
+ * the default bounds a wait near one second); a timeout makes
  * lrt_proposal_infer_ex return LRT_ERR_TIMEOUT after the block has drained its
  * issued tensor-core work and freed its tensor memory (the next call runs
  * normally).  0 makes every block give up at its first wait: the failure path,

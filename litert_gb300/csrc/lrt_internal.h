@@ -163,7 +163,7 @@ struct Tuning {
   int fma = 0;              // 1: variant 0 without counters runs the kernels compiled with FP contraction
   int first_hit = 0;        // 1: SBS / SVS renders and queries walk the BVH2 in the reference's order and
                             // stop at the first SDF leaf that hits (BVH2TraverseF32's result)
-  int tc_wait = 1 << 22;    // tcgen05 network engine: mbarrier polls per layer before it reports a timeout
+  int tc_wait = 1 << 20;    // tcgen05 network engine: mbarrier polls (up to ~1 us each) before a timeout
 };
 
 cudaError_t launch_render(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st, bool count,

@@ -4,7 +4,12 @@
 //
 // Parameter layout (FP32 master copy, 1633 floats): W1[32][16], b1[32],
 // W2[32][32], b2[32], W3[32], b3.  The BF16 copy the kernels read holds W1, W2
-// and W3 padded to an 8-row tile (rows 1..7 zero).
+// and W3 padded to an 8-row tile (rows 1..7 zero), then each layer's bias as
+// an extra 16-wide K block: output n's row holds the bias split into three BF16
+// terms (hi, mid, lo; their sum equals the FP32 bias to about 2^-24 of it) and
+// zeros.  Multiplied by a constant A block whose first three columns are 1, it
+// adds the bias inside the tensor core, after the layer's products, so neither
+// engine adds a bias on the CUDA cores.
 //
 // Fragment layouts (PTX mma.m16n8k16, .row.col, g = lane>>2, t = lane&3):
 //   A (16x16): a0 = (g, 2t..2t+1), a1 = (g+8, 2t..), a2 = (g, 2t+8..), a3 = (g+8, 2t+8..)
@@ -16,14 +21,10 @@
 #include <cuda_bf16.h>
 #include <cstdint>
 
+#include "mlp_image.h"
+
 namespace lrt {
 namespace mlp {
-
-constexpr int kIn = 16, kHid = 32;
-constexpr int kParams = 1633;
-constexpr int kOffW1 = 0, kOffB1 = 512, kOffW2 = 544, kOffB2 = 1568, kOffW3 = 1600, kOffB3 = 1632;
-// BF16 weight image: W1 (32x16), W2 (32x32), W3 padded (8x32)
-constexpr int kBfW1 = 0, kBfW2 = 512, kBfW3 = 1536, kBfWords = 1792;
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
   const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);   // .x (lo) in the low half
@@ -98,10 +99,19 @@ __device__ __forceinline__ void c_to_a(const float c[4][4], uint32_t a[2][4]) {
   }
 }
 
+// The constant A fragment of the bias blocks: columns 0..2 of every row are 1.
+__device__ __forceinline__ void ones_a(uint32_t a[4], int lane) {
+  const int t = lane & 3;
+  const uint32_t v = t == 0 ? 0x3F803F80u : t == 1 ? 0x00003F80u : 0u;   // (1, 1) / (1, 0) / (0, 0)
+  a[0] = v;
+  a[1] = v;
+  a[2] = 0u;
+  a[3] = 0u;
+}
+
 // Shared-memory weights of a block.
 struct Weights {
   __nv_bfloat16 w[kBfWords];
-  float b1[kHid], b2[kHid], b3;
 };
 
 // Forward of 32 samples held as a row-major [32][16] bf16 tile `x` (row = lane
@@ -112,22 +122,24 @@ __device__ __forceinline__ float forward_warp(const Weights &W, const __nv_bfloa
                                               float h1[2][4][4], float h2[2][4][4]) {
   const int g = lane >> 2, t = lane & 3;
   float out_lo[2], out_hi[2];
+  uint32_t a1s[4];
+  ones_a(a1s, lane);
 #pragma unroll
   for (int mt = 0; mt < 2; mt++) {
     uint32_t a[4];
     ld_a(a, x, kIn, mt * 16, 0, lane);
-    // Each layer sums its products in the tensor core from zero and adds the bias
-    // afterwards in FP32, as the tcgen05 engine's epilogue does, so both engines
-    // round at the same points.
+    // Each layer sums its products from zero, then its bias block (three BF16
+    // terms against the constant ones), all in the tensor core, as the tcgen05
+    // engine does: both engines round at the same points.
     float c1[4][4];
 #pragma unroll
     for (int nt = 0; nt < 4; nt++) {
-      const int col = nt * 8 + 2 * t;
       c1[nt][0] = c1[nt][1] = c1[nt][2] = c1[nt][3] = 0.0f;
       uint32_t b0, b1;
       ld_b_nk(b0, b1, W.w + kBfW1, kIn, nt * 8, 0, lane);
       mma16816(c1[nt], a, b0, b1);
-      c1[nt][0] += W.b1[col]; c1[nt][1] += W.b1[col + 1]; c1[nt][2] += W.b1[col]; c1[nt][3] += W.b1[col + 1];
+      ld_b_nk(b0, b1, W.w + kBfB1, 16, nt * 8, 0, lane);
+      mma16816(c1[nt], a1s, b0, b1);
 #pragma unroll
       for (int e = 0; e < 4; e++) c1[nt][e] = fmaxf(c1[nt][e], 0.0f);
     }
@@ -136,7 +148,6 @@ __device__ __forceinline__ float forward_warp(const Weights &W, const __nv_bfloa
     float c2[4][4];
 #pragma unroll
     for (int nt = 0; nt < 4; nt++) {
-      const int col = nt * 8 + 2 * t;
       c2[nt][0] = c2[nt][1] = c2[nt][2] = c2[nt][3] = 0.0f;
 #pragma unroll
       for (int kb = 0; kb < 2; kb++) {
@@ -144,7 +155,9 @@ __device__ __forceinline__ float forward_warp(const Weights &W, const __nv_bfloa
         ld_b_nk(b0, b1, W.w + kBfW2, kHid, nt * 8, kb * 16, lane);
         mma16816(c2[nt], a2[kb], b0, b1);
       }
-      c2[nt][0] += W.b2[col]; c2[nt][1] += W.b2[col + 1]; c2[nt][2] += W.b2[col]; c2[nt][3] += W.b2[col + 1];
+      uint32_t b0, b1;
+      ld_b_nk(b0, b1, W.w + kBfB2, 16, nt * 8, 0, lane);
+      mma16816(c2[nt], a1s, b0, b1);
 #pragma unroll
       for (int e = 0; e < 4; e++) c2[nt][e] = fmaxf(c2[nt][e], 0.0f);
     }
@@ -157,8 +170,13 @@ __device__ __forceinline__ float forward_warp(const Weights &W, const __nv_bfloa
       ld_b_nk(b0, b1, W.w + kBfW3, kHid, 0, kb * 16, lane);
       mma16816(c3, a3[kb], b0, b1);
     }
-    out_lo[mt] = c3[0] + W.b3;
-    out_hi[mt] = c3[2] + W.b3;
+    {
+      uint32_t b0, b1;
+      ld_b_nk(b0, b1, W.w + kBfB3, 16, 0, 0, lane);
+      mma16816(c3, a1s, b0, b1);
+    }
+    out_lo[mt] = c3[0];
+    out_hi[mt] = c3[2];
     if (KEEP) {
 #pragma unroll
       for (int nt = 0; nt < 4; nt++)

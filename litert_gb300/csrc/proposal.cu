@@ -148,11 +148,6 @@ __global__ void __launch_bounds__(128) gen_triples_kernel(DevScene s, const DevV
 // ---------------------------------------------------------------- training
 __device__ __forceinline__ void load_weights(Weights &W, const MlpState &m) {
   for (int i = threadIdx.x; i < kBfWords; i += blockDim.x) W.w[i] = m.wbf[i];
-  for (int i = threadIdx.x; i < kHid; i += blockDim.x) {
-    W.b1[i] = m.master[kOffB1 + i];
-    W.b2[i] = m.master[kOffB2 + i];
-  }
-  if (threadIdx.x == 0) W.b3 = m.master[kOffB3];
 }
 
 // per-column sums over the 32 rows of the warp's C tiles: lanes g == 0 (0..3)
@@ -350,14 +345,9 @@ __global__ void __launch_bounds__(128) mlp_train_kernel(TripleView data, MlpStat
     m.master[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
   }
   __syncthreads();
-  // refresh the bf16 image: W1, W2, W3 (row 0 of its 8-row tile)
-  for (int i = threadIdx.x; i < kBfWords; i += blockDim.x) {
-    float v = 0.0f;
-    if (i < kBfW2) v = m.master[kOffW1 + i];
-    else if (i < kBfW3) v = m.master[kOffW2 + (i - kBfW2)];
-    else if (i - kBfW3 < kHid) v = m.master[kOffW3 + (i - kBfW3)];
-    m.wbf[i] = __float2bfloat16_rn(v);
-  }
+  // refresh the bf16 image: W1, W2, W3 (row 0 of its 8-row tile), bias blocks
+  for (int i = threadIdx.x; i < kBfWords; i += blockDim.x)
+    reinterpret_cast<uint16_t *>(m.wbf)[i] = weight_image_word(m.master, i);
   if (threadIdx.x == 0) *m.ticket = 0u;
 }
 
@@ -388,44 +378,46 @@ __global__ void __launch_bounds__(128) mlp_infer_kernel(TripleView data, MlpStat
 // The network on the fifth-generation tensor cores, warp-specialised and
 // pipelined.  A persistent CTA of nine warps walks the 128-sample tiles of the
 // store that hold the requested window, up to four tiles in flight (one TMEM
-// accumulator of 32 columns each, tile j in accumulator j % 4):
+// accumulator of 32 columns and one shared-memory hidden buffer each, tile j in
+// slot j % 4).  Every layer is its products plus its bias block (three BF16
+// terms of the bias against a constant block of ones, mlp_image.h), summed in
+// the tensor core, so the epilogue adds no bias.
 //   warp 0 (one thread)  loads each tile's 4 KB of features with one bulk copy
-//                        (cp.async.bulk) into a ring of four shared-memory
+//                        (cp.async.bulk) into a ring of three shared-memory
 //                        stages -- the store's tile layout is the MMA's
-//                        operand layout -- and issues layer 1 (M = 128, N = 32,
-//                        K = 16) of the tile loaded three copies earlier, once
-//                        its accumulator is free;
+//                        operand layout -- and issues layer 1 (M = 128, N = 32:
+//                        K = 16 features, then K = 16 of the bias block) of the
+//                        tile loaded two copies earlier, once its slot is free;
 //   warps 1-8            two epilogue groups of four warps (even and odd tiles)
-//                        working on two tiles at once: each warp reads its 32
-//                        TMEM lanes, adds the bias, applies ReLU and BF16
-//                        rounding (one cvt.rn.relu.bf16x2.f32 per pair) into the
-//                        next layer's A operand in the tile's shared-memory
-//                        buffer; the group's first thread issues layer 2
-//                        (N = 32) and layer 3 (N = 16) as soon as its four warps
-//                        have written the layer's input, and after layer 3 each
-//                        warp writes column 0 plus the output bias.
+//                        working on two tiles at once.  Each warp reads its 32
+//                        TMEM lanes (rows) and applies ReLU and BF16 rounding
+//                        (one cvt.rn.relu.bf16x2.f32 per pair) into the next
+//                        layer's A operand in shared memory; the group's first
+//                        thread issues layer 2 (N = 32) and layer 3 (N = 16,
+//                        column 0 the output) as soon as its four warps have
+//                        written the layer's input; after layer 3 each warp
+//                        writes its rows' column 0.
 // Every hand-off is an mbarrier, waited on with the blocking try_wait (no CTA
-// barrier inside the loop).  Measured with clock64 stamps, the previous form --
-// one thread issuing layers 2 and 3 for both groups in tile order -- held each
-// layer 3 back until the other group's layer-2 input was ready (2,150 of the
-// 4,800 cycles a group spent per tile).  The weights are staged once per CTA in
-// the canonical K-major layout.  Waits are bounded by `wait_limit` polls: a
+// barrier inside the loop).  Measured with clock64 stamps and ncu, the epilogue
+// is what bounds the kernel: with the biases added on the CUDA cores it issued
+// about 1,400 warp instructions per tile.  The weights are staged once per CTA
+// in the canonical K-major layout.  Waits are bounded by `wait_limit` polls: a
 // timeout sets status bit 1 and makes the role leave its loop; the others run
 // out the same way, then each issuing thread waits (at most kTcWait polls) for
 // everything it issued, the loader for every copy it started, and the TMEM is
 // freed.
 constexpr uint32_t kTcLbo = 128;         // adjacent core matrices along K (weights, hidden operands)
-constexpr uint32_t kTcWait = 1u << 22;   // mbarrier polls of the final drain (and the default limit)
-constexpr int kTcStages = 4;             // feature tiles in shared memory
+constexpr uint32_t kTcWait = 1u << 20;   // mbarrier polls of the final drain (up to ~1 us each)
+constexpr int kTcStages = 3;             // feature tiles in shared memory
 constexpr int kTcAcc = 4;                // tiles in flight (TMEM accumulators, hidden buffers)
 constexpr int kTcThreads = 288;
 constexpr int kTcBlocksPerSm = 4;        // 4 x 128 TMEM columns
 constexpr uint32_t kTcHidBytes = 128 * kHid * 2;
 constexpr uint32_t kTcDynSmem = kTcStages * 4096 + kTcAcc * kTcHidBytes;
 
-// bias + ReLU + BF16 of one 32-wide accumulator row (this lane's TMEM lane, read in
-// two 16-column halves to keep registers low) into the A operand of the next layer
-__device__ __forceinline__ void hidden_to_smem(uint32_t trow, const float *bias, uint8_t *sH, uint32_t row) {
+// ReLU + BF16 of one 32-wide accumulator row (this lane's TMEM lane, read in two
+// 16-column halves to keep registers low) into the A operand of the next layer
+__device__ __forceinline__ void hidden_to_smem(uint32_t trow, uint8_t *sH, uint32_t row) {
 #pragma unroll
   for (int h = 0; h < 32; h += 16) {
     float v[16];
@@ -433,10 +425,10 @@ __device__ __forceinline__ void hidden_to_smem(uint32_t trow, const float *bias,
 #pragma unroll
     for (int j = 0; j < 16; j += 8) {
       uint4 q;
-      q.x = pack_bf16_relu(v[j] + bias[h + j], v[j + 1] + bias[h + j + 1]);
-      q.y = pack_bf16_relu(v[j + 2] + bias[h + j + 2], v[j + 3] + bias[h + j + 3]);
-      q.z = pack_bf16_relu(v[j + 4] + bias[h + j + 4], v[j + 5] + bias[h + j + 5]);
-      q.w = pack_bf16_relu(v[j + 6] + bias[h + j + 6], v[j + 7] + bias[h + j + 7]);
+      q.x = pack_bf16_relu(v[j], v[j + 1]);
+      q.y = pack_bf16_relu(v[j + 2], v[j + 3]);
+      q.z = pack_bf16_relu(v[j + 4], v[j + 5]);
+      q.w = pack_bf16_relu(v[j + 6], v[j + 7]);
       *reinterpret_cast<uint4 *>(sH + tc05::kmajor_offset(row, uint32_t(h + j), kTcLbo, 512)) = q;
     }
   }
@@ -448,33 +440,34 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) mlp_infer_tc_kerne
   extern __shared__ __align__(128) uint8_t tc_dyn[];
   uint8_t *const sX = tc_dyn;                           // kTcStages x 4 KB feature tiles
   uint8_t *const sH = tc_dyn + kTcStages * 4096;        // kTcAcc x hidden operand
-  __shared__ __align__(128) uint8_t sW1[kHid * kIn * 2];
-  __shared__ __align__(128) uint8_t sW2[kHid * kHid * 2];
-  __shared__ __align__(128) uint8_t sW3[16 * kHid * 2];
-  __shared__ __align__(16) float sb1[kHid];
-  __shared__ __align__(16) float sb2[kHid];
-  __shared__ float sb3;
+  __shared__ __align__(128) uint8_t sW1[kHid * kIn * 2], sB1[kHid * 16 * 2];
+  __shared__ __align__(128) uint8_t sW2[kHid * kHid * 2], sB2[kHid * 16 * 2];
+  __shared__ __align__(128) uint8_t sW3[16 * kHid * 2], sB3[16 * 16 * 2];
+  __shared__ __align__(128) uint8_t sOnes[128 * 16 * 2];
   __shared__ __align__(8) uint64_t full[kTcStages], empty[kTcStages];
-  __shared__ __align__(8) uint64_t l1[kTcAcc], l2[kTcAcc], l3[kTcAcc], h1[kTcAcc], h2[kTcAcc], afree[kTcAcc], fin[3];
+  __shared__ __align__(8) uint64_t l1[kTcAcc], l2[kTcAcc], l3[kTcAcc], afree[kTcAcc], fin[3];
   __shared__ uint32_t tmem_slot;
   const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
   const uint64_t t_first = data.first >> 7;
   const uint64_t n_tiles = data.n ? ((data.first + data.n - 1) >> 7) - t_first + 1 : 0;
   const uint32_t my_tiles = blockIdx.x < n_tiles ? uint32_t((n_tiles - 1 - blockIdx.x) / gridDim.x + 1) : 0u;
-  // weights into the canonical layout (W stored [n][k] is the K-major B operand)
-  for (uint32_t i = tid; i < kHid * kIn; i += kTcThreads)
-    *reinterpret_cast<__nv_bfloat16 *>(sW1 + tc05::kmajor_offset(i / kIn, i % kIn, kTcLbo, 256)) = m.wbf[kBfW1 + i];
-  for (uint32_t i = tid; i < kHid * kHid; i += kTcThreads)
-    *reinterpret_cast<__nv_bfloat16 *>(sW2 + tc05::kmajor_offset(i / kHid, i % kHid, kTcLbo, 512)) = m.wbf[kBfW2 + i];
+  // weights (W stored [n][k] is the K-major B operand), bias blocks and the ones
+  // block into the canonical layout
+  const __nv_bfloat16 zero = __float2bfloat16_rn(0.0f), one = __float2bfloat16_rn(1.0f);
+  auto put = [](uint8_t *base, uint32_t r, uint32_t k, uint32_t sbo, __nv_bfloat16 v) {
+    *reinterpret_cast<__nv_bfloat16 *>(base + tc05::kmajor_offset(r, k, kTcLbo, sbo)) = v;
+  };
+  for (uint32_t i = tid; i < kHid * kIn; i += kTcThreads) put(sW1, i / kIn, i % kIn, 256, m.wbf[kBfW1 + i]);
+  for (uint32_t i = tid; i < kHid * kHid; i += kTcThreads) put(sW2, i / kHid, i % kHid, 512, m.wbf[kBfW2 + i]);
   for (uint32_t i = tid; i < 16 * kHid; i += kTcThreads)
-    *reinterpret_cast<__nv_bfloat16 *>(sW3 + tc05::kmajor_offset(i / kHid, i % kHid, kTcLbo, 512)) =
-        i < kHid ? m.wbf[kBfW3 + i] : __float2bfloat16_rn(0.0f);
-  if (tid < kHid) {
-    sb1[tid] = m.master[kOffB1 + tid];
-    sb2[tid] = m.master[kOffB2 + tid];
+    put(sW3, i / kHid, i % kHid, 512, i < 8 * kHid ? m.wbf[kBfW3 + i] : zero);
+  for (uint32_t i = tid; i < kHid * 16; i += kTcThreads) {
+    put(sB1, i / 16, i % 16, 256, m.wbf[kBfB1 + i]);
+    put(sB2, i / 16, i % 16, 256, m.wbf[kBfB2 + i]);
   }
+  for (uint32_t i = tid; i < 16 * 16; i += kTcThreads) put(sB3, i / 16, i % 16, 256, i < 8 * 16 ? m.wbf[kBfB3 + i] : zero);
+  for (uint32_t i = tid; i < 128 * 16; i += kTcThreads) put(sOnes, i / 16, i % 16, 256, (i % 16) < 3 ? one : zero);
   if (tid == 0) {
-    sb3 = m.master[kOffB3];
     for (int i = 0; i < kTcStages; i++) {
       tc05::mbar_init(&full[i], 1);
       tc05::mbar_init(&empty[i], 1);
@@ -483,9 +476,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) mlp_infer_tc_kerne
       tc05::mbar_init(&l1[a], 1);
       tc05::mbar_init(&l2[a], 1);
       tc05::mbar_init(&l3[a], 1);
-      tc05::mbar_init(&h1[a], 4);
-      tc05::mbar_init(&h2[a], 4);
-      tc05::mbar_init(&afree[a], 4);
+      tc05::mbar_init(&afree[a], 1);
     }
     for (int k = 0; k < 3; k++) tc05::mbar_init(&fin[k], 1);
     tc05::fence_mbar_init();
@@ -496,14 +487,19 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) mlp_infer_tc_kerne
   __syncthreads();
   tc05::fence_after_sync();
   const uint32_t tbase = tmem_slot;
+  const uint32_t aOnes = tc05::smem_addr(sOnes);
   auto tile_of = [&](uint32_t j) { return t_first + blockIdx.x + uint64_t(j) * gridDim.x; };
   uint32_t issued = 0, consumed = 0;   // the loader's copies started / read by a layer 1
 
   if (warp == 0) {
-    // ---- loader and layer 1: tile j's copy is started three tiles ahead of its layer 1
+    // ---- loader and layer 1: tile j's copy is started two tiles ahead of its layer 1
     if (lane == 0) {
       constexpr uint32_t kId32 = tc05::idesc_bf16_f32(128, 32);
-      const uint32_t aX = tc05::smem_addr(sX), aW1 = tc05::smem_addr(sW1);
+      // descriptors built once; a stage's feature tile is dX plus its offset in 16-byte units
+      const uint64_t dX = tc05::smem_desc(tc05::smem_addr(sX), 2048, 128);
+      const uint64_t dW1 = tc05::smem_desc(tc05::smem_addr(sW1), kTcLbo, 256);
+      const uint64_t dB1 = tc05::smem_desc(tc05::smem_addr(sB1), kTcLbo, 256);
+      const uint64_t dOnes = tc05::smem_desc(aOnes, kTcLbo, 256);
       bool ok = true;
       for (uint32_t j = 0; ok && j < my_tiles + kTcStages - 1; j++) {
         if (j < my_tiles) {
@@ -524,8 +520,8 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) mlp_infer_tc_kerne
           }
           if (!tc05::mbar_wait(&full[st], (jj / kTcStages) & 1u, wait_limit)) { ok = false; break; }
           tc05::fence_after_sync();
-          tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(aX + st * 4096, 2048, 128),
-                         tc05::smem_desc(aW1, kTcLbo, 256), kId32, false);
+          tc05::mma_bf16(tbase + a * 32u, dX + uint64_t((st * 4096u) >> 4), dW1, kId32, false);
+          tc05::mma_bf16(tbase + a * 32u, dOnes, dB1, kId32, true);
           tc05::mma_commit(&l1[a]);
           tc05::mma_commit(&empty[st]);   // the stage is free once layer 1 has read it
           consumed = jj + 1;
@@ -537,73 +533,65 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) mlp_infer_tc_kerne
     }
   } else {
     // ---- epilogue: group g takes tiles g, g + 2, ...; warp w reads TMEM lanes
-    // 32 * (w % 4) .. + 31 (rows of the tile).  The group's first warp issues the
-    // group's layers 2 and 3 once all four warps have written the layer's input.
+    // 32 * (w % 4) .. + 31 (rows of the tile).  The group's first warp waits for
+    // each layer's completion barrier and issues the group's layers 2 and 3; the
+    // four warps meet on the group's named barrier (id 1 + g), where they sleep.
     constexpr uint32_t kId32 = tc05::idesc_bf16_f32(128, 32), kId16 = tc05::idesc_bf16_f32(128, 16);
     const uint32_t g = (warp - 1) >> 2, q = warp & 3u, row = 32u * q + lane, trow = tbase + ((32u * q) << 16);
+    const uint32_t bar = 1u + g;
     const bool leader = ((warp - 1) & 3u) == 0;   // the whole warp waits, its lane 0 issues
+    // the layers' shared-memory descriptors, built once (a slot's hidden operand
+    // descriptor is dH plus the slot's offset in 16-byte units)
+    struct LayerDesc {
+      uint64_t w0, w1, bias;
+      uint32_t idesc;
+    };
     const uint32_t aW2 = tc05::smem_addr(sW2), aW3 = tc05::smem_addr(sW3);
-    bool ok = true;
-    for (uint32_t j = g; j < my_tiles; j += 2) {
+    const LayerDesc d2{tc05::smem_desc(aW2, kTcLbo, 512), tc05::smem_desc(aW2 + 2 * kTcLbo, kTcLbo, 512),
+                       tc05::smem_desc(tc05::smem_addr(sB2), kTcLbo, 256), kId32};
+    const LayerDesc d3{tc05::smem_desc(aW3, kTcLbo, 512), tc05::smem_desc(aW3 + 2 * kTcLbo, kTcLbo, 512),
+                       tc05::smem_desc(tc05::smem_addr(sB3), kTcLbo, 256), kId16};
+    const uint64_t dH = tc05::smem_desc(tc05::smem_addr(sH), kTcLbo, 512);
+    const uint64_t dOnes = tc05::smem_desc(aOnes, kTcLbo, 256);
+    bool failed = false;
+    // the leader waits for `done`; false in every warp of the group on a timeout
+    auto group_wait = [&](uint64_t *done, uint32_t ph) {
+      bool bad = false;
+      if (leader) bad = !tc05::mbar_wait(done, ph, wait_limit);
+      return !tc05::bar_or(bar, 128, bad);
+    };
+    for (uint32_t j = g; j < my_tiles && !failed; j += 2) {
       const uint32_t a = j % kTcAcc, ph = (j / kTcAcc) & 1u;
       uint8_t *const hb = sH + a * kTcHidBytes;
-      const uint32_t h = tc05::smem_addr(hb);
-      if (!tc05::mbar_wait(&l1[a], ph, wait_limit)) { ok = false; break; }
-      tc05::fence_after_sync();
-      hidden_to_smem(trow + a * 32u, sb1, hb, row);
-      tc05::fence_proxy_async();
-      tc05::fence_before_sync();
-      __syncwarp();
-      if (lane == 0) tc05::mbar_arrive(&h1[a]);
-      if (leader) {   // layer 2 (N = 32, K = 2 x 16)
-        const bool ready = tc05::mbar_wait(&h1[a], ph, wait_limit);
-        if (lane == 0) {
-          if (ready) {
-            tc05::fence_after_sync();
-            tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(h, kTcLbo, 512), tc05::smem_desc(aW2, kTcLbo, 512), kId32,
-                           false);
-            tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(h + 2 * kTcLbo, kTcLbo, 512),
-                           tc05::smem_desc(aW2 + 2 * kTcLbo, kTcLbo, 512), kId32, true);
-            tc05::mma_commit(&l2[a]);
-          } else {
-            atomicOr(status, 2u);
-          }
+#pragma unroll 1
+      for (int layer = 1; layer <= 2; layer++) {
+        if (!group_wait(layer == 1 ? &l1[a] : &l2[a], ph)) { failed = true; break; }
+        tc05::fence_after_sync();
+        hidden_to_smem(trow + a * 32u, hb, row);
+        tc05::fence_proxy_async();
+        tc05::fence_before_sync();
+        tc05::bar_sync(bar, 128);   // the tile's 128 rows of this layer's output are in shared memory
+        if (leader && lane == 0) {  // the next layer: products of this layer's output, then its bias block
+          tc05::fence_after_sync();
+          const LayerDesc &L = layer == 1 ? d2 : d3;
+          const uint64_t ha = dH + uint64_t((a * kTcHidBytes) >> 4);   // the slot's hidden operand
+          const uint32_t d = tbase + a * 32u;
+          tc05::mma_bf16(d, ha, L.w0, L.idesc, false);
+          tc05::mma_bf16(d, ha + (2 * kTcLbo >> 4), L.w1, L.idesc, true);
+          tc05::mma_bf16(d, dOnes, L.bias, L.idesc, true);
+          tc05::mma_commit(layer == 1 ? &l2[a] : &l3[a]);
         }
-        __syncwarp();
       }
-      if (!tc05::mbar_wait(&l2[a], ph, wait_limit)) { ok = false; break; }
-      tc05::fence_after_sync();
-      hidden_to_smem(trow + a * 32u, sb2, hb, row);
-      tc05::fence_proxy_async();
-      tc05::fence_before_sync();
-      __syncwarp();
-      if (lane == 0) tc05::mbar_arrive(&h2[a]);
-      if (leader) {   // layer 3 (N = 16, K = 2 x 16)
-        const bool ready = tc05::mbar_wait(&h2[a], ph, wait_limit);
-        if (lane == 0) {
-          if (ready) {
-            tc05::fence_after_sync();
-            tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(h, kTcLbo, 512), tc05::smem_desc(aW3, kTcLbo, 512), kId16,
-                           false);
-            tc05::mma_bf16(tbase + a * 32u, tc05::smem_desc(h + 2 * kTcLbo, kTcLbo, 512),
-                           tc05::smem_desc(aW3 + 2 * kTcLbo, kTcLbo, 512), kId16, true);
-            tc05::mma_commit(&l3[a]);
-          } else {
-            atomicOr(status, 2u);
-          }
-        }
-        __syncwarp();
-      }
-      if (!tc05::mbar_wait(&l3[a], ph, wait_limit)) { ok = false; break; }
+      if (failed || !group_wait(&l3[a], ph)) { failed = true; break; }
       tc05::fence_after_sync();
       const float y = tc05::tmem_ld1(trow + a * 32u);
       const uint64_t gi = tile_of(j) * 128 + row;
-      if (gi >= data.first && gi < data.first + data.n) out[gi - data.first] = y + sb3;
+      if (gi >= data.first && gi < data.first + data.n) out[gi - data.first] = y;
       tc05::fence_before_sync();
-      __syncwarp();
-      if (lane == 0) tc05::mbar_arrive(&afree[a]);
+      tc05::bar_sync(bar, 128);     // all four warps have read the slot
+      if (leader && lane == 0) tc05::mbar_arrive(&afree[a]);
     }
-    if (!ok) atomicOr(status, 2u);
+    if (failed && leader && lane == 0) atomicOr(status, 2u);
     if (leader && lane == 0) {   // every MMA this thread issued has completed before the TMEM is freed
       tc05::mma_commit(&fin[1 + g]);
       if (!tc05::mbar_wait(&fin[1 + g], 0, kTcWait)) atomicOr(status, 2u);

@@ -11,6 +11,7 @@
 
 #include "ctx_internal.h"
 #include "lrt_proposal.h"
+#include "mlp_image.h"
 #include "proposal_internal.h"
 
 namespace lrt {
@@ -75,7 +76,7 @@ lrt_status ensure(lrt_ctx *ctx) {
   ctx->prop = p;
   LRT_CUDA(ctx, cudaSetDevice(ctx->device));
   for (auto *b : {&p->master, &p->grad, &p->adam_m, &p->adam_v}) LRT_CUDA(ctx, b->ensure(LRT_MLP_PARAMS));
-  LRT_CUDA(ctx, p->wbf.ensure(1792));
+  LRT_CUDA(ctx, p->wbf.ensure(lrt::mlp::kBfWords));
   LRT_CUDA(ctx, p->ticket.ensure(1));
   LRT_CUDA(ctx, p->count.ensure(1));
   LRT_CUDA(ctx, p->stats.ensure(4));
@@ -114,10 +115,8 @@ extern "C" lrt_status lrt_proposal_set_weights(lrt_ctx *ctx, const float *params
   ProposalState &p = *ctx->prop;
   LRT_CUDA(ctx, cudaSetDevice(ctx->device));
   LRT_CUDA(ctx, cudaMemcpy(p.master.p, params, 4 * LRT_MLP_PARAMS, cudaMemcpyHostToDevice));
-  std::vector<uint16_t> bf(1792, 0);
-  for (int i = 0; i < 512; i++) bf[i] = lrt::f2bf(params[i]);                 // W1
-  for (int i = 0; i < 1024; i++) bf[512 + i] = lrt::f2bf(params[544 + i]);    // W2
-  for (int i = 0; i < 32; i++) bf[1536 + i] = lrt::f2bf(params[1600 + i]);    // W3 (row 0 of 8)
+  std::vector<uint16_t> bf(lrt::mlp::kBfWords, 0);
+  for (int i = 0; i < lrt::mlp::kBfWords; i++) bf[i] = lrt::mlp::weight_image_word(params, i);
   LRT_CUDA(ctx, cudaMemcpy(p.wbf.p, bf.data(), bf.size() * 2, cudaMemcpyHostToDevice));
   LRT_CUDA(ctx, cudaMemset(p.adam_m.p, 0, 4 * LRT_MLP_PARAMS));
   LRT_CUDA(ctx, cudaMemset(p.adam_v.p, 0, 4 * LRT_MLP_PARAMS));

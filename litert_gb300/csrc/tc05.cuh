@@ -63,12 +63,15 @@ __device__ __forceinline__ void mma_commit(uint64_t *mbar) {
 __device__ __forceinline__ void mbar_init(uint64_t *mbar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(mbar)), "r"(count) : "memory");
 }
+// One poll: the thread may sleep up to kMbarSuspendNs (woken when the phase
+// completes), so a waiting warp issues few instructions.
+constexpr uint32_t kMbarSuspendNs = 1000;
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *mbar, uint32_t phase) {
   uint32_t ok = 0;
   asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
       : "=r"(ok)
-      : "r"(smem_addr(mbar)), "r"(phase)
+      : "r"(smem_addr(mbar)), "r"(phase), "r"(kMbarSuspendNs)
       : "memory");
   return ok != 0;
 }
@@ -89,13 +92,28 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
                "l"(src), "r"(bytes), "r"(smem_addr(mbar))
                : "memory");
 }
-// bounded wait: false after `limit` polls (the caller records the timeout)
+// bounded wait: false after `limit` polls, each at most about kMbarSuspendNs
+// (the caller records the timeout)
 __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t phase, uint32_t limit) {
   for (uint32_t i = 0; i < limit; i++)
     if (mbar_try_wait(mbar, phase)) return true;
   return false;
 }
 
+// named barrier `id` over `n` threads (whole warps); the waiting warps sleep
+__device__ __forceinline__ void bar_sync(uint32_t id, uint32_t n) {
+  asm volatile("barrier.cta.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+// the same, returning whether any of the `n` threads passed v = true
+__device__ __forceinline__ bool bar_or(uint32_t id, uint32_t n, bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n barrier.cta.red.or.pred q, %2, %3, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+      : "=r"(r)
+      : "r"(uint32_t(v)), "r"(id), "r"(n)
+      : "memory");
+  return r != 0;
+}
 __device__ __forceinline__ void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 // generic-proxy shared-memory writes made visible to the tensor core (async proxy)

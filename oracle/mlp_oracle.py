@@ -2,8 +2,10 @@
 and backward of the 16-32-32-1 ReLU MLP with the GPU kernels' BF16 rounding
 points (features and weights rounded to BF16; hidden activations and
 activation gradients rounded to BF16 where they enter a tensor-core product;
-FP32 elsewhere), accumulated in double.  Used by tests/ to check the GPU
-training kernel's loss and gradient."""
+FP32 elsewhere), accumulated in double, with the exact FP32 biases (the
+kernels add each bias inside the tensor core as three BF16 terms whose sum is
+within about 2^-24 of it).  Used by tests/ to check the GPU training kernel's
+loss and gradient."""
 import numpy as np
 
 OFF_W1, OFF_B1, OFF_W2, OFF_B2, OFF_W3, OFF_B3 = 0, 512, 544, 1568, 1600, 1632

@@ -51,7 +51,7 @@ def test_tcgen05_wait_timeout_then_recovers():
         with pytest.raises(lrt.LrtError) as e:
             pp.infer(s, 0, 5000, engine=pp.ENGINE_TCGEN05)
         assert e.value.status == 5   # LRT_ERR_TIMEOUT
-        s.set_tuning("tc_wait", 1 << 22)
+        s.set_tuning("tc_wait", 1 << 20)
         y_tc = pp.infer(s, 0, 5000, engine=pp.ENGINE_TCGEN05)
         y_mma = pp.infer(s, 0, 5000, engine=pp.ENGINE_MMA)
         assert np.abs(y_tc - y_mma).max() <= 1e-3 * (np.abs(y_mma).max() + 1e-6)
