@@ -374,22 +374,41 @@ __device__ bool brick_visit(const DevScene &s, uint32_t node, float3 pos, float3
       }
     }
   }
-  for (uint32_t step = 0; bnf.x < bnf.y && step < max_steps; step++) {
-    const float3 hit_pos = add(pos, scl(bnf.x, dir));
-    const float3 lp = scr(sub(hit_pos, B.bmin), B.scale);
-    const float3 vox = f3(floorf(clampf(lp.x, 1e-6f, bs - 1e-6f)), floorf(clampf(lp.y, 1e-6f, bs - 1e-6f)),
-                          floorf(clampf(lp.z, 1e-6f, bs - 1e-6f)));
-    const float3 min_pos = add(B.bmin, scl(B.d, vox));
-    const float3 max_pos = add(min_pos, scl(B.d, f3(1, 1, 1)));
-    float values[8];
-    load_vals(s, node, vox, values);
-    const float2 fnf = ray_box(pos, inv, min_pos.x, min_pos.y, min_pos.z, max_pos.x, max_pos.y, max_pos.z);
-    float vmin = values[0], vmax = fabsf(values[0]);
+  // Two nested loops: the inner one steps through voxels (applying the skips)
+  // until one needs Intersect or the brick ends; Intersect runs after it.  A
+  // lane's sequence of voxels is the single loop's, but the lanes of a warp that
+  // reach an intersected voxel after different numbers of steps run it together.
+  uint32_t step = 0;
+  for (;;) {
+    bool cand = false;
+    float3 vox, min_pos;
+    float2 fnf;
+    float values[8], vmax = 0.0f;
+    while (bnf.x < bnf.y && step < max_steps) {
+      const float3 hit_pos = add(pos, scl(bnf.x, dir));
+      const float3 lp = scr(sub(hit_pos, B.bmin), B.scale);
+      vox = f3(floorf(clampf(lp.x, 1e-6f, bs - 1e-6f)), floorf(clampf(lp.y, 1e-6f, bs - 1e-6f)),
+               floorf(clampf(lp.z, 1e-6f, bs - 1e-6f)));
+      min_pos = add(B.bmin, scl(B.d, vox));
+      const float3 max_pos = add(min_pos, scl(B.d, f3(1, 1, 1)));
+      load_vals(s, node, vox, values);
+      fnf = ray_box(pos, inv, min_pos.x, min_pos.y, min_pos.z, max_pos.x, max_pos.y, max_pos.z);
+      step++;
+      float vmin = values[0];
+      vmax = fabsf(values[0]);
 #pragma unroll
-    for (int i = 1; i < 8; i++) { vmin = fminf(vmin, values[i]); vmax = fmaxf(vmax, fabsf(values[i])); }
-    if (tNear < fnf.x && vmin > (BORDER ? fminf(rl->sdf, rl->skip_t) : 0.0f) + skip_margin(vmax)) {
-      skipped_intersect<BORDER>(rl, BORDER && !(vmin > rl->sdf + skip_margin(vmax)));
-    } else if (tNear < fnf.x) {
+      for (int i = 1; i < 8; i++) { vmin = fminf(vmin, values[i]); vmax = fmaxf(vmax, fabsf(values[i])); }
+      if (tNear < fnf.x) {
+        if (!(vmin > (BORDER ? fminf(rl->sdf, rl->skip_t) : 0.0f) + skip_margin(vmax))) {
+          cand = true;
+          break;
+        }
+        skipped_intersect<BORDER>(rl, BORDER && !(vmin > rl->sdf + skip_margin(vmax)));
+      }
+      bnf.x += mx(0.0f, fnf.y - bnf.x) + 1e-6f;
+    }
+    if (!cand) return false;
+    {
       const float3 start_q = scr(sub(add(pos, scl(fnf.x, dir)), min_pos), B.scale);
       const float qFar = (fnf.y - fnf.x) * B.scale;
       const float prev = BORDER ? rl->sdf : 0.0f;
@@ -434,7 +453,6 @@ __device__ bool brick_visit(const DevScene &s, uint32_t node, float3 pos, float3
     }
     bnf.x += mx(0.0f, fnf.y - bnf.x) + 1e-6f;
   }
-  return false;
 }
 
 // BVH2TraverseF32WithGrad (:106-167) with stopOnFirstHit; leaves hold one brick,
