@@ -5,7 +5,9 @@
 // jump: if every voxel of the voxel-index box spanned by the segment's entry
 // voxel and the predicted voxel (the predicted voxel excepted) is empty in the
 // brick's occupancy mask (no corner <= 0, so the reference's walk would run no
-// finder there), the walk starts at the predicted voxel's entry instead of the
+// finder there), and the walk's first voxel at the predicted voxel's entry (which
+// rounding may put next to it) is the predicted voxel or one of those empty
+// voxels, the walk starts at the predicted voxel's entry instead of the
 // brick's; from there on it is the reference walk with the reference finder
 // (BVH/BVH2Common.cpp:764-984, 437-522), which refines the crossing exactly.
 // Otherwise the plain walk runs from the brick entry.  Hits therefore equal the
@@ -100,9 +102,17 @@ __device__ float proposal_start(const DevScene &s, uint32_t brick, float3 rp, fl
   const float nx = inv.x * ((inv.x > 0.0f ? mp.x : mp.x + d) - rp.x);
   const float ny = inv.y * ((inv.y > 0.0f ? mp.y : mp.y + d) - rp.y);
   const float nz = inv.z * ((inv.z > 0.0f ? mp.z : mp.z + d) - rp.z);
+  const float start = fmx(fmx(nx, ny), nz);
+  // the walk's first voxel at that distance, as the walk computes it: on the entry
+  // plane, rounding may put it next to the predicted voxel; it must be the predicted
+  // voxel or one of the box's (empty) voxels, else no jump
+  const int3 w = walk_voxel(rp, rd, fmx(t0, start), bmin, scale, bs);
+  const bool w_ok = (w.x == vh.x && w.y == vh.y && w.z == vh.z) ||
+                    (w.x >= x0 && w.x <= x1 && w.y >= y0 && w.y <= y1 && w.z >= z0 && w.z <= z1);
+  if (!w_ok) return none;
   jumped = true;
   skipped = uint32_t(abs(vh.x - v0.x) + abs(vh.y - v0.y) + abs(vh.z - v0.z));   // voxel faces crossed
-  return fmx(fmx(nx, ny), nz);
+  return start;
 }
 
 __device__ __forceinline__ uint32_t hash3(uint32_t a, uint32_t b, uint32_t c) {
