@@ -176,7 +176,7 @@ __device__ __forceinline__ void visit_node(const DevScene &s, uint32_t ref, floa
     const uint32_t cha[4] = {ch.x, ch.y, ch.z, ch.w};
     // child entry distances and refs; a missed child sorts last (key -inf)
     float kt[4];
-    uint32_t kr[4], ki[4];
+    uint32_t kr[4];
     int nk = 0;
 #pragma unroll
     for (int i = 0; i < 4; i++) {
@@ -184,22 +184,28 @@ __device__ __forceinline__ void visit_node(const DevScene &s, uint32_t ref, floa
       const bool h = (tm.x <= tm.y) && (tm.y >= tNear) && (tm.x <= hit_t) && cha[i] != kEmptyChild;
       kt[i] = h ? tm.x : -__int_as_float(0x7f800000);
       kr[i] = cha[i];
-      ki[i] = uint32_t(i);
       nk += h ? 1 : 0;
     }
-    // far-to-near order (the nearest child is popped first) by a 5-exchange sorting
-    // network on registers: descending entry distance, equal distances in child
-    // order -- the order a stable insertion sort gives
-#define LRT_CE(a, b)                                                                        \
-    {                                                                                       \
-      const bool sw = kt[b] > kt[a] || (kt[b] == kt[a] && ki[b] < ki[a]);                   \
-      const float t0 = sw ? kt[b] : kt[a], t1 = sw ? kt[a] : kt[b];                         \
-      const uint32_t r0 = sw ? kr[b] : kr[a], r1 = sw ? kr[a] : kr[b];                      \
-      const uint32_t i0 = sw ? ki[b] : ki[a], i1 = sw ? ki[a] : ki[b];                      \
-      kt[a] = t0; kt[b] = t1; kr[a] = r0; kr[b] = r1; ki[a] = i0; ki[b] = i1;               \
-    }
-    LRT_CE(0, 1) LRT_CE(2, 3) LRT_CE(0, 2) LRT_CE(1, 3) LRT_CE(1, 2)
+    // a vote among the lanes that are here together (the traversal loop diverges)
+    if (__any_sync(__activemask(), nk > 1)) {
+      // far-to-near order (the nearest child is popped first) by a 5-exchange
+      // sorting network on registers, descending entry distance
+#define LRT_CE(a, b)                                                \
+      {                                                             \
+        const bool sw = kt[b] > kt[a];                              \
+        const float t0 = sw ? kt[b] : kt[a], t1 = sw ? kt[a] : kt[b]; \
+        const uint32_t r0 = sw ? kr[b] : kr[a], r1 = sw ? kr[a] : kr[b]; \
+        kt[a] = t0; kt[b] = t1; kr[a] = r0; kr[b] = r1;             \
+      }
+      LRT_CE(0, 1) LRT_CE(2, 3) LRT_CE(0, 2) LRT_CE(1, 3) LRT_CE(1, 2)
 #undef LRT_CE
+    } else {
+      // no lane voting here entered more than one child: move the entered one (if
+      // any) to the front, no ordering needed
+#pragma unroll
+      for (int i = 1; i < 4; i++)
+        if (kt[i] > kt[0]) { kt[0] = kt[i]; kr[0] = kr[i]; }
+    }
     // The host rejects trees deeper than the stack allows ((W-1)*depth + 1 entries),
     // so this bound never drops an entry.
 #pragma unroll
