@@ -123,7 +123,13 @@ lrt_status lrt_dr_get(lrt_ctx *ctx, uint32_t what, uint32_t view, void *out, uin
 /* dr::BVHDR::RayQuery_NearestHitWithGrad (diff_render/BVH2DR.cpp:12-102) on n rays
  * (float4 pos+tNear, float4 dir+tFar, host memory) with DR_RAY_FLAG_* bits
  * (1 dDiffuse/dColour, 2 dDiffuse/dPos, 4 dNorm/dPos, 8 border, 16 dDist/dPos)
- * and the render mode of the current preset.  Writes 32 words per ray: hit t,
+ * and the render mode of the current preset.  Bit 32 (no reference counterpart)
+ * runs the border integral's walk instead of the border walk: voxels whose
+ * corner values all exceed the preset's border_relax_eps are skipped from the
+ * start, and a ray is walked again in full where that could change its record;
+ * for every ray whose relaxation SDF ends below border_relax_eps the record is
+ * the border walk's, bit for bit (the others contribute nothing to the border
+ * integral; their relaxation fields may differ).  Writes 32 words per ray: hit t,
  * primId, colour[3], normal[3]; the border relaxation point missed_hit t, sdf,
  * colour[3], normal[3]; missed_indices[8]; missed_dSDF_dtheta[8]. */
 lrt_status lrt_dr_query_rays(lrt_ctx *ctx, uint32_t flags, const float *pos_near, const float *dir_far, uint32_t n,

@@ -27,7 +27,7 @@ namespace lrt {
 namespace drk {
 using namespace lrt::dev;
 
-enum : uint32_t { F_DCOLOR = 1, F_DDIFFUSE = 2, F_DNORM = 4, F_BORDER = 8, F_DDIST = 16 };
+enum : uint32_t { F_DCOLOR = 1, F_DDIFFUSE = 2, F_DNORM = 4, F_BORDER = 8, F_DDIST = 16, F_BORDER_EARLY = 32 };
 enum : uint32_t { R_DIFFUSE = 0, R_LAMBERT = 1, R_MASK = 2, R_LINEAR_DEPTH = 3, R_NORMAL = 4 };
 
 struct M3 {
@@ -535,11 +535,12 @@ __device__ void query(const DevScene &s, float3 P, float3 D, float tfar, HitRec 
 // A border sample's query: the walk with early skipping below relax_eps, and the
 // reference's own walk again where the skipping could have changed the record
 // (Relax::flags); the record is the reference walk's in either case.
-__device__ __forceinline__ void border_query(const DevScene &s, float3 P, float3 D, float eps, HitRec &hr, Relax &rl) {
+__device__ __forceinline__ void border_query(const DevScene &s, float3 P, float3 D, float eps, HitRec &hr, Relax &rl,
+                                             float tfar = 1e9f) {
   float skip_t = eps;
 #pragma unroll 1
   for (int pass = 0; pass < 2; pass++) {
-    query<true>(s, P, D, 1e9f, hr, &rl, skip_t);
+    query<true>(s, P, D, tfar, hr, &rl, skip_t);
     if (!(rl.flags & 1u) && !(rl.sdf < eps && !(rl.flags & 2u))) break;
     skip_t = __builtin_huge_valf();
   }
@@ -1307,8 +1308,8 @@ __global__ void dr_adam_kernel(float *x, float *V, float *S, const float *g, uin
 // RayQuery_NearestHitWithGrad on a batch of rays (diff_render/BVH2DR.cpp:12-102):
 // the hit (t, primId, colour, normal) and the border relaxation point (t, sdf,
 // colour, normal, indices, dSDF/dtheta), 32 words per ray
-__global__ void dr_query_kernel(DevScene s, uint32_t flags, const float4 *pos, const float4 *dir, uint32_t n,
-                                uint32_t *out) {
+__global__ void dr_query_kernel(DevScene s, uint32_t flags, float relax_eps, const float4 *pos, const float4 *dir,
+                                uint32_t n, uint32_t *out) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float4 P4 = pos[i], D4 = dir[i];
@@ -1317,7 +1318,9 @@ __global__ void dr_query_kernel(DevScene s, uint32_t flags, const float4 *pos, c
   const float tfar = D4.w <= 0.0f ? -D4.w : D4.w;
   HitRec hr;
   Relax rl;
-  if (flags & F_BORDER) {
+  if (flags & F_BORDER_EARLY) {   // the border integral's walk (early skipping below relax_eps)
+    border_query(s, P, D, relax_eps, hr, rl, tfar);
+  } else if (flags & F_BORDER) {
     query<true>(s, P, D, tfar, hr, &rl);
   } else {
     query<false>(s, P, D, tfar, hr, nullptr);
@@ -1347,9 +1350,9 @@ __global__ void dr_query_kernel(DevScene s, uint32_t flags, const float4 *pos, c
   for (int k = 0; k < 8; k++) { o[16 + k] = rl.idx[k]; o[24 + k] = __float_as_uint(rl.dth[k]); }
 }
 
-void launch_query(const DevScene &s, uint32_t flags, const float4 *pos, const float4 *dir, uint32_t n, uint32_t *out,
-                  cudaStream_t st) {
-  dr_query_kernel<<<(n + 127) / 128, 128, 0, st>>>(s, flags, pos, dir, n, out);
+void launch_query(const DevScene &s, uint32_t flags, float relax_eps, const float4 *pos, const float4 *dir, uint32_t n,
+                  uint32_t *out, cudaStream_t st) {
+  dr_query_kernel<<<(n + 127) / 128, 128, 0, st>>>(s, flags, relax_eps, pos, dir, n, out);
 }
 
 // per brick: its distance values gathered from the parameters (a float copy in

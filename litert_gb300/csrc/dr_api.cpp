@@ -750,7 +750,7 @@ extern "C" lrt_status lrt_dr_query_rays(lrt_ctx *ctx, uint32_t flags, const floa
                                         uint32_t n, uint32_t *out) {
   if (!ctx || !ctx->dr || !ctx->dr->has_scene) return fail(ctx, LRT_ERR_STATE, "lrt_dr_set_scene first");
   if (!pos_near || !dir_far || !out || n == 0) return fail(ctx, LRT_ERR_INVALID, "empty ray batch");
-  if (flags & ~31u) return fail(ctx, LRT_ERR_INVALID, "unknown ray flags");
+  if (flags & ~63u) return fail(ctx, LRT_ERR_INVALID, "unknown ray flags");
   DrState &st = *ctx->dr;
   LRT_CUDA(ctx, cudaSetDevice(ctx->device));
   DevBuf<float4> dp, dd;
@@ -764,7 +764,7 @@ extern "C" lrt_status lrt_dr_query_rays(lrt_ctx *ctx, uint32_t flags, const floa
   }
   drk::launch_brick_bounds(dev_scene(ctx), st.n_nodes, st.d_bounds.p, 0);
   drk::DevScene s = dev_scene(ctx);
-  drk::launch_query(s, flags, dp.p, dd.p, n, dout.p, 0);
+  drk::launch_query(s, flags, st.preset.border_relax_eps, dp.p, dd.p, n, dout.p, 0);
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpy(out, dout.p, size_t(n) * 32 * 4, cudaMemcpyDeviceToHost);
   dp.release(); dd.release(); dout.release();

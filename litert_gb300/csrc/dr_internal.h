@@ -83,8 +83,8 @@ void launch_adam(float *x, float *V, float *S, const float *g, uint32_t n, float
                  float b2, float eps, double c1, double c2, cudaStream_t st);
 void launch_scale(float *g, uint32_t n, float s, cudaStream_t st);
 void launch_brick_bounds(const DevScene &s, uint32_t n_nodes, float2 *out, cudaStream_t st);
-void launch_query(const DevScene &s, uint32_t flags, const float4 *pos, const float4 *dir, uint32_t n, uint32_t *out,
-                  cudaStream_t st);
+void launch_query(const DevScene &s, uint32_t flags, float relax_eps, const float4 *pos, const float4 *dir, uint32_t n,
+                  uint32_t *out, cudaStream_t st);
 
 }  // namespace drk
 }  // namespace lrt
