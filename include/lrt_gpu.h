@@ -199,7 +199,11 @@ lrt_status lrt_render_host(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views
  * latency are not acceptable.  Same results as lrt_render for the committed
  * scene (the inputs were allocated once, by lrt_commit_scene), rendered with
  * the plain finder: the "proposal" tuning key is ignored here (the proposal
- * kernels need the network's buffers, which this call does not touch).  The
+ * kernels need the network's buffers, which this call does not touch).  With
+ * "first_hit" set it renders the reference's first-hit walk like lrt_render,
+ * whose tree is put on the device by the first lrt_render, lrt_query_rays or
+ * lrt_set_bvh2 call after a commit; before that, this call returns
+ * LRT_ERR_STATE rather than allocate it.  The
  * per-call scratch -- the persistent kernel's work-queue head and the per-view
  * table -- lives in one file-scope device array of 256 +
  * LRT_NOALLOC_MAX_VIEWS * 160 bytes that every GPU loading the library keeps

@@ -908,9 +908,13 @@ extern "C" lrt_status lrt_render_noalloc(lrt_ctx *ctx, const lrt_view *views, ui
   }
   if (pix >= (1ull << 32) || tiles >= (1ull << 32)) return LRT_ERR_INVALID;
   if (!stack_fits(ctx)) return LRT_ERR_UNSUPPORTED;
+  // "first_hit": the reference's walk needs its tree on the device; uploading it
+  // would allocate, so an earlier call must have done so
+  const bool first_hit = ctx->tuning.first_hit && sdf_scene(ctx->dev);
+  if (first_hit && !ctx->ref_pairs_ready) return LRT_ERR_STATE;
   const cudaError_t e = launch_render_noalloc(ctx->dev, hv, n_views, uint32_t(tiles), hits16,
                                               reinterpret_cast<float4 *>(rgba), rgba8, ctx->device, ctx->num_sms,
-                                              static_cast<cudaStream_t>(stream), ctx->tuning);
+                                              static_cast<cudaStream_t>(stream), ctx->tuning, first_hit);
   if (e != cudaSuccess) return e == cudaErrorInvalidValue ? LRT_ERR_INVALID : LRT_ERR_CUDA;
   ctx->last_launches = 2;   // set-up kernel + render kernel
   return LRT_OK;

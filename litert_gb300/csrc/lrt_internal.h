@@ -201,7 +201,7 @@ cudaError_t launch_render_packet(const DevScene &s, const RenderLaunch &L, int n
 // lrt_render_noalloc: same kernels, scratch in a file-scope device array (trace.cu).
 cudaError_t launch_render_noalloc(const DevScene &s, const DevView *host_views, uint32_t n_views,
                                   uint32_t total_tiles, lrt_hit16 *hits16, float4 *rgba, uint32_t *rgba8,
-                                  int device, int num_sms, cudaStream_t st, const Tuning &tu);
+                                  int device, int num_sms, cudaStream_t st, const Tuning &tu, bool first_hit);
 cudaError_t launch_query(const DevScene &s, const float4 *pos_near, const float4 *dir_far, uint32_t n,
                          lrt_hit *out, cudaStream_t st);
 // The same two launches with the reference's first-hit BVH2 walk (trace_ref.cu);

@@ -355,7 +355,7 @@ __global__ void __launch_bounds__(256) noalloc_setup_kernel(const __grid_constan
 
 cudaError_t launch_render_noalloc(const DevScene &s, const DevView *host_views, uint32_t n_views,
                                   uint32_t total_tiles, lrt_hit16 *hits16, float4 *rgba, uint32_t *rgba8,
-                                  int device, int num_sms, cudaStream_t st, const Tuning &tu) {
+                                  int device, int num_sms, cudaStream_t st, const Tuning &tu, bool first_hit) {
   if (n_views == 0 || n_views > LRT_NOALLOC_MAX_VIEWS) return cudaErrorInvalidValue;
   unsigned char *scratch = nullptr;
   cudaError_t e = noalloc_scratch(device, &scratch);
@@ -378,7 +378,7 @@ cudaError_t launch_render_noalloc(const DevScene &s, const DevView *host_views, 
   L.rgba8 = rgba8;
   L.tile_counter = head;
   L.counters = nullptr;
-  return launch_render(s, L, num_sms, st, false, tu);
+  return first_hit ? launch_render_ref(s, L, num_sms, st) : launch_render(s, L, num_sms, st, false, tu);
 }
 
 }  // namespace lrt

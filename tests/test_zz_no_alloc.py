@@ -74,3 +74,40 @@ def test_render_noalloc_matches_render_on_two_calls():
         assert st == 1   # LRT_ERR_INVALID
     finally:
         s.close()
+
+
+def test_render_noalloc_first_hit_after_the_tree_is_on_the_device():
+    """With the "first_hit" tuning key the entry point renders the reference's
+    first-hit walk, as lrt_render does.  That walk's tree is put on the device
+    by the first allocating call after a commit; before it, the entry point
+    refuses (LRT_ERR_STATE) instead of allocating."""
+    import torch
+
+    s = _scene()
+    try:
+        s.set_tuning("first_hit", 1)
+        views = scenes.union_views(n_views=2, lo=96, hi=128)
+        npix = sum(w * h for w, h, _, _ in views)
+        va = lrt.make_views(views)
+        dev = torch.device("cuda", 0)
+        hits = torch.empty(npix * 4, dtype=torch.float32, device=dev)
+        stream = torch.cuda.current_stream(dev)
+
+        def call():
+            return lrt.lib().lrt_render_noalloc(s._ctx, C.cast(va, C.c_void_p), len(views),
+                                                C.c_void_p(hits.data_ptr()), None, None,
+                                                C.c_void_p(stream.cuda_stream))
+
+        assert call() == 7   # LRT_ERR_STATE: the walk's tree is not on the device yet
+        ref = s.render_host(views, hits=True)["hits"]   # lrt_render uploads it
+        for k in range(2):
+            hits.fill_(float("nan"))
+            assert call() == 0, f"call {k}"
+            torch.cuda.synchronize(dev)
+            got = hits.cpu().numpy().view(lrt.HIT16_DTYPE)
+            assert (got["primId"] != lrt.MISS).sum() > 0
+            assert np.array_equal(got["primId"], ref["primId"]), f"call {k}"
+            for f in ("t", "nx", "ny"):
+                assert np.array_equal(_bits(got[f]), _bits(ref[f])), f"call {k}: {f}"
+    finally:
+        s.close()
