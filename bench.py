@@ -378,6 +378,35 @@ def run_proposal(args, scene, dev, torch):
         ms = statistics.median(ts)
         out[name] = {"ms": ms, "mrays": n / (ms * 1e-3) / 1e6}
         recs[name] = hits.cpu().numpy().view(np.uint32).reshape(-1, 4).copy()
+    # the same with the network trained on the other target: the first voxel the
+    # walk runs the finder in (where a certified jump should land)
+    scene.set_tuning("proposal", 0)
+    scene.set_tuning("proposal_target", 1)
+    pp.set_weights(scene, pp.init_weights(7))
+    pp.clear(scene)
+    pp.collect(scene, train_views, capacity=min(50_000_000, len(train_views) * (1 << 20)))
+    losses_ff = pp.train(scene, args.prop_steps, batch=8192, lr=1e-3, seed=7)
+    scene.set_tuning("proposal_target", 0)
+    scene.set_tuning("proposal", 1)
+    g = scene.graph_create(eval_views, hits_ptr=hits.data_ptr())
+    for _ in range(3):
+        scene.graph_launch(g, stream.cuda_stream)
+    torch.cuda.synchronize(dev)
+    pp.stats(scene)
+    ts = []
+    for i in range(max(args.steps, 5)):
+        flush.fill_(float(i))
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        scene.graph_launch(g, stream.cuda_stream)
+        b.record(stream)
+        b.synchronize()
+        ts.append(a.elapsed_time(b))
+    stats["first_finder"] = pp.stats(scene)
+    lrt.Scene.graph_destroy(g)
+    ms_ff = statistics.median(ts)
+    out["first_finder"] = {"ms": ms_ff, "mrays": n / (ms_ff * 1e-3) / 1e6}
+    recs["first_finder"] = hits.cpu().numpy().view(np.uint32).reshape(-1, 4).copy()
     scene.set_tuning("proposal", 0)
     scene.set_tuning("fma", args.fma)
     st = stats["proposal"]
@@ -407,6 +436,11 @@ def run_proposal(args, scene, dev, torch):
             "trained": per_step(stats["proposal"]), "untrained": per_step(stats["untrained"]),
             "counters": counters,
             "untrained_mrays": out["untrained"]["mrays"],
+            "first_finder_target": {"mrays": out["first_finder"]["mrays"],
+                                    "speedup": out["first_finder"]["mrays"] / out["plain"]["mrays"],
+                                    "records_identical": bool(np.array_equal(recs["plain"], recs["first_finder"])),
+                                    "stats": per_step(stats["first_finder"]),
+                                    "loss_first": float(losses_ff[:10].mean()), "loss_last": float(losses_ff[-100:].mean())},
             "untrained_records_identical": bool(np.array_equal(recs["plain"], recs["untrained"])),
             "triples": int(n_trip), "train_steps": args.prop_steps, "batch": 8192,
             "loss_first": float(losses[:10].mean()), "loss_last": float(losses[-100:].mean()),

@@ -93,8 +93,9 @@ lrt_status lrt_set_preset(lrt_ctx *ctx, const lrt_preset *preset);
  * BVH/BVH2Common.cpp:3402-3405, 3407-3488 -- the reference's own result, which
  * depends on the tree: the committed BVH's pairs, or the caller's through
  * lrt_set_bvh2.  Triangle meshes have no early-out in the reference and keep
- * the closest hit.  Not used by lrt_render_noalloc, lrt_render_counters or the
- * autotuner).
+ * the closest hit.  Not used by lrt_render_counters or the autotuner;
+ * lrt_render_noalloc uses it once the BVH2 is on the device).
+ * "proposal_target": lrt_proposal_collect's target (see lrt_proposal.h).
  * "tc_wait" (default 1048576): how many times the tcgen05 network engine polls
  * a completion barrier before it gives up (a poll sleeps up to about 1 us, so
  * the default bounds a wait near one second); a timeout makes

@@ -31,8 +31,12 @@ lrt_status lrt_proposal_get_weights(lrt_ctx *ctx, float *params);
 
 /* Triples from the plain finder: renders the views (pixel centres) of the
  * committed SBS scene and appends, for every hit, the features of the hit
- * brick's segment and the crossing fraction, keeping at most `capacity`
- * triples in the context.  *n_total: triples held afterwards. */
+ * brick's segment and a target fraction of the segment, keeping at most
+ * `capacity` triples in the context.  *n_total: triples held afterwards.
+ * The target follows the "proposal_target" tuning key: 0 (default) the
+ * crossing; 1 the middle of the first voxel in which the walk would run the
+ * finder (occupied and entered past the ray's start), the farthest point a
+ * jump can be certified to. */
 lrt_status lrt_proposal_collect(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, uint64_t capacity,
                                 uint64_t *n_total);
 /* Drops every triple held. */

@@ -564,6 +564,9 @@ extern "C" lrt_status lrt_set_tuning(lrt_ctx *ctx, const char *key, int value) {
   } else if (k == "bvh_builder") {
     if (value < 0 || value > 2) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: bvh_builder is 0, 1 or 2");
     ctx->bvh_builder = value;
+  } else if (k == "proposal_target") {
+    if (value < 0 || value > 1) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: proposal_target is 0 or 1");
+    ctx->tuning.proposal_target = value;
   } else if (k == "first_hit") {
     if (value < 0 || value > 1) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: first_hit is 0 or 1");
     ctx->tuning.first_hit = value;

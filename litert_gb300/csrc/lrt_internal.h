@@ -164,6 +164,7 @@ struct Tuning {
   int first_hit = 0;        // 1: SBS / SVS renders and queries walk the BVH2 in the reference's order and
                             // stop at the first SDF leaf that hits (BVH2TraverseF32's result)
   int tc_wait = 1 << 20;    // tcgen05 network engine: mbarrier polls (up to ~1 us each) before a timeout
+  int proposal_target = 0; // training target of collected triples: 0 crossing fraction, 1 first finder voxel
 };
 
 cudaError_t launch_render(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st, bool count,

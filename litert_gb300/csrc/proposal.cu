@@ -127,8 +127,40 @@ __device__ __forceinline__ uint32_t hash3(uint32_t a, uint32_t b, uint32_t c) {
 // ---------------------------------------------------------------- triple generation
 // One thread per pixel of the views (regular pixel centres): plain closest-hit
 // trace; a hit yields (features of the hit brick's segment, crossing fraction).
+// The middle of the first voxel of the ray's walk through `brick` in which the
+// walk would run the finder (occupied, entered after tNear), as a distance along
+// the ray: the farthest point a jump can be certified to (every voxel before it
+// on the walk is empty).  The walk's own arithmetic (brick_intersect); t1 when
+// no voxel qualifies.
+__device__ float first_finder_voxel(const DevScene &s, uint32_t brick, float3 rp, float3 rd, float3 inv, float tNear,
+                                    float t0, float t1) {
+  const uint32_t bsz = s.sbs_hdr.brick_size;
+  const uint4 nd = __ldg(reinterpret_cast<const uint4 *>(s.bricks) + brick);
+  const float sz = float(nd.y & 0x0000FFFF), sz_inv = 2.0f / sz, bs = float(bsz), d = 2.0f / (sz * bs);
+  const float scale = 0.5f * sz * bs;
+  const float3 bmin = add(f3(-1, -1, -1), scl(sz_inv, f3(float(nd.x >> 16), float(nd.x & 0xFFFF), float(nd.y >> 16))));
+  const uint32_t *occ = s.occ + size_t(brick) * s.occ_words;
+  const bool posx = inv.x > 0.0f, posy = inv.y > 0.0f, posz = inv.z > 0.0f;
+  float t = t0;
+  const uint32_t max_steps = walk_step_bound(bsz, t1 - t0);
+  for (uint32_t step = 0; t < t1 && step < max_steps; step++) {
+    const int3 v = walk_voxel(rp, rd, t, bmin, scale, bs);
+    const float3 mp = add(bmin, scl(d, f3(float(v.x), float(v.y), float(v.z))));
+    const float ex = fmn(fmn(inv.x * ((posx ? mp.x + d : mp.x) - rp.x), inv.y * ((posy ? mp.y + d : mp.y) - rp.y)),
+                         inv.z * ((posz ? mp.z + d : mp.z) - rp.z));
+    const uint32_t vid = (uint32_t(v.x) * bsz + uint32_t(v.y)) * bsz + uint32_t(v.z);
+    if ((__ldg(&occ[vid >> 5]) >> (vid & 31u)) & 1u) {
+      const float en = fmx(fmx(inv.x * ((posx ? mp.x : mp.x + d) - rp.x), inv.y * ((posy ? mp.y : mp.y + d) - rp.y)),
+                           inv.z * ((posz ? mp.z : mp.z + d) - rp.z));
+      if (tNear < en) return fmn(fmx(0.5f * (en + ex), t0), t1);   // the voxel may reach past the segment
+    }
+    t += fmx(0.0f, ex - t) + 1e-6f;
+  }
+  return t1;
+}
+
 __global__ void __launch_bounds__(128) gen_triples_kernel(DevScene s, const DevView *views, uint32_t n_views,
-                                                          uint64_t total_pix, TripleBuf out) {
+                                                          uint64_t total_pix, TripleBuf out, uint32_t target) {
   const uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= total_pix) return;
   uint32_t v = 0;
@@ -152,7 +184,10 @@ __global__ void __launch_bounds__(128) gen_triples_kernel(DevScene s, const DevV
   dst[feat_u4(k, 0)] = make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]), pack_bf16(f[4], f[5]), pack_bf16(f[6], f[7]));
   dst[feat_u4(k, 1)] =
       make_uint4(pack_bf16(f[8], f[9]), pack_bf16(f[10], f[11]), pack_bf16(f[12], f[13]), pack_bf16(f[14], f[15]));
-  out.target[k] = (hit.t - t0) / (t1 - t0);
+  // target 0: the crossing's fraction of the segment (t*); 1: the first voxel the
+  // walk runs the finder in (where a jump should land)
+  const float tt = target ? first_finder_voxel(s, hit.prim, rp, rd, inv, 0.1f, t0, t1) : hit.t;
+  out.target[k] = (tt - t0) / (t1 - t0);
 }
 
 // ---------------------------------------------------------------- training
@@ -737,9 +772,9 @@ __global__ void __launch_bounds__(128, 4) render_proposal_kernel(DevScene s, Ren
 }  // namespace dev
 
 cudaError_t launch_gen_triples(const DevScene &s, const DevView *views, uint32_t n_views, uint64_t total_pix,
-                               const TripleBuf &out, cudaStream_t st) {
+                               const TripleBuf &out, uint32_t target, cudaStream_t st) {
   const uint64_t blocks = (total_pix + 127) / 128;
-  dev::gen_triples_kernel<<<unsigned(blocks), 128, 0, st>>>(s, views, n_views, total_pix, out);
+  dev::gen_triples_kernel<<<unsigned(blocks), 128, 0, st>>>(s, views, n_views, total_pix, out, target);
   return cudaGetLastError();
 }
 

@@ -188,7 +188,8 @@ extern "C" lrt_status lrt_proposal_collect(lrt_ctx *ctx, const lrt_view *views, 
   const unsigned long long start = p.n;
   LRT_CUDA(ctx, cudaMemcpy(p.count.p, &start, 8, cudaMemcpyHostToDevice));
   lrt::TripleBuf out{p.feat.p, p.target.p, p.count.p, capacity};
-  LRT_CUDA(ctx, lrt::launch_gen_triples(ctx->dev, p.views.p, n_views, pix, out, nullptr));
+  LRT_CUDA(ctx, lrt::launch_gen_triples(ctx->dev, p.views.p, n_views, pix, out,
+                                         uint32_t(ctx->tuning.proposal_target), nullptr));
   unsigned long long cnt = 0;
   LRT_CUDA(ctx, cudaMemcpy(&cnt, p.count.p, 8, cudaMemcpyDeviceToHost));
   p.n = cnt < capacity ? cnt : capacity;

@@ -46,7 +46,7 @@ struct MlpState {
 };
 
 cudaError_t launch_gen_triples(const DevScene &s, const DevView *views, uint32_t n_views, uint64_t total_pix,
-                               const TripleBuf &out, cudaStream_t st);
+                               const TripleBuf &out, uint32_t target, cudaStream_t st);
 cudaError_t launch_mlp_step(const TripleView &data, const MlpState &m, uint32_t batch, uint32_t step, uint32_t seed,
                             bool random, bool update, float lr, float b1, float b2, float eps, cudaStream_t st);
 cudaError_t launch_mlp_infer(const TripleView &data, const MlpState &m, float *out, cudaStream_t st);

@@ -166,10 +166,10 @@ def test_trained_network_skips_voxel_steps(union_scene):
 
 
 def test_tcgen05_matches_mma_on_collected_triples(union_scene):
-    """Both tensor-core engines round at the same points (products summed from zero
-    in the tensor core, bias added after in FP32, ReLU, BF16): on triples collected
-    from plain renders and a trained network their outputs agree to 1e-3 of the
-    output range."""
+    """Both tensor-core engines issue the same sums (products, then the bias's
+    three BF16 terms against a block of ones, all accumulated in FP32 in the
+    tensor core; ReLU, BF16): on triples collected from plain renders and a
+    trained network their outputs agree to 1e-3 of the output range."""
     pp.set_weights(union_scene, pp.init_weights(7))
     pp.clear(union_scene)
     n = pp.collect(union_scene, scenes.union_views(n_views=6, lo=192, hi=320, cam_seed=6), capacity=2_000_000)
@@ -182,3 +182,36 @@ def test_tcgen05_matches_mma_on_collected_triples(union_scene):
     print(f"{n} triples: max |tcgen05 - mma.sync| = {d.max():.3e} ({d.max() / rng:.3e} of the range), "
           f"{int((d > 0).sum())} outputs differ")
     assert d.max() <= 1e-3 * rng
+
+
+def test_first_finder_voxel_target(union_scene):
+    """The "proposal_target" tuning key 1: the same (ray, brick) triples and
+    features, each labelled with the middle of the first voxel the walk runs the
+    finder in (as a fraction of the segment) instead of the crossing; a network
+    trained on it renders the plain kernel's records bit for bit."""
+    views = scenes.union_views(n_views=2, lo=128, hi=192, cam_seed=6)
+    pp.set_weights(union_scene, pp.init_weights(7))
+    pp.clear(union_scene)
+    n0 = pp.collect(union_scene, views, capacity=200000)
+    f0, t0 = pp.get_triples(union_scene, 0, n0)
+    union_scene.set_tuning("proposal_target", 1)
+    try:
+        pp.clear(union_scene)
+        n1 = pp.collect(union_scene, views, capacity=200000)
+    finally:
+        union_scene.set_tuning("proposal_target", 0)
+    f1, t1 = pp.get_triples(union_scene, 0, n1)
+    assert n1 == n0 and n0 > 1000
+    order0, order1 = np.lexsort(f0.T), np.lexsort(f1.T)   # collection order is not fixed
+    assert np.array_equal(f0[order0], f1[order1])
+    assert np.all((t1 >= 0.0) & (t1 <= 1.0 + 1e-6))
+    assert not np.array_equal(np.sort(t0), np.sort(t1))
+    pp.train(union_scene, 400, batch=4096, lr=1e-3, seed=7)
+    test_views = scenes.union_views(n_views=2, lo=160, hi=256, cam_seed=8)
+    plain = union_scene.render_host(test_views, hits=True)["hits"].view(np.uint32).copy()
+    union_scene.set_tuning("proposal", 1)
+    try:
+        got = union_scene.render_host(test_views, hits=True)["hits"].view(np.uint32).copy()
+    finally:
+        union_scene.set_tuning("proposal", 0)
+    assert np.array_equal(got, plain)
