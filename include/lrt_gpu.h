@@ -96,6 +96,8 @@ lrt_status lrt_set_preset(lrt_ctx *ctx, const lrt_preset *preset);
  * the closest hit.  Not used by lrt_render_counters or the autotuner;
  * lrt_render_noalloc uses it once the BVH2 is on the device).
  * "proposal_target": lrt_proposal_collect's target (see lrt_proposal.h).
+ * "host_copy" (1 = default: lrt_render_host copies page-locked outputs chunk by
+ * chunk while the render runs; 0 = the kernel writes them across the host link).
  * "tc_wait" (default 1048576): how many times the tcgen05 network engine polls
  * a completion barrier before it gives up (a poll sleeps up to about 1 us, so
  * the default bounds a wait near one second); a timeout makes
@@ -187,8 +189,16 @@ lrt_status lrt_query_rays(lrt_ctx *ctx, const float *pos_near, const float *dir_
 lrt_status lrt_render(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, lrt_hit16 *hits16,
                       float *rgba, uint32_t *rgba8, void *stream);
 /* Same, with host output buffers, synchronous.  Page-locked buffers (cudaHostAlloc,
- * cudaHostRegister) are written by the render kernel directly across the host
- * link while it runs; pageable ones receive a copy of device buffers afterwards. */
+ * cudaHostRegister): the kernel renders into device buffers and counts each
+ * finished chunk of whole tile rows (about 1/48 of the batch), and a copy stream
+ * of the context moves each chunk to the host as soon as it is counted, while
+ * the rest renders (stream memory waits through the driver entry point
+ * cuStreamWaitValue32; the render stream releases every wait once the kernel has
+ * finished).  Where the chosen kernel does not count chunks (variant 1, 2 or 3,
+ * the proposal kernel), with more than 256 views, or with "host_copy" 0, the
+ * kernel writes the page-locked buffers itself across the host link.  Pageable
+ * buffers receive a copy of device buffers after the render.  The results are
+ * the same on every path. */
 lrt_status lrt_render_host(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, lrt_hit16 *hits16,
                            float *rgba, uint32_t *rgba8);
 /* Rendering that allocates nothing.  No counterpart in the reference.

@@ -19,6 +19,8 @@ struct ProposalState;
 void proposal_state_free(ProposalState *st);
 // the batched render launch of the context's kernel choice (plain or proposal)
 cudaError_t dispatch_render(struct ::lrt_ctx *ctx, const RenderLaunch &L, cudaStream_t st, bool count);
+// whether that launch (without counters) counts finished tiles in RenderLaunch::chunk_done
+bool dispatch_publishes_chunks(const struct ::lrt_ctx *ctx, bool color, uint32_t total_tiles);
 }  // namespace lrt
 
 namespace lrt {
@@ -112,6 +114,17 @@ struct lrt_ctx {
   DevBuf<unsigned long long> d_counters;
   DevView *h_views = nullptr;  // pinned staging for view uploads
   size_t h_views_cap = 0;
+  // output chunks of the last prepared batch (whole tile rows of one view each):
+  // the tiles that make a chunk and its pixel range in the batched outputs
+  struct Chunk {
+    uint32_t tiles;
+    uint64_t first_pixel, end_pixel;
+  };
+  std::vector<Chunk> chunks;
+  DevBuf<uint32_t> d_chunk_done;
+  cudaStream_t copy_stream = nullptr;   // lrt_render_host's chunk copies (non-blocking)
+  cudaEvent_t chunks_zeroed = nullptr;  // chunk counts cleared on the render stream
+  cudaEvent_t render_done = nullptr;    // the render and the counts' release
   // host-buffer entry points
   DevBuf<lrt_hit16> d_out_hits;
   DevBuf<float4> d_out_rgba;

@@ -1,6 +1,7 @@
 // C ABI of the GB300 ray-query engine: context, scene staging and commit
 // (the BVHRT host side, BVH/BVH2Common_host.cpp), batched rendering and ray
 // queries.  Host code only; kernels live in trace.cu.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -159,6 +160,10 @@ extern "C" void lrt_destroy(lrt_ctx *ctx) {
   ctx->d_q_pos.release();
   ctx->d_q_dir.release();
   ctx->d_q_out.release();
+  ctx->d_chunk_done.release();
+  if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+  if (ctx->chunks_zeroed) cudaEventDestroy(ctx->chunks_zeroed);
+  if (ctx->render_done) cudaEventDestroy(ctx->render_done);
   if (ctx->h_views) cudaFreeHost(ctx->h_views);
   delete ctx;
 }
@@ -564,6 +569,9 @@ extern "C" lrt_status lrt_set_tuning(lrt_ctx *ctx, const char *key, int value) {
   } else if (k == "bvh_builder") {
     if (value < 0 || value > 2) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: bvh_builder is 0, 1 or 2");
     ctx->bvh_builder = value;
+  } else if (k == "host_copy") {
+    if (value < 0 || value > 1) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: host_copy is 0 or 1");
+    ctx->tuning.host_copy = value;
   } else if (k == "proposal_target") {
     if (value < 0 || value > 1) return fail(ctx, LRT_ERR_INVALID, "lrt_set_tuning: proposal_target is 0 or 1");
     ctx->tuning.proposal_target = value;
@@ -779,6 +787,12 @@ static lrt_status prepare_views(lrt_ctx *ctx, const lrt_view *views, uint32_t n_
   }
   // The pinned staging buffer is reused; wait for the previous upload to finish.
   LRT_CUDA(ctx, cudaStreamSynchronize(st));
+  uint64_t all_pix = 0;
+  for (uint32_t v = 0; v < n_views; v++) all_pix += uint64_t(views[v].width) * views[v].height;
+  // output chunks for lrt_render_host's overlapped copies: whole tile rows of one
+  // view, about 1/48 of the batch each (at least 64 Ki pixels)
+  const uint64_t chunk_pix = std::max<uint64_t>(all_pix / 48, 65536);
+  ctx->chunks.clear();
   uint64_t pix = 0, tiles = 0;
   for (uint32_t v = 0; v < n_views; v++) {
     const lrt_view &in = views[v];
@@ -795,8 +809,17 @@ static lrt_status prepare_views(lrt_ctx *ctx, const lrt_view *views, uint32_t n_
     o.tiles_x = (in.width + tw - 1) / tw;
     lrt_inverse4x4(in.proj, o.proj_inv);       // UpdateCamera, Renderer/eye_ray_host.cpp:59-65
     lrt_inverse4x4(in.world_view, o.wv_inv);
+    const uint32_t tile_rows = (in.height + th - 1) / th;
+    o.rows_per_chunk = uint32_t(std::min<uint64_t>(
+        tile_rows, std::max<uint64_t>(1, chunk_pix / (uint64_t(in.width) * th))));
+    o.chunk_offset = uint32_t(ctx->chunks.size());
+    for (uint32_t r = 0; r < tile_rows; r += o.rows_per_chunk) {
+      const uint32_t r1 = std::min(tile_rows, r + o.rows_per_chunk);
+      ctx->chunks.push_back({(r1 - r) * o.tiles_x, pix + uint64_t(r) * th * in.width,
+                             pix + uint64_t(std::min(r1 * th, in.height)) * in.width});
+    }
     pix += uint64_t(in.width) * in.height;
-    tiles += uint64_t(o.tiles_x) * ((in.height + th - 1) / th);
+    tiles += uint64_t(o.tiles_x) * tile_rows;
   }
   if (pix >= (1ull << 32) || tiles >= (1ull << 32)) return fail(ctx, LRT_ERR_INVALID, "render: batch too large");
   LRT_CUDA(ctx, ctx->d_views.ensure(n_views));
@@ -809,8 +832,12 @@ static lrt_status prepare_views(lrt_ctx *ctx, const lrt_view *views, uint32_t n_
 // the tuned stack must hold the committed tree: (W-1)*depth + 1 entries, plus slack
 static bool stack_fits(const lrt_ctx *ctx) { return 3 * int(ctx->bvh.max_depth) + 4 <= ctx->tuning.stack; }
 
+// chunked: count finished tiles per output chunk (ctx->chunks) in d_chunk_done:
+// zeroed before the launch (event chunks_zeroed), and every count set to
+// 0x7F7F7F7F after it (event render_done), so that a wait for any chunk's count
+// ends once the render has, whatever the kernel published
 static lrt_status render_impl(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, lrt_hit16 *hits16, float *rgba,
-                              uint32_t *rgba8, cudaStream_t st, unsigned long long *counters) {
+                              uint32_t *rgba8, cudaStream_t st, unsigned long long *counters, bool chunked = false) {
   if (!ctx->committed) return fail(ctx, LRT_ERR_STATE, "render: commit the scene first");
   if (!stack_fits(ctx)) return fail(ctx, LRT_ERR_UNSUPPORTED, "render: the tuned stack is too small for this BVH");
   LRT_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -828,8 +855,19 @@ static lrt_status render_impl(lrt_ctx *ctx, const lrt_view *views, uint32_t n_vi
   L.rgba8 = rgba8;
   L.tile_counter = ctx->d_tile_counter.p;
   L.counters = counters;
+  const size_t chunk_bytes = ctx->chunks.size() * sizeof(uint32_t);
+  if (chunked) {
+    LRT_CUDA(ctx, ctx->d_chunk_done.ensure(ctx->chunks.size()));
+    LRT_CUDA(ctx, cudaMemsetAsync(ctx->d_chunk_done.p, 0, chunk_bytes, st));
+    LRT_CUDA(ctx, cudaEventRecord(ctx->chunks_zeroed, st));
+    L.chunk_done = ctx->d_chunk_done.p;
+  }
   LRT_CUDA(ctx, cudaMemsetAsync(ctx->d_tile_counter.p, 0, sizeof(uint32_t), st));
   LRT_CUDA(ctx, dispatch_render(ctx, L, st, counters != nullptr));
+  if (chunked) {
+    LRT_CUDA(ctx, cudaMemsetAsync(ctx->d_chunk_done.p, 0x7F, chunk_bytes, st));
+    LRT_CUDA(ctx, cudaEventRecord(ctx->render_done, st));
+  }
   ctx->last_launches = 1;
   return LRT_OK;
 }
@@ -851,19 +889,91 @@ static void *mapped_host(const void *host) {
   return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
-// Outputs in page-locked host memory are written by the kernel itself across the
-// host link while it renders (no staging buffer, no copy after the launch);
-// pageable outputs are rendered into device buffers and copied back.
+// cuStreamWaitValue32 (driver API, resolved at run time: the library does not
+// link the driver), or null where it is unavailable
+using WaitValue32Fn = CUresult (*)(CUstream, CUdeviceptr, cuuint32_t, unsigned int);
+static WaitValue32Fn stream_wait_value32() {
+  static const WaitValue32Fn fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuStreamWaitValue32", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      return WaitValue32Fn(nullptr);
+    }
+    return reinterpret_cast<WaitValue32Fn>(p);
+  }();
+  return fn;
+}
+
+// Page-locked outputs of a render whose kernel publishes chunk counts: the kernel
+// writes device buffers, and a non-blocking copy stream moves each chunk to the
+// host as soon as its tiles are counted, while later tiles render; only the last
+// chunk's copy follows the kernel.  Every operation of the render stream is
+// enqueued before the copy stream's waits, and the render stream ends by
+// releasing every count, so the waits end whenever the render does.
+static lrt_status render_host_chunked(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, uint64_t pix,
+                                      lrt_hit16 *hits16, float *rgba, uint32_t *rgba8, WaitValue32Fn wait) {
+  const cudaStream_t st = nullptr;
+  if (!ctx->copy_stream) LRT_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+  if (!ctx->chunks_zeroed) LRT_CUDA(ctx, cudaEventCreateWithFlags(&ctx->chunks_zeroed, cudaEventDisableTiming));
+  if (!ctx->render_done) LRT_CUDA(ctx, cudaEventCreateWithFlags(&ctx->render_done, cudaEventDisableTiming));
+  if (hits16) LRT_CUDA(ctx, ctx->d_out_hits.ensure(pix));
+  if (rgba) LRT_CUDA(ctx, ctx->d_out_rgba.ensure(pix));
+  if (rgba8) LRT_CUDA(ctx, ctx->d_out_rgba8.ensure(pix));
+  lrt_status s = render_impl(ctx, views, n_views, hits16 ? ctx->d_out_hits.p : nullptr,
+                             rgba ? reinterpret_cast<float *>(ctx->d_out_rgba.p) : nullptr,
+                             rgba8 ? ctx->d_out_rgba8.p : nullptr, st, nullptr, true);
+  if (s != LRT_OK) return s;
+  const cudaStream_t cs = ctx->copy_stream;
+  cudaError_t e = cudaStreamWaitEvent(cs, ctx->chunks_zeroed, 0);
+  bool waiting = true;   // false: a wait could not be enqueued; copy after the render instead
+  for (size_t c = 0; c < ctx->chunks.size() && e == cudaSuccess; c++) {
+    const lrt_ctx::Chunk &k = ctx->chunks[c];
+    if (waiting && wait(reinterpret_cast<CUstream>(cs), reinterpret_cast<CUdeviceptr>(ctx->d_chunk_done.p + c), k.tiles,
+                        CU_STREAM_WAIT_VALUE_GEQ) != CUDA_SUCCESS) {
+      waiting = false;
+      e = cudaStreamWaitEvent(cs, ctx->render_done, 0);
+    }
+    const uint64_t p0 = k.first_pixel, n = k.end_pixel - k.first_pixel;
+    if (hits16 && e == cudaSuccess)
+      e = cudaMemcpyAsync(hits16 + p0, ctx->d_out_hits.p + p0, n * sizeof(lrt_hit16), cudaMemcpyDeviceToHost, cs);
+    if (rgba && e == cudaSuccess)
+      e = cudaMemcpyAsync(rgba + 4 * p0, ctx->d_out_rgba.p + p0, n * sizeof(float4), cudaMemcpyDeviceToHost, cs);
+    if (rgba8 && e == cudaSuccess)
+      e = cudaMemcpyAsync(rgba8 + p0, ctx->d_out_rgba8.p + p0, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, cs);
+  }
+  // both streams drain whatever was enqueued (the render stream's release ends any wait)
+  const cudaError_t e1 = cudaStreamSynchronize(cs), e2 = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = e1 != cudaSuccess ? e1 : e2;
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "lrt_render_host");
+  return LRT_OK;
+}
+
+// Outputs in page-locked host memory: rendered into device buffers and copied
+// chunk by chunk while the render runs (render_host_chunked), or, where the
+// kernel does not publish chunks ("host_copy" 0, the packet / refill / leaf-queue
+// / proposal kernels), written by the kernel itself across the host link.
+// Pageable outputs are rendered into device buffers and copied back.
 extern "C" lrt_status lrt_render_host(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, lrt_hit16 *hits16,
                                       float *rgba, uint32_t *rgba8) {
   if (!ctx) return LRT_ERR_INVALID;
   if (!views || n_views == 0) return fail(ctx, LRT_ERR_INVALID, "render: no views");
-  uint64_t pix = 0;
-  for (uint32_t v = 0; v < n_views; v++) pix += uint64_t(views[v].width) * views[v].height;
+  uint64_t pix = 0, tiles = 0;
+  const uint32_t tw = uint32_t(ctx->tuning.tile_w), th = 32u / tw;
+  for (uint32_t v = 0; v < n_views; v++) {
+    pix += uint64_t(views[v].width) * views[v].height;
+    tiles += uint64_t((views[v].width + tw - 1) / tw) * ((views[v].height + th - 1) / th);
+  }
   LRT_CUDA(ctx, cudaSetDevice(ctx->device));
   lrt_hit16 *m_hits = hits16 ? static_cast<lrt_hit16 *>(mapped_host(hits16)) : nullptr;
   float *m_rgba = rgba ? static_cast<float *>(mapped_host(rgba)) : nullptr;
   uint32_t *m_rgba8 = rgba8 ? static_cast<uint32_t *>(mapped_host(rgba8)) : nullptr;
+  const WaitValue32Fn wait = ctx->tuning.host_copy ? stream_wait_value32() : nullptr;
+  if (wait && ctx->committed && (hits16 || rgba || rgba8) && (!hits16 || m_hits) && (!rgba || m_rgba) &&
+      (!rgba8 || m_rgba8) && n_views <= 256 && tiles < (1ull << 32) &&
+      dispatch_publishes_chunks(ctx, rgba || rgba8, uint32_t(tiles)))
+    return render_host_chunked(ctx, views, n_views, pix, hits16, rgba, rgba8, wait);
   if (hits16 && !m_hits) LRT_CUDA(ctx, ctx->d_out_hits.ensure(pix));
   if (rgba && !m_rgba) LRT_CUDA(ctx, ctx->d_out_rgba.ensure(pix));
   if (rgba8 && !m_rgba8) LRT_CUDA(ctx, ctx->d_out_rgba8.ensure(pix));

@@ -135,7 +135,10 @@ struct DevView {
   uint32_t tile_offset;  // first tile in the global tile space
   uint32_t tiles_x;      // tiles per row
   uint32_t tile_w_log2;  // a warp's tile is (1 << tile_w_log2) x (32 >> tile_w_log2) pixels
-  uint32_t _pad[2];
+  // outputs published in chunks (RenderLaunch::chunk_done): the view's tile rows
+  // r * rows_per_chunk .. (r + 1) * rows_per_chunk - 1 form chunk chunk_offset + r
+  uint32_t chunk_offset;
+  uint32_t rows_per_chunk;
   float proj_inv[16];
   float wv_inv[16];
 };
@@ -149,6 +152,9 @@ struct RenderLaunch {
   uint32_t *rgba8;
   uint32_t *tile_counter;       // scratch: persistent work queue head (zeroed before launch)
   unsigned long long *counters; // optional traversal counters [4]
+  // optional, zeroed before launch: per output chunk, the warp tiles whose outputs
+  // are written and fenced (render_kernel only; other kernels leave it untouched)
+  uint32_t *chunk_done = nullptr;
 };
 
 // Launch-shape and kernel choices (set through lrt_set_tuning).
@@ -160,6 +166,8 @@ struct Tuning {
   int tile_w = 8;           // warp tile width in pixels (4, 8, 16 or 32; height 32 / tile_w)
   int stack = 64;           // per-ray traversal stack entries (32 or 64; 32 only for shallow trees)
   int refill = 8;           // variant 2: idle lanes of a warp that trigger fetching new rays
+  int host_copy = 1;        // lrt_render_host into page-locked memory: 1 = render into device memory and copy
+                            // each finished chunk while the rest renders, 0 = the kernel writes host memory
   int fma = 0;              // 1: variant 0 without counters runs the kernels compiled with FP contraction
   int first_hit = 0;        // 1: SBS / SVS renders and queries walk the BVH2 in the reference's order and
                             // stop at the first SDF leaf that hits (BVH2TraverseF32's result)
@@ -167,6 +175,9 @@ struct Tuning {
   int proposal_target = 0; // training target of collected triples: 0 crossing fraction, 1 first finder voxel
 };
 
+// Whether launch_render runs render_kernel for this launch (the kernel that
+// publishes RenderLaunch::chunk_done); `color`: an rgba or rgba8 output.
+bool render_publishes_chunks(const DevScene &s, bool color, uint32_t total_tiles, const Tuning &tu);
 cudaError_t launch_render(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st, bool count,
                           const Tuning &tu);
 // NORMAL_MODE_SDF_SMOOTHED applies: the neighbour layout and a mode that needs normals

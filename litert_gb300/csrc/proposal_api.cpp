@@ -90,16 +90,30 @@ lrt_status ensure(lrt_ctx *ctx) {
 // the reference's first-hit walk when "first_hit" is set (SDF scenes), else the
 // plain kernels, or the proposal kernel for DX-layout SBS scenes with the NEWTON
 // finder when it is switched on and the network has weights
-cudaError_t dispatch_render(lrt_ctx *ctx, const RenderLaunch &L, cudaStream_t st, bool count) {
+static bool proposal_renders(const lrt_ctx *ctx, bool count) {
   const DevScene &s = ctx->dev;
-  if (ctx->tuning.first_hit && sdf_scene(s) && s.pairs) return launch_render_ref(s, L, ctx->num_sms, st);
   const uint32_t layout = s.sbs_hdr.aux_data & 0xFF000000u;
   const bool dx = s.type == LRT_TYPE_SDF_SBS && layout != LRT_SBS_LAYOUT_ID32F_IRGB32F &&
                   layout != LRT_SBS_LAYOUT_ID32F_IRGB32F_IN;
-  if (ctx->use_proposal && !count && dx && s.n_inst <= 1 && s.preset.sdf_node_intersect == LRT_INTERSECT_NEWTON && ctx->prop &&
-      ctx->prop->has_weights && s.preset.spp <= 1)
+  return ctx->use_proposal && !count && dx && s.n_inst <= 1 && s.preset.sdf_node_intersect == LRT_INTERSECT_NEWTON &&
+         ctx->prop && ctx->prop->has_weights && s.preset.spp <= 1;
+}
+
+cudaError_t dispatch_render(lrt_ctx *ctx, const RenderLaunch &L, cudaStream_t st, bool count) {
+  const DevScene &s = ctx->dev;
+  if (ctx->tuning.first_hit && sdf_scene(s) && s.pairs) return launch_render_ref(s, L, ctx->num_sms, st);
+  if (proposal_renders(ctx, count))
     return launch_render_proposal(s, L, mlp_state(*ctx->prop, nullptr), ctx->prop->stats.p, ctx->num_sms, st);
   return launch_render(s, L, ctx->num_sms, st, count, ctx->tuning);
+}
+
+// whether the kernel dispatch_render picks (without counters) publishes chunk_done:
+// the first-hit walk and launch_render's render_kernel paths do
+bool dispatch_publishes_chunks(const lrt_ctx *ctx, bool color, uint32_t total_tiles) {
+  const DevScene &s = ctx->dev;
+  if (ctx->tuning.first_hit && sdf_scene(s) && s.pairs) return true;
+  if (proposal_renders(ctx, false)) return false;
+  return render_publishes_chunks(s, color, total_tiles, ctx->tuning);
 }
 
 }  // namespace lrt

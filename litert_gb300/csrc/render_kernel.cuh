@@ -59,7 +59,17 @@ __device__ __noinline__ float4 shade_phong(const DevScene &s, const Hit &hit, fl
 
 // Persistent render kernel: each warp pulls 32-pixel tiles (8x4 by default, the
 // shape is tunable) of the flattened multi-view tile space from a global queue
-// head and traces one ray per lane.
+// head and traces one ray per lane.  With L.chunk_done set, a warp adds its
+// finished tiles to their output chunk's count, with every lane's stores fenced
+// first, when it moves on to a tile of another chunk and when it ends (tiles are
+// handed out in order, so a warp fences about once per chunk): a copy of a
+// chunk can start while later tiles render.
+__device__ __forceinline__ void publish_tiles(uint32_t *chunk_done, uint32_t chunk, uint32_t tiles, uint32_t lane) {
+  __threadfence();   // this lane's stores, device-wide
+  __syncwarp();      // every lane's fence (the warp is converged here)
+  if (lane == 0) atomicAdd(&chunk_done[chunk], tiles);
+}
+
 template <int TYPE, bool COUNT, int MODE, int STACK, int FP, bool PHONG = false, int FEAT = 0>
 __global__ void __launch_bounds__(128, 5) render_kernel(DevScene s, RenderLaunch L) {
   const uint32_t lane = threadIdx.x & 31u;
@@ -67,15 +77,28 @@ __global__ void __launch_bounds__(128, 5) render_kernel(DevScene s, RenderLaunch
   const uint32_t spp = s.preset.spp ? s.preset.spp : 1u;
   const uint32_t spp_sqrt = uint32_t(sqrtf(float(spp)));
   const float i_spp_sqrt = 1.0f / float(spp_sqrt);
+  uint32_t chunk = 0, pending = 0;   // finished tiles of output chunk `chunk` not yet counted
   for (;;) {
     uint32_t tile = 0;
     if (lane == 0) tile = atomicAdd(L.tile_counter, 1u);
     tile = __shfl_sync(0xffffffffu, tile, 0);
-    if (tile >= L.total_tiles) break;
+    if (tile >= L.total_tiles) {
+      if (L.chunk_done && pending) publish_tiles(L.chunk_done, chunk, pending, lane);
+      break;
+    }
     uint32_t v = 0;
     while (v + 1 < L.n_views && L.views[v + 1].tile_offset <= tile) v++;
     const DevView &V = L.views[v];
     const uint32_t lt = tile - V.tile_offset, lw = V.tile_w_log2;
+    if (L.chunk_done) {   // the same for the whole grid
+      const uint32_t c = V.chunk_offset + (lt / V.tiles_x) / V.rows_per_chunk;
+      if (pending && c != chunk) {
+        publish_tiles(L.chunk_done, chunk, pending, lane);
+        pending = 0;
+      }
+      chunk = c;
+      pending++;
+    }
     const uint32_t x = (lt % V.tiles_x) * (1u << lw) + (lane & ((1u << lw) - 1u));
     const uint32_t y = (lt / V.tiles_x) * (32u >> lw) + (lane >> lw);
     if (x >= V.width || y >= V.height) continue;   // all lanes meet again at the queue shuffle

@@ -243,36 +243,61 @@ cudaError_t launch_render_lq(const DevScene &s, const RenderLaunch &L, int num_s
   }
 }
 
-cudaError_t launch_render(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st, bool count,
-                          const Tuning &tu) {
-  if (s.n_inst > 1) return launch_render_inst(s, L, num_sms, st, false);
+// The kernel launch_render runs, decided from the scene, the outputs and the tuning.
+enum class RenderChoice { kInstances, kFeature1, kFeature2, kPhong, kPacket, kRefill, kLeafQueue, kFused, kPlain };
+
+static RenderChoice render_choice(const DevScene &s, bool color, uint32_t total_tiles, bool count, const Tuning &tu) {
+  if (s.n_inst > 1) return RenderChoice::kInstances;
   const uint32_t rm = s.preset.render_mode;
-  const bool phong = (rm == LRT_RENDER_MODE_PHONG || rm == LRT_RENDER_MODE_PHONG_NO_TEX) && (L.rgba || L.rgba8);
+  const bool phong = (rm == LRT_RENDER_MODE_PHONG || rm == LRT_RENDER_MODE_PHONG_NO_TEX) && color;
   switch (render_features(s)) {   // SBS only; smoothed normals need a normal mode, so never with ST_ITERATIONS
-    case 1:
-      return phong ? launch_feature_t<LRT_TYPE_SDF_SBS, true, 1>(s, L, num_sms, st)
-                   : launch_feature_t<LRT_TYPE_SDF_SBS, false, 1>(s, L, num_sms, st);
-    case 2: return launch_feature_t<LRT_TYPE_SDF_SBS, false, 2>(s, L, num_sms, st);
+    case 1: return RenderChoice::kFeature1;
+    case 2: return RenderChoice::kFeature2;
     default: break;
   }
-  if (phong) {
-    switch (s.type) {
-      case LRT_TYPE_MESH_TRIANGLE: return launch_phong_t<LRT_TYPE_MESH_TRIANGLE>(s, L, num_sms, st);
-      case LRT_TYPE_SDF_SVS: return launch_phong_t<LRT_TYPE_SDF_SVS>(s, L, num_sms, st);
-      default: return launch_phong_t<LRT_TYPE_SDF_SBS>(s, L, num_sms, st);
-    }
-  }
+  if (phong) return RenderChoice::kPhong;
   const bool sbs = s.type == LRT_TYPE_SDF_SBS || s.type == LRT_TYPE_SDF_SBS_COL || s.type == LRT_TYPE_SDF_SBS_TEX;
-  if (sbs && tu.variant == 1) return launch_render_packet(s, L, num_sms, st, count, tu);
+  if (sbs && tu.variant == 1) return RenderChoice::kPacket;
   const bool refill_ok = (s.type == LRT_TYPE_MESH_TRIANGLE ||
                           (s.type == LRT_TYPE_SDF_SBS && s.preset.sdf_node_intersect == LRT_INTERSECT_NEWTON)) &&
-                         s.preset.spp <= 1 && !count && uint64_t(L.total_tiles) * 32u < (1ull << 31);
-  if (tu.variant == 2 && refill_ok) return launch_refill(s, L, num_sms, st, tu);
-  if (tu.variant == 3 && sbs && render_features(s) == 0 && s.preset.spp <= 1 && !count)
-    return tu.fma ? launch_render_lq_fused(s, L, num_sms, st, tu) : launch_render_lq(s, L, num_sms, st, tu);
+                         s.preset.spp <= 1 && !count && uint64_t(total_tiles) * 32u < (1ull << 31);
+  if (tu.variant == 2 && refill_ok) return RenderChoice::kRefill;
+  if (tu.variant == 3 && sbs && render_features(s) == 0 && s.preset.spp <= 1 && !count) return RenderChoice::kLeafQueue;
   // contraction only for the SDF leaves: in the triangle test it would open cracks along shared edges
-  if (tu.fma && !count && tu.variant != 1 && s.type != LRT_TYPE_MESH_TRIANGLE)
-    return launch_render_fused(s, L, num_sms, st, tu);
+  if (tu.fma && !count && tu.variant != 1 && s.type != LRT_TYPE_MESH_TRIANGLE) return RenderChoice::kFused;
+  return RenderChoice::kPlain;
+}
+
+bool render_publishes_chunks(const DevScene &s, bool color, uint32_t total_tiles, const Tuning &tu) {
+  const RenderChoice c = render_choice(s, color, total_tiles, false, tu);
+  return c != RenderChoice::kPacket && c != RenderChoice::kRefill && c != RenderChoice::kLeafQueue;
+}
+
+cudaError_t launch_render(const DevScene &s, const RenderLaunch &L, int num_sms, cudaStream_t st, bool count,
+                          const Tuning &tu) {
+  const bool color = L.rgba || L.rgba8;
+  switch (render_choice(s, color, L.total_tiles, count, tu)) {
+    case RenderChoice::kInstances: return launch_render_inst(s, L, num_sms, st, false);
+    case RenderChoice::kFeature1: {
+      const uint32_t rm = s.preset.render_mode;
+      const bool phong = (rm == LRT_RENDER_MODE_PHONG || rm == LRT_RENDER_MODE_PHONG_NO_TEX) && color;
+      return phong ? launch_feature_t<LRT_TYPE_SDF_SBS, true, 1>(s, L, num_sms, st)
+                   : launch_feature_t<LRT_TYPE_SDF_SBS, false, 1>(s, L, num_sms, st);
+    }
+    case RenderChoice::kFeature2: return launch_feature_t<LRT_TYPE_SDF_SBS, false, 2>(s, L, num_sms, st);
+    case RenderChoice::kPhong:
+      switch (s.type) {
+        case LRT_TYPE_MESH_TRIANGLE: return launch_phong_t<LRT_TYPE_MESH_TRIANGLE>(s, L, num_sms, st);
+        case LRT_TYPE_SDF_SVS: return launch_phong_t<LRT_TYPE_SDF_SVS>(s, L, num_sms, st);
+        default: return launch_phong_t<LRT_TYPE_SDF_SBS>(s, L, num_sms, st);
+      }
+    case RenderChoice::kPacket: return launch_render_packet(s, L, num_sms, st, count, tu);
+    case RenderChoice::kRefill: return launch_refill(s, L, num_sms, st, tu);
+    case RenderChoice::kLeafQueue:
+      return tu.fma ? launch_render_lq_fused(s, L, num_sms, st, tu) : launch_render_lq(s, L, num_sms, st, tu);
+    case RenderChoice::kFused: return launch_render_fused(s, L, num_sms, st, tu);
+    case RenderChoice::kPlain: break;
+  }
   switch (s.type) {
     case LRT_TYPE_MESH_TRIANGLE: return launch_render_t<LRT_TYPE_MESH_TRIANGLE>(s, L, num_sms, st, count, tu);
     case LRT_TYPE_SDF_SVS: return launch_render_t<LRT_TYPE_SDF_SVS>(s, L, num_sms, st, count, tu);
