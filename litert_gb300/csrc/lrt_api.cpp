@@ -790,7 +790,8 @@ static lrt_status prepare_views(lrt_ctx *ctx, const lrt_view *views, uint32_t n_
   uint64_t all_pix = 0;
   for (uint32_t v = 0; v < n_views; v++) all_pix += uint64_t(views[v].width) * views[v].height;
   // output chunks for lrt_render_host's overlapped copies: whole tile rows of one
-  // view, about 1/48 of the batch each (at least 64 Ki pixels)
+  // view, about 1/48 of the batch each (at least 64 Ki pixels), a quarter of that
+  // in the last of several views (the copy of the last chunk follows the kernel)
   const uint64_t chunk_pix = std::max<uint64_t>(all_pix / 48, 65536);
   ctx->chunks.clear();
   uint64_t pix = 0, tiles = 0;
@@ -810,8 +811,9 @@ static lrt_status prepare_views(lrt_ctx *ctx, const lrt_view *views, uint32_t n_
     lrt_inverse4x4(in.proj, o.proj_inv);       // UpdateCamera, Renderer/eye_ray_host.cpp:59-65
     lrt_inverse4x4(in.world_view, o.wv_inv);
     const uint32_t tile_rows = (in.height + th - 1) / th;
+    const uint64_t view_chunk_pix = (n_views > 1 && v + 1 == n_views) ? chunk_pix / 4 : chunk_pix;
     o.rows_per_chunk = uint32_t(std::min<uint64_t>(
-        tile_rows, std::max<uint64_t>(1, chunk_pix / (uint64_t(in.width) * th))));
+        tile_rows, std::max<uint64_t>(1, view_chunk_pix / (uint64_t(in.width) * th))));
     o.chunk_offset = uint32_t(ctx->chunks.size());
     for (uint32_t r = 0; r < tile_rows; r += o.rows_per_chunk) {
       const uint32_t r1 = std::min(tile_rows, r + o.rows_per_chunk);
@@ -930,8 +932,10 @@ static lrt_status render_host_chunked(lrt_ctx *ctx, const lrt_view *views, uint3
   bool waiting = true;   // false: a wait could not be enqueued; copy after the render instead
   for (size_t c = 0; c < ctx->chunks.size() && e == cudaSuccess; c++) {
     const lrt_ctx::Chunk &k = ctx->chunks[c];
-    if (waiting && wait(reinterpret_cast<CUstream>(cs), reinterpret_cast<CUdeviceptr>(ctx->d_chunk_done.p + c), k.tiles,
-                        CU_STREAM_WAIT_VALUE_GEQ) != CUDA_SUCCESS) {
+    // the last chunk is finished when the kernel is: its copy waits for the event
+    if (waiting && (c + 1 == ctx->chunks.size() ||
+                    wait(reinterpret_cast<CUstream>(cs), reinterpret_cast<CUdeviceptr>(ctx->d_chunk_done.p + c),
+                         k.tiles, CU_STREAM_WAIT_VALUE_GEQ) != CUDA_SUCCESS)) {
       waiting = false;
       e = cudaStreamWaitEvent(cs, ctx->render_done, 0);
     }

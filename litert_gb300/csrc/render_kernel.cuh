@@ -65,8 +65,8 @@ __device__ __noinline__ float4 shade_phong(const DevScene &s, const Hit &hit, fl
 // handed out in order, so a warp fences about once per chunk): a copy of a
 // chunk can start while later tiles render.
 __device__ __forceinline__ void publish_tiles(uint32_t *chunk_done, uint32_t chunk, uint32_t tiles, uint32_t lane) {
-  __threadfence();   // this lane's stores, device-wide
-  __syncwarp();      // every lane's fence (the warp is converged here)
+  asm volatile("fence.acq_rel.gpu;" ::: "memory");   // this lane's stores before what follows, device-wide
+  __syncwarp();                                       // every lane's fence (the warp is converged here)
   if (lane == 0) atomicAdd(&chunk_done[chunk], tiles);
 }
 
@@ -144,12 +144,14 @@ __global__ void __launch_bounds__(128, 5) render_kernel(DevScene s, RenderLaunch
                                                                                         : first.prim;
       o.nx = first.c2;
       o.ny = first.c3;
-      reinterpret_cast<float4 *>(L.hits16)[pix] = *reinterpret_cast<const float4 *>(&o);
+      // outputs are written once and not read again here: evict-first stores keep
+      // the tree and the bricks in L2
+      __stcs(reinterpret_cast<float4 *>(L.hits16) + pix, *reinterpret_cast<const float4 *>(&o));
     }
     const float fs = float(spp);
     const float4 col = make_float4(acc.x / fs, acc.y / fs, acc.z / fs, acc.w / fs);
-    if (L.rgba) L.rgba[pix] = col;
-    if (L.rgba8) L.rgba8[pix] = encode_rgba8(col);
+    if (L.rgba) __stcs(L.rgba + pix, col);
+    if (L.rgba8) __stcs(L.rgba8 + pix, encode_rgba8(col));
   }
   if (COUNT) {
     atomicAdd(&L.counters[0], (unsigned long long)cnt.nodes);
