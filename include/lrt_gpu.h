@@ -194,7 +194,8 @@ lrt_status lrt_render(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, lrt
  * of the context moves each chunk to the host as soon as it is counted, while
  * the rest renders (stream memory waits through the driver entry point
  * cuStreamWaitValue32; the render stream releases every wait once the kernel has
- * finished).  Where the chosen kernel does not count chunks (variant 1, 2 or 3,
+ * finished); the batch's last chunks, at most 1/16 of it, the kernel writes to
+ * the host buffers itself, so that no copy is left once it ends.  Where the chosen kernel does not count chunks (variant 1, 2 or 3,
  * the proposal kernel), with more than 256 views, or with "host_copy" 0, the
  * kernel writes the page-locked buffers itself across the host link.  Pageable
  * buffers receive a copy of device buffers after the render.  The results are

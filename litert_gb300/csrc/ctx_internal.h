@@ -121,6 +121,7 @@ struct lrt_ctx {
     uint64_t first_pixel, end_pixel;
   };
   std::vector<Chunk> chunks;
+  size_t chunk_copy_end = 0;   // chunks from here on are written to the host by the kernel
   DevBuf<uint32_t> d_chunk_done;
   cudaStream_t copy_stream = nullptr;   // lrt_render_host's chunk copies (non-blocking)
   cudaEvent_t chunks_zeroed = nullptr;  // chunk counts cleared on the render stream

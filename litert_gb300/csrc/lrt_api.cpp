@@ -790,8 +790,7 @@ static lrt_status prepare_views(lrt_ctx *ctx, const lrt_view *views, uint32_t n_
   uint64_t all_pix = 0;
   for (uint32_t v = 0; v < n_views; v++) all_pix += uint64_t(views[v].width) * views[v].height;
   // output chunks for lrt_render_host's overlapped copies: whole tile rows of one
-  // view, about 1/48 of the batch each (at least 64 Ki pixels), a quarter of that
-  // in the last of several views (the copy of the last chunk follows the kernel)
+  // view, about 1/48 of the batch each (at least 64 Ki pixels)
   const uint64_t chunk_pix = std::max<uint64_t>(all_pix / 48, 65536);
   ctx->chunks.clear();
   uint64_t pix = 0, tiles = 0;
@@ -811,9 +810,8 @@ static lrt_status prepare_views(lrt_ctx *ctx, const lrt_view *views, uint32_t n_
     lrt_inverse4x4(in.proj, o.proj_inv);       // UpdateCamera, Renderer/eye_ray_host.cpp:59-65
     lrt_inverse4x4(in.world_view, o.wv_inv);
     const uint32_t tile_rows = (in.height + th - 1) / th;
-    const uint64_t view_chunk_pix = (n_views > 1 && v + 1 == n_views) ? chunk_pix / 4 : chunk_pix;
     o.rows_per_chunk = uint32_t(std::min<uint64_t>(
-        tile_rows, std::max<uint64_t>(1, view_chunk_pix / (uint64_t(in.width) * th))));
+        tile_rows, std::max<uint64_t>(1, chunk_pix / (uint64_t(in.width) * th))));
     o.chunk_offset = uint32_t(ctx->chunks.size());
     for (uint32_t r = 0; r < tile_rows; r += o.rows_per_chunk) {
       const uint32_t r1 = std::min(tile_rows, r + o.rows_per_chunk);
@@ -834,12 +832,22 @@ static lrt_status prepare_views(lrt_ctx *ctx, const lrt_view *views, uint32_t n_
 // the tuned stack must hold the committed tree: (W-1)*depth + 1 entries, plus slack
 static bool stack_fits(const lrt_ctx *ctx) { return 3 * int(ctx->bvh.max_depth) + 4 <= ctx->tuning.stack; }
 
+// Page-locked host outputs (mapped device addresses) the kernel writes directly.
+struct HostOutputs {
+  lrt_hit16 *hits16;
+  float *rgba;
+  uint32_t *rgba8;
+};
+
 // chunked: count finished tiles per output chunk (ctx->chunks) in d_chunk_done:
 // zeroed before the launch (event chunks_zeroed), and every count set to
 // 0x7F7F7F7F after it (event render_done), so that a wait for any chunk's count
-// ends once the render has, whatever the kernel published
+// ends once the render has, whatever the kernel published.  With `tail`, the
+// last whole chunks (at most 1/16 of the batch) are written to those host
+// outputs by the kernel itself; ctx->chunk_copy_end is the first of them.
 static lrt_status render_impl(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, lrt_hit16 *hits16, float *rgba,
-                              uint32_t *rgba8, cudaStream_t st, unsigned long long *counters, bool chunked = false) {
+                              uint32_t *rgba8, cudaStream_t st, unsigned long long *counters, bool chunked = false,
+                              const HostOutputs *tail = nullptr) {
   if (!ctx->committed) return fail(ctx, LRT_ERR_STATE, "render: commit the scene first");
   if (!stack_fits(ctx)) return fail(ctx, LRT_ERR_UNSUPPORTED, "render: the tuned stack is too small for this BVH");
   LRT_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -858,6 +866,22 @@ static lrt_status render_impl(lrt_ctx *ctx, const lrt_view *views, uint32_t n_vi
   L.tile_counter = ctx->d_tile_counter.p;
   L.counters = counters;
   const size_t chunk_bytes = ctx->chunks.size() * sizeof(uint32_t);
+  ctx->chunk_copy_end = ctx->chunks.size();
+  if (chunked && tail) {
+    uint64_t direct = 0;
+    while (ctx->chunk_copy_end > 1) {
+      const lrt_ctx::Chunk &k = ctx->chunks[ctx->chunk_copy_end - 1];
+      if (direct + (k.end_pixel - k.first_pixel) > pix / 16) break;
+      direct += k.end_pixel - k.first_pixel;
+      ctx->chunk_copy_end--;
+    }
+    if (ctx->chunk_copy_end < ctx->chunks.size()) {
+      L.direct_from = ctx->chunks[ctx->chunk_copy_end].first_pixel;
+      L.hits16_direct = tail->hits16;
+      L.rgba_direct = reinterpret_cast<float4 *>(tail->rgba);
+      L.rgba8_direct = tail->rgba8;
+    }
+  }
   if (chunked) {
     LRT_CUDA(ctx, ctx->d_chunk_done.ensure(ctx->chunks.size()));
     LRT_CUDA(ctx, cudaMemsetAsync(ctx->d_chunk_done.p, 0, chunk_bytes, st));
@@ -910,12 +934,14 @@ static WaitValue32Fn stream_wait_value32() {
 
 // Page-locked outputs of a render whose kernel publishes chunk counts: the kernel
 // writes device buffers, and a non-blocking copy stream moves each chunk to the
-// host as soon as its tiles are counted, while later tiles render; only the last
-// chunk's copy follows the kernel.  Every operation of the render stream is
-// enqueued before the copy stream's waits, and the render stream ends by
+// host as soon as its tiles are counted, while later tiles render; the kernel
+// writes the batch's last chunks (at most 1/16 of it) to the host outputs
+// itself, so no copy is left once it ends.  Every operation of the render stream
+// is enqueued before the copy stream's waits, and the render stream ends by
 // releasing every count, so the waits end whenever the render does.
 static lrt_status render_host_chunked(lrt_ctx *ctx, const lrt_view *views, uint32_t n_views, uint64_t pix,
-                                      lrt_hit16 *hits16, float *rgba, uint32_t *rgba8, WaitValue32Fn wait) {
+                                      lrt_hit16 *hits16, float *rgba, uint32_t *rgba8, const HostOutputs &mapped,
+                                      WaitValue32Fn wait) {
   const cudaStream_t st = nullptr;
   if (!ctx->copy_stream) LRT_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
   if (!ctx->chunks_zeroed) LRT_CUDA(ctx, cudaEventCreateWithFlags(&ctx->chunks_zeroed, cudaEventDisableTiming));
@@ -925,12 +951,12 @@ static lrt_status render_host_chunked(lrt_ctx *ctx, const lrt_view *views, uint3
   if (rgba8) LRT_CUDA(ctx, ctx->d_out_rgba8.ensure(pix));
   lrt_status s = render_impl(ctx, views, n_views, hits16 ? ctx->d_out_hits.p : nullptr,
                              rgba ? reinterpret_cast<float *>(ctx->d_out_rgba.p) : nullptr,
-                             rgba8 ? ctx->d_out_rgba8.p : nullptr, st, nullptr, true);
+                             rgba8 ? ctx->d_out_rgba8.p : nullptr, st, nullptr, true, &mapped);
   if (s != LRT_OK) return s;
   const cudaStream_t cs = ctx->copy_stream;
   cudaError_t e = cudaStreamWaitEvent(cs, ctx->chunks_zeroed, 0);
   bool waiting = true;   // false: a wait could not be enqueued; copy after the render instead
-  for (size_t c = 0; c < ctx->chunks.size() && e == cudaSuccess; c++) {
+  for (size_t c = 0; c < ctx->chunk_copy_end && e == cudaSuccess; c++) {
     const lrt_ctx::Chunk &k = ctx->chunks[c];
     // the last chunk is finished when the kernel is: its copy waits for the event
     if (waiting && (c + 1 == ctx->chunks.size() ||
@@ -977,7 +1003,8 @@ extern "C" lrt_status lrt_render_host(lrt_ctx *ctx, const lrt_view *views, uint3
   if (wait && ctx->committed && (hits16 || rgba || rgba8) && (!hits16 || m_hits) && (!rgba || m_rgba) &&
       (!rgba8 || m_rgba8) && n_views <= 256 && tiles < (1ull << 32) &&
       dispatch_publishes_chunks(ctx, rgba || rgba8, uint32_t(tiles)))
-    return render_host_chunked(ctx, views, n_views, pix, hits16, rgba, rgba8, wait);
+    return render_host_chunked(ctx, views, n_views, pix, hits16, rgba, rgba8, HostOutputs{m_hits, m_rgba, m_rgba8},
+                               wait);
   if (hits16 && !m_hits) LRT_CUDA(ctx, ctx->d_out_hits.ensure(pix));
   if (rgba && !m_rgba) LRT_CUDA(ctx, ctx->d_out_rgba.ensure(pix));
   if (rgba8 && !m_rgba8) LRT_CUDA(ctx, ctx->d_out_rgba8.ensure(pix));

@@ -155,6 +155,13 @@ struct RenderLaunch {
   // optional, zeroed before launch: per output chunk, the warp tiles whose outputs
   // are written and fenced (render_kernel only; other kernels leave it untouched)
   uint32_t *chunk_done = nullptr;
+  // optional: pixels from direct_from on are written through these pointers
+  // instead (page-locked host outputs, mapped: the batch's tail, which would
+  // otherwise be copied after the kernel)
+  uint64_t direct_from = ~0ull;
+  lrt_hit16 *hits16_direct = nullptr;
+  float4 *rgba_direct = nullptr;
+  uint32_t *rgba8_direct = nullptr;
 };
 
 // Launch-shape and kernel choices (set through lrt_set_tuning).

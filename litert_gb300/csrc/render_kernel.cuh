@@ -137,6 +137,7 @@ __global__ void __launch_bounds__(128, 5) render_kernel(DevScene s, RenderLaunch
       if (si == 0) first = hit;
     }
     const size_t pix = size_t(V.pix_offset) + size_t(y) * V.width + x;
+    const bool direct = pix >= L.direct_from;
     if (L.hits16) {
       lrt_hit16 o;
       o.t = first.t;
@@ -146,12 +147,12 @@ __global__ void __launch_bounds__(128, 5) render_kernel(DevScene s, RenderLaunch
       o.ny = first.c3;
       // outputs are written once and not read again here: evict-first stores keep
       // the tree and the bricks in L2
-      __stcs(reinterpret_cast<float4 *>(L.hits16) + pix, *reinterpret_cast<const float4 *>(&o));
+      __stcs(reinterpret_cast<float4 *>(direct ? L.hits16_direct : L.hits16) + pix, *reinterpret_cast<const float4 *>(&o));
     }
     const float fs = float(spp);
     const float4 col = make_float4(acc.x / fs, acc.y / fs, acc.z / fs, acc.w / fs);
-    if (L.rgba) __stcs(L.rgba + pix, col);
-    if (L.rgba8) __stcs(L.rgba8 + pix, encode_rgba8(col));
+    if (L.rgba) __stcs((direct ? L.rgba_direct : L.rgba) + pix, col);
+    if (L.rgba8) __stcs((direct ? L.rgba8_direct : L.rgba8) + pix, encode_rgba8(col));
   }
   if (COUNT) {
     atomicAdd(&L.counters[0], (unsigned long long)cnt.nodes);
