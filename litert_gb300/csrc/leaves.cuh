@@ -389,7 +389,8 @@ static __device__ __noinline__ void brick_colour(const DevScene &s, uint4 nd, fl
 // colour computed in this brick as the reference does (kept for ST_ITERATIONS,
 // where primId no longer names the brick; otherwise hit_colour computes it once
 // for the final hit, which gives the same values: the last brick that reports a
-// hit is the hit brick).
+// hit is the hit brick), bit 4 (value 16) the walk's position and voxel planes as
+// one FMA each (for the kernels compiled with contraction).
 template <bool COUNT, bool STAGED, int MODE = -1, int FEAT = 0>
 __device__ void brick_intersect(const DevScene &s, float3 ray_pos, float3 ray_dir, float3 inv, float tNear,
                                 uint32_t brick, Hit &hit, Counters &cnt, const float *staged = nullptr,
@@ -413,6 +414,10 @@ __device__ void brick_intersect(const DevScene &s, float3 ray_pos, float3 ray_di
   const float scale = 0.5f * sz * bs;
   const uint32_t *occ = s.occ + size_t(brick) * s.occ_words;
   const bool posx = inv.x > 0.0f, posy = inv.y > 0.0f, posz = inv.z > 0.0f;
+  // FEAT bit 4: local position lp0 + t * rds, voxel planes p * inv + noi
+  constexpr bool kFma = (FEAT & 16) != 0;
+  const float3 lp0 = scr(sub(ray_pos, bmin), scale), rds = scl(scale, ray_dir);
+  const float3 noi = f3(-(ray_pos.x * inv.x), -(ray_pos.y * inv.y), -(ray_pos.z * inv.z));
   float values[8];
   if (COUNT) cnt.leaves++;
   const uint32_t max_steps = walk_step_bound(bsz, bnf.y - bnf.x);
@@ -430,23 +435,32 @@ __device__ void brick_intersect(const DevScene &s, float3 ray_pos, float3 ray_di
     float2 fnf;
     float exit_t;
     while (bnf.x < bnf.y && step < max_steps) {
-      const float3 hit_pos = add(ray_pos, scl(bnf.x, ray_dir));
-      const float3 local_pos = scr(sub(hit_pos, bmin), scale);
+      float3 local_pos;
+      if (kFma) {
+        local_pos = f3(fmaf(bnf.x, rds.x, lp0.x), fmaf(bnf.x, rds.y, lp0.y), fmaf(bnf.x, rds.z, lp0.z));
+      } else {
+        const float3 hit_pos = add(ray_pos, scl(bnf.x, ray_dir));
+        local_pos = scr(sub(hit_pos, bmin), scale);
+      }
       vp = f3(floorf(fmn(fmx(local_pos.x, 1e-6f), bs - 1e-6f)), floorf(fmn(fmx(local_pos.y, 1e-6f), bs - 1e-6f)),
               floorf(fmn(fmx(local_pos.z, 1e-6f), bs - 1e-6f)));
       min_pos = add(bmin, scl(d, vp));
       // exit distance: far plane per axis (max_pos = min_pos + d*1)
-      const float fx = inv.x * ((posx ? min_pos.x + d : min_pos.x) - ray_pos.x);
-      const float fy = inv.y * ((posy ? min_pos.y + d : min_pos.y) - ray_pos.y);
-      const float fz = inv.z * ((posz ? min_pos.z + d : min_pos.z) - ray_pos.z);
+      const float ex = posx ? min_pos.x + d : min_pos.x, ey = posy ? min_pos.y + d : min_pos.y,
+                  ez = posz ? min_pos.z + d : min_pos.z;
+      const float fx = kFma ? fmaf(ex, inv.x, noi.x) : inv.x * (ex - ray_pos.x);
+      const float fy = kFma ? fmaf(ey, inv.y, noi.y) : inv.y * (ey - ray_pos.y);
+      const float fz = kFma ? fmaf(ez, inv.z, noi.z) : inv.z * (ez - ray_pos.z);
       exit_t = fmn(fmn(fx, fy), fz);
       const uint32_t vid = (uint32_t(vp.x) * bsz + uint32_t(vp.y)) * bsz + uint32_t(vp.z);
       step++;
       if (COUNT) cnt.voxels++;
       if ((__ldg(&occ[vid >> 5]) >> (vid & 31u)) & 1u) {
-        const float nx = inv.x * ((posx ? min_pos.x : min_pos.x + d) - ray_pos.x);
-        const float ny = inv.y * ((posy ? min_pos.y : min_pos.y + d) - ray_pos.y);
-        const float nz = inv.z * ((posz ? min_pos.z : min_pos.z + d) - ray_pos.z);
+        const float px_ = posx ? min_pos.x : min_pos.x + d, py_ = posy ? min_pos.y : min_pos.y + d,
+                    pz_ = posz ? min_pos.z : min_pos.z + d;
+        const float nx = kFma ? fmaf(px_, inv.x, noi.x) : inv.x * (px_ - ray_pos.x);
+        const float ny = kFma ? fmaf(py_, inv.y, noi.y) : inv.y * (py_ - ray_pos.y);
+        const float nz = kFma ? fmaf(pz_, inv.z, noi.z) : inv.z * (pz_ - ray_pos.z);
         fnf = make_float2(fmx(fmx(nx, ny), nz), exit_t);
         if (tNear < fnf.x) {
           float vmin;

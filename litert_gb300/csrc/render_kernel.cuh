@@ -119,7 +119,8 @@ __global__ void __launch_bounds__(128, 5) render_kernel(DevScene s, RenderLaunch
       float3 pos, dir;
       eye_ray(x, y, V.width, V.height, dx, dy, V.proj_inv, V.wv_inv, pos, dir);
       Hit hit;
-      trace<TYPE, COUNT, MODE, STACK, FEAT>(s, pos, 0.0f, dir, 1e9f, hit, cnt);
+      // the contracted kernels (FP = 1) also test inner-node slabs with one FMA per plane
+      trace<TYPE, COUNT, MODE, STACK, FEAT | (FP == 1 ? 16 : 0)>(s, pos, 0.0f, dir, 1e9f, hit, cnt);
       if (FEAT & 8) {   // colours and shading in the frame of the instance hit
         const DevScene sh = scene_of_instance(s, hit.prim != kMiss ? hit.inst : 0u);
         if (TYPE == LRT_TYPE_SDF_SBS && !(FEAT & 2)) hit_colour(sh, pos, dir, hit);

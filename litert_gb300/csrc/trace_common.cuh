@@ -95,6 +95,21 @@ __device__ __forceinline__ float2 ray_box(float3 o, float3 inv, float lox, float
   return make_float2(fmx(tmin, fmn(lo2, hi2)), fmn(tmax, fmx(lo2, hi2)));
 }
 
+// The same slab test with each plane distance as one FMA, lo * inv + noi with
+// noi = -(o * inv) per ray (one rounding where RayBoxIntersection2 rounds twice):
+// for the kernels compiled with contraction only.  |inv| <= 1e36 (SafeInverse),
+// so with boxes and origins within a few hundred units of the origin every term
+// is finite.
+__device__ __forceinline__ float2 ray_box_fma(float3 inv, float3 noi, float lox, float loy, float loz, float hix,
+                                              float hiy, float hiz) {
+  const float lo = fmaf(lox, inv.x, noi.x), hi = fmaf(hix, inv.x, noi.x);
+  const float lo1 = fmaf(loy, inv.y, noi.y), hi1 = fmaf(hiy, inv.y, noi.y);
+  const float lo2 = fmaf(loz, inv.z, noi.z), hi2 = fmaf(hiz, inv.z, noi.z);
+  const float tmin = fmx(fmn(lo, hi), fmn(lo1, hi1));
+  const float tmax = fmn(fmx(lo, hi), fmx(lo1, hi1));
+  return make_float2(fmx(tmin, fmn(lo2, hi2)), fmn(tmax, fmx(lo2, hi2)));
+}
+
 // octahedral encode, BVH/BVH2Common.cpp:29-35
 __device__ __forceinline__ float2 encode_normal(float3 v) {
   const float s = 1.0f / (fabsf(v.x) + fabsf(v.y) + fabsf(v.z));

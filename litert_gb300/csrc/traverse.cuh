@@ -6,9 +6,10 @@
 namespace lrt {
 namespace dev {
 
-template <bool COUNT, int STACK>
+template <bool COUNT, int STACK, bool FMA_SLAB = false>
 __device__ __forceinline__ void visit_node(const DevScene &s, uint32_t ref, float3 rp, float3 inv, float tNear,
-                                           float hit_t, uint2 *st, int &sp, Counters &cnt);
+                                           float hit_t, uint2 *st, int &sp, Counters &cnt,
+                                           float3 noi = make_float3(0.0f, 0.0f, 0.0f));
 
 constexpr int kRefStack = 80;   // BVH2TraverseF32's stack, BVH/BVH2Common.cpp:3412
 
@@ -87,6 +88,7 @@ __device__ __forceinline__ void trace_instance(const DevScene &s, float3 pos, fl
     return;
   }
 
+  const float3 noi = f3(-(rp.x * inv.x), -(rp.y * inv.y), -(rp.z * inv.z));   // FEAT bit 4's slab test
   // per-ray stack of (node ref, entry distance as float bits), one 8-byte entry each
   uint2 st[STACK];
   int sp = 0;
@@ -109,7 +111,10 @@ __device__ __forceinline__ void trace_instance(const DevScene &s, float3 pos, fl
         have_leaf = true;
         break;
       }
-      visit_node<COUNT, STACK>(s, ref, rp, inv, tNear, hit.t, st, sp, cnt);
+      if (FEAT & 16)
+        visit_node<COUNT, STACK, true>(s, ref, rp, inv, tNear, hit.t, st, sp, cnt, noi);
+      else
+        visit_node<COUNT, STACK>(s, ref, rp, inv, tNear, hit.t, st, sp, cnt);
     }
     if (!have_leaf) break;
     const float t_before = hit.t;
@@ -118,7 +123,7 @@ __device__ __forceinline__ void trace_instance(const DevScene &s, float3 pos, fl
     else if (TYPE == LRT_TYPE_SDF_SVS)
       svs_intersect<COUNT, MODE>(s, rp, rd, tNearSdf, leaf, hit, cnt);
     else
-      brick_intersect<COUNT, false, MODE, FEAT & 3>(s, rp, rd, inv, tNearSdf, leaf, hit, cnt);
+      brick_intersect<COUNT, false, MODE, FEAT & 19>(s, rp, rd, inv, tNearSdf, leaf, hit, cnt);
     if (stop_first && hit.t < t_before) break;
   }
 }
@@ -131,7 +136,9 @@ __device__ __forceinline__ void trace_instance(const DevScene &s, float3 pos, fl
 // FEAT bit 3: several instances of the geometry (s.insts), each tested and
 // walked in instance order with the closest hit so far -- the reference walks
 // its TLAS over the instance boxes (:3508-3547) with the same hit.t culling, so
-// the closest hit is the same; hit.inst names the instance hit.
+// the closest hit is the same; hit.inst names the instance hit.  FEAT bit 4
+// (value 16): inner-node slab tests as one FMA per plane (ray_box_fma), for the
+// kernels compiled with contraction.
 template <int TYPE, bool COUNT, int MODE = -1, int STACK = kStackSize, int FEAT = 0>
 __device__ void trace(const DevScene &s, float3 pos, float tNear, float3 dir, float tFar, Hit &hit, Counters &cnt) {
   const bool stop_first = (tFar <= 0.0f);
@@ -157,9 +164,9 @@ __device__ void trace(const DevScene &s, float3 pos, float tNear, float3 dir, fl
 
 // One inner node of the per-ray traversal: test the four child boxes with the
 // reference slab test and push the entered ones far-to-near.
-template <bool COUNT, int STACK>
+template <bool COUNT, int STACK, bool FMA_SLAB>
 __device__ __forceinline__ void visit_node(const DevScene &s, uint32_t ref, float3 rp, float3 inv, float tNear,
-                                           float hit_t, uint2 *st, int &sp, Counters &cnt) {
+                                           float hit_t, uint2 *st, int &sp, Counters &cnt, float3 noi) {
   {
     const WNode4 *nd = s.nodes + ref;
     if (COUNT) cnt.nodes++;
@@ -180,7 +187,8 @@ __device__ __forceinline__ void visit_node(const DevScene &s, uint32_t ref, floa
     int nk = 0;
 #pragma unroll
     for (int i = 0; i < 4; i++) {
-      const float2 tm = ray_box(rp, inv, lxa[i], lya[i], lza[i], hxa[i], hya[i], hza[i]);
+      const float2 tm = FMA_SLAB ? ray_box_fma(inv, noi, lxa[i], lya[i], lza[i], hxa[i], hya[i], hza[i])
+                                 : ray_box(rp, inv, lxa[i], lya[i], lza[i], hxa[i], hya[i], hza[i]);
       const bool h = (tm.x <= tm.y) && (tm.y >= tNear) && (tm.x <= hit_t) && cha[i] != kEmptyChild;
       kt[i] = h ? tm.x : -__int_as_float(0x7f800000);
       kr[i] = cha[i];
