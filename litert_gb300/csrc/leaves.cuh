@@ -408,16 +408,17 @@ __device__ void brick_intersect(const DevScene &s, float3 ray_pos, float3 ray_di
   const float d = 2.0f / (sz * bs);
   const float3 bmin = add(f3(-1, -1, -1), scl(sz_inv, f3(px, py, pz)));
   const float3 bmax = add(bmin, scl(sz_inv, f3(1, 1, 1)));
-  float2 bnf = ray_box(ray_pos, inv, bmin.x, bmin.y, bmin.z, bmax.x, bmax.y, bmax.z);
+  // FEAT bit 4: slab and voxel-plane distances p * inv + noi, local position lp0 + t * rds
+  constexpr bool kFma = (FEAT & 16) != 0;
+  const float3 noi = f3(-(ray_pos.x * inv.x), -(ray_pos.y * inv.y), -(ray_pos.z * inv.z));
+  float2 bnf = kFma ? ray_box_fma(inv, noi, bmin.x, bmin.y, bmin.z, bmax.x, bmax.y, bmax.z)
+                    : ray_box(ray_pos, inv, bmin.x, bmin.y, bmin.z, bmax.x, bmax.y, bmax.z);
   bnf.x = fmx(bnf.x, start_t);
   const float old_t = hit.t;
   const float scale = 0.5f * sz * bs;
   const uint32_t *occ = s.occ + size_t(brick) * s.occ_words;
   const bool posx = inv.x > 0.0f, posy = inv.y > 0.0f, posz = inv.z > 0.0f;
-  // FEAT bit 4: local position lp0 + t * rds, voxel planes p * inv + noi
-  constexpr bool kFma = (FEAT & 16) != 0;
   const float3 lp0 = scr(sub(ray_pos, bmin), scale), rds = scl(scale, ray_dir);
-  const float3 noi = f3(-(ray_pos.x * inv.x), -(ray_pos.y * inv.y), -(ray_pos.z * inv.z));
   float values[8];
   if (COUNT) cnt.leaves++;
   const uint32_t max_steps = walk_step_bound(bsz, bnf.y - bnf.x);
@@ -452,7 +453,8 @@ __device__ void brick_intersect(const DevScene &s, float3 ray_pos, float3 ray_di
       const float fy = kFma ? fmaf(ey, inv.y, noi.y) : inv.y * (ey - ray_pos.y);
       const float fz = kFma ? fmaf(ez, inv.z, noi.z) : inv.z * (ez - ray_pos.z);
       exit_t = fmn(fmn(fx, fy), fz);
-      const uint32_t vid = (uint32_t(vp.x) * bsz + uint32_t(vp.y)) * bsz + uint32_t(vp.z);
+      // (x * bsz + y) * bsz + z formed in float (integers below 2^24: exact), one conversion
+      const uint32_t vid = uint32_t(fmaf(fmaf(vp.x, bs, vp.y), bs, vp.z));
       step++;
       if (COUNT) cnt.voxels++;
       if ((__ldg(&occ[vid >> 5]) >> (vid & 31u)) & 1u) {
@@ -472,7 +474,7 @@ __device__ void brick_intersect(const DevScene &s, float3 ray_pos, float3 ray_di
           }
         }
       }
-      bnf.x += fmx(0.0f, exit_t - bnf.x) + 1e-6f;
+      bnf.x = kFma ? fmx(bnf.x, exit_t) + 1e-6f : bnf.x + fmx(0.0f, exit_t - bnf.x) + 1e-6f;
     }
     if (!cand) break;
     const float3 start_pos = add(ray_pos, scl(fnf.x, ray_dir));
@@ -480,7 +482,7 @@ __device__ void brick_intersect(const DevScene &s, float3 ray_pos, float3 ray_di
     const float qFar = (fnf.y - fnf.x) * scale;
     local_surface<COUNT, MODE>(pr, s, type, ray_dir, values, brick, d, 0.0f, qFar, fnf, start_q, hit, cnt);
     if ((FEAT & 1) && hit.t != old_t) smooth_normal(s, brick, vp, start_q, fnf.x, d, ray_dir, v_size, hit);
-    bnf.x += fmx(0.0f, exit_t - bnf.x) + 1e-6f;
+    bnf.x = kFma ? fmx(bnf.x, exit_t) + 1e-6f : bnf.x + fmx(0.0f, exit_t - bnf.x) + 1e-6f;
   }
   if ((FEAT & 2) && hit.t < old_t && (h.aux_data & 0xFF000000u) != LRT_SBS_LAYOUT_DX &&
       (h.aux_data & 0xFF000000u) != LRT_SBS_LAYOUT_UNDEFINED)
