@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(128, 5) render_kernel(DevScene s, RenderLaunch
     const DevView &V = L.views[v];
     const uint32_t lt = tile - V.tile_offset, lw = V.tile_w_log2;
     if (L.chunk_done) {   // the same for the whole grid
-      const uint32_t c = V.chunk_offset + (lt / V.tiles_x) / V.rows_per_chunk;
+      const uint32_t c = V.chunk_offset + lt / (V.tiles_x * V.rows_per_chunk);   // floor(floor(a/b)/c) = floor(a/(bc))
       if (pending && c != chunk) {
         publish_tiles(L.chunk_done, chunk, pending, lane);
         pending = 0;
