@@ -197,13 +197,18 @@ def run_device_bvh(args, h, nodes, values, views, tuned, hits, flush, stream, to
 
 
 def cpu_sample(views, n_target, seed=0):
-    """A strided pixel sample over all views: list of (view index, pixel ids)."""
+    """An evenly spaced pixel sample over all views: list of (view index, pixel
+    ids).  Pixel i * (w * h) // k for i < k (every pixel when k = w * h), so the
+    sample's counters do not drift with its size (a whole-number stride cut to
+    k pixels would keep only the top rows of each view)."""
     total = sum(w * h for w, h, _, _ in views)
     out = []
     for vi, (w, h, _, _) in enumerate(views):
-        k = max(1, int(round(n_target * (w * h) / total)))
-        stride = max(1, (w * h) // k)
-        out.append((vi, np.arange(seed % stride, w * h, stride, dtype=np.uint32)[:k]))
+        n = w * h
+        k = min(n, max(1, int(round(n_target * n / total))))
+        idx = (np.arange(k, dtype=np.uint64) * np.uint64(n)) // np.uint64(k)
+        idx = np.minimum(idx + np.uint64(seed % max(1, n // k)), np.uint64(n - 1))
+        out.append((vi, idx.astype(np.uint32)))
     return out
 
 
