@@ -474,7 +474,8 @@ __device__ void brick_intersect(const DevScene &s, float3 ray_pos, float3 ray_di
           }
         }
       }
-      bnf.x = kFma ? fmx(bnf.x, exit_t) + 1e-6f : bnf.x + fmx(0.0f, exit_t - bnf.x) + 1e-6f;
+      if (kFma) bnf.x = fmx(bnf.x, exit_t) + 1e-6f;
+      else bnf.x += fmx(0.0f, exit_t - bnf.x) + 1e-6f;   // the reference's rounding: t + (step + 1e-6)
     }
     if (!cand) break;
     const float3 start_pos = add(ray_pos, scl(fnf.x, ray_dir));
@@ -482,7 +483,8 @@ __device__ void brick_intersect(const DevScene &s, float3 ray_pos, float3 ray_di
     const float qFar = (fnf.y - fnf.x) * scale;
     local_surface<COUNT, MODE>(pr, s, type, ray_dir, values, brick, d, 0.0f, qFar, fnf, start_q, hit, cnt);
     if ((FEAT & 1) && hit.t != old_t) smooth_normal(s, brick, vp, start_q, fnf.x, d, ray_dir, v_size, hit);
-    bnf.x = kFma ? fmx(bnf.x, exit_t) + 1e-6f : bnf.x + fmx(0.0f, exit_t - bnf.x) + 1e-6f;
+    if (kFma) bnf.x = fmx(bnf.x, exit_t) + 1e-6f;
+    else bnf.x += fmx(0.0f, exit_t - bnf.x) + 1e-6f;   // the reference's rounding: t + (step + 1e-6)
   }
   if ((FEAT & 2) && hit.t < old_t && (h.aux_data & 0xFF000000u) != LRT_SBS_LAYOUT_DX &&
       (h.aux_data & 0xFF000000u) != LRT_SBS_LAYOUT_UNDEFINED)
