@@ -3,14 +3,18 @@ seconds.
 
 * Headline scene: the 1024^3 smooth union (213,585 bricks of 8^3) rendered in all
   16 uneven views (33.6 M rays) in one batched launch.  The bit-exact kernel's
-  records equal the oracle's on a strided sample of 40,000 pixels across the
-  views; the contracted kernel meets the forward tolerance against the bit-exact
-  one on all rays (hit mask and depth within 1e-4 of the scene extent apart from
-  < 0.01 % grazing rays).
+  records equal the oracle's on every one of the 33.6 M pixels (the oracle on all
+  host cores, about 2 s on 16): the same hit mask, t and normal bit for bit, and
+  the same brick apart from crossings exactly on a shared brick face, where t is
+  equal (measured: 21 of 33.6 M); the contracted kernel meets the forward
+  tolerance against the bit-exact one on all rays (hit mask and depth within 1e-4
+  of the scene extent apart from < 0.01 % grazing rays).
 * Reconstruction: the 8-view 512^2 workload on the 128^3 grid (2.25 M
   parameters); one view's gradient (interior + border integral) equals the
   oracle's within 1e-3 of its norm.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -21,17 +25,6 @@ from oracle import oracle_dr as od
 from _util import canon_bits
 
 pytestmark = pytest.mark.gpu
-
-
-def _strided(views, n_target):
-    total = sum(w * h for w, h, _, _ in views)
-    out, off = [], 0
-    for vi, (w, h, _, _) in enumerate(views):
-        k = max(1, int(round(n_target * (w * h) / total)))
-        stride = max(1, (w * h) // k)
-        out.append((vi, off, np.arange(stride // 2, w * h, stride, dtype=np.uint32)[:k]))
-        off += w * h
-    return out
 
 
 def test_headline_scene_full_size():
@@ -50,25 +43,28 @@ def test_headline_scene_full_size():
     s.set_tuning("fma", 1)
     fused = s.render_host(views, hits=True)["hits"]
     s.close()
-    # the bit-exact kernel against the oracle on a strided sample
+    # the bit-exact kernel against the oracle on every pixel
     osc = orc.Scene("sbs", sbs=(orc.SbsHeader(h.brick_size, h.brick_pad, h.bytes_per_value, h.aux_data), nodes,
                                 values), intersect=lrt.INTERSECT_NEWTON, render_mode=lrt.RENDER_MODE_NORMAL)
-    n_cmp = n_hit = 0
-    for vi, off, pix in _strided(views, 40000):
-        w, hh, wv, pj = views[vi]
-        o, _ = osc.render_pixels(w, hh, lrt.inverse4x4(pj), lrt.inverse4x4(wv), pix)
-        gsel = exact[off + pix.astype(np.int64)]
+    n_cmp = n_hit = n_face = 0
+    off = 0
+    for w, hh, wv, pj in views:
+        pix = np.arange(w * hh, dtype=np.uint32)
+        o, _ = osc.render_pixels(w, hh, lrt.inverse4x4(pj), lrt.inverse4x4(wv), pix, threads=os.cpu_count() or 1)
+        gsel = exact[off:off + w * hh]
+        off += w * hh
         mo = o["primId"] != lrt.MISS
         assert np.array_equal(gsel["primId"] != lrt.MISS, mo)
         assert np.array_equal(canon_bits(gsel["t"][mo]), canon_bits(o["t"][mo]))
         # bricks do not overlap: equal t in two bricks needs a crossing exactly on a shared face
         same = mo & (gsel["primId"] == o["primId"])
-        assert (mo & ~same).sum() <= 2
+        n_face += int((mo & ~same).sum())
         assert np.array_equal(canon_bits(gsel["nx"][same]), canon_bits(o["coords"][same, 2]))
         assert np.array_equal(canon_bits(gsel["ny"][same]), canon_bits(o["coords"][same, 3]))
         n_cmp += pix.size
         n_hit += int(mo.sum())
-    assert n_cmp >= 39000 and n_hit > 5000
+    assert n_cmp == n_rays and n_hit > 5_000_000
+    assert n_face <= 1e-6 * n_rays, n_face
     # the contracted kernel against the bit-exact one on every ray: rays whose hit or
     # depth differs (beyond 1e-4 of the extent 2) are grazing rays -- a tangent
     # crossing found by one kernel and missed by the other, the ray going on to a
