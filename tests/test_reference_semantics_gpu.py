@@ -1,8 +1,7 @@
 """GPU parity against the reference's own semantics at the benchmark sizes.
 
 * Triangle mesh at full size: the 327,680-triangle displaced icosphere rendered at
-  1920x1080 from the seeded camera, compared on a strided sample of 230k pixels
-  with the oracle (IntersectAllTrianglesInLeaf, BVH/BVH2Common.cpp:2776-2840;
+  1920x1080 from the seeded camera, compared on every pixel with the oracle (IntersectAllTrianglesInLeaf, BVH/BVH2Common.cpp:2776-2840;
   triangles have no first-hit early-out, so the reference returns the closest hit
   too).  The bar is the forward tolerance: hit mask identical apart from < 0.01 %
   of the pixels, depth within 1e-4 of the scene extent (2), normals within 1e-3;
@@ -12,18 +11,22 @@
   first SDF leaf that reports a hit (BVH/BVH2Common.cpp:3402-3405, 3478), the
   default kernels return the closest one.  On the small sphere configuration (all
   65,536 pixels) the two agree within the tolerance (measured: no difference).
-  On a 48k-pixel sample of the 16-view 1024^3 headline they do not: 212 pixels
-  (0.44 %, max |dt| 0.89) hit a farther brick first, where sibling boxes of the
-  BVH2 overlap -- a property of the reference's early-out on a given tree, not of
-  the arithmetic.  The "first_hit" tuning reproduces the reference's result on
-  the same tree bit for bit (checked here on the same sample), and the count of
-  closest-vs-first differences is held to its measured size.
+  On the 16-view 1024^3 headline (all 33.6 M pixels) they do not: about 0.4 % of
+  the pixels hit a farther brick first, where sibling boxes of the BVH2 overlap --
+  a property of the reference's early-out on a given tree, not of the arithmetic.
+  The "first_hit" tuning reproduces the reference's result on the same tree bit
+  for bit on every pixel (NaN normals of zero gradients compared as NaN), and the count of closest-vs-first differences is held to
+  its measured size.  The oracle runs on all host cores.
 """
+import os
+
 import numpy as np
 import pytest
 
 from litert_gb300 import lrt, scenes
 from oracle import oracle as orc
+
+from _util import canon_bits
 
 pytestmark = pytest.mark.gpu
 
@@ -32,13 +35,13 @@ DEPTH_TOL = 1e-4 * EXTENT
 MASK_FRAC = 1e-4        # 0.01 % of the pixels
 
 
-def _strided(views, n_target):
-    total = sum(w * h for w, h, _, _ in views)
+THREADS = os.cpu_count() or 1
+
+
+def _all_pixels(views):
     out, off = [], 0
     for vi, (w, h, _, _) in enumerate(views):
-        k = max(1, int(round(n_target * (w * h) / total)))
-        stride = max(1, (w * h) // k)
-        out.append((vi, off, np.arange(stride // 2, w * h, stride, dtype=np.uint32)[:k]))
+        out.append((vi, off, np.arange(w * h, dtype=np.uint32)))
         off += w * h
     return out
 
@@ -76,11 +79,11 @@ def test_mesh_full_size_against_oracle():
     g_all = s.render_host([view], hits=True)["hits"]
     s.close()
     osc = orc.Scene("mesh", mesh=(verts, faces), render_mode=lrt.RENDER_MODE_NORMAL)
-    (_, _, pix), = _strided([view], 230_000)
-    o, _ = osc.render_pixels(w, h, lrt.inverse4x4(pj), lrt.inverse4x4(wv), pix)
-    g = g_all[pix.astype(np.int64)]
+    pix = np.arange(w * h, dtype=np.uint32)
+    o, _ = osc.render_pixels(w, h, lrt.inverse4x4(pj), lrt.inverse4x4(wv), pix, threads=THREADS)
+    g = g_all
     r = _tolerance_report(g, o)
-    assert r["n"] >= 200_000 and r["hits"] > 50_000, r
+    assert r["n"] == w * h and r["hits"] > 500_000, r
     assert r["mask"] <= MASK_FRAC * r["n"], r
     assert r["depth"] == 0, r
     both = r["both"]
@@ -95,7 +98,7 @@ def test_mesh_full_size_against_oracle():
     assert np.abs(ng - no).max() <= 1e-3
     # the kernel is the uncontracted one: depths are bit-identical
     assert np.array_equal(g["t"][both].view(np.uint32), o["t"][both].view(np.uint32))
-    print(f"mesh 1920x1080: {r['n']} sampled rays, {r['hits']} hits, mask diffs {r['mask']}, "
+    print(f"mesh 1920x1080: {r['n']} rays, {r['hits']} hits, mask diffs {r['mask']}, "
           f"shared-edge ties {int(ties.sum())} ({tie_rate:.2e} of hits)")
 
 
@@ -106,7 +109,7 @@ def _first_hit_counts(s, osc_first, views, sample, fma):
     max_dt = 0.0
     for vi, off, pix in sample:
         w, hh, wv, pj = views[vi]
-        o, _ = osc_first.render_pixels(w, hh, lrt.inverse4x4(pj), lrt.inverse4x4(wv), pix)
+        o, _ = osc_first.render_pixels(w, hh, lrt.inverse4x4(pj), lrt.inverse4x4(wv), pix, threads=THREADS)
         r = _tolerance_report(g_all[off + pix.astype(np.int64)], o)
         n += r["n"]
         hits += r["hits"]
@@ -153,11 +156,11 @@ def headline():
 @pytest.mark.parametrize("fma", [0, 1])
 def test_closest_vs_first_hit_headline(headline, fma):
     s, osc, views = headline
-    r = _first_hit_counts(s, osc, views, _strided(views, 48_000), fma)
+    r = _first_hit_counts(s, osc, views, _all_pixels(views), fma)
     print(f"headline 16 views fma={fma}: {r}")
-    assert r["n"] >= 47_000 and r["hits"] > 5000
+    assert r["n"] == sum(w * h for w, h, _, _ in views) and r["hits"] > 5_000_000
     assert r["mask"] <= MASK_FRAC * r["n"], r
-    # measured 212 of 48,000 (first hits in a farther brick behind overlapping boxes)
+    # first hits in a farther brick behind overlapping boxes (measured: 212 of a 48,000-pixel sample)
     assert r["depth"] <= 0.01 * r["n"], r
 
 
@@ -170,13 +173,16 @@ def test_first_hit_mode_reproduces_reference_on_headline(headline):
     finally:
         s.set_tuning("first_hit", 0)
     n = 0
-    for vi, off, pix in _strided(views, 48_000):
+    for vi, off, pix in _all_pixels(views):
         w, hh, wv, pj = views[vi]
-        o, _ = osc.render_pixels(w, hh, lrt.inverse4x4(pj), lrt.inverse4x4(wv), pix)
+        o, _ = osc.render_pixels(w, hh, lrt.inverse4x4(pj), lrt.inverse4x4(wv), pix, threads=THREADS)
         g = g_all[off + pix.astype(np.int64)]
         assert np.array_equal(g["primId"], o["primId"])
         hit = o["primId"] != lrt.MISS
         assert np.array_equal(g["t"][hit].view(np.uint32), o["t"][hit].view(np.uint32))
-        assert np.array_equal(g["nx"][hit].view(np.uint32), o["coords"][hit, 2].view(np.uint32))
+        # bit for bit; a zero gradient's normal is NaN on both sides, with the payload of
+        # each machine (measured: 63 of 9.9 M hits)
+        assert np.array_equal(canon_bits(g["nx"][hit]), canon_bits(o["coords"][hit, 2]))
+        assert np.array_equal(canon_bits(g["ny"][hit]), canon_bits(o["coords"][hit, 3]))
         n += pix.size
-    assert n >= 47_000
+    assert n == sum(w * h for w, h, _, _ in views)
