@@ -391,15 +391,19 @@ __device__ bool brick_visit(const DevScene &s, uint32_t node, float3 pos, float3
                floorf(clampf(lp.z, 1e-6f, bs - 1e-6f)));
       min_pos = add(B.bmin, scl(B.d, vox));
       const float3 max_pos = add(min_pos, scl(B.d, f3(1, 1, 1)));
-      load_vals(s, node, vox, values);
       fnf = ray_box(pos, inv, min_pos.x, min_pos.y, min_pos.z, max_pos.x, max_pos.y, max_pos.z);
       step++;
-      float vmin = values[0];
-      vmax = fabsf(values[0]);
-#pragma unroll
-      for (int i = 1; i < 8; i++) { vmin = fminf(vmin, values[i]); vmax = fmaxf(vmax, fabsf(values[i])); }
+      // the voxel's min v and max |v| over its 8 corners (dr_brick_bounds_kernel
+      // folds them in the corner order of load_vals); its corners are loaded only
+      // for the voxel that goes to Intersect
+      const uint32_t bsz = s.brick_size;
+      const float2 vb = __ldg(&s.vbounds[(size_t)node * (bsz * bsz * bsz) +
+                                         (uint32_t(vox.x) * bsz + uint32_t(vox.y)) * bsz + uint32_t(vox.z)]);
+      const float vmin = vb.x;
+      vmax = vb.y;
       if (tNear < fnf.x) {
         if (!(vmin > (BORDER ? fminf(rl->sdf, rl->skip_t) : 0.0f) + skip_margin(vmax))) {
+          load_vals(s, node, vox, values);
           cand = true;
           break;
         }
@@ -1356,10 +1360,13 @@ void launch_query(const DevScene &s, uint32_t flags, float relax_eps, const floa
 }
 
 // per brick: its distance values gathered from the parameters (a float copy in
-// the brick's own order) with their min v and max |v| (one warp per brick),
+// the brick's own order) with their min v and max |v| (one warp per brick), and
+// per voxel the min and max |.| of its 8 corner values, folded in the walks'
+// corner order (what brick_visit tests before it loads a voxel's corners);
 // refreshed whenever the parameters change
 __global__ void dr_brick_bounds_kernel(const uint4 *nodes, const uint32_t *values, const float *P, uint32_t n_nodes,
-                                       uint32_t v3, float2 *out, float *bvals) {
+                                       uint32_t v3, float2 *out, float *bvals, float2 *vbounds, uint32_t bsz,
+                                       uint32_t v_size) {
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= n_nodes) return;
   const uint32_t off = __ldg(&nodes[warp]).z;
@@ -1376,12 +1383,27 @@ __global__ void dr_brick_bounds_kernel(const uint4 *nodes, const uint32_t *value
     mx_ = fmaxf(mx_, __shfl_xor_sync(0xFFFFFFFFu, mx_, o));
   }
   if (lane == 0) out[warp] = make_float2(mn_, mx_);
+  __syncwarp();   // the warp's gathered values, for the per-voxel bounds
+  const float *b = bvals + (size_t)warp * v3;
+  const uint32_t b3 = bsz * bsz * bsz;
+  for (uint32_t k = lane; k < b3; k += 32) {
+    const uint32_t x = k / (bsz * bsz), y = (k / bsz) % bsz, z = k % bsz;
+    float vmin = b[vid(x, y, z, v_size)], vmax = fabsf(vmin);
+#pragma unroll
+    for (int i = 1; i < 8; i++) {
+      const float v = b[vid(x + ((i & 4) >> 2), y + ((i & 2) >> 1), z + (i & 1), v_size)];
+      vmin = fminf(vmin, v);
+      vmax = fmaxf(vmax, fabsf(v));
+    }
+    vbounds[(size_t)warp * b3 + k] = make_float2(vmin, vmax);
+  }
 }
 
 void launch_brick_bounds(const DevScene &s, uint32_t n_nodes, float2 *out, cudaStream_t st) {
   const uint32_t v3 = s.v_size * s.v_size * s.v_size;
   dr_brick_bounds_kernel<<<(n_nodes + 7) / 8, 256, 0, st>>>(s.nodes, s.values, s.P, n_nodes, v3, out,
-                                                             const_cast<float *>(s.bvals));
+                                                             const_cast<float *>(s.bvals),
+                                                             const_cast<float2 *>(s.vbounds), s.brick_size, s.v_size);
 }
 
 __global__ void dr_scale_kernel(float *g, uint32_t n, float s) {

@@ -29,6 +29,7 @@ struct DrState {
   DevBuf<float4> d_pairs;
   DevBuf<float2> d_bounds;     // per-brick distance bounds for the exact skips
   DevBuf<float> d_bvals;       // per-brick gathered distance values
+  DevBuf<float2> d_vbounds;    // per-voxel corner bounds (the walks' skip test)
   // views
   std::vector<lrt_view> views;
   std::vector<lrt_view> orig_views;   // the reference as lrt_dr_set_reference received it
@@ -60,6 +61,7 @@ void dr_state_free(DrState *st) {
   st->d_pairs.release();
   st->d_bounds.release();
   st->d_bvals.release();
+  st->d_vbounds.release();
   st->d_ref.release();
   st->d_img.release();
   st->d_depth.release();
@@ -137,6 +139,7 @@ drk::DevScene dev_scene(lrt_ctx *ctx) {
   s.n_pairs = uint32_t(st.pairs.size());
   s.brick_bounds = st.d_bounds.p;
   s.bvals = st.d_bvals.p;
+  s.vbounds = st.d_vbounds.p;
   s.brick_size = st.hdr.brick_size;
   s.v_size = st.hdr.brick_size + 2 * st.hdr.brick_pad + 1;
   s.layout_in = (st.hdr.aux_data & 0xFF000000u) == (5u << 24) ? 1u : 0u;
@@ -389,6 +392,7 @@ extern "C" lrt_status lrt_dr_set_scene(lrt_ctx *ctx, const lrt_sbs_header *hdr, 
   LRT_CUDA(ctx, cudaMemset(st.d_status.p, 0, 4));
   LRT_CUDA(ctx, st.d_bounds.ensure(n_nodes));
   LRT_CUDA(ctx, st.d_bvals.ensure(size_t(n_nodes) * v3));
+  LRT_CUDA(ctx, st.d_vbounds.ensure(size_t(n_nodes) * hdr->brick_size * hdr->brick_size * hdr->brick_size));
   st.has_scene = true;
   return prepare_extras(ctx);
 }

@@ -26,6 +26,7 @@ struct DevScene {
   uint32_t n_pairs;
   const float2 *brick_bounds; // per brick: min distance value, max |distance value|
   const float *bvals;         // per brick: its v^3 distance values gathered from P
+  const float2 *vbounds;      // per voxel (brick-major, x-major in the brick): min and max |.| of its 8 corners
   uint32_t brick_size, v_size, layout_in, need_normal;
   float inst_bmin[3], inst_bmax[3];
   float inst_inv[12];        // rows 0..2 of the instance's inverse transform
